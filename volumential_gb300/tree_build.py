@@ -1,0 +1,351 @@
+"""Box trees with tensor Gauss-Legendre nodes on the leaves, and their list-1
+(neighbour source box) CSR.
+
+Host-side builder for the inputs of the list-1 evaluation.  It follows the
+layout of ``volumential/tree_interactive_build.py:1274-1441``
+(``build_particle_tree_from_box_tree``) and of boxtree's traversal:
+
+* boxes are numbered level by level (root = box 0), ``box_levels`` is uint8,
+  ``box_centers`` is ``[dim, aligned_nboxes]`` with ``aligned_nboxes`` rounded
+  up to a multiple of 32 (``tree_interactive_build.py:1356``);
+* particles are the ``q**dim`` Gauss-Legendre nodes of every leaf, stored
+  box-contiguously; inside a leaf they follow ``meshgrid(indexing="ij")``
+  order, so the box-local index is the mode id with axis 0 slowest
+  (``meshgen.py:979-998``) and ``sorted_target_ids`` is the identity;
+* sources are targets (``sources_are_targets=True``);
+* list 1 of a leaf is every leaf whose closure touches it, itself included.
+
+Adaptive trees are refined by a user criterion and then 2:1 balanced over
+faces, edges and corners (``tree_interactive_build.py:202-432``), so every
+list-1 pair is a case of the list-1 gallery.
+"""
+
+from __future__ import annotations
+
+import itertools
+from dataclasses import dataclass, field
+
+import numpy as np
+
+__all__ = [
+    "ParticleTree",
+    "Traversal",
+    "gauss_legendre_unit",
+    "build_uniform_tree",
+    "build_adaptive_tree",
+    "build_tree_from_leaves",
+    "build_list1_traversal",
+]
+
+
+def gauss_legendre_unit(q_order):
+    """Nodes (ascending) and weights of the q-point Gauss-Legendre rule on [-1, 1]."""
+    x, w = np.polynomial.legendre.leggauss(int(q_order))
+    return x, w
+
+
+@dataclass
+class ParticleTree:
+    dim: int
+    q_order: int
+    root_extent: float
+    root_vertex: np.ndarray
+    nboxes: int
+    aligned_nboxes: int
+    box_centers: np.ndarray          # f64 [dim, aligned_nboxes]
+    box_levels: np.ndarray           # u8 [nboxes]
+    box_coords: np.ndarray           # i64 [nboxes, dim] integer box index on its level
+    box_is_leaf: np.ndarray          # bool [nboxes]
+    box_target_starts: np.ndarray    # i32 [nboxes]
+    box_target_counts_nonchild: np.ndarray  # i32 [nboxes]
+    leaf_boxes: np.ndarray           # i32 [nleaves], in particle order
+    targets: np.ndarray              # f64 [dim, N]
+    weights: np.ndarray              # f64 [N] quadrature weights
+    level_start_box_nrs: np.ndarray  # i32 [nlevels + 1]
+    sources_are_targets: bool = True
+
+    @property
+    def ntargets(self):
+        return int(self.targets.shape[1])
+
+    @property
+    def nsources(self):
+        return self.ntargets
+
+    @property
+    def sources(self):
+        return self.targets
+
+    @property
+    def box_source_starts(self):
+        return self.box_target_starts
+
+    @property
+    def box_source_counts_nonchild(self):
+        return self.box_target_counts_nonchild
+
+    @property
+    def sorted_target_ids(self):
+        return np.arange(self.ntargets, dtype=np.int32)
+
+    @property
+    def user_source_ids(self):
+        return np.arange(self.ntargets, dtype=np.int32)
+
+    @property
+    def nlevels(self):
+        return int(self.box_levels.max()) + 1 if self.nboxes else 0
+
+    def box_local_mode_ids(self):
+        """Box-local particle index (``expansion_wrangler_fpnd.py:408-424``)."""
+        nq = self.q_order ** self.dim
+        return np.tile(np.arange(nq, dtype=np.int32), self.ntargets // nq)
+
+
+@dataclass
+class Traversal:
+    tree: ParticleTree
+    target_boxes: np.ndarray                   # i32 [n_tgt_boxes]
+    neighbor_source_boxes_starts: np.ndarray   # i32 [n_tgt_boxes + 1]
+    neighbor_source_boxes_lists: np.ndarray    # i32 [nnz]
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nnz(self):
+        return int(self.neighbor_source_boxes_lists.size)
+
+
+# {{{ keys: one int64 per (level, integer coordinates)
+
+def _level_offsets(dim, max_level):
+    sizes = [1 << (dim * lev) for lev in range(max_level + 2)]
+    return np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+
+
+def _lin(coords, level):
+    coords = np.asarray(coords, dtype=np.int64)
+    out = np.zeros(coords.shape[:-1], dtype=np.int64)
+    for a in range(coords.shape[-1]):
+        out = (out << np.int64(level)) | coords[..., a]
+    return out
+
+# }}}
+
+
+def _balance(leaves_by_level, dim, max_level):
+    """Refine leaves until adjacent leaves differ by at most one level."""
+    deltas = np.array(list(itertools.product((-1, 0, 1), repeat=dim)), dtype=np.int64)
+    while True:
+        offs = _level_offsets(dim, max_level)
+        keys = np.sort(np.concatenate(
+            [offs[lev] + _lin(c, lev) for lev, c in leaves_by_level.items() if len(c)]))
+        to_refine = {}
+        # A leaf at level L forces every leaf that contains a same-level
+        # neighbour position and sits at level < L-1 to split.
+        for lev in sorted(leaves_by_level, reverse=True):
+            c = leaves_by_level[lev]
+            if len(c) == 0 or lev < 2:
+                continue
+            npos = (c[:, None, :] + deltas[None, :, :]).reshape(-1, dim)
+            inside = np.all((npos >= 0) & (npos < (1 << lev)), axis=1)
+            npos = npos[inside]
+            for coarse in range(0, lev - 1):
+                cc = npos >> (lev - coarse)
+                k = offs[coarse] + _lin(cc, coarse)
+                pos = np.searchsorted(keys, k)
+                pos = np.minimum(pos, len(keys) - 1)
+                hit = keys[pos] == k
+                if np.any(hit):
+                    to_refine.setdefault(coarse, []).append(np.unique(cc[hit], axis=0))
+        if not to_refine:
+            return leaves_by_level
+        for lev, lst in to_refine.items():
+            split = np.unique(np.concatenate(lst), axis=0)
+            cur = leaves_by_level[lev]
+            cur_k = _lin(cur, lev)
+            keep = ~np.isin(cur_k, _lin(split, lev))
+            leaves_by_level[lev] = cur[keep]
+            kids = (split[:, None, :] * 2 + np.array(
+                list(itertools.product((0, 1), repeat=dim)), dtype=np.int64)[None]
+                    ).reshape(-1, dim)
+            nxt = leaves_by_level.get(lev + 1, np.zeros((0, dim), dtype=np.int64))
+            leaves_by_level[lev + 1] = np.concatenate([nxt, kids])
+            max_level = max(max_level, lev + 1)
+
+
+def build_tree_from_leaves(leaves_by_level, *, dim, q_order, a=-0.5, b=0.5):
+    """Assemble a :class:`ParticleTree` from leaf integer coordinates per level."""
+    dim = int(dim)
+    q = int(q_order)
+    root_extent = float(b - a)
+    root_vertex = np.full(dim, float(a))
+    levels = sorted(lev for lev, c in leaves_by_level.items() if len(c))
+    max_level = levels[-1]
+
+    # all boxes: leaves plus their ancestors
+    per_level = {lev: np.zeros((0, dim), dtype=np.int64) for lev in range(max_level + 1)}
+    leaf_keys = set()
+    for lev in levels:
+        c = np.asarray(leaves_by_level[lev], dtype=np.int64)
+        per_level[lev] = np.concatenate([per_level[lev], c])
+        leaf_keys.update((lev, int(k)) for k in _lin(c, lev).tolist())
+        anc = c
+        for up in range(lev - 1, -1, -1):
+            anc = np.unique(anc >> 1, axis=0)
+            per_level[up] = np.concatenate([per_level[up], anc])
+    coords_list, lev_list = [], []
+    for lev in range(max_level + 1):
+        c = np.unique(per_level[lev], axis=0)   # lexicographic order
+        coords_list.append(c)
+        lev_list.append(np.full(len(c), lev, dtype=np.uint8))
+    box_coords = np.concatenate(coords_list)
+    box_levels = np.concatenate(lev_list)
+    nboxes = len(box_levels)
+    aligned = ((nboxes + 31) // 32) * 32
+    level_start = np.concatenate([[0], np.cumsum([len(c) for c in coords_list])]).astype(np.int32)
+
+    extents = root_extent / (2.0 ** box_levels.astype(np.float64))
+    centers = np.zeros((dim, aligned), dtype=np.float64)
+    centers[:, :nboxes] = (root_vertex[:, None]
+                           + (box_coords.T.astype(np.float64) + 0.5) * extents[None, :])
+
+    is_leaf = np.array([(int(l), int(k)) in leaf_keys for l, k in zip(
+        box_levels.tolist(),
+        np.concatenate([_lin(c, lev) for lev, c in enumerate(coords_list)]).tolist())])
+
+    leaf_boxes = np.flatnonzero(is_leaf).astype(np.int32)
+    nq = q ** dim
+    starts = np.zeros(nboxes, dtype=np.int32)
+    counts = np.zeros(nboxes, dtype=np.int32)
+    starts[leaf_boxes] = np.arange(len(leaf_boxes), dtype=np.int32) * nq
+    counts[leaf_boxes] = nq
+    # non-leaf boxes point at their first descendant's particles (unused)
+
+    x, w = gauss_legendre_unit(q)
+    grids = np.meshgrid(*([x] * dim), indexing="ij")
+    ref = np.stack([g.ravel() for g in grids], axis=0)       # [dim, nq]
+    wgrid = np.meshgrid(*([w] * dim), indexing="ij")
+    wref = np.prod(np.stack([g.ravel() for g in wgrid], axis=0), axis=0)
+    lc = centers[:, leaf_boxes]                               # [dim, nleaves]
+    le = extents[leaf_boxes]
+    targets = (lc[:, :, None] + 0.5 * le[None, :, None] * ref[:, None, :]).reshape(dim, -1)
+    weights = ((0.5 * le[:, None]) ** dim * wref[None, :]).reshape(-1)
+
+    return ParticleTree(
+        dim=dim, q_order=q, root_extent=root_extent, root_vertex=root_vertex,
+        nboxes=nboxes, aligned_nboxes=aligned, box_centers=centers,
+        box_levels=box_levels, box_coords=box_coords, box_is_leaf=is_leaf,
+        box_target_starts=starts, box_target_counts_nonchild=counts,
+        leaf_boxes=leaf_boxes, targets=np.ascontiguousarray(targets),
+        weights=np.ascontiguousarray(weights), level_start_box_nrs=level_start)
+
+
+def build_uniform_tree(dim, level, q_order, a=-0.5, b=0.5):
+    """Complete tree whose leaves are all at ``level`` on ``[a, b]^dim``."""
+    n = 1 << int(level)
+    c = np.array(list(itertools.product(range(n), repeat=dim)), dtype=np.int64)
+    return build_tree_from_leaves({int(level): c}, dim=dim, q_order=q_order, a=a, b=b)
+
+
+def build_adaptive_tree(dim, q_order, refine_fn, *, max_level, min_level=0,
+                        a=-0.5, b=0.5, max_leaves=None):
+    """2:1-balanced adaptive tree.
+
+    ``refine_fn(nodes[dim, nboxes, nq]) -> bool[nboxes]`` decides, from the
+    values of the leaf's Gauss-Legendre nodes, whether a leaf splits.  Leaves
+    below ``min_level`` always split; none splits beyond ``max_level``.
+    """
+    dim = int(dim)
+    root_extent = float(b - a)
+    x, _ = gauss_legendre_unit(q_order)
+    grids = np.meshgrid(*([x] * dim), indexing="ij")
+    ref = np.stack([g.ravel() for g in grids], axis=0)
+    kids = np.array(list(itertools.product((0, 1), repeat=dim)), dtype=np.int64)
+
+    leaves = {}
+    active = np.zeros((1, dim), dtype=np.int64)
+    for lev in range(0, int(max_level) + 1):
+        if len(active) == 0:
+            break
+        if lev < min_level:
+            split = np.ones(len(active), dtype=bool)
+        elif lev == max_level:
+            split = np.zeros(len(active), dtype=bool)
+        else:
+            ext = root_extent / 2 ** lev
+            ctr = a + (active.astype(np.float64) + 0.5) * ext          # [n, dim]
+            nodes = ctr.T[:, :, None] + 0.5 * ext * ref[:, None, :]    # [dim, n, nq]
+            split = np.asarray(refine_fn(nodes), dtype=bool)
+        leaves[lev] = active[~split]
+        active = (active[split][:, None, :] * 2 + kids[None]).reshape(-1, dim)
+        if max_leaves is not None and sum(len(v) for v in leaves.values()) + len(active) > max_leaves:
+            raise ValueError("adaptive tree exceeds max_leaves")
+    leaves = _balance({k: v for k, v in leaves.items()}, dim, int(max_level))
+    return build_tree_from_leaves(leaves, dim=dim, q_order=q_order, a=a, b=b)
+
+
+def build_list1_traversal(tree: ParticleTree) -> Traversal:
+    """Target boxes (leaves) and their list-1 source boxes as CSR."""
+    dim = tree.dim
+    levels = tree.box_levels.astype(np.int64)
+    max_level = int(levels.max())
+    offs = _level_offsets(dim, max_level)
+    keys = offs[levels] + _lin_per_box(tree.box_coords, levels)
+    is_leaf = tree.box_is_leaf
+    leaf_key_sorted_idx = np.argsort(keys[is_leaf])
+    leaf_keys = keys[is_leaf][leaf_key_sorted_idx]
+    leaf_ids = np.flatnonzero(is_leaf)[leaf_key_sorted_idx]
+
+    def lookup(k):
+        pos = np.minimum(np.searchsorted(leaf_keys, k), len(leaf_keys) - 1)
+        hit = leaf_keys[pos] == k
+        return np.where(hit, leaf_ids[pos], -1)
+
+    deltas = np.array(list(itertools.product((-1, 0, 1), repeat=dim)), dtype=np.int64)
+    fine = np.array(list(itertools.product((-1, 0, 1, 2), repeat=dim)), dtype=np.int64)
+    fine = fine[~np.all((fine >= 0) & (fine <= 1), axis=1)]
+
+    targets = tree.leaf_boxes.astype(np.int64)
+    tl = levels[targets]
+    tc = tree.box_coords[targets]
+    cand = []
+    # same level and one level coarser
+    for lev_shift in (0, 1):
+        for d in deltas:
+            pos = tc + d
+            clev = tl - lev_shift
+            valid = np.all((pos >= 0) & (pos < (1 << tl)[:, None]), axis=1) & (clev >= 0)
+            cpos = pos >> lev_shift
+            k = np.where(valid, offs[np.maximum(clev, 0)] + _lin_per_box(cpos, np.maximum(clev, 0)), -1)
+            ids = np.where(valid, lookup(k), -1)
+            if lev_shift == 1:
+                # a coarser box containing the leaf itself is its ancestor, never a leaf
+                ids = np.where(np.all(cpos == (tc >> 1), axis=1), -1, ids)
+            cand.append(ids)
+    # one level finer
+    for d in fine:
+        pos = 2 * tc + d
+        flev = tl + 1
+        valid = np.all((pos >= 0) & (pos < (1 << flev)[:, None]), axis=1) & (flev <= max_level)
+        k = np.where(valid, offs[np.minimum(flev, max_level)] +
+                     _lin_per_box(np.where(valid[:, None], pos, 0), np.minimum(flev, max_level)), -1)
+        cand.append(np.where(valid, lookup(k), -1))
+    cand = np.sort(np.stack(cand, axis=1), axis=1)
+    keep = cand >= 0
+    keep[:, 1:] &= cand[:, 1:] != cand[:, :-1]
+    nnz_per = keep.sum(axis=1)
+    starts = np.concatenate([[0], np.cumsum(nnz_per)]).astype(np.int32)
+    flat = cand[keep].astype(np.int32)
+    return Traversal(tree=tree, target_boxes=tree.leaf_boxes.astype(np.int32),
+                     neighbor_source_boxes_starts=starts,
+                     neighbor_source_boxes_lists=flat)
+
+
+def _lin_per_box(coords, levels):
+    """Linear index of integer coordinates with a per-row level."""
+    coords = np.asarray(coords, dtype=np.int64)
+    levels = np.asarray(levels, dtype=np.int64)
+    out = np.zeros(coords.shape[0], dtype=np.int64)
+    for a in range(coords.shape[1]):
+        out = (out << levels) | coords[:, a]
+    return out
