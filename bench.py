@@ -1,0 +1,460 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 list-1 near-field evaluation.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload c2|c1|c3]
+
+Workload (default ``c2``): 3D Laplace volume potential, list-1 near field only,
+FP64, adaptive 2:1-balanced octree on [-0.5, 0.5]^3 refined where the density
+variation over a leaf exceeds 1e-3 (23,087 leaves, q=4, 1,477,568 points),
+density a sum of 16 seeded Gaussians; seeded synthetic tables in the
+reference's compact layout (the evaluation is linear in the table values).
+
+One step = one list-1 evaluation of all target points for one right-hand side
+(the reference's ``near_field`` launch).  Between timed steps the L2 cache is
+flushed by writing a 256 MiB buffer (outside the timed events).  ``value`` is
+points/s with every input resident in HBM (CUDA events on the launching
+stream); ``e2e`` is the same metric through the public API
+(``NearFieldFromCSR.__call__``) with the density copied from pinned host
+memory and the potential copied back every step.
+
+``--impl reference`` times the reference algorithm on the host cores: the C
+restatement of ``volumential/list1.py``'s ``near_field`` kernel (the pocl CPU
+path of the reference cannot run without pyopencl/loopy), one OpenMP work item
+per target box, on a bounded sample of the same workload per step.
+
+With N > 1 (torchrun) every rank runs an independent replica of the workload
+(the path has no exchange step); ranks synchronise with a barrier around the
+timed region and the maximum time over ranks is reported.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "list-1 near-field pts/s & solves/s at ≤1e-9 rel err vs FP64; p50/p99 latency"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[1])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    p.add_argument("--workload", choices=("c2", "c1", "c3"), default="c2")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=10.0,
+                   help="target CPU time of the cpu_baseline sample")
+    return p.parse_args(argv)
+
+
+# {{{ environment
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d.get("bf16_tflops", 1900.0)), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            for name, val in zip(names, r[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+# }}}
+
+
+def build_workload(name):
+    from volumential_gb300 import workloads as W
+    if name == "c1":
+        return W.config_c1()
+    if name == "c3":
+        return W.config_c3(nrhs=1)
+    return W.config_c2()
+
+
+def algorithmic_bytes(w, nrhs=1, out_complex=False, coef_complex=False, table_bytes=8):
+    """Compulsory bytes of one list-1 evaluation (each array touched once)."""
+    tr = w.traversal
+    n = w.n_points
+    ntb = len(tr.target_boxes)
+    s_in = 16 if coef_complex else 8
+    s_out = 16 if out_complex else 8
+    n_compact = sum(int(np.asarray(t.get_reduced_table_data()[1]).size) for t in w.tables)
+    return (n * nrhs * (s_in + s_out) + 4 * (ntb + 1) + 4 * tr.nnz + 4 * ntb
+            + w.tree.nboxes * (8 * w.dim + 1 + 4 + 4) + n_compact * table_bytes + 2048)
+
+
+def gpu_arm(args):
+    import torch
+
+    from volumential_gb300.expansion_wrangler_fpnd import (
+        FPNDExpansionWrangler,
+        FPNDTreeIndependentDataForWrangler,
+    )
+    from volumential_gb300.plan import as_device_tensor, tree_view_from_arrays
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    w = build_workload(args.workload)
+    ti = FPNDTreeIndependentDataForWrangler(target_kernels=[w.kernel])
+    dtype = np.complex128 if w.kernel.is_complex_valued else np.float64
+    wr = FPNDExpansionWrangler(ti, w.traversal, w.tables, dtype=dtype, quad_order=w.q)
+    tr = w.traversal
+    payload = wr.get_payload(w.kernel)
+    nf = wr.near_field_evaluator(w.kernel, payload)
+    kw = wr._near_field_kwargs(payload, tr.target_boxes, tr.neighbor_source_boxes_starts,
+                               tr.neighbor_source_boxes_lists, None)
+    # resident tree arrays (device tensors) for both the kernel and the API runs
+    tree_keys = ("target_boxes", "neighbor_source_boxes_starts",
+                 "neighbor_source_boxes_lists", "box_centers", "box_levels",
+                 "box_source_starts", "box_source_counts_nonchild", "box_target_starts",
+                 "box_target_counts_nonchild", "source_mode_ids", "target_point_ids")
+    for k in tree_keys:
+        kw[k] = as_device_tensor(kw[k])
+    plan = nf.get_plan(
+        table_data_combined=kw["table_data_combined"],
+        mode_nmlz_combined=kw["mode_nmlz_combined"], case_indices=kw["case_indices"],
+        encoding_base=kw["encoding_base"], encoding_shift=kw["encoding_shift"],
+        table_root_extent=kw["table_root_extent"],
+        table_starting_level=kw["table_starting_level"],
+        **{n: kw[n] for n in kw if n.startswith("arithmetic_")})
+    view, keep = tree_view_from_arrays(root_extent=kw["root_extent"],
+                                       **{k: kw[k] for k in tree_keys})
+    n = w.n_points
+    coef_np = np.ascontiguousarray(w.coefs[0])
+    coef_complex = np.iscomplexobj(coef_np)
+    coefs = as_device_tensor(coef_np)
+    out_complex = plan.complex_table or coef_complex
+    out = torch.empty(n, dtype=torch.complex128 if out_complex else torch.float64,
+                      device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def step():
+        plan.eval_fp64(view, coefs, out, stream=sh, nrhs=1)
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        step()
+    plan.raise_on_status(sh)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e0, e1 in evs:
+        flush.fill_(float(len(evs)))
+        e0.record(stream)
+        step()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    clock_info = clocks.stop()
+    plan.raise_on_status(sh)
+
+    # e2e through the public API: pinned host density in, host potential out
+    host_in = torch.from_numpy(coef_np).pin_memory()
+    host_out = torch.empty(n, dtype=out.dtype).pin_memory()
+    dev_in = torch.empty_like(coefs)
+    dev_out = torch.empty_like(out)
+    api_kw = dict(kw)
+    api_kw.pop("mode_coefs", None)
+
+    def api_step():
+        dev_in.copy_(host_in, non_blocking=True)
+        res, _ = nf(None, result=dev_out, mode_coefs=dev_in, **api_kw)
+        host_out.copy_(res, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for _ in range(max(1, args.warmup)):
+        api_step()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.fill_(2.0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        api_step()
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+    if world > 1:
+        t = torch.tensor([sum(e2e_ms)], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    else:
+        e2e_total = float(sum(e2e_ms))
+
+    result = {
+        "w": w, "step_ms": step_ms, "total_ms": total_ms, "wall_s": wall,
+        "clocks": clock_info, "e2e_total_ms": e2e_total, "e2e_ms": e2e_ms,
+        "out": host_out.numpy().copy(), "out_complex": out_complex,
+        "coef_complex": coef_complex, "h2d": int(host_in.numel() * host_in.element_size()),
+        "d2h": int(host_out.numel() * host_out.element_size()), "plan_bytes": plan.device_bytes(),
+        "world": world, "rank": rank,
+    }
+    return result
+
+
+def oracle_sample(w, fraction, nthreads=0, seed=0):
+    """Time the C oracle on a seeded sample of target boxes; returns
+    (seconds, sampled points, sampled target point ids, result values)."""
+    from tests.helpers import oracle_for_workload  # test infrastructure
+    from tests.helpers import LAP2, LAP3, FIXED
+    policy = {"c1": LAP2, "c2": LAP3, "c3": FIXED}
+    tr = w.traversal
+    ntb = len(tr.target_boxes)
+    rng = np.random.default_rng(seed)
+    k = max(1, int(round(fraction * ntb)))
+    pick = np.sort(rng.choice(ntb, size=k, replace=False))
+    st = tr.neighbor_source_boxes_starts
+    lens = st[pick + 1] - st[pick]
+    sub_starts = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    sub_lists = np.concatenate([tr.neighbor_source_boxes_lists[st[i]:st[i + 1]]
+                                for i in pick]).astype(np.int32)
+    tree = w.tree
+    name = "c2" if w.dim == 3 else ("c3" if w.kernel.is_complex_valued else "c1")
+    prob = oracle_for_workload(w, policy[name])
+    local = tree.box_local_mode_ids()
+    t0 = time.perf_counter()
+    res = prob.near_field(
+        target_boxes=tr.target_boxes[pick], neighbor_source_boxes_starts=sub_starts,
+        neighbor_source_boxes_lists=sub_lists, box_centers=tree.box_centers,
+        box_levels=tree.box_levels, box_source_starts=tree.box_target_starts,
+        box_source_counts_nonchild=tree.box_target_counts_nonchild,
+        box_target_starts=tree.box_target_starts,
+        box_target_counts_nonchild=tree.box_target_counts_nonchild,
+        source_mode_ids=local, target_point_ids=local, mode_coefs=w.coefs[0],
+        nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    nq = w.q ** w.dim
+    ids = (tree.box_target_starts[tr.target_boxes[pick]][:, None]
+           + np.arange(nq)[None, :]).ravel()
+    return dt, int(k * nq), ids, res[ids]
+
+
+def calibrated_fraction(w, seconds, nthreads):
+    frac = 0.002
+    while True:
+        dt, _, _, _ = oracle_sample(w, frac, nthreads)
+        if dt > 0.5 or frac >= 1.0:
+            break
+        frac = min(1.0, frac * 4)
+    return min(1.0, frac * seconds / max(dt, 1e-3))
+
+
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def reference_arm(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    w = build_workload(args.workload)
+    nthreads = os.cpu_count() or 1
+    budget = min(10.0, 150.0 / max(1, args.warmup + args.steps))
+    frac = calibrated_fraction(w, budget, nthreads)
+    for i in range(args.warmup):
+        oracle_sample(w, frac, nthreads, seed=i)
+    times, pts = [], 0
+    for i in range(args.steps):
+        dt, n, _, _ = oracle_sample(w, frac, nthreads, seed=1000 + i)
+        times.append(dt)
+        pts += n
+    total = sum(times)
+    value = pts / total
+    sample = (f"{frac * 100:.2f}% of the target boxes per step (seeded), "
+              f"{pts // args.steps} target points per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "points/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "points": w.n_points,
+                   "leaves": int(len(w.traversal.target_boxes)), "q": w.q,
+                   "dim": w.dim, "nrhs": 1, "cpu": cpu_model()},
+        "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def gb300_main(args):
+    world, rank, _ = dist_env()
+    r = gpu_arm(args)
+    w = r["w"]
+    K = args.steps
+    n = w.n_points
+    value = world * n * K / (r["total_ms"] / 1e3)
+    ms_per_step = r["total_ms"] / K
+    step_ms = np.asarray(r["step_ms"])
+    hbm, _, peak_kind = peaks()
+    B = algorithmic_bytes(w, out_complex=r["out_complex"], coef_complex=r["coef_complex"],
+                          table_bytes=16 if w.tables[0].dtype == np.complex128 else 8)
+    P = w.pair_count()
+    flops = (4 if (r["out_complex"]) else 2) * P
+    kernel_s = float(np.mean(step_ms)) / 1e3
+    achieved_gbs = B / kernel_s / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(f"plain_fp64/{w.name}")
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world,
+        "steps": K, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "dim": w.dim, "q": w.q, "nrhs": 1,
+                   "points": n, "leaves": int(len(w.traversal.target_boxes)),
+                   "list1_box_pairs": w.traversal.nnz, "point_pairs": P,
+                   "path": "plain_fp64", "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "solves_per_s": 1e3 / ms_per_step,
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                       "p99": float(np.percentile(step_ms, 99))},
+        "e2e": {"value": world * n * K / (r["e2e_total_ms"] / 1e3), "unit": "points/s",
+                "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
+                "latency_ms": {"p50": float(np.percentile(r["e2e_ms"], 50)),
+                               "p99": float(np.percentile(r["e2e_ms"], 99))}},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm, "traffic": traffic,
+                     "peak_source": peak_kind, "algorithmic_bytes": int(B),
+                     "fp64_tflops": flops / kernel_s / 1e12,
+                     "note": "plain FP64 kernel: bound by the FP64 pipe, not HBM"},
+        "clocks": r["clocks"],
+        "gpu_launches": K,
+        "plan_device_bytes": r["plan_bytes"],
+    }
+
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        nthreads = os.cpu_count() or 1
+        frac = calibrated_fraction(w, args.cpu_seconds, nthreads)
+        dt, pts, ids, ref = oracle_sample(w, frac, nthreads, seed=7)
+        got = r["out"][ids]
+        err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        line["cpu_baseline"] = {
+            "value": pts / dt, "unit": "points/s", "cores": nthreads, "kind": "port",
+            "sample": f"{frac * 100:.2f}% of the target boxes (seeded), {pts} target points, "
+                      f"{dt:.1f} s on {cpu_model()}"}
+        line["rel_l2_vs_oracle_sample"] = err
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gb300_main(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,158 @@
+/*
+ * vl1 -- list-1 near-field evaluation on GB300 (sm_103a), C ABI.
+ *
+ * Drop-in boundary for volumential's list-1 evaluator.  The reference runs one
+ * loopy-generated OpenCL kernel, ``near_field``, from
+ * ``NearFieldFromCSR.__call__`` (volumential/list1.py:1260-1487; kernel body
+ * list1.py:1050-1200).  The Python package ``volumential_gb300`` keeps the
+ * reference's class and argument names and calls the entry points below
+ * through ctypes.  All array pointers in ``vl1_tree_view`` and the coefficient
+ * / result pointers are DEVICE pointers owned by the caller; the plan owns the
+ * table, the normalizers and the orbit descriptors (uploaded once per table
+ * set, like the reference's payload cache, expansion_wrangler_fpnd.py:2939-3158).
+ * Every call is ordered on the given CUDA stream and returns without a host
+ * synchronisation; device-side validation writes a status word that
+ * ``vl1_status_read`` returns.  No entry point throws, traps or aborts.
+ */
+#ifndef VL1_H
+#define VL1_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The Python layer maps them to the reference's exceptions. */
+enum {
+  VL1_OK = 0,
+  VL1_E_INVALID_CASE = 1,      /* case code outside the gallery (case_indices == -1);
+                                  the reference reads out of bounds here */
+  VL1_E_ENTRY_OOB = 2,         /* reconstructed row outside the table */
+  VL1_E_LAYOUT = 3,            /* box count > q^dim or mode id out of range
+                                  (expansion_wrangler_fpnd.py:427-463) */
+  VL1_E_LEVEL = 4,             /* table level outside [0, n_tables) */
+  VL1_E_NONFINITE = 5,         /* non-finite output (volume_fmm.py:991-995) */
+  VL1_E_UNSUPPORTED_RECON = 6, /* reconstruction kind other than arithmetic orbit
+                                  (list1.py:903-1048 generated/dense fallbacks) */
+  VL1_E_TIMEOUT = 7,           /* a bounded device wait gave up */
+  VL1_E_CUDA = 8,              /* a CUDA runtime call failed */
+  VL1_E_ARG = 9,               /* invalid argument */
+  VL1_E_NOMEM = 10,            /* device allocation failed */
+  VL1_E_UNSUPPORTED = 11       /* configuration not supported by this build */
+};
+
+enum { VL1_REAL64 = 0, VL1_COMPLEX128 = 1 };
+enum { VL1_RECON_SCALAR_ARITH = 0, VL1_RECON_SIGNED_ARITH = 1 };
+enum { VL1_DISP_NONE = 0, VL1_DISP_LOG2D = 1 };
+enum { VL1_LEVEL_ZERO = 0, VL1_LEVEL_PER_LEVEL = 1 };
+
+typedef struct vl1_plan vl1_plan;
+
+/* Table payload and kernel policy of one NearFieldFromCSR instance.
+ * Replaces the payload dict of expansion_wrangler_fpnd.py:3129-3158 and the
+ * table_data_shapes / policy strings of list1.py:91-207, 361-437.
+ * All pointers are HOST pointers; vl1_plan_create copies them. */
+typedef struct {
+  int32_t dim;                 /* 2 or 3 */
+  int32_t quad_order;          /* q, n_q_points = q^dim */
+  int32_t n_tables;            /* table levels */
+  int32_t n_table_entries;     /* compact rows per level */
+  int32_t n_cases;             /* 33 (2D) or 139 (3D) */
+  int32_t n_case_orbits;       /* canonical cases */
+  int32_t value_type;          /* VL1_REAL64 or VL1_COMPLEX128 (table + normalizers) */
+  int32_t reconstruction_kind; /* VL1_RECON_* */
+  const void *table_data;      /* [n_tables][n_table_entries] */
+  const void *mode_nmlz;       /* [n_tables][n_q_points] */
+  const int64_t *case_indices; /* [n_case_codes], -1 where no case */
+  int32_t n_case_codes;        /* encoding_base^dim */
+  int32_t encoding_base;       /* 13 */
+  double encoding_shift;       /* 6 */
+  double case_encoding_bias;   /* 1e-10 (list1.py:46) */
+  const uint16_t *case_orbit_ranks;  /* [n_cases] */
+  const uint8_t *case_axis_perm;     /* [n_cases][dim] */
+  const int8_t *case_axis_sign;      /* [n_cases][dim] */
+  const uint8_t *case_axis_group;    /* [n_cases][dim] */
+  const int32_t *case_value_offsets; /* [n_case_orbits + 1] */
+  const uint8_t *axis_sign_power;    /* [dim] */
+  const int8_t *axis_direction_signs;/* [dim] */
+  int32_t direction_sign_axis;       /* -1 when no directional derivative */
+  int32_t scaling_exponent;    /* scaling = (sbox_extent/table_root_extent)^p */
+  int32_t displacement_kind;   /* VL1_DISP_* */
+  double displacement_coef;    /* -0.5/pi for the 2D Laplace log term */
+  int32_t table_level_kind;    /* VL1_LEVEL_* */
+  double table_root_extent;
+  int32_t table_starting_level;
+} vl1_plan_desc;
+
+/* Tree arrays of one call (list1.py:1264-1354 keyword arguments).
+ * DEVICE pointers, caller owned. */
+typedef struct {
+  int32_t n_target_boxes;
+  const int32_t *target_boxes;                 /* [n_target_boxes] */
+  const int32_t *neighbor_source_boxes_starts; /* [n_target_boxes + 1] */
+  const int32_t *neighbor_source_boxes_lists;  /* [nnz] */
+  int64_t aligned_nboxes;                      /* stride of box_centers */
+  const double *box_centers;                   /* [dim][aligned_nboxes] */
+  const uint8_t *box_levels;                   /* [nboxes] */
+  const int32_t *box_source_starts;
+  const int32_t *box_source_counts_nonchild;
+  const int32_t *box_target_starts;
+  const int32_t *box_target_counts_nonchild;
+  const int32_t *source_mode_ids;              /* [n_particles] */
+  const int32_t *target_point_ids;             /* [n_particles] */
+  int64_t n_particles;
+  double root_extent;
+} vl1_tree_view;
+
+typedef struct {
+  int32_t code;        /* first error code seen since the last reset */
+  int32_t count;       /* number of faulting items */
+  int32_t detail0;     /* e.g. the target box of the first fault */
+  int32_t detail1;     /* e.g. the list position of the first fault */
+} vl1_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int32_t vl1_version(void);
+
+/* Human-readable message of the last error of the calling host thread. */
+const char *vl1_last_error_string(void);
+
+/* Upload the table payload and build the expanded per-case blocks.
+ * Replaces _get_cached_nearfield_payload (expansion_wrangler_fpnd.py:2939-3158)
+ * plus the per-pair RECONSTRUCT_ENTRY work of list1.py:604-854, which the
+ * plan performs once per (table level, case, source mode, target point). */
+int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out);
+int32_t vl1_plan_destroy(vl1_plan *plan);
+
+/* Plain FP64 list-1 evaluation (the reference's near_field kernel,
+ * list1.py:1050-1159, potential_kind=1) for nrhs right-hand sides.
+ * coefs:  [nrhs][n_particles] of coef_type (VL1_REAL64 or VL1_COMPLEX128)
+ * result: [nrhs][n_particles], complex128 if the table or the coefficients are
+ *         complex, else float64; overwritten (not accumulated), like
+ *         result[target_id] = sum(...) in list1.py:1137.
+ * stream: a cudaStream_t (NULL = legacy default stream). */
+int32_t vl1_eval_fp64(vl1_plan *plan, const vl1_tree_view *tree,
+                      const void *coefs, int32_t coef_type, int32_t nrhs,
+                      void *result, void *stream);
+
+/* Row and sign of every (table level 0, case, source mode, target point) as the
+ * device computes them: rows/signs are device arrays [n_cases][nq][nq].
+ * Exposes the integer index of list1.py:604-854 for bit-exact checks. */
+int32_t vl1_orbit_index_map(vl1_plan *plan, int32_t *rows, int8_t *signs,
+                            void *stream);
+
+/* Copy the device status word to the host (synchronises the stream) and,
+ * when reset != 0, clear it. */
+int32_t vl1_status_read(vl1_plan *plan, vl1_status *out, int32_t reset,
+                        void *stream);
+
+/* Bytes of device memory the plan holds (tables, blocks, descriptors). */
+int64_t vl1_plan_device_bytes(const vl1_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VL1_H */

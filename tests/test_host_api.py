@@ -1,0 +1,363 @@
+"""Host-side behaviour of the drop-in API (no GPU needed).
+
+Restates the reference's device-free tests: the scaling-policy strings of
+``NearFieldFromCSR`` (test/test_volume_fmm.py:3572-3750) and the
+``drive_volume_fmm(list1_only=True)`` contracts with mock wranglers
+(test/test_volume_fmm.py:6892-7300), plus the tree builder, the layout
+validation and the C ABI library's exported symbols.
+"""
+
+import ctypes
+import itertools
+import os
+import re
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from volumential_gb300 import _build, _lib
+from volumential_gb300.expansion_wrangler_fpnd import (
+    _compute_box_local_ids,
+    _validate_table_box_particle_layout,
+)
+from volumential_gb300.expansion_wrangler_interface import ExpansionWranglerInterface
+from volumential_gb300.kernels import (
+    AxisSourceDerivative,
+    AxisTargetDerivative,
+    ConstantKernel,
+    HelmholtzKernel,
+    LaplaceKernel,
+)
+from volumential_gb300.list1 import (
+    NearFieldFromCSR,
+    parse_displacement_code,
+    parse_policy,
+    parse_scaling_code,
+    parse_table_level_code,
+)
+from volumential_gb300.tree_build import (
+    build_adaptive_tree,
+    build_list1_traversal,
+    build_uniform_tree,
+)
+from volumential_gb300.volume_fmm import drive_volume_fmm
+
+SHAPES1 = {"n_tables": 1, "n_q_points": 1, "n_cases": 1, "n_table_entries": 1}
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+# {{{ scaling policy (test/test_volume_fmm.py:3572-3750)
+
+def test_helmholtz_infer_scaling_rejected():
+    with pytest.raises(RuntimeError, match="infer_kernel_scaling is unsupported"):
+        NearFieldFromCSR(HelmholtzKernel(3), SHAPES1, potential_kind=1,
+                         infer_kernel_scaling=True)
+
+
+def test_policy_per_level_tables_for_helmholtz():
+    nf = NearFieldFromCSR(HelmholtzKernel(3), dict(SHAPES1, n_tables=3))
+    p = nf.get_kernel_scaling_policy()
+    assert p.mode == "per_level_tables"
+    assert not p.infer_kernel_scaling and not p.single_table_scaling_supported
+    assert p.reference_table_level is None
+    assert p.scaling_code == "1.0" and p.displacement_code == "0.0"
+    assert "sbox_level" in p.table_level_code
+    assert p.scaling_code == nf.codegen_compute_scaling()
+    assert p.displacement_code == nf.codegen_compute_displacement()
+    assert p.table_level_code == nf.codegen_get_table_level()
+    assert parse_policy(p) == {"scaling_exponent": 0, "displacement_kind": 0,
+                               "displacement_coef": 0.0,
+                               "table_level_kind": _lib.VL1_LEVEL_PER_LEVEL}
+
+
+def test_policy_fixed_single_table_for_helmholtz():
+    nf = NearFieldFromCSR(HelmholtzKernel(3), SHAPES1)
+    p = nf.get_kernel_scaling_policy()
+    assert p.mode == "fixed_single_table"
+    assert p.reference_table_level == 0
+    assert (p.scaling_code, p.displacement_code, p.table_level_code) == ("1.0", "0.0", "0.0")
+    assert "runtime checks reject mixed source levels" in p.notes
+    assert parse_policy(p)["scaling_exponent"] == 0
+
+
+def test_laplace_derivative_infer_scaling_is_first_order():
+    for knl in (AxisTargetDerivative(0, LaplaceKernel(3)),
+                AxisSourceDerivative(1, LaplaceKernel(3))):
+        nf = NearFieldFromCSR(knl, SHAPES1)
+        assert "".join(nf.codegen_compute_scaling().split()) == "sbox_extent/table_root_extent"
+        assert parse_scaling_code(nf.codegen_compute_scaling()) == 1
+
+
+def test_laplace_policy_canonical_table():
+    nf = NearFieldFromCSR(LaplaceKernel(2), SHAPES1)
+    p = nf.get_kernel_scaling_policy()
+    assert p.mode == "canonical_single_table" and p.infer_kernel_scaling
+    assert p.single_table_scaling_supported and p.reference_table_level == 0
+    assert "sbox_extent" in p.scaling_code
+    assert "log(sbox_extent / table_root_extent)" in p.displacement_code
+    assert p.table_level_code == "0.0"
+    parsed = parse_policy(p)
+    assert parsed["scaling_exponent"] == 2
+    assert parsed["displacement_kind"] == _lib.VL1_DISP_LOG2D
+    assert parsed["displacement_coef"] == pytest.approx(-0.5 / np.pi, rel=1e-15)
+
+
+def test_custom_scaling_policy_documents_user_code():
+    nf = NearFieldFromCSR(HelmholtzKernel(3), SHAPES1, kernel_scaling_code="2 * BOX_extent",
+                          kernel_displacement_code="BOX_level")
+    p = nf.get_kernel_scaling_policy()
+    assert p.mode == "custom_single_table"
+    assert p.scaling_code == "2 * sbox_extent"
+    assert p.displacement_code == "sbox_level"
+    assert p.table_level_code == "0.0"
+    with pytest.raises(NotImplementedError):
+        parse_policy(p)
+
+
+def test_laplace_2d_derivative_has_no_log_displacement():
+    for knl in (AxisTargetDerivative(0, LaplaceKernel(2)),
+                AxisSourceDerivative(1, LaplaceKernel(2))):
+        nf = NearFieldFromCSR(knl, SHAPES1)
+        assert "".join(nf.codegen_compute_displacement().split()) == "0.0"
+
+
+def test_constant_kernel_scaling_codes():
+    assert parse_scaling_code(NearFieldFromCSR(ConstantKernel(3), SHAPES1)
+                              .codegen_compute_scaling()) == 3
+    assert parse_scaling_code(NearFieldFromCSR(ConstantKernel(2), SHAPES1)
+                              .codegen_compute_scaling()) == 2
+
+
+def test_helmholtz_split_policy_codes_parse():
+    """The split rules of expansion_wrangler_fpnd.py:4777-4833."""
+    assert parse_scaling_code("(sbox_extent * sbox_extent) / "
+                              "(table_root_extent * table_root_extent)") == 2
+    assert parse_scaling_code("(table_root_extent) / (sbox_extent)") == -1
+    kind, coef = parse_displacement_code(
+        f"-0.5 / {np.pi!r} * scaling * log(sbox_extent / table_root_extent) * "
+        "mode_nmlz[table_lev, sid]")
+    assert kind == _lib.VL1_DISP_LOG2D and coef == pytest.approx(-0.5 / np.pi)
+    assert parse_table_level_code("0.0") == _lib.VL1_LEVEL_ZERO
+
+
+def test_batch_size_must_be_positive():
+    nf = NearFieldFromCSR(LaplaceKernel(2), SHAPES1, list1_target_batch_size=0)
+    with pytest.raises(ValueError, match="must be positive"):
+        nf._target_batch_size()
+
+
+def test_vec_id_code_matches_reference_form():
+    nf = NearFieldFromCSR(LaplaceKernel(2), SHAPES1)
+    code = nf.codegen_vec_id()
+    assert code.startswith("((0.0) * encoding_base+((box_centers[0, target_box_id]")
+    assert "/ sbox_extent * 4.0 + encoding_shift + 1e-10" in code
+
+# }}}
+
+
+# {{{ drive_volume_fmm contracts (test/test_volume_fmm.py:6892-7300)
+
+class _MockWrangler(ExpansionWranglerInterface):
+    dtype = np.float64
+
+    def __init__(self, out=None, source_map=None):
+        self._out = out
+        self._source_map = source_map
+        self.reordered_src_weights = None
+        self.reordered_src_func = None
+
+    def output_zeros(self):
+        return np.array([0.0])
+
+    def reorder_sources(self, source_array):
+        src = np.asarray(source_array)
+        return src if self._source_map is None else src[self._source_map]
+
+    def reorder_potentials(self, potentials):
+        return potentials
+
+    def form_multipoles(self, level_start_source_box_nrs, source_boxes, src_weights):
+        self.reordered_src_weights = np.asarray(src_weights[0]).copy()
+        return None, None
+
+    def coarsen_multipoles(self, a, b, mpoles):
+        return mpoles, None
+
+    def eval_direct(self, target_boxes, starts, lists, mode_coefs):
+        self.reordered_src_func = np.asarray(mode_coefs).copy()
+        if self._out is not None:
+            return self._out.copy(), None
+        return np.array([np.sum(mode_coefs)]), None
+
+    def finalize_potentials(self, potentials):
+        return potentials
+
+
+def _traversal(ns=3, nt=5):
+    e = np.array([], dtype=np.int32)
+    return SimpleNamespace(
+        tree=SimpleNamespace(nsources=ns, ntargets=nt, sources_are_targets=True),
+        level_start_source_box_nrs=e, source_boxes=e, level_start_source_parent_box_nrs=e,
+        source_parent_boxes=e, target_boxes=e, neighbor_source_boxes_starts=e,
+        neighbor_source_boxes_lists=e)
+
+
+def test_list1_multi_source_superposition():
+    src0 = np.array([1.0, 2.0, 3.0])
+    src1 = np.array([10.0, 20.0, 30.0])
+    sw = np.empty(2, dtype=object)
+    sw[:] = [src0, src1]
+    sf = np.empty(2, dtype=object)
+    sf[:] = [src0, src1]
+    result = drive_volume_fmm(_traversal(), _MockWrangler(), sw, sf, list1_only=True)
+    if isinstance(result, np.ndarray) and result.dtype == object:
+        result = result[0]
+    assert np.allclose(result, [66.0])
+
+
+def test_rejects_mismatched_source_field_counts():
+    src0 = np.array([1.0, 2.0, 3.0])
+    sw = np.empty(2, dtype=object)
+    sw[:] = [src0, 10 * src0]
+    with pytest.raises(ValueError, match="same field count"):
+        drive_volume_fmm(_traversal(3, 3), _MockWrangler(), sw, src0)
+
+
+def test_reorders_src_func_with_source_permutation():
+    w = _MockWrangler(source_map=np.array([2, 0, 1]))
+    result = drive_volume_fmm(_traversal(), w, np.array([1.0, 2.0, 4.0]),
+                              np.array([10.0, 20.0, 40.0]), list1_only=True)
+    assert np.allclose(w.reordered_src_weights, [4.0, 1.0, 2.0])
+    assert np.allclose(w.reordered_src_func, [40.0, 10.0, 20.0])
+    assert np.allclose(result, [70.0])
+
+
+def test_nonfinite_list1_values_raise():
+    w = _MockWrangler(out=np.array([np.nan, 1.0]))
+    with pytest.raises(RuntimeError, match="non-finite values"):
+        drive_volume_fmm(_traversal(3, 2), w, np.array([1.0, 2.0, 3.0]),
+                         np.array([10.0, 20.0, 30.0]), list1_only=True)
+
+
+def test_rejects_removed_p2p_fallback_option():
+    with pytest.raises(TypeError, match="allow_list1_p2p_fallback"):
+        drive_volume_fmm(_traversal(), _MockWrangler(), np.ones(3), np.ones(3),
+                         list1_only=True, allow_list1_p2p_fallback=True)
+
+
+def test_non_list1_drive_is_not_implemented():
+    with pytest.raises(NotImplementedError, match="list1_only"):
+        drive_volume_fmm(_traversal(), _MockWrangler(), np.ones(3), np.ones(3))
+
+# }}}
+
+
+# {{{ tree builder and layout checks
+
+def _brute_list1(tree):
+    ext = tree.root_extent / 2.0 ** tree.box_levels.astype(float)
+    out = {}
+    for t in tree.leaf_boxes:
+        gap = np.max(np.abs(tree.box_centers[:, tree.leaf_boxes]
+                            - tree.box_centers[:, [t]])
+                     - 0.5 * (ext[tree.leaf_boxes] + ext[t])[None, :], axis=0)
+        out[int(t)] = sorted(int(s) for s in tree.leaf_boxes[gap < 1e-12])
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_list1_csr_matches_brute_force(dim):
+    rng = np.random.default_rng(dim)
+    centers = rng.uniform(-0.5, 0.5, (3, dim))
+
+    def refine(nodes):
+        v = sum(np.exp(-np.sum((nodes - c[:, None, None]) ** 2, axis=0) / 0.05 ** 2)
+                for c in centers)
+        return (v.max(-1) - v.min(-1)) > 1e-3
+
+    for tree in (build_uniform_tree(dim, 2, 2),
+                 build_adaptive_tree(dim, 2, refine, max_level=6 if dim == 2 else 4,
+                                     min_level=2)):
+        trav = build_list1_traversal(tree)
+        ref = _brute_list1(tree)
+        st = trav.neighbor_source_boxes_starts
+        for i, t in enumerate(trav.target_boxes):
+            got = trav.neighbor_source_boxes_lists[st[i]:st[i + 1]].tolist()
+            assert got == ref[int(t)]
+            lv = tree.box_levels.astype(int)
+            assert np.all(np.abs(lv[got] - lv[t]) <= 1)
+
+
+def test_uniform_tree_sizes():
+    tree = build_uniform_tree(2, 5, 4)
+    trav = build_list1_traversal(tree)
+    assert tree.ntargets == 16384 and len(trav.target_boxes) == 1024
+    assert tree.nboxes == 1365 and tree.aligned_nboxes % 32 == 0
+    assert trav.nnz == (3 * 32 - 2) ** 2
+    assert np.all(tree.box_levels[trav.target_boxes] == 5)
+
+
+def test_leaf_nodes_are_gauss_legendre_in_ij_order():
+    tree = build_uniform_tree(2, 1, 3, a=0.0, b=2.0)
+    x, w = np.polynomial.legendre.leggauss(3)
+    leaf = tree.leaf_boxes[0]
+    pts = tree.targets[:, tree.box_target_starts[leaf]:tree.box_target_starts[leaf] + 9]
+    c = tree.box_centers[:, leaf]
+    gx, gy = np.meshgrid(c[0] + 0.5 * x, c[1] + 0.5 * x, indexing="ij")
+    assert np.allclose(pts[0], gx.ravel()) and np.allclose(pts[1], gy.ravel())
+    assert np.isclose(tree.weights.sum(), 4.0)
+
+
+def test_box_local_ids_and_layout_validation():
+    tree = build_uniform_tree(2, 2, 2)
+    trav = build_list1_traversal(tree)
+    local = _compute_box_local_ids(tree, 4)
+    assert np.array_equal(local[:8], [0, 1, 2, 3, 0, 1, 2, 3])
+    _validate_table_box_particle_layout(tree, trav.target_boxes,
+                                        trav.neighbor_source_boxes_lists, 4)
+    with pytest.raises(ValueError, match="requires exactly"):
+        _validate_table_box_particle_layout(tree, trav.target_boxes,
+                                            trav.neighbor_source_boxes_lists, 9)
+    with pytest.raises(ValueError, match="not divisible"):
+        _compute_box_local_ids(tree, 3)
+
+# }}}
+
+
+# {{{ the C ABI library
+
+def _header_functions():
+    with open(os.path.join(ROOT, "include", "vl1.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"^\s*(?:int32_t|int64_t|const char \*)\s*(vl1_\w+)\(",
+                                 text, flags=re.M)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    path = _build.build()
+    lib = ctypes.CDLL(path)
+    declared = _header_functions()
+    assert len(declared) >= 8
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(declared) == set(_lib.SIGNATURES)
+    handle = _lib.lib()
+    assert handle.vl1_version() >= 100
+
+
+def test_capi_rejects_bad_plan_descriptions_without_a_gpu():
+    lib = _lib.lib()
+    d = _lib.PlanDesc()
+    d.dim = 4
+    out = ctypes.c_void_p()
+    assert lib.vl1_plan_create(ctypes.byref(d), ctypes.byref(out)) == _lib.VL1_E_UNSUPPORTED
+    assert b"dim" in lib.vl1_last_error_string()
+    d.dim = 2
+    d.reconstruction_kind = 7
+    assert lib.vl1_plan_create(ctypes.byref(d), ctypes.byref(out)) == \
+        _lib.VL1_E_UNSUPPORTED_RECON
+    assert lib.vl1_plan_create(None, ctypes.byref(out)) == _lib.VL1_E_ARG
+    assert lib.vl1_eval_fp64(None, None, None, 0, 1, None, None) == _lib.VL1_E_ARG
+
+# }}}

@@ -1,0 +1,153 @@
+"""ctypes binding of ``libvl1.so`` (the C ABI declared in ``include/vl1.h``).
+
+There is no CPU fallback: if the library cannot be loaded, or no CUDA device
+is present, every evaluation raises.  The library is built in-tree by
+``volumential_gb300._build`` (``__graft_entry__.build()`` calls it).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+__all__ = ["lib", "PlanDesc", "TreeView", "Status", "VL1Error", "check",
+           "STATUS_NAMES"]
+
+VL1_OK = 0
+VL1_E_INVALID_CASE = 1
+VL1_E_ENTRY_OOB = 2
+VL1_E_LAYOUT = 3
+VL1_E_LEVEL = 4
+VL1_E_NONFINITE = 5
+VL1_E_UNSUPPORTED_RECON = 6
+VL1_E_TIMEOUT = 7
+VL1_E_CUDA = 8
+VL1_E_ARG = 9
+VL1_E_NOMEM = 10
+VL1_E_UNSUPPORTED = 11
+
+STATUS_NAMES = {
+    VL1_OK: "VL1_OK", VL1_E_INVALID_CASE: "VL1_E_INVALID_CASE",
+    VL1_E_ENTRY_OOB: "VL1_E_ENTRY_OOB", VL1_E_LAYOUT: "VL1_E_LAYOUT",
+    VL1_E_LEVEL: "VL1_E_LEVEL", VL1_E_NONFINITE: "VL1_E_NONFINITE",
+    VL1_E_UNSUPPORTED_RECON: "VL1_E_UNSUPPORTED_RECON",
+    VL1_E_TIMEOUT: "VL1_E_TIMEOUT", VL1_E_CUDA: "VL1_E_CUDA", VL1_E_ARG: "VL1_E_ARG",
+    VL1_E_NOMEM: "VL1_E_NOMEM", VL1_E_UNSUPPORTED: "VL1_E_UNSUPPORTED",
+}
+
+VL1_REAL64 = 0
+VL1_COMPLEX128 = 1
+VL1_RECON_SCALAR_ARITH = 0
+VL1_RECON_SIGNED_ARITH = 1
+VL1_DISP_NONE = 0
+VL1_DISP_LOG2D = 1
+VL1_LEVEL_ZERO = 0
+VL1_LEVEL_PER_LEVEL = 1
+
+
+class VL1Error(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32), ("quad_order", C.c_int32), ("n_tables", C.c_int32),
+        ("n_table_entries", C.c_int32), ("n_cases", C.c_int32),
+        ("n_case_orbits", C.c_int32), ("value_type", C.c_int32),
+        ("reconstruction_kind", C.c_int32),
+        ("table_data", C.c_void_p), ("mode_nmlz", C.c_void_p),
+        ("case_indices", C.c_void_p), ("n_case_codes", C.c_int32),
+        ("encoding_base", C.c_int32), ("encoding_shift", C.c_double),
+        ("case_encoding_bias", C.c_double),
+        ("case_orbit_ranks", C.c_void_p), ("case_axis_perm", C.c_void_p),
+        ("case_axis_sign", C.c_void_p), ("case_axis_group", C.c_void_p),
+        ("case_value_offsets", C.c_void_p), ("axis_sign_power", C.c_void_p),
+        ("axis_direction_signs", C.c_void_p), ("direction_sign_axis", C.c_int32),
+        ("scaling_exponent", C.c_int32), ("displacement_kind", C.c_int32),
+        ("displacement_coef", C.c_double), ("table_level_kind", C.c_int32),
+        ("table_root_extent", C.c_double), ("table_starting_level", C.c_int32),
+    ]
+
+
+class TreeView(C.Structure):
+    _fields_ = [
+        ("n_target_boxes", C.c_int32), ("target_boxes", C.c_void_p),
+        ("neighbor_source_boxes_starts", C.c_void_p),
+        ("neighbor_source_boxes_lists", C.c_void_p),
+        ("aligned_nboxes", C.c_int64), ("box_centers", C.c_void_p),
+        ("box_levels", C.c_void_p), ("box_source_starts", C.c_void_p),
+        ("box_source_counts_nonchild", C.c_void_p), ("box_target_starts", C.c_void_p),
+        ("box_target_counts_nonchild", C.c_void_p), ("source_mode_ids", C.c_void_p),
+        ("target_point_ids", C.c_void_p), ("n_particles", C.c_int64),
+        ("root_extent", C.c_double),
+    ]
+
+
+class Status(C.Structure):
+    _fields_ = [("code", C.c_int32), ("count", C.c_int32),
+                ("detail0", C.c_int32), ("detail1", C.c_int32)]
+
+
+# symbol -> (restype, argtypes); the single source of truth for what the
+# library must export (checked by the CPU test suite)
+SIGNATURES = {
+    "vl1_version": (C.c_int32, []),
+    "vl1_last_error_string": (C.c_char_p, []),
+    "vl1_plan_create": (C.c_int32, [C.POINTER(PlanDesc), C.POINTER(C.c_void_p)]),
+    "vl1_plan_destroy": (C.c_int32, [C.c_void_p]),
+    "vl1_eval_fp64": (C.c_int32, [C.c_void_p, C.POINTER(TreeView), C.c_void_p,
+                                  C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "vl1_orbit_index_map": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]),
+    "vl1_status_read": (C.c_int32, [C.c_void_p, C.POINTER(Status), C.c_int32,
+                                    C.c_void_p]),
+    "vl1_plan_device_bytes": (C.c_int64, [C.c_void_p]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib():
+    """Load (building first if needed) and return the ctypes library."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.LIB
+            if not os.path.exists(path) or not _build.up_to_date():
+                _build.build()
+            handle = C.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = handle
+        return _lib
+
+
+def last_error():
+    msg = lib().vl1_last_error_string()
+    return msg.decode() if msg else ""
+
+
+def check(code, what=""):
+    if code != VL1_OK:
+        raise VL1Error(code, f"{what}: {last_error()}" if what else last_error())
+
+
+def ptr(x):
+    """Raw pointer of a torch tensor / numpy array (None -> NULL)."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError(f"cannot take the address of {type(x)!r}")

@@ -1,0 +1,478 @@
+"""FPND expansion wrangler, list-1 stage ("Far field by Particles, Near field Direct").
+
+Restates the list-1 part of ``volumential/expansion_wrangler_fpnd.py``:
+
+* ``_compute_box_local_ids``               -- ``:408-424``
+* ``_validate_table_box_particle_layout``  -- ``:427-514``
+* ``_build_fast_scalar_arithmetic_orbit_reconstruction`` -- ``:1667-1726``
+* ``_prepare_table_data_and_entry_map``    -- ``:1805-2066`` (arithmetic path)
+* payload cache                            -- ``:2939-3158``
+* ``eval_direct_single_out_kernel`` / ``eval_direct`` -- ``:3222-3489``
+
+plus ``eval_direct_batched``: all right-hand sides of one call in one launch
+(per-RHS outputs; ``drive_volume_fmm`` sums them, which is the reference's
+superposition of fields, ``volume_fmm.py:1028-1031``).
+
+The far-field stages of the reference's wrangler (multipoles, M2L, locals)
+are not part of this package: the wrangler supports ``list1_only`` drives.
+"""
+
+from __future__ import annotations
+
+import collections
+import logging
+import math
+
+import numpy as np
+
+from .expansion_wrangler_interface import ExpansionWranglerInterface
+from .list1 import NearFieldFromCSR
+from .orbit_arithmetic import metadata_nbytes
+
+logger = logging.getLogger(__name__)
+
+_ARITHMETIC_RECONSTRUCTION_KINDS = {"scalar-arithmetic-orbit", "signed-arithmetic-orbit"}
+
+__all__ = [
+    "FPNDExpansionWrangler", "FPNDSumpyExpansionWrangler",
+    "FPNDTreeIndependentDataForWrangler", "_compute_box_local_ids",
+    "_validate_table_box_particle_layout", "_prepare_table_data_and_entry_map",
+    "_build_fast_scalar_arithmetic_orbit_reconstruction",
+]
+
+
+def _np(x):
+    if x is None:
+        return None
+    if hasattr(x, "detach"):
+        return x.detach().cpu().numpy()
+    if hasattr(x, "get") and not isinstance(x, np.ndarray):
+        return np.asarray(x.get())
+    return np.asarray(x)
+
+
+def _compute_box_local_ids(tree, n_q_points):
+    """Box-local particle index of every particle, in tree order."""
+    if not getattr(tree, "sources_are_targets", False):
+        raise ValueError(
+            "table-based near-field evaluation requires sources and targets "
+            "to coincide (tree.sources_are_targets=True)")
+    n = int(tree.ntargets)
+    if n % n_q_points != 0:
+        raise ValueError("particle count is not divisible by box-local quadrature size")
+    local = np.tile(np.arange(n_q_points, dtype=np.int32), n // n_q_points)
+    return local[_np(tree.sorted_target_ids)]
+
+
+def _validate_table_box_particle_layout(tree, target_boxes, source_boxes, n_q_points):
+    counts = _np(tree.box_target_counts_nonchild)
+    tc = counts[_np(target_boxes).astype(np.int64)]
+    sc = counts[_np(source_boxes).astype(np.int64)]
+    if np.all(tc == n_q_points) and np.all(sc == n_q_points):
+        return
+    bad_t = np.unique(tc[tc != n_q_points])
+    bad_s = np.unique(sc[sc != n_q_points])
+    raise ValueError(
+        "table-based near-field evaluation requires exactly "
+        f"{n_q_points} quadrature points per active source/target box; "
+        f"found target counts {bad_t.tolist()} and source counts "
+        f"{bad_s.tolist()}. Build the particle tree from the mesh box-tree "
+        "(build_particle_tree_from_box_tree) to preserve per-cell quadrature layout.")
+
+
+def _build_fast_scalar_arithmetic_orbit_reconstruction(table):
+    if not hasattr(table, "_get_scalar_arithmetic_invariant_entry_info"):
+        return None
+    info = table._get_scalar_arithmetic_invariant_entry_info()
+    if info is None:
+        return None
+    md = info["arithmetic_metadata"]
+    layout = np.asarray(info["entry_ids"], dtype=np.int64)
+    n_orbits = int(np.asarray(md["case_value_offsets"]).size - 1)
+    return {
+        "kind": "scalar-arithmetic-orbit",
+        "case_orbit_ranks": np.asarray(md["case_orbit_ranks"], dtype=np.uint16),
+        "case_axis_perm": np.asarray(md["case_axis_perm"], dtype=np.uint8),
+        "case_axis_sign": np.asarray(md["case_axis_sign"], dtype=np.int8),
+        "case_axis_group": np.asarray(md["case_axis_group"], dtype=np.uint8),
+        "case_value_offsets": np.asarray(md["case_value_offsets"], dtype=np.int32),
+        "axis_sign_power": np.asarray(md["axis_sign_power"], dtype=np.uint8),
+        "axis_direction_signs": np.asarray(md["axis_direction_signs"], dtype=np.int8),
+        "direction_sign_axis": int(md["direction_sign_axis"]),
+        "layout_entry_ids": layout,
+        "layout_entry_scales": np.ones(len(layout), dtype=np.int8),
+        "n_case_orbits": n_orbits,
+        "metadata_bytes": metadata_nbytes(md),
+        "dense_arithmetic_layout_entry_count": int(n_orbits * table.n_pairs),
+        "compact_value_entry_count": int(len(layout)),
+        "representative_entry_count": int(len(layout)),
+        "distinct_layout_entry_count": int(len(np.unique(layout))),
+        "duplicate_layout_entry_count": 0,
+        "unused_layout_entry_count": 0,
+        "sign_convention_conflict_count": 0,
+    }
+
+
+def _prepare_table_data_and_entry_map(table_levels):
+    """Compact table of every level, normalizers and the reconstruction info.
+
+    Returns ``(table_data_combined, mode_nmlz_combined,
+    exterior_mode_nmlz_combined, table_entry_ids, table_entry_scales,
+    reconstruction_info)`` like the reference.  Reduced (orbit-compact) and
+    full tables are both accepted; a full table contributes the values of the
+    orbit representatives.  Kernels without an arithmetic orbit
+    reconstruction (the reference's generated/dense fallbacks) raise.
+    """
+    if not table_levels:
+        raise ValueError("table_levels cannot be empty")
+    table0 = table_levels[0]
+    reduced = [bool(getattr(t, "table_data_is_symmetry_reduced", False))
+               for t in table_levels]
+    if any(r != reduced[0] for r in reduced[1:]):
+        raise RuntimeError("mixed full/reduced near-field table storage across levels")
+    dtype = np.dtype(getattr(table0, "dtype", np.float64))
+    info = _build_fast_scalar_arithmetic_orbit_reconstruction(table0)
+    if info is None:
+        raise NotImplementedError(
+            "only the arithmetic orbit reconstruction has a GB300 kernel; this table "
+            "needs the generated-orbit or dense fallback (list1.py:903-1048)")
+    layout = info["layout_entry_ids"]
+    if len(layout) == 0:
+        raise RuntimeError("near-field reconstruction layout contains no entries")
+    for i, t in enumerate(table_levels):
+        if not t.has_entry_data_for_full_indices(layout):
+            raise RuntimeError(
+                "near-field reconstruction layout references missing data" if i == 0 else
+                "near-field levels disagree on reconstruction layout availability")
+    tdc = np.zeros((len(table_levels), len(layout)), dtype=dtype)
+    nm = np.zeros((len(table_levels), len(table0.mode_normalizers)),
+                  dtype=table0.mode_normalizers.dtype)
+    ext = np.zeros((len(table_levels), len(table0.kernel_exterior_normalizers)),
+                   dtype=table0.kernel_exterior_normalizers.dtype)
+    for lev, t in enumerate(table_levels):
+        tdc[lev] = t.get_entry_data_for_full_indices(layout)
+        nm[lev] = t.mode_normalizers
+        ext[lev] = t.kernel_exterior_normalizers
+    return (tdc, nm, ext, np.empty(0, dtype=np.int32), np.empty(0, dtype=dtype), info)
+
+
+class FPNDTreeIndependentDataForWrangler:
+    """Tree-independent wrangler data (target kernels, exclude_self)."""
+
+    def __init__(self, cl_context=None, multipole_expansion_factory=None,
+                 local_expansion_factory=None, target_kernels=(), exclude_self=True,
+                 **kwargs):
+        self.cl_context = cl_context
+        self.multipole_expansion_factory = multipole_expansion_factory
+        self.local_expansion_factory = local_expansion_factory
+        self.target_kernels = tuple(target_kernels)
+        self.exclude_self = exclude_self
+        self.extra = kwargs
+
+
+class _TimingFuture:
+    def __init__(self, events):
+        self.events = [e for e in events if e is not None]
+
+    def result(self):
+        return {}
+
+    def done(self):
+        return True
+
+    def __call__(self):
+        return 0.0
+
+
+class FPNDExpansionWrangler(ExpansionWranglerInterface):
+    """List-1 stage of the FPND wrangler on GB300.
+
+    ``near_field_table``: a table, a per-level list of tables, or a dict
+    ``{repr(kernel): table or list}`` (``expansion_wrangler_fpnd.py:2368-2404``).
+    """
+
+    def __init__(self, tree_indep, traversal, near_field_table, dtype=np.float64,
+                 fmm_level_to_order=None, quad_order=None, potential_kind=1,
+                 source_extra_kwargs=None, kernel_extra_kwargs=None,
+                 self_extra_kwargs=None, list1_extra_kwargs=None, queue=None,
+                 helmholtz_split=False, **kwargs):
+        if helmholtz_split:
+            raise NotImplementedError(
+                "the Helmholtz split correction (online P2P remainder) is not part of "
+                "the GB300 list-1 path; use Helmholtz tables (fixed or per-level)")
+        self.tree_indep = tree_indep
+        self.traversal = traversal
+        self.tree = traversal.tree
+        self.dtype = np.dtype(dtype)
+        self.queue = queue
+        self.potential_kind = potential_kind
+        self.quad_order = quad_order
+        self.source_extra_kwargs = source_extra_kwargs or {}
+        self.kernel_extra_kwargs = kernel_extra_kwargs or {}
+        self.self_extra_kwargs = self_extra_kwargs or {}
+        self.list1_extra_kwargs = dict(list1_extra_kwargs or {})
+        self.helmholtz_split = False
+
+        knames = [repr(k) for k in tree_indep.target_kernels]
+        if isinstance(near_field_table, dict):
+            tables = {}
+            for kn in knames:
+                if kn not in near_field_table:
+                    raise RuntimeError(f"missing near-field table for kernel {kn}")
+                v = near_field_table[kn]
+                tables[kn] = list(v) if isinstance(v, (list, tuple)) else [v]
+        else:
+            v = near_field_table
+            lst = list(v) if isinstance(v, (list, tuple)) else [v]
+            tables = {kn: lst for kn in knames}
+        self.near_field_table = tables
+        for kn, lst in tables.items():
+            self._check_table_levels(kn, lst)
+        self._payload_cache = collections.OrderedDict()
+        self._payload_cache_max = 16
+        self._layout_validated = set()
+
+    # {{{ table bookkeeping (expansion_wrangler_fpnd.py:2414-2472)
+
+    def _check_table_levels(self, kname, tables):
+        t0 = tables[0]
+        root = float(self.tree.root_extent)
+        for lev, t in enumerate(tables):
+            expected = float(t0.source_box_extent) * 0.5 ** lev
+            if not math.isclose(float(t.source_box_extent), expected, rel_tol=1e-12):
+                raise RuntimeError(
+                    f"near-field tables for {kname} must halve the source box extent per "
+                    f"level: level {lev} has {t.source_box_extent}, expected {expected}")
+        ratio = root / float(t0.source_box_extent)
+        if ratio <= 0:
+            raise RuntimeError("invalid table source_box_extent")
+
+    def table_starting_level(self, table0):
+        return int(np.round(np.log(float(self.tree.root_extent)
+                                   / float(table0.source_box_extent)) / np.log(2)))
+
+    # }}}
+
+    def eval_dtype(self, out_kernel):
+        cfg = self.dtype
+        if out_kernel.is_complex_valued:
+            return cfg if cfg.kind == "c" else (
+                np.dtype(np.complex64) if cfg == np.float32 else np.dtype(np.complex128))
+        return cfg if cfg.kind == "f" else (
+            np.dtype(np.float32) if cfg == np.complex64 else np.dtype(np.float64))
+
+    def get_payload(self, out_kernel, tables=None):
+        """Device-ready payload of ``out_kernel``'s tables (LRU of 16)."""
+        kname = repr(out_kernel)
+        tables = tables or self.near_field_table[kname]
+        eval_dtype = self.eval_dtype(out_kernel)
+        key = (kname, tuple(id(t) for t in tables),
+               tuple(int(np.asarray(t.data).ctypes.data) for t in tables),
+               tuple(int(np.asarray(t.data).size) for t in tables), eval_dtype.str)
+        hit = self._payload_cache.get(key)
+        if hit is not None:
+            self._payload_cache.move_to_end(key)
+            return hit
+        table0 = tables[0]
+        vals = sorted({int(c) for v in table0.interaction_case_vecs for c in v})
+        base, shift = vals[-1] - vals[0] + 1, -vals[0]
+        tdc, nm, ext, _, _, info = _prepare_table_data_and_entry_map(tables)
+        if eval_dtype.kind != "c" and np.iscomplexobj(tdc):
+            raise TypeError("complex table data for a real-valued output kernel")
+        tdc = tdc.astype(eval_dtype)
+        nm = nm.astype(eval_dtype)
+        ext = ext.astype(eval_dtype)
+        shapes = {
+            "n_tables": len(tables), "quad_order": table0.quad_order,
+            "n_q_points": table0.n_q_points, "n_cases": table0.n_cases,
+            "n_table_entries": tdc.shape[1], "reconstruction_kind": info["kind"],
+            "n_arithmetic_case_orbits": int(info["n_case_orbits"]),
+        }
+        payload = {
+            "base": base, "shift": shift, "case_indices": np.asarray(table0.case_indices),
+            "table_data": tdc, "mode_nmlz": nm, "exterior_mode_nmlz": ext,
+            "table_data_shapes": shapes, "reconstruction_info": info,
+            "table_root_extent": float(table0.source_box_extent),
+            "table_starting_level": self.table_starting_level(table0),
+            "reconstruction_diagnostics": {
+                "kind": info["kind"],
+                "online_value_bytes": int(tdc.nbytes),
+                "generated_reconstruction_metadata_bytes": int(info["metadata_bytes"]),
+                "normalizer_auxiliary_bytes": int(nm.nbytes + ext.nbytes),
+                "value_dense_block_equivalents": float(tdc.shape[1] / table0.n_pairs),
+            },
+        }
+        self._payload_cache[key] = payload
+        while len(self._payload_cache) > self._payload_cache_max:
+            self._payload_cache.popitem(last=False)
+        return payload
+
+    def _near_field_kwargs(self, payload, target_boxes, starts, lists, mode_coefs):
+        tree = self.tree
+        nq = payload["table_data_shapes"]["n_q_points"]
+        local = _compute_box_local_ids(tree, nq)
+        key = (id(target_boxes), id(lists), nq)
+        if key not in self._layout_validated:
+            _validate_table_box_particle_layout(tree, target_boxes, lists, nq)
+            self._layout_validated.add(key)
+        info = payload["reconstruction_info"]
+        counts = _np(tree.box_target_counts_nonchild).astype(np.int32)
+        return dict(
+            box_centers=tree.box_centers, box_levels=tree.box_levels,
+            box_source_counts_nonchild=counts, box_source_starts=tree.box_target_starts,
+            box_target_counts_nonchild=counts, box_target_starts=tree.box_target_starts,
+            case_indices=payload["case_indices"], encoding_base=payload["base"],
+            encoding_shift=payload["shift"], mode_nmlz_combined=payload["mode_nmlz"],
+            exterior_mode_nmlz_combined=payload["exterior_mode_nmlz"],
+            neighbor_source_boxes_starts=starts, root_extent=tree.root_extent,
+            neighbor_source_boxes_lists=lists, mode_coefs=mode_coefs,
+            source_mode_ids=local, table_data_combined=payload["table_data"],
+            target_boxes=target_boxes, target_point_ids=local,
+            table_root_extent=payload["table_root_extent"],
+            table_starting_level=payload["table_starting_level"],
+            arithmetic_case_orbit_ranks=info["case_orbit_ranks"],
+            arithmetic_case_axis_perm=info["case_axis_perm"],
+            arithmetic_case_axis_sign=info["case_axis_sign"],
+            arithmetic_case_axis_group=info["case_axis_group"],
+            arithmetic_case_value_offsets=info["case_value_offsets"],
+            arithmetic_axis_sign_power=info["axis_sign_power"],
+            arithmetic_axis_direction_signs=info["axis_direction_signs"],
+            arithmetic_direction_sign_axis=info["direction_sign_axis"])
+
+    def near_field_evaluator(self, out_kernel, payload, list1_extra_kwargs=None):
+        kw = dict(self.list1_extra_kwargs if list1_extra_kwargs is None
+                  else list1_extra_kwargs)
+        return NearFieldFromCSR(out_kernel, payload["table_data_shapes"],
+                                potential_kind=self.potential_kind, **kw)
+
+    def eval_direct_single_out_kernel(self, out_pot, out_kernel, target_boxes,
+                                      neighbor_source_boxes_starts,
+                                      neighbor_source_boxes_lists, mode_coefs,
+                                      near_field_tables=None, list1_extra_kwargs=None):
+        payload = self.get_payload(out_kernel, near_field_tables)
+        tables = near_field_tables or self.near_field_table[repr(out_kernel)]
+        if len(tables) > 1:
+            min_lev = int(np.min(_np(self.tree.box_levels)[_np(target_boxes).astype(np.int64)]))
+            largest = float(self.tree.root_extent) * 0.5 ** min_lev
+            if not float(tables[0].source_box_extent) >= largest - 1e-15:
+                raise RuntimeError(
+                    "Insufficient list of tables: the coarsest level mesh cells at level "
+                    f"{min_lev} are not covered.")
+        near_field = self.near_field_evaluator(out_kernel, payload, list1_extra_kwargs)
+        kw = self._near_field_kwargs(payload, target_boxes, neighbor_source_boxes_starts,
+                                     neighbor_source_boxes_lists, mode_coefs)
+        res, evt = near_field(self.queue, result=out_pot, **kw)
+        return res, evt
+
+    def output_zeros(self):
+        import torch
+        n = int(self.tree.ntargets)
+        out = []
+        for k in self.tree_indep.target_kernels:
+            dt = torch.complex128 if self.eval_dtype(k).kind == "c" else torch.float64
+            out.append(torch.zeros(n, dtype=dt, device="cuda"))
+        return out
+
+    def eval_direct(self, target_boxes, neighbor_source_boxes_starts,
+                    neighbor_source_boxes_lists, mode_coefs):
+        from .plan import as_device_tensor
+        pot = self.output_zeros()
+        coefs = as_device_tensor(mode_coefs)
+        events = []
+        for i, k in enumerate(self.tree_indep.target_kernels):
+            pot[i], evt = self.eval_direct_single_out_kernel(
+                pot[i], k, target_boxes, neighbor_source_boxes_starts,
+                neighbor_source_boxes_lists, coefs)
+            events.append(evt)
+        return pot, _TimingFuture(events)
+
+    def eval_direct_batched(self, target_boxes, neighbor_source_boxes_starts,
+                            neighbor_source_boxes_lists, mode_coefs, *, precision="fp64"):
+        """All right-hand sides at once: ``mode_coefs`` is ``[nrhs, N]``.
+
+        Returns one ``[nrhs, N]`` tensor per target kernel (per-RHS outputs).
+        ``precision`` is ``"fp64"`` (FP64 kernel) or ``"mixed"`` (tensor-core
+        contraction with exact split products, see ``batched.py``).
+        """
+        import torch
+
+        from .plan import as_device_tensor, stream_handle, tree_view_from_arrays
+        coefs = as_device_tensor(mode_coefs)
+        if coefs.dim() == 1:
+            coefs = coefs[None, :]
+        nrhs = int(coefs.shape[0])
+        outs, events = [], []
+        for k in self.tree_indep.target_kernels:
+            payload = self.get_payload(k)
+            nf = self.near_field_evaluator(k, payload)
+            kw = self._near_field_kwargs(payload, target_boxes, neighbor_source_boxes_starts,
+                                         neighbor_source_boxes_lists, None)
+            plan = nf.get_plan(
+                table_data_combined=kw["table_data_combined"],
+                mode_nmlz_combined=kw["mode_nmlz_combined"], case_indices=kw["case_indices"],
+                encoding_base=kw["encoding_base"], encoding_shift=kw["encoding_shift"],
+                table_root_extent=kw["table_root_extent"],
+                table_starting_level=kw["table_starting_level"],
+                **{n: kw[n] for n in kw if n.startswith("arithmetic_")})
+            nf._check_single_table_levels(kw["neighbor_source_boxes_lists"],
+                                          kw["box_levels"], kw["table_starting_level"])
+            view, keep = tree_view_from_arrays(**{n: kw[n] for n in (
+                "target_boxes", "neighbor_source_boxes_starts", "neighbor_source_boxes_lists",
+                "box_centers", "box_levels", "box_source_starts",
+                "box_source_counts_nonchild", "box_target_starts",
+                "box_target_counts_nonchild", "source_mode_ids", "target_point_ids",
+                "root_extent")})
+            c = coefs
+            if c.dtype not in (torch.float64, torch.complex128):
+                c = c.to(torch.complex128 if c.is_complex() else torch.float64)
+            c = c.contiguous()
+            out_complex = plan.complex_table or c.is_complex()
+            out = torch.empty((nrhs, int(view.n_particles)),
+                              dtype=torch.complex128 if out_complex else torch.float64,
+                              device="cuda")
+            stream = stream_handle(self.queue)
+            if precision == "fp64":
+                plan.eval_fp64(view, c, out, stream=stream, nrhs=nrhs)
+            else:
+                from .batched import eval_mixed
+                eval_mixed(plan, view, c, out, stream=stream, nrhs=nrhs, keep=keep)
+            evt = torch.cuda.Event()
+            evt.record()
+            plan.raise_on_status(stream)
+            outs.append(out)
+            events.append(evt)
+            del keep
+        return outs, _TimingFuture(events)
+
+    # {{{ reordering and bookkeeping of drive_volume_fmm
+
+    def reorder_sources(self, source_array):
+        from .plan import as_device_tensor
+        x = as_device_tensor(source_array)
+        idx = as_device_tensor(_np(self.tree.user_source_ids).astype(np.int64))
+        return x[..., idx]
+
+    def reorder_targets(self, target_array):
+        return self.reorder_sources(target_array)
+
+    def reorder_potentials(self, potentials):
+        from .plan import as_device_tensor
+        idx = as_device_tensor(_np(self.tree.sorted_target_ids).astype(np.int64))
+        return [p[..., idx] for p in potentials]
+
+    def finalize_potentials(self, potentials):
+        return potentials
+
+    def form_multipoles(self, level_start_source_box_nrs, source_boxes, src_weights):
+        # far field is outside the list-1 path; drive_volume_fmm(list1_only=True)
+        # discards it in the reference as well
+        return None, None
+
+    def coarsen_multipoles(self, level_start_source_parent_box_nrs, source_parent_boxes,
+                           mpoles):
+        return mpoles, None
+
+    # }}}
+
+
+FPNDSumpyExpansionWrangler = FPNDExpansionWrangler

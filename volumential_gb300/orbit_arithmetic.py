@@ -40,6 +40,8 @@ __all__ = [
     "canonical_case_vector",
     "compact_case_value_count",
     "rank_sorted_multiset",
+    "canonical_entry_axes",
+    "evaluate_arithmetic_orbit_entry",
     "evaluate_compact_arithmetic_entry",
     "build_arithmetic_case_metadata",
     "enumerate_scalar_arithmetic_representatives",
@@ -184,12 +186,11 @@ def rank_sorted_multiset(values, alphabet):
     return int(rank)
 
 
-def evaluate_compact_arithmetic_entry(case_id, source_mode_id, target_point_id,
-                                      metadata, q_order, dim):
-    """Compact row and sign of one full entry (scalar reference restatement).
-
-    ``metadata`` is the dict returned by :func:`build_arithmetic_case_metadata`.
-    """
+def canonical_entry_axes(case_id, source_mode_id, target_point_id, metadata,
+                         q_order, dim):
+    """Per-axis (source, target) node indices after reflection/folding and the
+    group sort, with the groups, axis signs and entry sign
+    (``volumential/orbit_arithmetic.py:372-432`` and the sort of ``:486-507``)."""
     q = int(q_order)
     perm = metadata["case_axis_perm"][case_id]
     signs = metadata["case_axis_sign"][case_id]
@@ -217,6 +218,40 @@ def evaluate_compact_arithmetic_entry(case_id, source_mode_id, target_point_id,
         src.append(s)
         tgt.append(t)
 
+    # compare-exchange network over axes of one group: (0,1) in 2D,
+    # (0,1), (1,2), (0,1), (0,2) in 3D
+    network = [(0, 1)] if dim == 2 else [(0, 1), (1, 2), (0, 1), (0, 2)]
+    for a, b in network:
+        if groups[a] == groups[b] and (src[b], tgt[b]) < (src[a], tgt[a]):
+            src[a], src[b] = src[b], src[a]
+            tgt[a], tgt[b] = tgt[b], tgt[a]
+    return src, tgt, groups, [int(x) for x in signs], entry_sign
+
+
+def evaluate_arithmetic_orbit_entry(case_id, source_mode_id, target_point_id,
+                                    metadata, q_order, dim):
+    """Uncompacted canonical entry id ``orbit * n_pairs + src * nq + tgt`` and
+    sign (``volumential/orbit_arithmetic.py:435-515``)."""
+    src, tgt, _, _, sign = canonical_entry_axes(
+        case_id, source_mode_id, target_point_id, metadata, q_order, dim)
+    nq = int(q_order) ** int(dim)
+    orbit = int(metadata["case_orbit_ranks"][case_id])
+    return (orbit * nq * nq + encode_mode_axes(src, q_order) * nq
+            + encode_mode_axes(tgt, q_order)), sign
+
+
+def evaluate_compact_arithmetic_entry(case_id, source_mode_id, target_point_id,
+                                      metadata, q_order, dim):
+    """Compact row and sign of one full entry (scalar reference restatement).
+
+    ``metadata`` is the dict returned by :func:`build_arithmetic_case_metadata`.
+    Each group of axes contributes the lexicographic rank of its sorted
+    multiset of pair codes ``src * q + tgt``; group ranks combine in mixed
+    radix; the case orbit's offset is added.
+    """
+    q = int(q_order)
+    src, tgt, groups, signs, entry_sign = canonical_entry_axes(
+        case_id, source_mode_id, target_point_id, metadata, q_order, dim)
     q2 = q * q
     compact = 0
     for g in range(max(groups) + 1):

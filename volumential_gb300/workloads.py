@@ -1,0 +1,213 @@
+"""Seeded synthetic workloads of the list-1 benchmark configurations.
+
+The reference measures nothing on a public dataset; its benchmark shapes are
+stated as configurations (uniform/adaptive quadtrees and octrees on
+``[-0.5, 0.5]^dim`` with tensor Gauss-Legendre nodes, densities that are sums
+of Gaussians ``a * exp(-|x - c|^2 / w^2)`` with seeded centres, log-uniform
+widths and N(0, 1) amplitudes).  This module builds them with
+``numpy.random.default_rng(seed)``.
+
+Table values: the list-1 evaluation is linear in the table, so parity and
+throughput do not depend on the values.  ``synthetic_tables`` fills the compact
+(orbit-reduced) layout with seeded values of the magnitude of a Laplace table;
+``kernel_tables`` uses the FP64 GPU table builder when one is available for
+the kernel.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .kernels import ConstantKernel, HelmholtzKernel, LaplaceKernel
+from .nearfield_potential_table import NearFieldInteractionTable
+from .tree_build import (
+    Traversal,
+    build_adaptive_tree,
+    build_list1_traversal,
+    build_uniform_tree,
+)
+
+__all__ = ["GaussianMixture", "random_gaussian_mixture", "synthetic_tables",
+           "Workload", "config_c1", "config_c2", "config_c3", "uniform_workload",
+           "adaptive_workload"]
+
+
+@dataclass
+class GaussianMixture:
+    centers: np.ndarray   # [n_terms, dim]
+    widths: np.ndarray    # [n_terms]
+    amps: np.ndarray      # [n_terms]
+
+    def __call__(self, points):
+        """Density at ``points`` ([dim, ...]); returns [...]."""
+        pts = np.asarray(points)
+        out = np.zeros(pts.shape[1:])
+        for c, w, a in zip(self.centers, self.widths, self.amps):
+            d2 = np.zeros(pts.shape[1:])
+            for ax in range(pts.shape[0]):
+                d2 += (pts[ax] - c[ax]) ** 2
+            out += a * np.exp(-d2 / (w * w))
+        return out
+
+
+def random_gaussian_mixture(rng, dim, n_terms, width_range, a=-0.5, b=0.5):
+    lo, hi = width_range
+    return GaussianMixture(
+        centers=rng.uniform(a, b, size=(n_terms, dim)),
+        widths=np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_terms)),
+        amps=rng.standard_normal(n_terms))
+
+
+def synthetic_tables(dim, q, kernel, *, n_tables=1, seed=0, source_box_extent=1.0,
+                     complex_values=False):
+    """Tables with the reference's compact layout filled with seeded values.
+
+    Level ``l`` has source box extent ``source_box_extent / 2**l``.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for lev in range(n_tables):
+        t = NearFieldInteractionTable(
+            q, dim=dim, sumpy_kernel=kernel,
+            source_box_extent=source_box_extent * 0.5 ** lev,
+            dtype=np.complex128 if complex_values else np.float64)
+        info = t._get_scalar_arithmetic_invariant_entry_info()
+        n = len(info["entry_ids"])
+        vals = rng.standard_normal(n) * 0.1
+        if complex_values:
+            vals = vals + 1j * rng.standard_normal(n) * 0.1
+        t.set_reduced_table_data(info["entry_ids"], vals)
+        if dim == 2:
+            t.build_normalizer_table()
+        out.append(t)
+    return out
+
+
+@dataclass
+class Workload:
+    name: str
+    dim: int
+    q: int
+    kernel: object
+    traversal: Traversal
+    tables: list
+    coefs: np.ndarray            # [nrhs, N] (float64 or complex128)
+    seed: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def tree(self):
+        return self.traversal.tree
+
+    @property
+    def n_points(self):
+        return self.tree.ntargets
+
+    @property
+    def nrhs(self):
+        return int(self.coefs.shape[0])
+
+    def pair_count(self):
+        """P = sum over list-1 box pairs of n_target * n_source points."""
+        tr = self.traversal
+        counts = self.tree.box_target_counts_nonchild.astype(np.int64)
+        nt = np.repeat(counts[tr.target_boxes], np.diff(tr.neighbor_source_boxes_starts))
+        ns = counts[tr.neighbor_source_boxes_lists]
+        return int(np.sum(nt * ns))
+
+
+def _densities(rng, tree, nrhs, n_terms, width_range):
+    cols = []
+    mixes = []
+    for _ in range(nrhs):
+        k = int(rng.integers(n_terms[0], n_terms[1] + 1)) if isinstance(n_terms, tuple) \
+            else int(n_terms)
+        mix = random_gaussian_mixture(rng, tree.dim, k, width_range)
+        mixes.append(mix)
+        cols.append(mix(tree.targets))
+    return np.stack(cols), mixes
+
+
+def uniform_workload(name, dim, level, q, *, kernel=None, nrhs=1, seed=0,
+                     n_terms=8, width_range=(0.02, 0.1), n_tables=1,
+                     complex_table=False):
+    rng = np.random.default_rng(seed)
+    tree = build_uniform_tree(dim, level, q)
+    trav = build_list1_traversal(tree)
+    kernel = kernel or LaplaceKernel(dim)
+    coefs, mixes = _densities(rng, tree, nrhs, n_terms, width_range)
+    tables = synthetic_tables(dim, q, kernel, n_tables=n_tables, seed=seed + 17,
+                              source_box_extent=tree.root_extent,
+                              complex_values=complex_table)
+    return Workload(name, dim, q, kernel, trav, tables, coefs, seed,
+                    meta={"level": level, "mixtures": mixes})
+
+
+def adaptive_workload(name, dim, q, *, tol, max_level, min_level=2, kernel=None,
+                      nrhs=1, seed=0, n_terms=16, width_range=(0.01, 0.08),
+                      max_leaves=None):
+    """Adaptive tree refined where the density's variation over a leaf's
+    nodes (max - min) exceeds ``tol``, then 2:1 balanced."""
+    rng = np.random.default_rng(seed)
+    mix = random_gaussian_mixture(rng, dim, n_terms, width_range)
+
+    def refine(nodes):
+        v = mix(nodes)
+        return (v.max(axis=-1) - v.min(axis=-1)) > tol
+
+    tree = build_adaptive_tree(dim, q, refine, max_level=max_level, min_level=min_level,
+                               max_leaves=max_leaves)
+    trav = build_list1_traversal(tree)
+    kernel = kernel or LaplaceKernel(dim)
+    cols = [mix(tree.targets)]
+    for _ in range(nrhs - 1):
+        m = random_gaussian_mixture(rng, dim, n_terms, width_range)
+        cols.append(m(tree.targets))
+    tables = synthetic_tables(dim, q, kernel, seed=seed + 17,
+                              source_box_extent=tree.root_extent)
+    return Workload(name, dim, q, kernel, trav, tables, np.stack(cols), seed,
+                    meta={"tol": tol, "max_level": max_level, "mixture": mix})
+
+
+def config_c1(seed=1000):
+    """2D Laplace, uniform level 5, q=4 (1024 leaves, 16,384 points), 1 RHS."""
+    return uniform_workload("c1_lap2d_uniform_l5_q4", 2, 5, 4, seed=seed, n_terms=8,
+                            width_range=(0.02, 0.1))
+
+
+def config_c2(seed=2006, tol=1e-3, max_level=6):
+    """3D Laplace, adaptive 2:1-balanced octree, q=4, 16 Gaussians (w in
+    [0.01, 0.08]), refined where the leaf variation (max - min of the density
+    at the leaf's 64 nodes) exceeds ``tol``, leaves on levels 3..6.  With the
+    default seed: 23,087 leaves, 1,477,568 points, 565,335 list-1 box pairs,
+    2.32e9 point pairs."""
+    return adaptive_workload("c2_lap3d_adaptive_q4", 3, 4, tol=tol, max_level=max_level,
+                             seed=seed, n_terms=16, width_range=(0.01, 0.08))
+
+
+def config_c3(seed=3000, nrhs=256, k=20.0):
+    """2D Helmholtz (k=20, fixed single complex table at level 6), uniform
+    level 6, q=5 (102,400 points), ``nrhs`` Gaussian-sum densities."""
+    w = uniform_workload("c3_helm2d_uniform_l6_q5", 2, 6, 5, seed=seed, nrhs=nrhs,
+                         n_terms=8, width_range=(0.02, 0.1),
+                         kernel=HelmholtzKernel(2), complex_table=True)
+    # fixed single table built at the active source level (root extent / 64)
+    t = synthetic_tables(2, 5, w.kernel, seed=seed + 17,
+                         source_box_extent=w.tree.root_extent / 64.0,
+                         complex_values=True)
+    w.tables = t
+    w.meta["k"] = k
+    return w
+
+
+def constant_workload(dim, q, level=1):
+    """Completeness case: constant kernel table, density 1 on [-1, 1]^dim."""
+    tree = build_uniform_tree(dim, level, q, a=-1.0, b=1.0)
+    trav = build_list1_traversal(tree)
+    t = NearFieldInteractionTable(q, dim=dim, sumpy_kernel=ConstantKernel(dim),
+                                  source_box_extent=1.0)
+    t.build_constant_table()
+    return Workload(f"constant{dim}d_q{q}", dim, q, LaplaceKernel(dim), trav, [t],
+                    np.ones((1, tree.ntargets)), 0)
