@@ -157,9 +157,24 @@ def algorithmic_bytes(w, nrhs=1, out_complex=False, coef_complex=False, table_by
             + w.tree.nboxes * (8 * w.dim + 1 + 4 + 4) + n_compact * table_bytes + 2048)
 
 
+def _timed_steps(torch, fn, flush, steps, stream):
+    """Run ``fn`` ``steps`` times, each bracketed by CUDA events on ``stream``
+    with an L2 flush before it (outside the events); returns per-step ms."""
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    for e0, e1 in evs:
+        flush.fill_(1.0)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+
 def gpu_arm(args):
     import torch
 
+    from volumential_gb300.batched import eval_mixed, get_schedule
     from volumential_gb300.expansion_wrangler_fpnd import (
         FPNDExpansionWrangler,
         FPNDTreeIndependentDataForWrangler,
@@ -202,59 +217,65 @@ def gpu_arm(args):
     coef_complex = np.iscomplexobj(coef_np)
     coefs = as_device_tensor(coef_np)
     out_complex = plan.complex_table or coef_complex
-    out = torch.empty(n, dtype=torch.complex128 if out_complex else torch.float64,
-                      device="cuda")
+    odt = torch.complex128 if out_complex else torch.float64
+    out_plain = torch.empty(n, dtype=odt, device="cuda")
+    out_mixed = torch.empty(n, dtype=odt, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
 
-    def step():
-        plan.eval_fp64(view, coefs, out, stream=sh, nrhs=1)
+    def plain_step():
+        plan.eval_fp64(view, coefs, out_plain, stream=sh, nrhs=1)
 
+    def mixed_step():
+        eval_mixed(plan, view, coefs, out_mixed, stream=sh, nrhs=1, keep=keep)
+
+    t_sched = time.perf_counter()
+    sched = get_schedule(plan, view, keep, 1, sh)
+    t_sched = time.perf_counter() - t_sched
     for _ in range(args.warmup):
         flush.fill_(1.0)
-        step()
+        plain_step()
+        mixed_step()
     plan.raise_on_status(sh)
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
     clocks.start()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for e0, e1 in evs:
-        flush.fill_(float(len(evs)))
-        e0.record(stream)
-        step()
-        e1.record(stream)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    res = {}
+    for name, fn in (("plain", plain_step), ("mixed", mixed_step)):
+        step_ms = _timed_steps(torch, fn, flush, args.steps, stream)
+        total = float(sum(step_ms))
+        if world > 1:
+            t = torch.tensor([total], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        res[name] = {"step_ms": step_ms, "total_ms": total}
     if world > 1:
         torch.distributed.barrier()
-    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
     clock_info = clocks.stop()
     plan.raise_on_status(sh)
+    yp = out_plain.cpu().numpy()
+    ym = out_mixed.cpu().numpy()
+    mixed_err = float(np.linalg.norm(ym - yp) / np.linalg.norm(yp))
+    headline = "mixed" if mixed_err <= 1e-9 else "plain"
 
     # e2e through the public API: pinned host density in, host potential out
     host_in = torch.from_numpy(coef_np).pin_memory()
-    host_out = torch.empty(n, dtype=out.dtype).pin_memory()
+    host_out = torch.empty(n, dtype=odt).pin_memory()
     dev_in = torch.empty_like(coefs)
-    dev_out = torch.empty_like(out)
+    dev_out = torch.empty(n, dtype=odt, device="cuda")
     api_kw = dict(kw)
     api_kw.pop("mode_coefs", None)
+    nf.extra_kwargs["list1_precision"] = "mixed" if headline == "mixed" else "fp64"
 
     def api_step():
         dev_in.copy_(host_in, non_blocking=True)
-        res, _ = nf(None, result=dev_out, mode_coefs=dev_in, **api_kw)
-        host_out.copy_(res, non_blocking=True)
+        r_, _ = nf(None, result=dev_out, mode_coefs=dev_in, **api_kw)
+        host_out.copy_(r_, non_blocking=True)
         torch.cuda.current_stream().synchronize()
 
     for _ in range(max(1, args.warmup)):
@@ -266,22 +287,25 @@ def gpu_arm(args):
         t1 = time.perf_counter()
         api_step()
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
+    e2e_total = float(sum(e2e_ms))
     if world > 1:
-        t = torch.tensor([sum(e2e_ms)], device="cuda", dtype=torch.float64)
+        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_total = float(t.item())
-    else:
-        e2e_total = float(sum(e2e_ms))
+    api_err = float(np.linalg.norm(host_out.numpy() - yp) / np.linalg.norm(yp))
 
-    result = {
-        "w": w, "step_ms": step_ms, "total_ms": total_ms, "wall_s": wall,
-        "clocks": clock_info, "e2e_total_ms": e2e_total, "e2e_ms": e2e_ms,
-        "out": host_out.numpy().copy(), "out_complex": out_complex,
+    return {
+        "w": w, "res": res, "clocks": clock_info, "e2e_total_ms": e2e_total,
+        "e2e_ms": e2e_ms, "out": yp, "out_complex": out_complex,
         "coef_complex": coef_complex, "h2d": int(host_in.numel() * host_in.element_size()),
-        "d2h": int(host_out.numel() * host_out.element_size()), "plan_bytes": plan.device_bytes(),
-        "world": world, "rank": rank,
+        "d2h": int(host_out.numel() * host_out.element_size()),
+        "plan_bytes": plan.device_bytes(), "world": world, "rank": rank,
+        "mixed_err": mixed_err, "api_err": api_err, "headline": headline,
+        "schedule": {"tiles": sched.n_tiles, "tile_keys": sched.n_tile_keys,
+                     "mean_keys_per_tile": sched.mean_keys_per_tile,
+                     "build_s": t_sched, "workspace_bytes": int(sched.workspace.numel())},
+        "geometry": plan.mixed_geometry(),
     }
-    return result
 
 
 def oracle_sample(w, fraction, nthreads=0, seed=0):
@@ -388,46 +412,70 @@ def gb300_main(args):
     w = r["w"]
     K = args.steps
     n = w.n_points
-    value = world * n * K / (r["total_ms"] / 1e3)
-    ms_per_step = r["total_ms"] / K
-    step_ms = np.asarray(r["step_ms"])
-    hbm, _, peak_kind = peaks()
+    hbm, bf16, peak_kind = peaks()
     B = algorithmic_bytes(w, out_complex=r["out_complex"], coef_complex=r["coef_complex"],
                           table_bytes=16 if w.tables[0].dtype == np.complex128 else 8)
     P = w.pair_count()
-    flops = (4 if (r["out_complex"]) else 2) * P
-    kernel_s = float(np.mean(step_ms)) / 1e3
-    achieved_gbs = B / kernel_s / 1e9
+    F = (4 if r["out_complex"] else 2) * P   # FP64-equivalent algorithmic flops
+
+    def path_summary(name):
+        step_ms = np.asarray(r["res"][name]["step_ms"])
+        t = float(np.mean(step_ms)) / 1e3
+        return {
+            "value": world * n * K / (r["res"][name]["total_ms"] / 1e3),
+            "ms_per_step": r["res"][name]["total_ms"] / K,
+            "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                           "p99": float(np.percentile(step_ms, 99))},
+            "hbm_gbs": B / t / 1e9, "hbm_frac": B / t / 1e9 / hbm,
+            "fp64eq_tflops": F / t / 1e12,
+        }
+
+    plain = path_summary("plain")
+    mixed = path_summary("mixed")
+    head = mixed if r["headline"] == "mixed" else plain
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(f"plain_fp64/{w.name}")
+            traffic = json.load(f).get(f"{r['headline']}/{w.name}")
+    kernel_s = head["ms_per_step"] / 1e3
+    # binding roof of the algorithmic work: max(bytes / HBM, flops / tensor peak)
+    t_hbm, t_tc = B / (hbm * 1e9), F / (bf16 * 1e12)
+    if r["headline"] == "mixed" and t_tc > t_hbm:
+        roof = {"bound": "tensor", "achieved": F / kernel_s / 1e12, "peak": bf16,
+                "unit": "TFLOP/s", "frac": F / kernel_s / 1e12 / bf16}
+    else:
+        roof = {"bound": "hbm", "achieved": B / kernel_s / 1e9, "peak": hbm,
+                "unit": "GB/s", "frac": B / kernel_s / 1e9 / hbm}
+    roof.update({"traffic": traffic, "peak_source": peak_kind, "algorithmic_bytes": int(B),
+                 "algorithmic_flops_fp64eq": int(F),
+                 "roof_time_us": 1e6 * max(t_hbm, t_tc)})
 
     line = {
-        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world,
-        "steps": K, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "metric": METRIC, "value": head["value"], "unit": "points/s", "n_gpus": world,
+        "steps": K, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
+        "dtype": "bf16-digits/fp32-exact/f64" if r["headline"] == "mixed" else "f64",
+        "data": "synthetic",
         "config": {"workload": w.name, "dim": w.dim, "q": w.q, "nrhs": 1,
                    "points": n, "leaves": int(len(w.traversal.target_boxes)),
                    "list1_box_pairs": w.traversal.nnz, "point_pairs": P,
-                   "path": "plain_fp64", "l2": "flushed between steps (256 MiB write)",
+                   "path": r["headline"], "l2": "flushed between steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "solves_per_s": 1e3 / ms_per_step,
-        "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
-                       "p99": float(np.percentile(step_ms, 99))},
+        "rel_l2_vs_fp64": r["mixed_err"] if r["headline"] == "mixed" else 0.0,
+        "solves_per_s": 1e3 / head["ms_per_step"],
+        "latency_ms": head["latency_ms"],
         "e2e": {"value": world * n * K / (r["e2e_total_ms"] / 1e3), "unit": "points/s",
                 "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
                 "latency_ms": {"p50": float(np.percentile(r["e2e_ms"], 50)),
-                               "p99": float(np.percentile(r["e2e_ms"], 99))}},
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm, "traffic": traffic,
-                     "peak_source": peak_kind, "algorithmic_bytes": int(B),
-                     "fp64_tflops": flops / kernel_s / 1e12,
-                     "note": "plain FP64 kernel: bound by the FP64 pipe, not HBM"},
+                               "p99": float(np.percentile(r["e2e_ms"], 99))},
+                "rel_l2_vs_fp64": r["api_err"], "api": "NearFieldFromCSR.__call__"},
+        "roofline": roof,
+        "paths": {"plain_fp64": plain, "mixed": dict(mixed, rel_l2_vs_fp64=r["mixed_err"]),
+                  "speedup_mixed_over_plain": plain["ms_per_step"] / mixed["ms_per_step"]},
+        "mixed_schedule": r["schedule"], "mixed_geometry": r["geometry"],
         "clocks": r["clocks"],
-        "gpu_launches": K,
+        "gpu_launches": K * (1 if r["headline"] == "plain" else (3 if w.dim == 3 else 5)),
         "plan_device_bytes": r["plan_bytes"],
     }
 
@@ -443,7 +491,7 @@ def gb300_main(args):
             "value": pts / dt, "unit": "points/s", "cores": nthreads, "kind": "port",
             "sample": f"{frac * 100:.2f}% of the target boxes (seeded), {pts} target points, "
                       f"{dt:.1f} s on {cpu_model()}"}
-        line["rel_l2_vs_oracle_sample"] = err
+        line["rel_l2_plain_vs_oracle_sample"] = err
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0

@@ -103,8 +103,24 @@ typedef struct {
   const int32_t *source_mode_ids;              /* [n_particles] */
   const int32_t *target_point_ids;             /* [n_particles] */
   int64_t n_particles;
+  int64_t nboxes;                              /* length of box_levels */
   double root_extent;
 } vl1_tree_view;
+
+/* Work schedule of the mixed-precision path for one tree and rhs count
+ * (built by the host from vl1_classify_pairs).  A tile is 128 rows, each row
+ * one (target box index j, rhs r) item encoded j * nrhs + r (-1 = empty row).
+ * Tile t covers keys key_ids[tile_key_start[t] .. tile_key_start[t+1]); a key is
+ * table_level * n_cases + case.  key_xrow[k * 128 + row] is the first digit
+ * row (source box S, rhs r): (S * 5) * nrhs + r, or -1 when the row's target
+ * box has no list-1 pair of that key.  DEVICE pointers, caller owned. */
+typedef struct {
+  int32_t n_tiles;
+  const int32_t *tile_rows;
+  const int32_t *tile_key_start;
+  const int32_t *key_ids;
+  const int32_t *key_xrow;
+} vl1_mixed_schedule;
 
 typedef struct {
   int32_t code;        /* first error code seen since the last reset */
@@ -136,6 +152,33 @@ int32_t vl1_plan_destroy(vl1_plan *plan);
 int32_t vl1_eval_fp64(vl1_plan *plan, const vl1_tree_view *tree,
                       const void *coefs, int32_t coef_type, int32_t nrhs,
                       void *result, void *stream);
+
+/* Table key (table_level * n_cases + case) of every list-1 pair, computed with
+ * the reference's FP64 case encoding (list1.py:439-459, 1084-1091) and table
+ * level rule (list1.py:361-437); keys: device array [nnz], -1 for pairs whose
+ * case code is outside the gallery (also reported in the status word). */
+int32_t vl1_classify_pairs(vl1_plan *plan, const vl1_tree_view *tree, int32_t *keys,
+                           void *stream);
+
+/* Bytes of caller-provided device workspace vl1_eval_mixed needs. */
+int64_t vl1_mixed_workspace_bytes(const vl1_plan *plan, const vl1_tree_view *tree,
+                                  int32_t nrhs);
+
+/* Operand geometry of the mixed path: out[0..4] = padded source points, K
+ * chunk, K chunks, padded output columns, output columns per CTA. */
+int32_t vl1_mixed_geometry(const vl1_plan *plan, int32_t *out5);
+
+/* Mixed-precision list-1 evaluation on the tensor cores: the same sum as
+ * vl1_eval_fp64 (list1.py:1050-1159) computed from exact BF16 digit products
+ * (5 signed 8-bit digits of a 40-bit fixed-point form of table and scaled
+ * densities) with FP32 exact partial sums, int32 diagonal accumulation and a
+ * final FP64 combination; relative error ~2^-40 of sum |table| |density|.
+ * coefs: real [nrhs][n_particles] float64; result as in vl1_eval_fp64.
+ * workspace: caller-provided device memory of vl1_mixed_workspace_bytes. */
+int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,
+                       const vl1_mixed_schedule *schedule, const double *coefs,
+                       int32_t nrhs, void *result, void *workspace,
+                       int64_t workspace_bytes, void *stream);
 
 /* Row and sign of every (table level 0, case, source mode, target point) as the
  * device computes them: rows/signs are device arrays [n_cases][nq][nq].

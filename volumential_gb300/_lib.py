@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _build
 
-__all__ = ["lib", "PlanDesc", "TreeView", "Status", "VL1Error", "check",
+__all__ = ["lib", "PlanDesc", "TreeView", "MixedSchedule", "Status", "VL1Error", "check",
            "STATUS_NAMES"]
 
 VL1_OK = 0
@@ -86,7 +86,14 @@ class TreeView(C.Structure):
         ("box_source_counts_nonchild", C.c_void_p), ("box_target_starts", C.c_void_p),
         ("box_target_counts_nonchild", C.c_void_p), ("source_mode_ids", C.c_void_p),
         ("target_point_ids", C.c_void_p), ("n_particles", C.c_int64),
-        ("root_extent", C.c_double),
+        ("nboxes", C.c_int64), ("root_extent", C.c_double),
+    ]
+
+
+class MixedSchedule(C.Structure):
+    _fields_ = [
+        ("n_tiles", C.c_int32), ("tile_rows", C.c_void_p), ("tile_key_start", C.c_void_p),
+        ("key_ids", C.c_void_p), ("key_xrow", C.c_void_p),
     ]
 
 
@@ -106,6 +113,13 @@ SIGNATURES = {
                                   C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "vl1_orbit_index_map": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p]),
+    "vl1_classify_pairs": (C.c_int32, [C.c_void_p, C.POINTER(TreeView), C.c_void_p,
+                                       C.c_void_p]),
+    "vl1_mixed_workspace_bytes": (C.c_int64, [C.c_void_p, C.POINTER(TreeView), C.c_int32]),
+    "vl1_mixed_geometry": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_eval_mixed": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
+                                   C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,
+                                   C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "vl1_status_read": (C.c_int32, [C.c_void_p, C.POINTER(Status), C.c_int32,
                                     C.c_void_p]),
     "vl1_plan_device_bytes": (C.c_int64, [C.c_void_p]),

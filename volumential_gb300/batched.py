@@ -1,0 +1,200 @@
+"""Mixed-precision (tensor-core) list-1 evaluation: host side.
+
+``eval_mixed`` runs ``vl1_eval_mixed`` (``include/vl1.h``): the list-1 sum of
+``volumential/list1.py:1050-1159`` computed from exact BF16 digit products on
+the tcgen05 tensor cores with FP64 final sums (relative error ~2^-40 of
+sum |table| |density|, see ``csrc/vl1_mixed.cu``).
+
+The device kernel walks a *schedule*: tiles of 128 rows, each row one
+(target box, right-hand side) item, and for each tile the list of table keys
+(table level, interaction case) its target boxes use.  The schedule depends
+only on the tree, the plan and the rhs count, so it is built once (from the
+per-pair keys that ``vl1_classify_pairs`` computes with the reference's FP64
+case encoding) and cached.  Target boxes are ordered by their key signature
+so that a tile's boxes share keys and little tensor-core work is spent on
+rows without a pair of the current key.
+"""
+
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import threading
+
+import numpy as np
+
+from . import _lib
+
+__all__ = ["MixedSchedule", "get_schedule", "eval_mixed", "DIGITS", "ROWS_PER_TILE"]
+
+DIGITS = 5
+ROWS_PER_TILE = 128
+
+_cache: "collections.OrderedDict" = collections.OrderedDict()
+_lock = threading.Lock()
+_CACHE_MAX = 8
+
+
+class MixedSchedule:
+    """Device-resident schedule (and workspace) of one (plan, tree, nrhs)."""
+
+    def __init__(self, plan, view, keep, nrhs, stream):
+        import torch
+
+        lib = _lib.lib()
+        self.nrhs = int(nrhs)
+        n_tb = int(view.n_target_boxes)
+        nnz = int(keep["lists"].numel())
+        n_keys_total = plan.n_tables * plan.n_cases
+        keys_dev = torch.empty(max(nnz, 1), dtype=torch.int32, device="cuda")
+        _lib.check(lib.vl1_classify_pairs(plan.handle, C.byref(view), keys_dev.data_ptr(),
+                                          C.c_void_p(stream)), "vl1_classify_pairs")
+        plan.raise_on_status(stream)
+        keys = keys_dev[:nnz].cpu().numpy().astype(np.int64)
+        starts = keep["starts"].cpu().numpy().astype(np.int64)
+        lists = keep["lists"].cpu().numpy().astype(np.int64)
+        self._check_modes(keep, plan.nq)
+
+        tb_of_pair = np.repeat(np.arange(n_tb, dtype=np.int64), np.diff(starts))
+        # target boxes ordered by key signature (bitmask of keys), then index
+        if n_tb:
+            mask = np.zeros((n_tb, n_keys_total), dtype=bool)
+            mask[tb_of_pair, keys] = True
+            packed = np.packbits(mask, axis=1)
+            _, sig = np.unique(packed, axis=0, return_inverse=True)
+            order = np.lexsort((np.arange(n_tb), sig.ravel()))
+        else:
+            order = np.zeros(0, dtype=np.int64)
+        rows = (order[:, None] * self.nrhs + np.arange(self.nrhs)[None, :]).ravel()
+        n_tiles = (len(rows) + ROWS_PER_TILE - 1) // ROWS_PER_TILE
+        tile_rows = np.full(n_tiles * ROWS_PER_TILE, -1, dtype=np.int64)
+        tile_rows[:len(rows)] = rows
+        tile_rows = tile_rows.reshape(n_tiles, ROWS_PER_TILE)
+
+        # (box, key) -> source box lookup
+        comb = tb_of_pair * n_keys_total + keys
+        srt = np.argsort(comb, kind="stable")
+        comb_sorted = comb[srt]
+        src_sorted = lists[srt]
+        if len(comb_sorted) > 1 and np.any(comb_sorted[1:] == comb_sorted[:-1]):
+            raise RuntimeError("a target box has two list-1 source boxes with the same case")
+
+        key_start = [0]
+        key_ids = []
+        key_xrow = []
+        for t in range(n_tiles):
+            tr_ = tile_rows[t]
+            valid = tr_ >= 0
+            js = np.where(valid, tr_ // self.nrhs, 0)
+            rs = np.where(valid, tr_ % self.nrhs, 0)
+            boxes = np.unique(js[valid])
+            pair_idx = np.concatenate([np.arange(starts[j], starts[j + 1]) for j in boxes]) \
+                if len(boxes) else np.zeros(0, dtype=np.int64)
+            tkeys = np.unique(keys[pair_idx])
+            for k in tkeys:
+                q = js * n_keys_total + k
+                pos = np.searchsorted(comb_sorted, q)
+                pos = np.minimum(pos, len(comb_sorted) - 1)
+                hit = valid & (comb_sorted[pos] == q)
+                s_box = src_sorted[pos]
+                xr = np.where(hit, (s_box * DIGITS) * self.nrhs + rs, -1)
+                key_xrow.append(xr)
+                key_ids.append(k)
+            key_start.append(len(key_ids))
+
+        self.n_tiles = n_tiles
+        self.n_tile_keys = len(key_ids)
+        self.mean_keys_per_tile = self.n_tile_keys / max(n_tiles, 1)
+        i32 = torch.int32
+        self.tile_rows = torch.from_numpy(tile_rows.ravel().astype(np.int32)).to("cuda")
+        self.tile_key_start = torch.from_numpy(np.asarray(key_start, dtype=np.int32)).to("cuda")
+        self.key_ids = torch.from_numpy(np.asarray(key_ids, dtype=np.int32)
+                                        if key_ids else np.zeros(1, np.int32)).to("cuda")
+        self.key_xrow = torch.from_numpy(
+            np.concatenate(key_xrow).astype(np.int32) if key_xrow
+            else np.zeros(ROWS_PER_TILE, np.int32)).to("cuda")
+        s = _lib.MixedSchedule()
+        s.n_tiles = n_tiles
+        s.tile_rows = self.tile_rows.data_ptr()
+        s.tile_key_start = self.tile_key_start.data_ptr()
+        s.key_ids = self.key_ids.data_ptr()
+        s.key_xrow = self.key_xrow.data_ptr()
+        self.c_struct = s
+        ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
+        if ws < 0:
+            raise RuntimeError("vl1_mixed_workspace_bytes failed")
+        self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
+        del i32
+
+    @staticmethod
+    def _check_modes(keep, nq):
+        """Source mode ids must be distinct inside a box (the mixed path places
+        every source point at its mode's column)."""
+        counts = keep["src_counts"].cpu().numpy().astype(np.int64)
+        starts = keep["src_starts"].cpu().numpy().astype(np.int64)
+        smode = keep["smode"].cpu().numpy()
+        boxes = np.flatnonzero(counts > 0)
+        if not len(boxes):
+            return
+        c = np.minimum(counts[boxes], nq)
+        full = c == nq
+        if np.any(full):
+            idx = starts[boxes[full]][:, None] + np.arange(nq)[None, :]
+            m = np.sort(smode[idx], axis=1)
+            if not np.array_equal(m, np.broadcast_to(np.arange(nq), m.shape)):
+                raise ValueError(
+                    "the mixed-precision path requires every box's source mode ids to be "
+                    f"a permutation of 0..{nq - 1}")
+        for b, cnt in zip(boxes[~full], c[~full]):
+            m = smode[starts[b]:starts[b] + cnt]
+            if len(np.unique(m)) != len(m):
+                raise ValueError("duplicate source mode ids inside a box")
+
+
+def _tree_token(keep):
+    return tuple((t.data_ptr(), t._version, tuple(t.shape)) for t in keep.values())
+
+
+def get_schedule(plan, view, keep, nrhs, stream):
+    key = (id(plan), _tree_token(keep), int(nrhs))
+    with _lock:
+        hit = _cache.get(key)
+        if hit is not None:
+            _cache.move_to_end(key)
+            return hit[0]
+    sched = MixedSchedule(plan, view, keep, nrhs, stream)
+    with _lock:
+        # keep the tree tensors alive with the schedule so the token stays unique
+        _cache[key] = (sched, dict(keep), plan)
+        while len(_cache) > _CACHE_MAX:
+            _cache.popitem(last=False)
+    return sched
+
+
+def eval_mixed(plan, view, coefs, out, *, stream, nrhs, keep):
+    """Tensor-core evaluation of ``nrhs`` right-hand sides into ``out``.
+
+    ``coefs``: CUDA float64 (or complex128) tensor with ``nrhs * N`` values;
+    ``out``: CUDA tensor of the plain path's output dtype and size.
+    """
+    import torch
+
+    n = int(view.n_particles)
+    if coefs.is_complex():
+        # y(re + i im) = y(re) + i y(im): two real evaluations in one launch
+        c2 = torch.cat([coefs.real.reshape(nrhs, n), coefs.imag.reshape(nrhs, n)]).contiguous()
+        tmp = torch.empty((2 * nrhs, n), dtype=torch.complex128 if plan.complex_table
+                          else torch.float64, device="cuda")
+        eval_mixed(plan, view, c2, tmp, stream=stream, nrhs=2 * nrhs, keep=keep)
+        res = tmp[:nrhs] + 1j * tmp[nrhs:]
+        out.view(nrhs, n).copy_(res)
+        return
+    if coefs.dtype != torch.float64 or not coefs.is_contiguous():
+        raise TypeError("mixed path coefficients must be a contiguous float64 tensor")
+    sched = get_schedule(plan, view, keep, nrhs, stream)
+    lib = _lib.lib()
+    st = lib.vl1_eval_mixed(plan.handle, C.byref(view), C.byref(sched.c_struct),
+                            coefs.data_ptr(), int(nrhs), out.data_ptr(),
+                            sched.workspace.data_ptr(), int(sched.workspace.numel()),
+                            C.c_void_p(stream))
+    _lib.check(st, "vl1_eval_mixed")

@@ -3,6 +3,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <cmath>
 #include <new>
 
 #include "vl1_internal.cuh"
@@ -201,6 +202,26 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
     }
   }
   if (!st) {
+    // tensor-core digit operands of the blocks
+    const MixedGeom g = mixed_geometry(d.nq, d.table_cplx);
+    const int64_t elems = (int64_t)d.n_tables * d.n_cases * g.n_kc * kDigits * (int64_t)g.np * g.kc;
+    void *ptr = nullptr;
+    st = plan_alloc(p, &ptr, 2 * (size_t)elems);
+    if (!st) {
+      p->mixed.adig = static_cast<__nv_bfloat16 *>(ptr);
+      double amax = 0.0;
+      const double *tv = static_cast<const double *>(desc->table_data);
+      const int64_t ntv = (int64_t)d.n_tables * d.n_entries * (d.table_cplx ? 2 : 1);
+      for (int64_t i = 0; i < ntv; ++i) amax = fmax(amax, fabs(tv[i]));
+      if (!(amax < 1e300)) {
+        set_error("table data contains non-finite values");
+        st = VL1_E_NONFINITE;
+      } else {
+        st = build_mixed_operands(p, amax, 0);
+      }
+    }
+  }
+  if (!st) {
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) st = cuda_fail(e, "plan block expansion");
   }
@@ -263,6 +284,7 @@ static int32_t make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &
   tr.smode = t->source_mode_ids;
   tr.tmode = t->target_point_ids;
   tr.n_particles = t->n_particles;
+  tr.nboxes = t->nboxes;
   tr.root_extent = t->root_extent;
   return VL1_OK;
 }
@@ -287,6 +309,62 @@ int32_t vl1_eval_fp64(vl1_plan *plan, const vl1_tree_view *tree, const void *coe
   }
   return launch_plain(plan, tr, static_cast<const double *>(coefs),
                       coef_type == VL1_COMPLEX128, nrhs, static_cast<double *>(result),
+                      static_cast<cudaStream_t>(stream));
+}
+
+int32_t vl1_classify_pairs(vl1_plan *plan, const vl1_tree_view *tree, int32_t *keys,
+                           void *stream) {
+  if (!plan || !keys) {
+    set_error("vl1_classify_pairs: null argument");
+    return VL1_E_ARG;
+  }
+  TreeDev tr;
+  int32_t st = make_tree(plan, tree, tr);
+  if (st) return st;
+  if (tr.n_tgt_boxes == 0) return VL1_OK;
+  return launch_classify(plan, tr, keys, static_cast<cudaStream_t>(stream));
+}
+
+int64_t vl1_mixed_workspace_bytes(const vl1_plan *plan, const vl1_tree_view *tree,
+                                  int32_t nrhs) {
+  if (!plan || !tree || nrhs < 1) return -1;
+  return mixed_workspace_bytes(plan, tree->nboxes, tree->n_target_boxes, nrhs);
+}
+
+int32_t vl1_mixed_geometry(const vl1_plan *plan, int32_t *out5) {
+  if (!plan || !out5) {
+    set_error("vl1_mixed_geometry: null argument");
+    return VL1_E_ARG;
+  }
+  const MixedGeom &g = plan->mixed.geom;
+  out5[0] = g.kp;
+  out5[1] = g.kc;
+  out5[2] = g.n_kc;
+  out5[3] = g.np;
+  out5[4] = g.nch;
+  return VL1_OK;
+}
+
+int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,
+                       const vl1_mixed_schedule *schedule, const double *coefs,
+                       int32_t nrhs, void *result, void *workspace,
+                       int64_t workspace_bytes, void *stream) {
+  if (!plan || !schedule || nrhs < 1) {
+    set_error("vl1_eval_mixed: null plan/schedule or nrhs < 1");
+    return VL1_E_ARG;
+  }
+  TreeDev tr;
+  int32_t st = make_tree(plan, tree, tr);
+  if (st) return st;
+  if (tr.n_tgt_boxes == 0) return VL1_OK;
+  if (!coefs || !result || tr.nboxes < 1 || schedule->n_tiles < 0 ||
+      (schedule->n_tiles > 0 && (!schedule->tile_rows || !schedule->tile_key_start ||
+                                 !schedule->key_ids || !schedule->key_xrow))) {
+    set_error("vl1_eval_mixed: invalid coefficients, result, nboxes or schedule");
+    return VL1_E_ARG;
+  }
+  return launch_mixed(plan, tr, tr.nboxes, *schedule, coefs, nrhs,
+                      static_cast<double *>(result), workspace, workspace_bytes,
                       static_cast<cudaStream_t>(stream));
 }
 

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "vl1.h"
+#include "vl1_mixed.cuh"
 
 namespace vl1 {
 
@@ -39,6 +40,7 @@ struct TreeDev {
   const int32_t *src_starts, *src_counts, *tgt_starts, *tgt_counts;
   const int32_t *smode, *tmode;
   int64_t n_particles;
+  int64_t nboxes;
   double root_extent;
 };
 
@@ -52,6 +54,7 @@ struct vl1_plan {
   void *allocs[16];
   int n_allocs;
   vl1_status *status;   // device
+  vl1::MixedPlan mixed;
 };
 
 namespace vl1 {
@@ -64,6 +67,14 @@ int32_t launch_expand_blocks(vl1_plan *plan, cudaStream_t s);
 int32_t launch_index_map(vl1_plan *plan, int32_t *rows, int8_t *signs, cudaStream_t s);
 int32_t launch_plain(vl1_plan *plan, const TreeDev &tree, const double *coefs,
                      int coef_cplx, int nrhs, double *result, cudaStream_t s);
+MixedGeom mixed_geometry(int nq, int table_cplx);
+int32_t build_mixed_operands(vl1_plan *plan, double table_absmax, cudaStream_t s);
+int64_t mixed_workspace_bytes(const vl1_plan *plan, int64_t nboxes, int64_t n_tgt_boxes,
+                              int nrhs);
+int32_t launch_classify(vl1_plan *plan, const TreeDev &tree, int32_t *keys, cudaStream_t s);
+int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
+                     const vl1_mixed_schedule &sched, const double *coefs, int nrhs,
+                     double *result, void *workspace, int64_t ws_bytes, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Device helpers

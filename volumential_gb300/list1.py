@@ -20,7 +20,10 @@ Differences from the reference that a caller can see:
   ``NotImplementedError``;
 * invalid cases (a case code outside the gallery) and layout violations are
   reported by the kernel through a status word and raised as exceptions,
-  where the reference would read out of bounds.
+  where the reference would read out of bounds;
+* ``list1_precision`` (an extra keyword, default ``"fp64"``) selects the plain
+  FP64 kernel or the tensor-core path (``"mixed"``: exact BF16 digit products,
+  FP64 sums, relative error ~2^-40 of sum |table| |density|).
 """
 
 from __future__ import annotations
@@ -589,7 +592,14 @@ class NearFieldFromCSR(NearFieldEvalBase):
                     f"{out.dtype}")
 
         stream = stream_handle(queue)
-        plan.eval_fp64(view, coefs, out, stream=stream, nrhs=1)
+        precision = self.extra_kwargs.get("list1_precision", "fp64")
+        if precision == "fp64":
+            plan.eval_fp64(view, coefs, out, stream=stream, nrhs=1)
+        elif precision == "mixed":
+            from .batched import eval_mixed
+            eval_mixed(plan, view, coefs, out, stream=stream, nrhs=1, keep=keep)
+        else:
+            raise ValueError(f"list1_precision must be 'fp64' or 'mixed', got {precision!r}")
         evt = torch.cuda.Event()
         evt.record(torch.cuda.current_stream() if queue is None else queue)
         del keep

@@ -103,6 +103,7 @@ def tree_view_from_arrays(*, target_boxes, neighbor_source_boxes_starts,
     v.source_mode_ids = keep["smode"].data_ptr()
     v.target_point_ids = keep["tmode"].data_ptr()
     v.n_particles = int(keep["tmode"].numel())
+    v.nboxes = int(keep["levels"].numel())
     v.root_extent = float(root_extent)
     validate_tree_arrays(keep, dim=int(keep["centers"].shape[0]))
     return v, keep
@@ -273,6 +274,11 @@ class Plan:
         st = self._lib.vl1_eval_fp64(self.handle, C.byref(view), coefs.data_ptr(), ctype,
                                      int(nrhs), out.data_ptr(), C.c_void_p(stream))
         _lib.check(st, "vl1_eval_fp64")
+
+    def mixed_geometry(self):
+        out = (C.c_int32 * 5)()
+        _lib.check(self._lib.vl1_mixed_geometry(self.handle, out), "vl1_mixed_geometry")
+        return dict(zip(("kp", "kc", "n_kc", "np", "nch"), list(out)))
 
     def read_status(self, stream=None, reset=True):
         s = _lib.Status()
