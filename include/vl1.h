@@ -180,6 +180,27 @@ int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,
                        int32_t nrhs, void *result, void *workspace,
                        int64_t workspace_bytes, void *stream);
 
+/* Size of the fixed scratch array used by vl1_eval_mixed_noalloc (32 MiB). */
+#define VL1_NOALLOC_SCRATCH_BYTES (32LL << 20)
+
+/* vl1_eval_mixed without caller-provided workspace, for callers that cannot
+ * allocate device memory (a host code that owns all device memory through its
+ * own pool and only hands over the arrays it computes on; a latency-critical
+ * loop where cudaMalloc's device synchronisation or failure is not an option).
+ * No counterpart in the reference: it has no device-side scratch to manage.
+ * Same inputs and outputs as vl1_eval_mixed; the scratch lives in a fixed
+ * VL1_NOALLOC_SCRATCH_BYTES array inside this library (held on every GPU that
+ * loads the library, until the process exits).  Problems needing more scratch
+ * than that (vl1_mixed_workspace_bytes) are rejected with VL1_E_ARG.  No
+ * cudaMalloc, cudaFree or other allocating call is made.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller.  The plan must belong to the current device. */
+int32_t vl1_eval_mixed_noalloc(vl1_plan *plan, const vl1_tree_view *tree,
+                               const vl1_mixed_schedule *schedule, const double *coefs,
+                               int32_t nrhs, void *result, void *stream);
+
 /* Row and sign of every (table level 0, case, source mode, target point) as the
  * device computes them: rows/signs are device arrays [n_cases][nq][nq].
  * Exposes the integer index of list1.py:604-854 for bit-exact checks. */

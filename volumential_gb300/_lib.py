@@ -30,6 +30,7 @@ VL1_E_CUDA = 8
 VL1_E_ARG = 9
 VL1_E_NOMEM = 10
 VL1_E_UNSUPPORTED = 11
+VL1_NOALLOC_SCRATCH_BYTES = 32 << 20
 
 STATUS_NAMES = {
     VL1_OK: "VL1_OK", VL1_E_INVALID_CASE: "VL1_E_INVALID_CASE",
@@ -120,6 +121,9 @@ SIGNATURES = {
     "vl1_eval_mixed": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
                                    C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,
                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "vl1_eval_mixed_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
+                                           C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,
+                                           C.c_void_p, C.c_void_p]),
     "vl1_status_read": (C.c_int32, [C.c_void_p, C.POINTER(Status), C.c_int32,
                                     C.c_void_p]),
     "vl1_plan_device_bytes": (C.c_int64, [C.c_void_p]),
