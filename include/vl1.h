@@ -111,9 +111,10 @@ typedef struct {
  * (built by the host from vl1_classify_pairs).  A tile is 128 rows, each row
  * one (target box index j, rhs r) item encoded j * nrhs + r (-1 = empty row).
  * Tile t covers keys key_ids[tile_key_start[t] .. tile_key_start[t+1]); a key is
- * table_level * n_cases + case.  key_xrow[k * 128 + row] is the first digit
- * row (source box S, rhs r): (S * 5) * nrhs + r, or -1 when the row's target
- * box has no list-1 pair of that key.  DEVICE pointers, caller owned. */
+ * table_level * n_cases + case.  key_xrow[k * 128 + row] is the density row
+ * (source box S, rhs r) encoded S * nrhs + r, or -1 when the row's target box
+ * has no list-1 pair of that key.  DEVICE pointers, caller owned; key_xrow
+ * 16-byte aligned. */
 typedef struct {
   int32_t n_tiles;
   const int32_t *tile_rows;

@@ -95,3 +95,8 @@ def test_mixed_matches_plain_fp64_on_config1(cuda):
                                       tr.neighbor_source_boxes_lists, w.coefs,
                                       precision="mixed")
     assert rel_l2(mixed[0].cpu().numpy(), plain[0].cpu().numpy()) <= TOL_MIXED
+
+
+def test_mixed_2d_q9_k_padded_to_rounds(cuda):
+    # 81 modes: K pads to 128 (two exact rounds of two 32-wide chunks)
+    _check(W.uniform_workload("m9", 2, 3, 9, seed=39), LAP2)

@@ -79,9 +79,8 @@ class MixedSchedule:
         if len(comb_sorted) > 1 and np.any(comb_sorted[1:] == comb_sorted[:-1]):
             raise RuntimeError("a target box has two list-1 source boxes with the same case")
 
-        key_start = [0]
-        key_ids = []
-        key_xrow = []
+        tile_key_ids = []
+        tile_key_xrow = []
         for t in range(n_tiles):
             tr_ = tile_rows[t]
             valid = tr_ >= 0
@@ -91,15 +90,28 @@ class MixedSchedule:
             pair_idx = np.concatenate([np.arange(starts[j], starts[j + 1]) for j in boxes]) \
                 if len(boxes) else np.zeros(0, dtype=np.int64)
             tkeys = np.unique(keys[pair_idx])
+            xrs = []
             for k in tkeys:
                 q = js * n_keys_total + k
                 pos = np.searchsorted(comb_sorted, q)
                 pos = np.minimum(pos, len(comb_sorted) - 1)
                 hit = valid & (comb_sorted[pos] == q)
                 s_box = src_sorted[pos]
-                xr = np.where(hit, (s_box * DIGITS) * self.nrhs + rs, -1)
-                key_xrow.append(xr)
-                key_ids.append(k)
+                xrs.append(np.where(hit, s_box * self.nrhs + rs, -1))
+            tile_key_ids.append(tkeys)
+            tile_key_xrow.append(xrs)
+
+        # longest tiles first: CTAs start in grid order, so the tiles with the
+        # most keys are not left for the last wave
+        lpt = np.argsort(-np.asarray([len(k) for k in tile_key_ids], dtype=np.int64),
+                         kind="stable")
+        tile_rows = tile_rows[lpt]
+        key_start = [0]
+        key_ids = []
+        key_xrow = []
+        for t in lpt:
+            key_ids.extend(int(k) for k in tile_key_ids[t])
+            key_xrow.extend(tile_key_xrow[t])
             key_start.append(len(key_ids))
 
         self.n_tiles = n_tiles

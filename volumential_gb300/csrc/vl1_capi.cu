@@ -363,6 +363,10 @@ int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,
     set_error("vl1_eval_mixed: invalid coefficients, result, nboxes or schedule");
     return VL1_E_ARG;
   }
+  if (reinterpret_cast<uintptr_t>(schedule->key_xrow) % 16 != 0) {
+    set_error("vl1_eval_mixed: schedule key_xrow must be 16-byte aligned");
+    return VL1_E_ARG;
+  }
   return launch_mixed(plan, tr, tr.nboxes, *schedule, coefs, nrhs,
                       static_cast<double *>(result), workspace, workspace_bytes,
                       static_cast<cudaStream_t>(stream));

@@ -31,7 +31,6 @@ namespace vl1 {
 
 namespace {
 
-constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
@@ -63,7 +62,7 @@ __device__ __forceinline__ int scale_exponent(double v) {
 
 __global__ void build_adig_kernel(DevDesc d, MixedGeom g, __nv_bfloat16 *adig, int a_exp) {
   // element (key, kchunk, digit, n, k) of [key][kchunk][digit][NP][KC]
-  // (core-matrix K-major order inside each [NP][KC] tile)
+  // (swizzled K-major order inside each [NP][KC] tile, as in shared memory)
   const int64_t per_tile = (int64_t)g.np * g.kc;
   const int64_t n_elems = (int64_t)d.n_tables * d.n_cases * g.n_kc * kDigits * per_tile;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n_elems;
@@ -90,7 +89,7 @@ __global__ void build_adig_kernel(DevDesc d, MixedGeom g, __nv_bfloat16 *adig, i
     int dig[kDigits];
     fixed_digits(v, a_exp, dig);
     const int64_t tile = ((int64_t)key * g.n_kc + kc) * kDigits + digit;
-    const uint32_t off = tc::kmajor_offset(n, k, g.kc);  // bytes
+    const uint32_t off = tc::kmajor_swizzled_offset(n, k, g.kc);  // bytes
     adig[tile * per_tile + off / 2] = __int2bfloat16_rn(dig[digit]);
   }
 }
@@ -134,26 +133,25 @@ __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const doubl
   }
 }
 
-// x digits: row ((b * kDigits + digit) * nrhs + r), KP bf16 per row, source
-// points placed at their mode id; plus one zero row at the end.
+// x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bf16 (kp * 5
+// values), so that the digits of one pipeline unit are kc-wide row pieces at
+// column (kchunk * 5 + digit) * kc; source points sit at their mode id.
 __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
                                 int nrhs, const int *x_exp, __nv_bfloat16 *xdig, int kp,
-                                int64_t zero_row, vl1_status *st) {
+                                int kc, vl1_status *st) {
   const int64_t n = (int64_t)nboxes * nrhs;
+  const int row_elems = kp * kDigits;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
+    __nv_bfloat16 *row = xdig + idx * row_elems;
+    for (int k = 0; k < row_elems; k += 8)
+      *reinterpret_cast<uint4 *>(row + k) = make_uint4(0u, 0u, 0u, 0u);
     int cnt = tr.src_counts[b];
     if (cnt <= 0) continue;
     if (cnt > d.nq) {
       report(st, VL1_E_LAYOUT, b, cnt);
       cnt = d.nq;
-    }
-    __nv_bfloat16 *rows[kDigits];
-#pragma unroll
-    for (int i = 0; i < kDigits; ++i) {
-      rows[i] = xdig + (((int64_t)b * kDigits + i) * nrhs + r) * kp;
-      for (int k = 0; k < kp; ++k) rows[i][k] = __int2bfloat16_rn(0);
     }
     const double sc = pair_scaling(d, level_extent(tr.root_extent, tr.levels[b]));
     const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
@@ -166,12 +164,11 @@ __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double 
       }
       int dig[kDigits];
       fixed_digits(sc * c[s], e, dig);
+      const int base = (m / kc) * kDigits * kc + (m % kc);
 #pragma unroll
-      for (int i = 0; i < kDigits; ++i) rows[i][m] = __int2bfloat16_rn(dig[i]);
+      for (int i = 0; i < kDigits; ++i) row[base + i * kc] = __int2bfloat16_rn(dig[i]);
     }
   }
-  if (blockIdx.x == 0)
-    for (int k = threadIdx.x; k < kp; k += blockDim.x) xdig[zero_row * kp + k] = __int2bfloat16_rn(0);
 }
 
 // 2D log displacement: w[b, r] = dispfac(b) * sum_s nmlz[lev(b), s] * coef
@@ -228,8 +225,8 @@ struct MixedParams {
   MixedGeom g;
   int nrhs;
   vl1_mixed_schedule sched;
-  const __nv_bfloat16 *xdig;
-  int64_t zero_row;
+  const __nv_bfloat16 *xdig;   // density digit rows [n_xrows][kp * 5]
+  int32_t n_xrows;
   const __nv_bfloat16 *adig;
   const int *x_exp;
   int a_exp;
@@ -241,34 +238,96 @@ struct MixedParams {
   vl1_status *st;
 };
 
-// digit pairs: 6 exact groups (one pair each) then 2 FP32 tail groups
-__constant__ int8_t c_exact_i[6] = {1, 1, 2, 1, 2, 3};
-__constant__ int8_t c_exact_j[6] = {1, 2, 1, 3, 2, 1};
+// Warp roles of mixed_kernel (warp index w):
+//   w <  4      producers: per pipeline unit, warp w gathers the density digit
+//               pieces of tile rows 32w .. 32w+31 with cp.async (consecutive
+//               lanes on consecutive 16-byte pieces of a row's 5 * kc digits,
+//               zero-filled for rows without a source box); each lane's
+//               copies arrive on full[stage] when they land.  Warp 0 also
+//               loads the five table digit tiles by bulk copies (TMA).
+//   w == 4      tensor-core issuer (one lane)
+//   w >= 5      readout: TMEM lane quadrant w % 4, RC columns each
+// Pipeline unit = (key, K chunk of kc <= 32 source points); a "round" = the
+// units of one key that share an exact accumulation (K <= 64).  Exact
+// diagonal accumulators (i+j = 2, 3, 4) are double-buffered in TMEM (one
+// buffer per round parity) so the readout of round r overlaps the products of
+// round r+1; the tail diagonals (i+j = 5, 6) accumulate over the whole tile.
+// The table digit planes j = 1..5 of a stage are stacked along N, so one MMA
+// multiplies density digit i by several table digits j at once; its output
+// column blocks land on consecutive diagonals i + j.
+constexpr int kStages = 3;
+constexpr uint32_t kExactCols = 3;   // accumulators per buffer
+constexpr int kProducerWarps = 4;
+constexpr int kMmaWarp = 4;
+constexpr int kReadWarp0 = 5;
+constexpr uint32_t kSleepNs = 200000;      // longest sleep of one wait poll
+constexpr uint32_t kSleepPolls = 10000;    // polls before a wait gives up (~2 s)
 
-template <int NCH>
-__global__ void __launch_bounds__(NCH >= 64 ? 256 : 128)
+struct Barriers {
+  uint64_t full[kStages];
+  uint64_t empty[kStages];
+  uint64_t accf[2];
+  uint64_t acce[2];
+};
+
+__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t phase,
+                                              volatile int *abort_flag) {
+  for (uint32_t i = 0; i < kSleepPolls; ++i) {
+    if (tc::mbar_try_wait_sleep(bar, phase, kSleepNs)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_addr(bar)) : "memory");
+}
+
+// One group of MMAs: density digit i times the stacked table digits
+// j0 .. j0 + nb - 1, into nb consecutive diagonal blocks.
+struct MmaGroup {
+  int i, j0, nb, exact;  // exact: into the round buffer (else the tail blocks)
+};
+// exact diagonals 2..4: (1; 1..3), (2; 1..2), (3; 1); tails 5..6:
+// (1; 4..5), (2; 3..4), (3; 2..3), (4; 1..2), (5; 1)
+__device__ constexpr MmaGroup kGroups[8] = {{1, 1, 3, 1}, {2, 1, 2, 1}, {3, 1, 1, 1},
+                                            {1, 4, 2, 0}, {2, 3, 2, 0}, {3, 2, 2, 0},
+                                            {4, 1, 2, 0}, {5, 1, 1, 0}};
+
+template <int NCH, int KC>
+__global__ void __launch_bounds__(32 * (kReadWarp0 + 4 * (NCH / 16)), 1)
 mixed_kernel(const __grid_constant__ MixedParams p) {
-  constexpr int NGROUPS = 8;
-  // groups at NCH-column strides; a 32-column read of the last group must fit
-  constexpr uint32_t TCOLS = NCH * (NGROUPS - 1) + (NCH > 32 ? NCH : 32) <= 256 ? 256 : 512;
-  extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t bar_load, bar_mma;
+  constexpr int RC = 16;                            // columns per readout warp
+  constexpr int NREAD = 4 * (NCH / RC);             // readout warps
+  // TMEM: [buffer 0: 3 x NCH][tail d5][tail d6][buffer 1: 3 x NCH]
+  constexpr uint32_t COLS = NCH * 8 > 256 ? 512 : (NCH * 8 > 128 ? 256 : 128);
+  constexpr uint32_t XBYTES = 128u * KC * 2u;      // one digit plane of the rows
+  constexpr uint32_t ABYTES = (uint32_t)NCH * KC * 2u;   // one digit plane of the table
+  constexpr uint32_t STAGE_BYTES = kDigits * (XBYTES + ABYTES);
+  constexpr uint32_t ROW_BYTES = KC * 2u;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // swizzle atoms need a 1024-byte aligned base (the launch adds 1 KiB slack)
+  uint8_t *smem = reinterpret_cast<uint8_t *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  __shared__ Barriers bars;
   __shared__ uint32_t tmem_base;
-  __shared__ int s_abort;
+  __shared__ volatile int s_abort;
   __shared__ int s_rows[128];
-
-  const int KC = p.g.kc;
-  const uint32_t xbytes = 128u * KC * 2u;    // one digit of the row operand
-  const uint32_t abytes = (uint32_t)NCH * KC * 2u;
-  uint8_t *xs = smem;
-  uint8_t *as = smem + kDigits * xbytes;
+  __shared__ int s_xrow[kStages][128];
 
   const int tile = blockIdx.x;
   const int chunk = blockIdx.y;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
-  const int row = ((warp & 3) << 5) | (tid & 31);   // TMEM lane of this thread
-  const int wg = tid >> 7;                           // column slice
+  const int lane = tid & 31;
+
+  const int k0 = p.sched.tile_key_start[tile], k1 = p.sched.tile_key_start[tile + 1];
+  const int n_keys = k1 - k0;
+  const int upr = (p.g.kp < 64 ? p.g.kp : 64) / KC;   // units per round
+  const int rpk = (p.g.kp + 63) / 64;                  // rounds per key
+  const int n_rounds = n_keys * rpk;
+  const int n_units = n_rounds * upr;
 
   if (tid < 128) {
     int v = p.sched.tile_rows[(int64_t)tile * 128 + tid];
@@ -279,185 +338,257 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
     s_rows[tid] = v;
   }
   if (tid == 0) {
-    tc::mbar_init(&bar_load, 1);
-    tc::mbar_init(&bar_mma, 1);
+    for (int s = 0; s < kStages; ++s) {
+      // 128 producer lanes (cp.async arrivals) + the table copies' expect_tx
+      tc::mbar_init(&bars.full[s], 32 * kProducerWarps + 1);
+      tc::mbar_init(&bars.empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&bars.accf[b], 1);
+      tc::mbar_init(&bars.acce[b], NREAD);
+    }
     tc::fence_mbar_init();
     s_abort = 0;
   }
-  if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, TCOLS);
+  if (warp == kMmaWarp) {
+    tc::tmem_alloc(&tmem_base, COLS);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tbase = tmem_base;
-  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
 
-  int acc[3][32];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int c = 0; c < 32; ++c) acc[a][c] = 0;
-
-  const int k0 = p.sched.tile_key_start[tile], k1 = p.sched.tile_key_start[tile + 1];
-  const uint32_t idesc = tc::idesc_bf16_f32(128, NCH);
-  const uint32_t sbo = (uint32_t)KC * 16u;
-  const int nchunk16 = KC / 8;
-  uint32_t phase = 0;
-  bool first_unit = true;
-
-  for (int kidx = k0; kidx < k1; ++kidx) {
-    const int key = p.sched.key_ids[kidx];
-    if (key < 0 || key >= p.d.n_tables * p.d.n_cases) {
-      if (tid == 0) report(p.st, VL1_E_ARG, tile, kidx);
-      continue;
+  if (warp < kProducerWarps) {
+    // ------------------------------------------------------------ producers
+    constexpr int NC16 = KC / 8;               // 16-byte pieces per digit row
+    constexpr int PPR = kDigits * NC16;        // pieces per row and unit
+    const int64_t row_elems = (int64_t)p.g.kp * kDigits;
+    for (int u = 0; u < n_units; ++u) {
+      const int s = u % kStages;
+      const int use = u / kStages;
+      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) break;
+      uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
+      uint8_t *as = xs + kDigits * XBYTES;
+      const int round = u / upr;
+      const int kidx = k0 + round / rpk;
+      const int kc = (round % rpk) * upr + u % upr;   // K chunk index within the key
+      int key = p.sched.key_ids[kidx];
+      const bool key_ok = key >= 0 && key < p.d.n_tables * p.d.n_cases;
+      if (!key_ok) {
+        if (warp == 0 && lane == 0) report(p.st, VL1_E_ARG, tile, kidx);
+        key = 0;
+      }
+      if (warp == 0) {
+        if (lane == 0) tc::mbar_arrive_expect_tx(&bars.full[s], kDigits * ABYTES);
+        __syncwarp();
+        if (lane < kDigits) {
+          const int64_t base =
+              (((int64_t)key * p.g.n_kc + kc) * kDigits + lane) * p.g.np * KC +
+              (int64_t)chunk * NCH * KC;
+          tc::bulk_g2s(as + lane * ABYTES, p.adig + base, ABYTES, &bars.full[s]);
+        }
+      }
+      // source rows of this warp's 32 tile rows (-1: no source box)
+      int *xr_s = s_xrow[s];
+      {
+        const int r = 32 * warp + lane;
+        int xr = key_ok ? p.sched.key_xrow[(int64_t)kidx * 128 + r] : -1;
+        if (xr >= p.n_xrows) {
+          report(p.st, VL1_E_ARG, tile, r);
+          xr = -1;
+        }
+        xr_s[r] = xr;
+      }
+      __syncwarp();
+      // piece pc = it * 32 + lane of the warp's 32 * PPR pieces: row pc / PPR,
+      // piece q = pc % PPR = digit * NC16 + 16-byte column
+      int rl = lane / PPR, q = lane % PPR;
+      const int64_t col0 = (int64_t)kc * kDigits * KC;
+#pragma unroll 4
+      for (int it = 0; it < PPR; ++it) {
+        const int r = 32 * warp + rl;
+        const int xr = xr_s[r];
+        const int dg = q / NC16, c = q - dg * NC16;
+        uint8_t *dst = xs + dg * XBYTES + tc::kmajor_swizzled_offset(r, c * 8, KC);
+        const bool have = xr >= 0;
+        const __nv_bfloat16 *src = p.xdig + (have ? (int64_t)xr * row_elems + col0 + q * 8 : 0);
+        tc::cp_async16_zfill(dst, src, have ? 16u : 0u);
+        q += 32 % PPR;
+        rl += 32 / PPR;
+        if (q >= PPR) {
+          q -= PPR;
+          ++rl;
+        }
+      }
+      tc::cp_async_arrive_noinc(&bars.full[s]);
+      __syncwarp();   // xr_s of this stage is rewritten only after the stage is released
     }
-    for (int kc = 0; kc < p.g.n_kc; ++kc) {
-      // ---- stage operands: A digits by bulk copy, X digit rows by cp.async
-      if (tid == 0) {
-        tc::mbar_arrive_expect_tx(&bar_load, kDigits * abytes);
-        const int64_t base = (((int64_t)key * p.g.n_kc + kc) * kDigits) * p.g.np * KC +
-                             (int64_t)chunk * NCH * KC;
-        for (int dg = 0; dg < kDigits; ++dg)
-          tc::bulk_g2s(as + dg * abytes, p.adig + base + (int64_t)dg * p.g.np * KC, abytes,
-                       &bar_load);
-      }
-      const int n_items = 128 * kDigits * nchunk16;
-      for (int it = tid; it < n_items; it += blockDim.x) {
-        const int c16 = it % nchunk16;
-        const int rd = it / nchunk16;
-        const int r = rd & 127;
-        const int dg = rd >> 7;
-        const int xr = p.sched.key_xrow[(int64_t)kidx * 128 + r];
-        const bool valid = xr >= 0 && (int64_t)xr + (int64_t)(kDigits - 1) * p.nrhs < p.zero_row;
-        if (xr >= 0 && !valid && dg == 0 && c16 == 0) report(p.st, VL1_E_ARG, tile, r);
-        const int64_t src_row = valid ? (int64_t)xr + (int64_t)dg * p.nrhs : p.zero_row;
-        tc::cp_async16(xs + dg * xbytes + tc::kmajor_offset(r, c16 * 8, KC),
-                       p.xdig + src_row * p.g.kp + kc * KC + c16 * 8);
-      }
-      tc::cp_async_commit();
-      tc::cp_async_wait_all();
-      if (!tc::mbar_wait_bounded(&bar_load, phase, kWaitLimit)) s_abort = 1;
-      tc::fence_proxy_async_smem();
-      tc::tc_fence_before();
-      __syncthreads();
-      tc::tc_fence_after();
-      if (s_abort) break;
-
-      // ---- tensor-core products
-      if (tid == 0) {
-        const uint32_t xa = tc::smem_addr(xs), aa = tc::smem_addr(as);
-        for (int g = 0; g < NGROUPS; ++g) {
-          const uint32_t dcol = tbase + (uint32_t)(g * NCH);
-          bool first = true;
-          // exact groups: one pair; tails: pairs with i + j = 5 (g = 6), 6 (g = 7)
-          const int diag = g < 6 ? 0 : g - 1;
-          const int np_ = g < 6 ? 1 : diag - 1;
-          for (int q = 0; q < np_; ++q) {
-            const int i = g < 6 ? c_exact_i[g] : q + 1;
-            const int j = g < 6 ? c_exact_j[g] : diag - q - 1;
-            for (int kk = 0; kk < KC / 16; ++kk) {
-              const uint64_t ad = tc::smem_desc_kmajor_noswizzle(
-                  xa + (uint32_t)(i - 1) * xbytes + kk * 256u, 128u, sbo);
-              const uint64_t bd = tc::smem_desc_kmajor_noswizzle(
-                  aa + (uint32_t)(j - 1) * abytes + kk * 256u, 128u, sbo);
-              const uint32_t accumulate = g < 6 ? !first : !(first && first_unit);
-              tc::mma_bf16(dcol, ad, bd, idesc, accumulate);
-              first = false;
+  } else if (warp == kMmaWarp) {
+    // ------------------------------------------------------- tensor cores
+    if (lane == 0) {
+      const uint32_t tail_col = tbase + kExactCols * NCH;
+      int u = 0;
+      bool aborted = false;
+      for (int round = 0; round < n_rounds && !aborted; ++round) {
+        const int b = round & 1;
+        if (round >= 2 && !wait_or_abort(&bars.acce[b], ((round >> 1) - 1) & 1, &s_abort)) {
+          aborted = true;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t exact_col = tbase + (uint32_t)b * 5 * NCH;
+        for (int iu = 0; iu < upr; ++iu, ++u) {
+          const int s = u % kStages;
+          if (!wait_or_abort(&bars.full[s], (u / kStages) & 1, &s_abort)) {
+            aborted = true;
+            break;
+          }
+          // the digit rows were written by cp.async (generic proxy): order
+          // them before the tensor cores' (async proxy) reads
+          tc::fence_proxy_async_smem();
+          tc::tc_fence_after();
+          const uint32_t xa = tc::smem_addr(smem + (size_t)s * STAGE_BYTES);
+          // descriptors advance by (byte offset >> 4) in their address field
+          const uint64_t xd = tc::smem_desc_kmajor_swizzled(xa, ROW_BYTES);
+          const uint64_t adsc = tc::smem_desc_kmajor_swizzled(xa + kDigits * XBYTES, ROW_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < KC / 16; ++kk) {
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+              const MmaGroup gr = kGroups[g];
+              const uint32_t col = gr.exact ? exact_col + (uint32_t)(gr.i + gr.j0 - 2) * NCH
+                                            : tail_col + (uint32_t)(gr.i + gr.j0 - 5) * NCH;
+              const bool first = gr.exact ? (g == 0 && iu == 0 && kk == 0)
+                                          : (g == 3 && u == 0 && kk == 0);
+              const uint64_t ad = xd + (((uint32_t)(gr.i - 1) * XBYTES + kk * 32u) >> 4);
+              const uint64_t bd = adsc + (((uint32_t)(gr.j0 - 1) * ABYTES + kk * 32u) >> 4);
+              tc::mma_bf16(col, ad, bd, tc::idesc_bf16_f32(128, NCH * gr.nb), first ? 0u : 1u);
             }
           }
+          tc::mma_commit(&bars.empty[s]);   // stage free once these products finish
         }
-        tc::mma_commit(&bar_mma);
+        if (!aborted) tc::mma_commit(&bars.accf[b]);
       }
-      if (!tc::mbar_wait_bounded(&bar_mma, phase, kWaitLimit)) s_abort = 1;
-      tc::tc_fence_after();
-      __syncthreads();
-      if (s_abort) break;
-
-      // ---- exact groups: integer accumulation
-#pragma unroll
-      for (int g = 0; g < 6; ++g) {
-        uint32_t r32[32];
-        tc::tmem_ld32(tbase + lane_off + (uint32_t)(g * NCH + wg * 32), r32);
-        tc::tmem_ld_wait();
-        const int a = g == 0 ? 0 : (g <= 2 ? 1 : 2);   // i + j - 2 of the pair
-#pragma unroll
-        for (int c = 0; c < 32; ++c)
-          acc[a][c] += __float_as_int(__uint_as_float(r32[c]) + kMagic) - kMagicBits;
-      }
-      tc::tc_fence_before();
-      __syncthreads();
-      tc::tc_fence_after();
-      phase ^= 1u;
-      first_unit = false;
     }
-    if (s_abort) break;
-  }
-
-  if (!s_abort) {
-    // ---- FP32 tails (weights 2^-40 and 2^-48 of the scale); a tile without
-    // keys has only zero (plus displacement) outputs
-    float tail[32];
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ readout
+    const int rw = warp - kReadWarp0;      // 0 .. NREAD-1
+    const int quad = warp & 3;             // TMEM lanes 32*quad .. +31
+    const int cb = rw >> 2;                // RC-column block
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    const int row = quad * 32 + lane;
+    // exact sum of the diagonals per output, units of 2^(e-32)
+    long long acc[RC];
 #pragma unroll
-    for (int c = 0; c < 32; ++c) tail[c] = 0.0f;
-#pragma unroll
-    for (int g = 6; g < 8; ++g) {
-      if (k1 == k0) break;
-      uint32_t r32[32];
-      tc::tmem_ld32(tbase + lane_off + (uint32_t)(g * NCH + wg * 32), r32);
+    for (int c = 0; c < RC; ++c) acc[c] = 0;
+    bool ok = true;
+    for (int round = 0; round < n_rounds; ++round) {
+      const int b = round & 1;
+      if (!wait_or_abort(&bars.accf[b], (round >> 1) & 1, &s_abort)) {
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t col = tbase + lane_off + (uint32_t)b * 5 * NCH + cb * RC;
+      uint32_t r16[16];
+      int dsum[16];
+      tc::tmem_ld16(col, r16);               // i + j = 2: |x| < 2^22
       tc::tmem_ld_wait();
-      const float wgt = g == 6 ? 1.0f : 1.0f / 256.0f;
 #pragma unroll
-      for (int c = 0; c < 32; ++c) tail[c] += __uint_as_float(r32[c]) * wgt;
+      for (int c = 0; c < 16; ++c)
+        dsum[c] = __float_as_int(__uint_as_float(r16[c]) + kMagic) - kMagicBits;
+      tc::tmem_ld16(col + NCH, r16);         // i + j = 3: |x| < 2^23
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        acc[c] += ((long long)dsum[c] << 16) + ((long long)__float2int_rn(__uint_as_float(r16[c])) << 8);
+      tc::tmem_ld16(col + 2 * NCH, r16);     // i + j = 4: |x| < 2^24
+      tc::tmem_ld_wait();
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars.acce[b]);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[c] += (long long)__float2int_rn(__uint_as_float(r16[c]));
     }
-    const int v = s_rows[row];
-    if (v >= 0) {
-      const int j = v / p.nrhs, r = v % p.nrhs;
-      const int tbox = p.target_boxes[j];
-      const int tbeg = p.tgt_starts[tbox];
-      const int ntgt = min(p.tgt_counts[tbox], p.d.nq);
-      const int e = p.a_exp + p.x_exp[r];
-      const double w2 = ldexp(1.0, e - 16), w3 = ldexp(1.0, e - 24),
-                   w4 = ldexp(1.0, e - 32), w5 = ldexp(1.0, e - 40);
-      const bool oc = p.d.table_cplx;
-      double disp_re = 0.0, disp_im = 0.0;
-      if (p.disp) {
-        const int64_t di = (int64_t)j * p.nrhs + r;
-        disp_re = oc ? p.disp[2 * di] : p.disp[di];
-        disp_im = oc ? p.disp[2 * di + 1] : 0.0;
+    // ---- park the exact sums (one int64 per output, units of 2^(e-32)) and
+    // the FP32 tails (units of 2^(e-40)) in the idle pipeline buffers
+    if (ok && !s_abort) {
+      long long *s_comb = reinterpret_cast<long long *>(smem);
+      float *s_tail = reinterpret_cast<float *>(s_comb + 128 * NCH);
+      const uint32_t col = tbase + lane_off + kExactCols * NCH + cb * RC;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) s_comb[row * NCH + cb * RC + c] = acc[c];
+      uint32_t r16[16];
+      float tl[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) tl[c] = 0.0f;
+      if (n_rounds > 0) {
+        tc::tmem_ld16(col, r16);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) tl[c] = __uint_as_float(r16[c]);
+        tc::tmem_ld16(col + NCH, r16);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) tl[c] += __uint_as_float(r16[c]) * (1.0f / 256.0f);
       }
 #pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const int n = chunk * NCH + wg * 32 + c;
-        if (wg * 32 + c >= NCH) break;
-        int t = n, part = 0;
-        if (oc && n >= p.d.nq) {
-          t = n - p.d.nq;
-          part = 1;
-        }
-        if (t >= ntgt || n >= (oc ? 2 * p.d.nq : p.d.nq)) continue;
-        double y = (double)acc[0][c] * w2 + (double)acc[1][c] * w3 +
-                   (double)acc[2][c] * w4 + (double)tail[c] * w5;
-        y += part ? disp_im : disp_re;
-        const int64_t o = (int64_t)r * p.n_particles + tbeg + t;
-        if (oc)
-          p.result[2 * o + part] = y;
-        else
-          p.result[o] = y;
-      }
+      for (int c = 0; c < 16; ++c) s_tail[row * NCH + cb * RC + c] = tl[c];
     }
   }
-  if (s_abort && tid == 0) {
-    // give in-flight copies and products a bounded chance to land before the
-    // accumulators are released
-    tc::mbar_wait_bounded(&bar_load, phase, kWaitLimit);
-    tc::mbar_wait_bounded(&bar_mma, phase, kWaitLimit);
-    report(p.st, VL1_E_TIMEOUT, tile, chunk);
-  }
+
+  // ---- all warps: FP64 combination and coalesced writes (a row's outputs
+  // are the consecutive target points of one box)
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, TCOLS);
+  if (!s_abort) {
+    const long long *s_comb = reinterpret_cast<const long long *>(smem);
+    const float *s_tail = reinterpret_cast<const float *>(s_comb + 128 * NCH);
+    const bool oc = p.d.table_cplx;
+    const int ncols = oc ? 2 * p.d.nq : p.d.nq;
+    for (int item = tid; item < 128 * NCH; item += blockDim.x) {
+      const int rw_ = item / NCH, cc = item - rw_ * NCH;
+      const int v = s_rows[rw_];
+      const int n = chunk * NCH + cc;
+      if (v < 0 || n >= ncols) continue;
+      const int j = v / p.nrhs, r = v - (v / p.nrhs) * p.nrhs;
+      const int tbox = p.target_boxes[j];
+      int t = n, part = 0;
+      if (oc && n >= p.d.nq) {
+        t = n - p.d.nq;
+        part = 1;
+      }
+      if (t >= min(p.tgt_counts[tbox], p.d.nq)) continue;
+      const int e = p.a_exp + p.x_exp[r];
+      double y = n_keys > 0 ? fma((double)s_tail[item], ldexp(1.0, e - 40),
+                                  (double)s_comb[item] * ldexp(1.0, e - 32))
+                            : 0.0;
+      if (p.disp) {
+        const int64_t di = (int64_t)j * p.nrhs + r;
+        y += oc ? p.disp[2 * di + part] : p.disp[di];
+      }
+      const int64_t o = (int64_t)r * p.n_particles + p.tgt_starts[tbox] + t;
+      if (oc)
+        p.result[2 * o + part] = y;
+      else
+        p.result[o] = y;
+    }
+  }
+  __syncthreads();
+  if (s_abort && tid == 0) report(p.st, VL1_E_TIMEOUT, tile, chunk);
+  if (warp == kMmaWarp) tc::tmem_dealloc(tbase, COLS);
+}
+
+template <int NCH, int KC>
+cudaError_t launch_mixed_kernel(dim3 grid, int threads, size_t smem, cudaStream_t s,
+                                const MixedParams &mp) {
+  cudaError_t e = cudaFuncSetAttribute(mixed_kernel<NCH, KC>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  mixed_kernel<NCH, KC><<<grid, threads, smem, s>>>(mp);
+  return cudaGetLastError();
 }
 
 int grid_for(int64_t n, int threads) {
@@ -471,8 +602,9 @@ int grid_for(int64_t n, int threads) {
 MixedGeom mixed_geometry(int nq, int table_cplx) {
   MixedGeom g;
   g.kp = ((nq + 15) / 16) * 16;
-  g.kc = g.kp <= 64 ? g.kp : 64;
-  g.kp = ((g.kp + g.kc - 1) / g.kc) * g.kc;
+  g.kc = g.kp <= 32 ? g.kp : 32;
+  // above one chunk, K is whole exact rounds of 64 (two chunks of 32)
+  if (g.kp > 32) g.kp = ((g.kp + 63) / 64) * 64;
   g.n_kc = g.kp / g.kc;
   const int n = table_cplx ? 2 * nq : nq;
   g.np = ((n + 15) / 16) * 16;
@@ -509,7 +641,7 @@ int64_t mixed_workspace_bytes(const vl1_plan *plan, int64_t nboxes, int64_t n_tg
   const int cv = plan->d.table_cplx ? 2 : 1;
   int64_t b = 0;
   b += ((int64_t)nrhs * 4 + 255) / 256 * 256;                   // x exponents
-  b += ((nboxes * kDigits * nrhs + 1) * g.kp * 2 + 255) / 256 * 256;  // x digits
+  b += (nboxes * nrhs * g.kp * kDigits * 2 + 255) / 256 * 256;  // x digits
   if (plan->d.disp_kind == VL1_DISP_LOG2D) {
     b += (nboxes * nrhs * cv * 8 + 255) / 256 * 256;            // per-box displacement
     b += (n_tgt_boxes * nrhs * cv * 8 + 255) / 256 * 256;       // per-target displacement
@@ -541,8 +673,13 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   const int64_t exp_bytes = ((int64_t)nrhs * 4 + 255) / 256 * 256;
   w += exp_bytes;
   __nv_bfloat16 *xdig = reinterpret_cast<__nv_bfloat16 *>(w);
-  const int64_t zero_row = nboxes * kDigits * nrhs;
-  w += ((zero_row + 1) * g.kp * 2 + 255) / 256 * 256;
+  const int64_t n_xrows = nboxes * nrhs;
+  if (n_xrows >= INT32_MAX) {
+    set_error("mixed path: %lld density rows exceed the 32-bit row index",
+              (long long)n_xrows);
+    return VL1_E_UNSUPPORTED;
+  }
+  w += (n_xrows * g.kp * kDigits * 2 + 255) / 256 * 256;
   double *wbox = nullptr, *disp = nullptr;
   if (d.disp_kind == VL1_DISP_LOG2D) {
     wbox = reinterpret_cast<double *>(w);
@@ -555,7 +692,7 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   x_exponent_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
                                                       x_exp);
   x_digits_kernel<<<grid_for(nbr, 128), 128, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs, x_exp,
-                                                    xdig, g.kp, zero_row, plan->status);
+                                                    xdig, g.kp, g.kc, plan->status);
   if (disp) {
     disp_box_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
                                                       wbox);
@@ -572,7 +709,7 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.nrhs = nrhs;
   mp.sched = sched;
   mp.xdig = xdig;
-  mp.zero_row = zero_row;
+  mp.n_xrows = (int32_t)n_xrows;
   mp.adig = plan->mixed.adig;
   mp.x_exp = x_exp;
   mp.a_exp = plan->mixed.a_exp;
@@ -584,22 +721,29 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.n_particles = tree.n_particles;
   mp.result = result;
   mp.st = plan->status;
-  const size_t smem = (size_t)kDigits * (128 + g.nch) * g.kc * 2;
+  const size_t pipe = (size_t)kStages * kDigits * (128 + g.nch) * g.kc * 2;
+  const size_t park = (size_t)128 * g.nch * 12;   // int64 sums + float tails
+  const size_t smem = (pipe > park ? pipe : park) + 1024;
   dim3 grid(sched.n_tiles, g.np / g.nch);
-  if (g.nch == 64) {
-    cudaFuncSetAttribute(mixed_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    mixed_kernel<64><<<grid, 256, smem, s>>>(mp);
-  } else if (g.nch == 32) {
-    cudaFuncSetAttribute(mixed_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    mixed_kernel<32><<<grid, 128, smem, s>>>(mp);
+  const int threads = 32 * (kReadWarp0 + 4 * (g.nch / 16));
+  if (g.kc == 32) {
+    if (g.nch == 64)
+      e = launch_mixed_kernel<64, 32>(grid, threads, smem, s, mp);
+    else if (g.nch == 32)
+      e = launch_mixed_kernel<32, 32>(grid, threads, smem, s, mp);
+    else
+      e = launch_mixed_kernel<16, 32>(grid, threads, smem, s, mp);
+  } else if (g.kc == 16) {
+    if (g.nch == 64)
+      e = launch_mixed_kernel<64, 16>(grid, threads, smem, s, mp);
+    else if (g.nch == 32)
+      e = launch_mixed_kernel<32, 16>(grid, threads, smem, s, mp);
+    else
+      e = launch_mixed_kernel<16, 16>(grid, threads, smem, s, mp);
   } else {
-    cudaFuncSetAttribute(mixed_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    mixed_kernel<16><<<grid, 128, smem, s>>>(mp);
+    set_error("mixed path: unsupported K chunk %d", g.kc);
+    return VL1_E_UNSUPPORTED;
   }
-  e = cudaGetLastError();
   return e == cudaSuccess ? VL1_OK : cuda_fail(e, "mixed_kernel launch");
 }
 

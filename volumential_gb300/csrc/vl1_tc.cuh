@@ -40,6 +40,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
   return ok != 0;
 }
 
+// As mbar_try_wait, but the thread may sleep (up to `hint_ns`) until the
+// phase completes instead of returning at once; a sleeping warp takes no
+// issue slots from the warps doing work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t phase,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(phase), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Wait for the given phase parity; gives up after `limit` polls.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase,
                                                   uint32_t limit) {
@@ -59,9 +75,36 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       : "memory");
 }
 
+// ------------------------------------------- row gather (2D TMA, gather4)
+// Four rows (r0..r3) of a 2D tensor, columns [col, col + box width), into
+// `dst` (four consecutive box rows, swizzled as the tensor map says, by the
+// absolute shared-memory address).  Rows outside the tensor read as zero and
+// still count their bytes on `bar`.  The box must be one row high.
+__device__ __forceinline__ void gather4_g2s(void *dst, const void *tmap, int col, int r0,
+                                            int r1, int r2, int r3, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_addr(dst)),
+      "l"(tmap), "r"(col), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_addr(bar))
+      : "memory");
+}
+
 // ---------------------------------------------------- cp.async (16 bytes)
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+// 16 bytes, of which the first `src_bytes` (0 or 16) are read and the rest
+// zero-filled; with src_bytes == 0 nothing is read from `src`
+__device__ __forceinline__ void cp_async16_zfill(void *dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+// arrive on `bar` once every prior cp.async of this thread has completed
+// (the arrival is part of the barrier's initial count)
+__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar))
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() {
@@ -110,6 +153,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
 }
+// 32 lanes x 16 consecutive 32-bit columns -> 16 registers per thread
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+        "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -128,6 +181,35 @@ __device__ __forceinline__ uint64_t smem_desc_kmajor_noswizzle(uint32_t saddr, u
   d |= (uint64_t)1 << 46;  // descriptor version for the sm_100 family
   // base offset 0, lbo mode 0, layout type 0 (no swizzle)
   return d;
+}
+
+// Shared-memory matrix descriptor, K-major, swizzled rows of `row_bytes`
+// (32, 64 or 128 bytes = 16, 32 or 64 bf16 along K).  Eight rows form one
+// swizzle atom of 8 * row_bytes bytes (aligned to that size); the 16-byte
+// chunk c of row r sits at chunk c ^ (bits 7.. of the row's offset), as the
+// hardware applies it to absolute shared-memory addresses.
+//   sbo: byte distance between atoms adjacent along M/N (8 * row_bytes)
+__device__ __forceinline__ uint64_t smem_desc_kmajor_swizzled(uint32_t saddr, uint32_t row_bytes) {
+  const uint64_t layout = row_bytes == 128 ? 2 : (row_bytes == 64 ? 4 : 6);
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;                                   // lbo (unused): 16 bytes
+  d |= (uint64_t)(((8 * row_bytes) >> 4) & 0x3FFF) << 32;   // sbo
+  d |= (uint64_t)1 << 46;
+  d |= layout << 61;
+  return d;
+}
+
+// Byte offset of element (row, k) in a K-major swizzled operand with `kc`
+// bf16 per row (row bytes 2*kc in {32, 64, 128}), relative to an atom-aligned
+// base.
+__host__ __device__ __forceinline__ uint32_t kmajor_swizzled_offset(uint32_t row, uint32_t k,
+                                                                    uint32_t kc) {
+  const uint32_t row_bytes = 2u * kc;
+  const uint32_t mask = row_bytes / 16u - 1u;
+  const uint32_t a = (row & 7u) * row_bytes + (k >> 3) * 16u + (k & 7u) * 2u;
+  const uint32_t chunk = ((a >> 4) & mask) ^ ((a >> 7) & mask);
+  return (row >> 3) * 8u * row_bytes + (a & ~(mask << 4)) + (chunk << 4);
 }
 
 // Instruction descriptor of kind::f16: BF16 x BF16 -> FP32, both K-major.
