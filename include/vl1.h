@@ -107,20 +107,49 @@ typedef struct {
   double root_extent;
 } vl1_tree_view;
 
+/* One CTA's share of the mixed-precision work: keys [key_begin, key_end) of
+ * one tile (indices into key_ids / key_xrow, inside the tile's own range).
+ * A tile with many keys is split into `nparts` items (part 0 .. nparts-1);
+ * each writes its exact partial sums to partial slot `slot`, and the item that
+ * finishes last adds the slots slot - part .. slot - part + nparts - 1 in slot
+ * order and writes the tile's results.  Unsplit items have split = -1,
+ * part = 0, nparts = 1, slot = -1. */
+typedef struct {
+  int32_t tile;
+  int32_t key_begin;
+  int32_t key_end;
+  int32_t split;       /* index of the split tile (its counters), or -1 */
+  int32_t part;
+  int32_t nparts;
+  int32_t slot;        /* partial-sum slot, or -1 */
+  int32_t reserved;
+} vl1_mixed_item;
+
 /* Work schedule of the mixed-precision path for one tree and rhs count
  * (built by the host from vl1_classify_pairs).  A tile is 128 rows, each row
  * one (target box index j, rhs r) item encoded j * nrhs + r (-1 = empty row).
  * Tile t covers keys key_ids[tile_key_start[t] .. tile_key_start[t+1]); a key is
  * table_level * n_cases + case.  key_xrow[k * 128 + row] is the density row
  * (source box S, rhs r) encoded S * nrhs + r, or -1 when the row's target box
- * has no list-1 pair of that key.  DEVICE pointers, caller owned; key_xrow
- * 16-byte aligned. */
+ * has no list-1 pair of that key.
+ * items: n_items work items, launched in this order (longest first balances
+ * the GPU); n_items == 0 means one item per tile covering all its keys.
+ * split_counters: n_splits * (output column chunks) int32, zero before the
+ * first call; every call leaves them zero.  split_partials: n_slots *
+ * (128 * padded output columns) * 12 bytes of scratch for split tiles.
+ * DEVICE pointers, caller owned; key_xrow 16-byte aligned. */
 typedef struct {
   int32_t n_tiles;
   const int32_t *tile_rows;
   const int32_t *tile_key_start;
   const int32_t *key_ids;
   const int32_t *key_xrow;
+  int32_t n_items;
+  const vl1_mixed_item *items;
+  int32_t n_splits;
+  int32_t n_slots;
+  int32_t *split_counters;
+  void *split_partials;
 } vl1_mixed_schedule;
 
 typedef struct {

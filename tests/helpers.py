@@ -92,3 +92,32 @@ def rel_l2(a, b):
     b = np.asarray(b)
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+MIXED_TREE_KEYS = ("target_boxes", "neighbor_source_boxes_starts",
+                   "neighbor_source_boxes_lists", "box_centers", "box_levels",
+                   "box_source_starts", "box_source_counts_nonchild", "box_target_starts",
+                   "box_target_counts_nonchild", "source_mode_ids", "target_point_ids")
+
+
+def plan_and_view(w):
+    """(plan, tree view, kept device arrays) of a workload, for calls that go
+    below the wrangler (schedules, C ABI entry points)."""
+    from volumential_gb300.plan import tree_view_from_arrays
+
+    wr = wrangler_for(w)
+    tr = w.traversal
+    payload = wr.get_payload(w.kernel)
+    nf = wr.near_field_evaluator(w.kernel, payload)
+    kw = wr._near_field_kwargs(payload, tr.target_boxes, tr.neighbor_source_boxes_starts,
+                               tr.neighbor_source_boxes_lists, None)
+    plan = nf.get_plan(
+        table_data_combined=kw["table_data_combined"],
+        mode_nmlz_combined=kw["mode_nmlz_combined"], case_indices=kw["case_indices"],
+        encoding_base=kw["encoding_base"], encoding_shift=kw["encoding_shift"],
+        table_root_extent=kw["table_root_extent"],
+        table_starting_level=kw["table_starting_level"],
+        **{n: kw[n] for n in kw if n.startswith("arithmetic_")})
+    view, keep = tree_view_from_arrays(root_extent=kw["root_extent"],
+                                       **{k: kw[k] for k in MIXED_TREE_KEYS})
+    return plan, view, keep

@@ -361,3 +361,38 @@ def test_capi_rejects_bad_plan_descriptions_without_a_gpu():
     assert lib.vl1_eval_fp64(None, None, None, 0, 1, None, None) == _lib.VL1_E_ARG
 
 # }}}
+
+
+def test_mixed_work_items_cover_every_key_once():
+    from volumential_gb300.batched import MixedSchedule
+
+    rng = np.random.default_rng(5)
+    counts = rng.integers(0, 40, size=60)
+    counts[3] = 0
+    key_start = np.concatenate([[0], np.cumsum(counts)])
+    for cap in (1, 3, 8, 1000):
+        items, n_splits, n_slots = MixedSchedule._work_items(key_start, cap)
+        lens = [it[2] - it[1] for it in items]
+        assert lens == sorted(lens, reverse=True)
+        assert max(lens) <= cap
+        covered = np.zeros(int(key_start[-1]), dtype=int)
+        slots = set()
+        parts = {}
+        for tile, k0, k1, split, part, nparts, slot, _ in items:
+            assert key_start[tile] <= k0 <= k1 <= key_start[tile + 1]
+            covered[k0:k1] += 1
+            if split < 0:
+                assert (part, nparts, slot) == (0, 1, -1)
+                assert (k0, k1) == (key_start[tile], key_start[tile + 1])
+            else:
+                assert 0 <= part < nparts and 0 <= slot < n_slots
+                slots.add(slot)
+                parts.setdefault(split, []).append((part, slot, tile))
+        assert np.all(covered == 1)
+        assert len(slots) == n_slots and len(parts) == n_splits
+        for split, ps in parts.items():
+            ps.sort()
+            assert [p for p, _, _ in ps] == list(range(len(ps)))
+            assert len({t for _, _, t in ps}) == 1
+            base = ps[0][1]
+            assert [s for _, s, _ in ps] == list(range(base, base + len(ps)))

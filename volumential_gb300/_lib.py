@@ -91,10 +91,19 @@ class TreeView(C.Structure):
     ]
 
 
+class MixedItem(C.Structure):
+    _fields_ = [("tile", C.c_int32), ("key_begin", C.c_int32), ("key_end", C.c_int32),
+                ("split", C.c_int32), ("part", C.c_int32), ("nparts", C.c_int32),
+                ("slot", C.c_int32), ("reserved", C.c_int32)]
+
+
 class MixedSchedule(C.Structure):
     _fields_ = [
         ("n_tiles", C.c_int32), ("tile_rows", C.c_void_p), ("tile_key_start", C.c_void_p),
         ("key_ids", C.c_void_p), ("key_xrow", C.c_void_p),
+        ("n_items", C.c_int32), ("items", C.c_void_p),
+        ("n_splits", C.c_int32), ("n_slots", C.c_int32),
+        ("split_counters", C.c_void_p), ("split_partials", C.c_void_p),
     ]
 
 

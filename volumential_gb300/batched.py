@@ -38,7 +38,7 @@ _CACHE_MAX = 8
 class MixedSchedule:
     """Device-resident schedule (and workspace) of one (plan, tree, nrhs)."""
 
-    def __init__(self, plan, view, keep, nrhs, stream):
+    def __init__(self, plan, view, keep, nrhs, stream, max_keys_per_item=None):
         import torch
 
         lib = _lib.lib()
@@ -125,18 +125,72 @@ class MixedSchedule:
         self.key_xrow = torch.from_numpy(
             np.concatenate(key_xrow).astype(np.int32) if key_xrow
             else np.zeros(ROWS_PER_TILE, np.int32)).to("cuda")
+        geo = plan.mixed_geometry()
+        n_chunks = geo["np"] // geo["nch"]
+        items, n_splits, n_slots = self._work_items(np.asarray(key_start, dtype=np.int64),
+                                                    max_keys_per_item)
+        self.n_items = len(items)
+        self.n_splits = n_splits
+        self.max_keys_per_item = int(max(1, max((it[2] - it[1] for it in items), default=1)))
+        self.items = torch.from_numpy(np.asarray(items, dtype=np.int32).reshape(-1, 8)
+                                      if items else np.zeros((1, 8), np.int32)).to("cuda")
+        self.split_counters = torch.zeros(max(1, n_splits * n_chunks), dtype=torch.int32,
+                                          device="cuda")
+        self.split_partials = torch.empty(max(16, n_slots * ROWS_PER_TILE * geo["np"] * 12),
+                                          dtype=torch.uint8, device="cuda")
         s = _lib.MixedSchedule()
         s.n_tiles = n_tiles
         s.tile_rows = self.tile_rows.data_ptr()
         s.tile_key_start = self.tile_key_start.data_ptr()
         s.key_ids = self.key_ids.data_ptr()
         s.key_xrow = self.key_xrow.data_ptr()
+        s.n_items = len(items)
+        s.items = self.items.data_ptr()
+        s.n_splits = n_splits
+        s.n_slots = n_slots
+        s.split_counters = self.split_counters.data_ptr()
+        s.split_partials = self.split_partials.data_ptr()
         self.c_struct = s
         ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
         if ws < 0:
             raise RuntimeError("vl1_mixed_workspace_bytes failed")
         self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
         del i32
+
+    @staticmethod
+    def _work_items(key_start, max_keys_per_item):
+        """Work items (one CTA each): whole tiles, and tiles with more than
+        ``max_keys_per_item`` keys split into nearly equal key ranges.  The
+        default cap is one SM's share of all tile keys, so that no item is
+        longer than the average load of an SM.  Items are ordered longest
+        first (CTAs start in grid order)."""
+        import torch
+
+        n_tiles = len(key_start) - 1
+        total = int(key_start[-1])
+        if max_keys_per_item is None:
+            n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()) \
+                .multi_processor_count
+            max_keys_per_item = max(4, -(-total // max(1, n_sm)))
+        cap = max(1, int(max_keys_per_item))
+        items = []
+        n_splits = 0
+        n_slots = 0
+        for t in range(n_tiles):
+            k0, k1 = int(key_start[t]), int(key_start[t + 1])
+            nk = k1 - k0
+            nparts = max(1, -(-nk // cap))
+            if nparts == 1:
+                items.append((t, k0, k1, -1, 0, 1, -1, 0))
+                continue
+            bounds = [k0 + (nk * i) // nparts for i in range(nparts + 1)]
+            for part in range(nparts):
+                items.append((t, bounds[part], bounds[part + 1], n_splits, part, nparts,
+                              n_slots + part, 0))
+            n_splits += 1
+            n_slots += nparts
+        items.sort(key=lambda it: -(it[2] - it[1]))   # stable: ties keep tile order
+        return items, n_splits, n_slots
 
     @staticmethod
     def _check_modes(keep, nq):
@@ -167,14 +221,14 @@ def _tree_token(keep):
     return tuple((t.data_ptr(), t._version, tuple(t.shape)) for t in keep.values())
 
 
-def get_schedule(plan, view, keep, nrhs, stream):
-    key = (id(plan), _tree_token(keep), int(nrhs))
+def get_schedule(plan, view, keep, nrhs, stream, max_keys_per_item=None):
+    key = (id(plan), _tree_token(keep), int(nrhs), max_keys_per_item)
     with _lock:
         hit = _cache.get(key)
         if hit is not None:
             _cache.move_to_end(key)
             return hit[0]
-    sched = MixedSchedule(plan, view, keep, nrhs, stream)
+    sched = MixedSchedule(plan, view, keep, nrhs, stream, max_keys_per_item)
     with _lock:
         # keep the tree tensors alive with the schedule so the token stays unique
         _cache[key] = (sched, dict(keep), plan)
@@ -183,11 +237,13 @@ def get_schedule(plan, view, keep, nrhs, stream):
     return sched
 
 
-def eval_mixed(plan, view, coefs, out, *, stream, nrhs, keep):
+def eval_mixed(plan, view, coefs, out, *, stream, nrhs, keep, max_keys_per_item=None):
     """Tensor-core evaluation of ``nrhs`` right-hand sides into ``out``.
 
     ``coefs``: CUDA float64 (or complex128) tensor with ``nrhs * N`` values;
     ``out``: CUDA tensor of the plain path's output dtype and size.
+    ``max_keys_per_item``: split tiles with more keys over several CTAs
+    (default: one SM's share of the work).
     """
     import torch
 
@@ -197,13 +253,14 @@ def eval_mixed(plan, view, coefs, out, *, stream, nrhs, keep):
         c2 = torch.cat([coefs.real.reshape(nrhs, n), coefs.imag.reshape(nrhs, n)]).contiguous()
         tmp = torch.empty((2 * nrhs, n), dtype=torch.complex128 if plan.complex_table
                           else torch.float64, device="cuda")
-        eval_mixed(plan, view, c2, tmp, stream=stream, nrhs=2 * nrhs, keep=keep)
+        eval_mixed(plan, view, c2, tmp, stream=stream, nrhs=2 * nrhs, keep=keep,
+                   max_keys_per_item=max_keys_per_item)
         res = tmp[:nrhs] + 1j * tmp[nrhs:]
         out.view(nrhs, n).copy_(res)
         return
     if coefs.dtype != torch.float64 or not coefs.is_contiguous():
         raise TypeError("mixed path coefficients must be a contiguous float64 tensor")
-    sched = get_schedule(plan, view, keep, nrhs, stream)
+    sched = get_schedule(plan, view, keep, nrhs, stream, max_keys_per_item)
     lib = _lib.lib()
     st = lib.vl1_eval_mixed(plan.handle, C.byref(view), C.byref(sched.c_struct),
                             coefs.data_ptr(), int(nrhs), out.data_ptr(),

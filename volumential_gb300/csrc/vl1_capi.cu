@@ -286,6 +286,23 @@ static int32_t make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &
   tr.n_particles = t->n_particles;
   tr.nboxes = t->nboxes;
   tr.root_extent = t->root_extent;
+  // same operation sequence as level_extent / pair_scaling on the device
+  // (products and quotients only, so no contraction can change the rounding)
+  for (int l = 0; l < kScaleLevels; ++l) {
+    const double ext = t->root_extent * (1.0 / (double)(1LL << l));
+    const int sp = plan->d.scaling_exponent;
+    if (sp == 0) {
+      tr.level_scale[l] = 1.0;
+      continue;
+    }
+    const int n = sp > 0 ? sp : -sp;
+    double num = ext, den = plan->d.table_root_extent;
+    for (int k = 1; k < n; ++k) {
+      num = num * ext;
+      den = den * plan->d.table_root_extent;
+    }
+    tr.level_scale[l] = sp > 0 ? num / den : den / num;
+  }
   return VL1_OK;
 }
 
@@ -365,6 +382,14 @@ int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,
   }
   if (reinterpret_cast<uintptr_t>(schedule->key_xrow) % 16 != 0) {
     set_error("vl1_eval_mixed: schedule key_xrow must be 16-byte aligned");
+    return VL1_E_ARG;
+  }
+  if (schedule->n_items < 0 || (schedule->n_items > 0 && !schedule->items) ||
+      schedule->n_splits < 0 || schedule->n_slots < 0 ||
+      (schedule->n_splits > 0 &&
+       (!schedule->split_counters || !schedule->split_partials || schedule->n_slots < 2 ||
+        reinterpret_cast<uintptr_t>(schedule->split_partials) % 16 != 0))) {
+    set_error("vl1_eval_mixed: invalid work items or split scratch in the schedule");
     return VL1_E_ARG;
   }
   return launch_mixed(plan, tr, tr.nboxes, *schedule, coefs, nrhs,

@@ -42,7 +42,11 @@ struct TreeDev {
   int64_t n_particles;
   int64_t nboxes;
   double root_extent;
+  // scaling of a source box of level l (l < kScaleLevels), computed on the
+  // host with the same IEEE operations as pair_scaling(level_extent(l))
+  double level_scale[32];
 };
+constexpr int kScaleLevels = 32;
 
 }  // namespace vl1
 
@@ -210,6 +214,14 @@ __device__ __forceinline__ double pair_scaling(const DevDesc &d, double ext) {
     den = __dmul_rn(den, d.table_root_extent);
   }
   return p > 0 ? __ddiv_rn(num, den) : __ddiv_rn(den, num);
+}
+
+// scaling of a source box of `level`: from the per-call table when the level
+// is in it (the FP64 pipe is narrow on this GPU; the division chain of
+// pair_scaling is then done once per level on the host)
+__device__ __forceinline__ double box_scaling(const DevDesc &d, const TreeDev &tr, int level) {
+  if (level < kScaleLevels) return tr.level_scale[level];
+  return pair_scaling(d, level_extent(tr.root_extent, level));
 }
 
 // table level of a source box (list1.py:361-437, 1086-1087)

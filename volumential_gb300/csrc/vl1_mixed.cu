@@ -37,12 +37,35 @@ constexpr int kMagicBits = 0x4B400000;
 // ----------------------------------------------------------------- helpers
 
 // |v| as a fixed-point integer m with v = sign * 2^(e - 40) * m, m < 2^40,
-// rounded to nearest; digits are the five base-256 digits of m.
+// rounded to nearest (ties to even); digits are the five base-256 digits of
+// m.  Integer arithmetic on the IEEE-754 fields only: it equals
+// round(ldexp(|v|, 40 - e)) without touching the FP64 pipe, which is narrow
+// on this GPU.
 __device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits]) {
-  const double sc = ldexp(fabs(v), kFixedBits - e);
-  long long m = __double2ll_rn(sc);
-  if (m >= (1ll << kFixedBits)) m = (1ll << kFixedBits) - 1;  // v at the scale bound
-  const int sgn = v < 0 ? -1 : 1;
+  const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(v));
+  const unsigned long long mag = bits & 0x7FFFFFFFFFFFFFFFull;
+  const int ef = (int)(mag >> 52);
+  // |v| = M * 2^ev
+  const unsigned long long M = ef ? ((mag & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : mag;
+  const int ev = ef ? ef - 1075 : -1074;
+  const long long sh = (long long)ev + kFixedBits - (long long)e;
+  unsigned long long m;
+  if (M == 0) {
+    m = 0;
+  } else if (sh >= 0) {
+    // saturates when |v| is not below 2^e (m >= 2^40 after the shift)
+    m = (sh > kFixedBits || M >= (1ull << (kFixedBits - sh))) ? (1ull << kFixedBits) : (M << sh);
+  } else if (sh < -63) {
+    m = 0;
+  } else {
+    const int k = (int)-sh;
+    const unsigned long long q = M >> k;
+    const unsigned long long rem = M & ((1ull << k) - 1ull);
+    const unsigned long long half = 1ull << (k - 1);
+    m = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+  }
+  if (m >= (1ull << kFixedBits)) m = (1ull << kFixedBits) - 1;  // v at the scale bound
+  const int sgn = (bits >> 63) ? -1 : 1;
 #pragma unroll
   for (int i = 0; i < kDigits; ++i) {
     const int shift = kFixedBits - kDigitBits * (i + 1);
@@ -50,12 +73,15 @@ __device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits
   }
 }
 
-// exponent e with |v| < 2^e (0 for v == 0)
+// exponent e with |v| < 2^e, as frexp returns it (-1074 for v == 0), from the
+// IEEE-754 fields
 __device__ __forceinline__ int scale_exponent(double v) {
-  if (v == 0.0) return -1074;
-  int e;
-  frexp(fabs(v), &e);
-  return e;
+  const unsigned long long mag =
+      static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7FFFFFFFFFFFFFFFull;
+  if (mag == 0) return -1074;
+  const int ef = (int)(mag >> 52);
+  if (ef) return ef - 1022;
+  return (64 - __clzll((long long)mag)) - 1074;   // subnormal
 }
 
 // ------------------------------------------------- plan: A digit operands
@@ -115,22 +141,43 @@ __global__ void classify_pairs_kernel(DevDesc d, TreeDev tr, int32_t *keys, vl1_
   }
 }
 
-// max exponent of scaling * coefficient per rhs
+// Per-call preparation kernels: one warp per density row (source box b, rhs r).
+
+// max exponent of scaling * coefficient per rhs: warp maxima are combined
+// per block in shared memory (rhs < kExpSmem), then one global atomic per
+// block and rhs
+constexpr int kExpSmem = 256;
 __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
                                   int nrhs, int *x_exp) {
+  __shared__ int s_max[kExpSmem];
+  const bool use_smem = nrhs <= kExpSmem;
+  if (use_smem)
+    for (int r = threadIdx.x; r < nrhs; r += blockDim.x) s_max[r] = -1074;
+  __syncthreads();
   const int64_t n = (int64_t)nboxes * nrhs;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
-       idx += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
+       idx += warps) {
     const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-    int cnt = tr.src_counts[b];
+    const int cnt = min(tr.src_counts[b], d.nq);
     if (cnt <= 0) continue;
-    cnt = min(cnt, d.nq);
-    const double sc = pair_scaling(d, level_extent(tr.root_extent, tr.levels[b]));
+    const double sc = box_scaling(d, tr, tr.levels[b]);
     const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
     int e = -1074;
-    for (int s = 0; s < cnt; ++s) e = max(e, scale_exponent(sc * c[s]));
-    atomicMax(x_exp + r, e);
+    for (int s = lane; s < cnt; s += 32) e = max(e, scale_exponent(sc * c[s]));
+    e = __reduce_max_sync(0xffffffffu, e);
+    if (lane == 0) {
+      if (use_smem)
+        atomicMax(s_max + r, e);
+      else
+        atomicMax(x_exp + r, e);
+    }
   }
+  __syncthreads();
+  if (use_smem)
+    for (int r = threadIdx.x; r < nrhs; r += blockDim.x)
+      if (s_max[r] > -1074) atomicMax(x_exp + r, s_max[r]);
 }
 
 // x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bf16 (kp * 5
@@ -141,22 +188,25 @@ __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double 
                                 int kc, vl1_status *st) {
   const int64_t n = (int64_t)nboxes * nrhs;
   const int row_elems = kp * kDigits;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
-       idx += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
+       idx += warps) {
     const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
     __nv_bfloat16 *row = xdig + idx * row_elems;
-    for (int k = 0; k < row_elems; k += 8)
+    for (int k = lane * 8; k < row_elems; k += 32 * 8)
       *reinterpret_cast<uint4 *>(row + k) = make_uint4(0u, 0u, 0u, 0u);
+    __syncwarp();
     int cnt = tr.src_counts[b];
     if (cnt <= 0) continue;
     if (cnt > d.nq) {
-      report(st, VL1_E_LAYOUT, b, cnt);
+      if (lane == 0) report(st, VL1_E_LAYOUT, b, cnt);
       cnt = d.nq;
     }
-    const double sc = pair_scaling(d, level_extent(tr.root_extent, tr.levels[b]));
+    const double sc = box_scaling(d, tr, tr.levels[b]);
     const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
     const int e = x_exp[r];
-    for (int s = 0; s < cnt; ++s) {
+    for (int s = lane; s < cnt; s += 32) {
       const int m = tr.smode[tr.src_starts[b] + s];
       if (m < 0 || m >= d.nq) {
         report(st, VL1_E_LAYOUT, b, -1 - s);
@@ -239,14 +289,17 @@ struct MixedParams {
 };
 
 // Warp roles of mixed_kernel (warp index w):
-//   w <  4      producers: per pipeline unit, warp w gathers the density digit
-//               pieces of tile rows 32w .. 32w+31 with cp.async (consecutive
+//   w <  8      producers: per pipeline unit, warp w gathers the density digit
+//               pieces of tile rows 16w .. 16w+15 with cp.async (consecutive
 //               lanes on consecutive 16-byte pieces of a row's 5 * kc digits,
 //               zero-filled for rows without a source box); each lane's
-//               copies arrive on full[stage] when they land.  Warp 0 also
-//               loads the five table digit tiles by bulk copies (TMA).
-//   w == 4      tensor-core issuer (one lane)
-//   w >= 5      readout: TMEM lane quadrant w % 4, RC columns each
+//               copies arrive on full[stage] when they land.  Eight warps keep
+//               enough 16-byte requests in flight to cover the L2 latency of
+//               these scattered rows.
+//   w == 8      table loader (one lane): the five table digit tiles of the
+//               unit's key by bulk copies (TMA), counted on full[stage]
+//   w == 9      tensor-core issuer (one lane)
+//   w >= 10     readout: TMEM lane quadrant w % 4, RC columns each
 // Pipeline unit = (key, K chunk of kc <= 32 source points); a "round" = the
 // units of one key that share an exact accumulation (K <= 64).  Exact
 // diagonal accumulators (i+j = 2, 3, 4) are double-buffered in TMEM (one
@@ -257,9 +310,11 @@ struct MixedParams {
 // column blocks land on consecutive diagonals i + j.
 constexpr int kStages = 3;
 constexpr uint32_t kExactCols = 3;   // accumulators per buffer
-constexpr int kProducerWarps = 4;
-constexpr int kMmaWarp = 4;
-constexpr int kReadWarp0 = 5;
+constexpr int kProducerWarps = 8;
+constexpr int kRowsPerProducer = 128 / kProducerWarps;
+constexpr int kLoaderWarp = 8;
+constexpr int kMmaWarp = 9;
+constexpr int kReadWarp0 = 10;
 constexpr uint32_t kSleepNs = 200000;      // longest sleep of one wait poll
 constexpr uint32_t kSleepPolls = 10000;    // polls before a wait gives up (~2 s)
 
@@ -314,20 +369,49 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
   __shared__ uint32_t tmem_base;
   __shared__ volatile int s_abort;
   __shared__ int s_rows[128];
-  __shared__ int s_xrow[kStages][128];
 
-  const int tile = blockIdx.x;
   const int chunk = blockIdx.y;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
 
-  const int k0 = p.sched.tile_key_start[tile], k1 = p.sched.tile_key_start[tile + 1];
+  // this CTA's work item: a tile, or a key range of a split tile
+  vl1_mixed_item item;
+  if (p.sched.n_items > 0) {
+    item = p.sched.items[blockIdx.x];
+  } else {
+    item.tile = blockIdx.x;
+    item.key_begin = p.sched.tile_key_start[blockIdx.x];
+    item.key_end = p.sched.tile_key_start[blockIdx.x + 1];
+    item.split = -1;
+    item.part = 0;
+    item.nparts = 1;
+    item.slot = -1;
+  }
+  const int tile = item.tile;
+  {
+    bool bad = tile < 0 || tile >= p.sched.n_tiles;
+    if (!bad) {
+      const int t0 = p.sched.tile_key_start[tile], t1 = p.sched.tile_key_start[tile + 1];
+      bad = item.key_begin < t0 || item.key_end > t1 || item.key_begin > item.key_end;
+    }
+    if (item.split >= 0)
+      bad = bad || item.split >= p.sched.n_splits || item.part < 0 ||
+            item.part >= item.nparts || item.slot - item.part < 0 ||
+            item.slot - item.part + item.nparts > p.sched.n_slots;
+    else
+      bad = bad || item.split != -1;
+    if (bad) {
+      if (tid == 0) report(p.st, VL1_E_ARG, blockIdx.x, -1);
+      return;   // uniform across the CTA, before any barrier or TMEM use
+    }
+  }
+
+  const int k0 = item.key_begin, k1 = item.key_end;
   const int n_keys = k1 - k0;
   const int upr = (p.g.kp < 64 ? p.g.kp : 64) / KC;   // units per round
   const int rpk = (p.g.kp + 63) / 64;                  // rounds per key
   const int n_rounds = n_keys * rpk;
-  const int n_units = n_rounds * upr;
 
   if (tid < 128) {
     int v = p.sched.tile_rows[(int64_t)tile * 128 + tid];
@@ -339,7 +423,7 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      // 128 producer lanes (cp.async arrivals) + the table copies' expect_tx
+      // producer lanes (cp.async arrivals) + the table copies' expect_tx
       tc::mbar_init(&bars.full[s], 32 * kProducerWarps + 1);
       tc::mbar_init(&bars.empty[s], 1);
     }
@@ -364,66 +448,92 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
     constexpr int NC16 = KC / 8;               // 16-byte pieces per digit row
     constexpr int PPR = kDigits * NC16;        // pieces per row and unit
     const int64_t row_elems = (int64_t)p.g.kp * kDigits;
-    for (int u = 0; u < n_units; ++u) {
-      const int s = u % kStages;
-      const int use = u / kStages;
-      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) break;
-      uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
-      uint8_t *as = xs + kDigits * XBYTES;
-      const int round = u / upr;
-      const int kidx = k0 + round / rpk;
-      const int kc = (round % rpk) * upr + u % upr;   // K chunk index within the key
-      int key = p.sched.key_ids[kidx];
+    // lanes < kRowsPerProducer hold the source row of tile row my_row
+    const int my_row = kRowsPerProducer * warp + (lane % kRowsPerProducer);
+    // key id and this lane's source row, fetched one key ahead
+    int nkey = 0, nxr = -1;
+    if (n_keys > 0) {
+      nkey = p.sched.key_ids[k0];
+      nxr = p.sched.key_xrow[(int64_t)k0 * 128 + my_row];
+    }
+    int u = 0;
+    bool aborted = false;
+    for (int kidx = k0; kidx < k1 && !aborted; ++kidx) {
+      int key = nkey, xr_lane = nxr;
+      if (kidx + 1 < k1) {
+        nkey = p.sched.key_ids[kidx + 1];
+        nxr = p.sched.key_xrow[(int64_t)(kidx + 1) * 128 + my_row];
+      }
       const bool key_ok = key >= 0 && key < p.d.n_tables * p.d.n_cases;
       if (!key_ok) {
         if (warp == 0 && lane == 0) report(p.st, VL1_E_ARG, tile, kidx);
-        key = 0;
+        xr_lane = -1;
       }
-      if (warp == 0) {
-        if (lane == 0) tc::mbar_arrive_expect_tx(&bars.full[s], kDigits * ABYTES);
-        __syncwarp();
-        if (lane < kDigits) {
-          const int64_t base =
-              (((int64_t)key * p.g.n_kc + kc) * kDigits + lane) * p.g.np * KC +
-              (int64_t)chunk * NCH * KC;
-          tc::bulk_g2s(as + lane * ABYTES, p.adig + base, ABYTES, &bars.full[s]);
+      if (xr_lane >= p.n_xrows) {
+        report(p.st, VL1_E_ARG, tile, my_row);
+        xr_lane = -1;
+      }
+      for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
+        const int s = u % kStages;
+        const int use = u / kStages;
+        if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) {
+          aborted = true;
+          break;
         }
-      }
-      // source rows of this warp's 32 tile rows (-1: no source box)
-      int *xr_s = s_xrow[s];
-      {
-        const int r = 32 * warp + lane;
-        int xr = key_ok ? p.sched.key_xrow[(int64_t)kidx * 128 + r] : -1;
-        if (xr >= p.n_xrows) {
-          report(p.st, VL1_E_ARG, tile, r);
-          xr = -1;
+        uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
+        // piece pc = it * 32 + lane of the warp's kRowsPerProducer * PPR
+        // pieces: row pc / PPR, piece q = pc % PPR = digit * NC16 + 16-byte column
+        int rl = lane / PPR, q = lane % PPR;
+        const int64_t col0 = (int64_t)kc * kDigits * KC;
+#pragma unroll 2
+        for (int it = 0; it < kRowsPerProducer * PPR / 32; ++it) {
+          const int xr = __shfl_sync(0xffffffffu, xr_lane, rl);
+          const int dg = q / NC16, c = q - dg * NC16;
+          uint8_t *dst = xs + dg * XBYTES +
+                         tc::kmajor_swizzled_offset(kRowsPerProducer * warp + rl, c * 8, KC);
+          const bool have = xr >= 0;
+          const __nv_bfloat16 *src =
+              p.xdig + (have ? (int64_t)xr * row_elems + col0 + q * 8 : 0);
+          tc::cp_async16_zfill(dst, src, have ? 16u : 0u);
+          q += 32 % PPR;
+          rl += 32 / PPR;
+          if (q >= PPR) {
+            q -= PPR;
+            ++rl;
+          }
         }
-        xr_s[r] = xr;
+        tc::cp_async_arrive_noinc(&bars.full[s]);
       }
-      __syncwarp();
-      // piece pc = it * 32 + lane of the warp's 32 * PPR pieces: row pc / PPR,
-      // piece q = pc % PPR = digit * NC16 + 16-byte column
-      int rl = lane / PPR, q = lane % PPR;
-      const int64_t col0 = (int64_t)kc * kDigits * KC;
-#pragma unroll 4
-      for (int it = 0; it < PPR; ++it) {
-        const int r = 32 * warp + rl;
-        const int xr = xr_s[r];
-        const int dg = q / NC16, c = q - dg * NC16;
-        uint8_t *dst = xs + dg * XBYTES + tc::kmajor_swizzled_offset(r, c * 8, KC);
-        const bool have = xr >= 0;
-        const __nv_bfloat16 *src = p.xdig + (have ? (int64_t)xr * row_elems + col0 + q * 8 : 0);
-        tc::cp_async16_zfill(dst, src, have ? 16u : 0u);
-        q += 32 % PPR;
-        rl += 32 / PPR;
-        if (q >= PPR) {
-          q -= PPR;
-          ++rl;
-        }
-      }
-      tc::cp_async_arrive_noinc(&bars.full[s]);
-      __syncwarp();   // xr_s of this stage is rewritten only after the stage is released
     }
+  } else if (warp == kLoaderWarp) {
+    // ---------------------------------------------------------- table loader
+    if (lane == 0) {
+      int u = 0;
+      bool aborted = false;
+      int nkey = n_keys > 0 ? p.sched.key_ids[k0] : 0;
+      for (int kidx = k0; kidx < k1 && !aborted; ++kidx) {
+        int key = nkey;
+        if (kidx + 1 < k1) nkey = p.sched.key_ids[kidx + 1];
+        if (key < 0 || key >= p.d.n_tables * p.d.n_cases) key = 0;   // reported by warp 0
+        for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
+          const int s = u % kStages;
+          const int use = u / kStages;
+          if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) {
+            aborted = true;
+            break;
+          }
+          uint8_t *as = smem + (size_t)s * STAGE_BYTES + kDigits * XBYTES;
+          tc::mbar_arrive_expect_tx(&bars.full[s], kDigits * ABYTES);
+          const int64_t base = (((int64_t)key * p.g.n_kc + kc) * kDigits) * p.g.np * KC +
+                               (int64_t)chunk * NCH * KC;
+#pragma unroll
+          for (int dg = 0; dg < kDigits; ++dg)
+            tc::bulk_g2s(as + dg * ABYTES, p.adig + base + (int64_t)dg * p.g.np * KC, ABYTES,
+                         &bars.full[s]);
+        }
+      }
+    }
+    __syncwarp();
   } else if (warp == kMmaWarp) {
     // ------------------------------------------------------- tensor cores
     if (lane == 0) {
@@ -540,16 +650,47 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
   }
 
   // ---- all warps: FP64 combination and coalesced writes (a row's outputs
-  // are the consecutive target points of one box)
+  // are the consecutive target points of one box).  A split tile's parts
+  // store their exact partial sums; the part that finishes last adds them in
+  // slot order (integers exactly, tails in FP64) and writes the results.
   tc::tc_fence_before();
   __syncthreads();
-  if (!s_abort) {
-    const long long *s_comb = reinterpret_cast<const long long *>(smem);
-    const float *s_tail = reinterpret_cast<const float *>(s_comb + 128 * NCH);
+  __shared__ int s_last;
+  const long long *comb_src = reinterpret_cast<const long long *>(smem);
+  const float *tail_src = reinterpret_cast<const float *>(comb_src + 128 * NCH);
+  bool write = !s_abort;
+  const uint8_t *g_parts = nullptr;   // slot region of part 0 of a split tile
+  if (item.split >= 0) {
+    const int64_t slot_bytes = (int64_t)128 * NCH * 12;
+    uint8_t *base = static_cast<uint8_t *>(p.sched.split_partials) +
+                    ((int64_t)(item.slot - item.part) * gridDim.y + chunk) * slot_bytes;
+    const int64_t part_stride = (int64_t)gridDim.y * slot_bytes;
+    g_parts = base;
+    if (!s_abort) {
+      long long *my_comb = reinterpret_cast<long long *>(base + item.part * part_stride);
+      float *my_tail = reinterpret_cast<float *>(base + item.part * part_stride +
+                                                 (int64_t)128 * NCH * 8);
+      for (int i = tid; i < 128 * NCH; i += blockDim.x) {
+        my_comb[i] = comb_src[i];
+        my_tail[i] = tail_src[i];
+      }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+      const int done = atomicAdd(p.sched.split_counters + item.split * gridDim.y + chunk, 1);
+      s_last = done == item.nparts - 1;
+    }
+    __syncthreads();
+    write = write && s_last;
+    if (write) __threadfence();
+  }
+  if (write) {
     const bool oc = p.d.table_cplx;
     const int ncols = oc ? 2 * p.d.nq : p.d.nq;
-    for (int item = tid; item < 128 * NCH; item += blockDim.x) {
-      const int rw_ = item / NCH, cc = item - rw_ * NCH;
+    const int64_t part_stride_e = (int64_t)gridDim.y * 128 * NCH * 12;
+    for (int it = tid; it < 128 * NCH; it += blockDim.x) {
+      const int rw_ = it / NCH, cc = it - rw_ * NCH;
       const int v = s_rows[rw_];
       const int n = chunk * NCH + cc;
       if (v < 0 || n >= ncols) continue;
@@ -561,10 +702,22 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
         part = 1;
       }
       if (t >= min(p.tgt_counts[tbox], p.d.nq)) continue;
+      long long comb;
+      double tail;
+      if (item.split >= 0) {
+        comb = 0;
+        tail = 0.0;
+        for (int q = 0; q < item.nparts; ++q) {
+          const uint8_t *pb = g_parts + q * part_stride_e;
+          comb += __ldcg(reinterpret_cast<const long long *>(pb) + it);
+          tail += (double)__ldcg(reinterpret_cast<const float *>(pb + (int64_t)128 * NCH * 8) + it);
+        }
+      } else {
+        comb = comb_src[it];
+        tail = (double)tail_src[it];
+      }
       const int e = p.a_exp + p.x_exp[r];
-      double y = n_keys > 0 ? fma((double)s_tail[item], ldexp(1.0, e - 40),
-                                  (double)s_comb[item] * ldexp(1.0, e - 32))
-                            : 0.0;
+      double y = fma(tail, ldexp(1.0, e - 40), (double)comb * ldexp(1.0, e - 32));
       if (p.disp) {
         const int64_t di = (int64_t)j * p.nrhs + r;
         y += oc ? p.disp[2 * di + part] : p.disp[di];
@@ -575,6 +728,8 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
       else
         p.result[o] = y;
     }
+    // the last part leaves the counter at zero for the next call
+    if (item.split >= 0 && tid == 0) p.sched.split_counters[item.split * gridDim.y + chunk] = 0;
   }
   __syncthreads();
   if (s_abort && tid == 0) report(p.st, VL1_E_TIMEOUT, tile, chunk);
@@ -689,10 +844,10 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   cudaError_t e = cudaMemsetAsync(x_exp, 0x80, exp_bytes, s);  // large negative exponents
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(x_exp)");
   const int64_t nbr = nboxes * nrhs;
-  x_exponent_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
-                                                      x_exp);
-  x_digits_kernel<<<grid_for(nbr, 128), 128, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs, x_exp,
-                                                    xdig, g.kp, g.kc, plan->status);
+  x_exponent_kernel<<<grid_for(nbr * 32, 256) < 152 * 8 ? grid_for(nbr * 32, 256) : 152 * 8,
+                      256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs, x_exp);
+  x_digits_kernel<<<grid_for(nbr * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
+                                                         x_exp, xdig, g.kp, g.kc, plan->status);
   if (disp) {
     disp_box_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
                                                       wbox);
@@ -724,7 +879,7 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   const size_t pipe = (size_t)kStages * kDigits * (128 + g.nch) * g.kc * 2;
   const size_t park = (size_t)128 * g.nch * 12;   // int64 sums + float tails
   const size_t smem = (pipe > park ? pipe : park) + 1024;
-  dim3 grid(sched.n_tiles, g.np / g.nch);
+  dim3 grid(sched.n_items > 0 ? sched.n_items : sched.n_tiles, g.np / g.nch);
   const int threads = 32 * (kReadWarp0 + 4 * (g.nch / 16));
   if (g.kc == 32) {
     if (g.nch == 64)
