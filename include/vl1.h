@@ -136,7 +136,7 @@ typedef struct {
  * the GPU); n_items == 0 means one item per tile covering all its keys.
  * split_counters: n_splits * (output column chunks) int32, zero before the
  * first call; every call leaves them zero.  split_partials: n_slots *
- * (128 * padded output columns) * 12 bytes of scratch for split tiles.
+ * (128 * padded output columns) * 8 bytes of scratch for split tiles.
  * DEVICE pointers, caller owned; key_xrow 16-byte aligned. */
 typedef struct {
   int32_t n_tiles;

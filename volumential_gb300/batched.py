@@ -136,7 +136,7 @@ class MixedSchedule:
                                       if items else np.zeros((1, 8), np.int32)).to("cuda")
         self.split_counters = torch.zeros(max(1, n_splits * n_chunks), dtype=torch.int32,
                                           device="cuda")
-        self.split_partials = torch.empty(max(16, n_slots * ROWS_PER_TILE * geo["np"] * 12),
+        self.split_partials = torch.empty(max(16, n_slots * ROWS_PER_TILE * geo["np"] * 8),
                                           dtype=torch.uint8, device="cuda")
         s = _lib.MixedSchedule()
         s.n_tiles = n_tiles
@@ -157,22 +157,14 @@ class MixedSchedule:
         self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
         del i32
 
-    @staticmethod
-    def _work_items(key_start, max_keys_per_item):
-        """Work items (one CTA each): whole tiles, and tiles with more than
-        ``max_keys_per_item`` keys split into nearly equal key ranges.  The
-        default cap is one SM's share of all tile keys, so that no item is
-        longer than the average load of an SM.  Items are ordered longest
-        first (CTAs start in grid order)."""
-        import torch
+    # cost model of one work item in pipeline units of one key: CTA start-up
+    # and result write-back, and the extra partial-sum traffic of a split part
+    ITEM_OVERHEAD_KEYS = 3.0
+    SPLIT_OVERHEAD_KEYS = 1.0
 
+    @staticmethod
+    def _split_items(key_start, cap):
         n_tiles = len(key_start) - 1
-        total = int(key_start[-1])
-        if max_keys_per_item is None:
-            n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()) \
-                .multi_processor_count
-            max_keys_per_item = max(4, -(-total // max(1, n_sm)))
-        cap = max(1, int(max_keys_per_item))
         items = []
         n_splits = 0
         n_slots = 0
@@ -191,6 +183,44 @@ class MixedSchedule:
             n_slots += nparts
         items.sort(key=lambda it: -(it[2] - it[1]))   # stable: ties keep tile order
         return items, n_splits, n_slots
+
+    @classmethod
+    def _makespan(cls, items, n_sm):
+        """Greedy list-scheduling finish time of ``items`` (in key units) on
+        ``n_sm`` one-CTA-per-SM slots, launched in order."""
+        import heapq
+
+        slots = [0.0] * n_sm
+        for it in items:
+            cost = (it[2] - it[1]) + cls.ITEM_OVERHEAD_KEYS + \
+                (cls.SPLIT_OVERHEAD_KEYS if it[3] >= 0 else 0.0)
+            heapq.heapreplace(slots, slots[0] + cost)
+        return max(slots)
+
+    @classmethod
+    def _work_items(cls, key_start, max_keys_per_item, n_sm=None):
+        """Work items (one CTA each): whole tiles, and tiles with more than a
+        cap of keys split into nearly equal key ranges, ordered longest first
+        (CTAs start in grid order).  Without an explicit cap, the cap among
+        one SM's share of all keys and its 1/2 .. 1/6 with the shortest
+        modelled finish time is taken."""
+        total = int(key_start[-1])
+        if max_keys_per_item is not None:
+            return cls._split_items(key_start, max(1, int(max_keys_per_item)))
+        if n_sm is None:
+            import torch
+
+            n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()) \
+                .multi_processor_count
+        share = max(1, -(-total // max(1, n_sm)))
+        best = None
+        for div in (1, 2, 3, 4, 5, 6):
+            cap = max(4, -(-share // div))
+            cand = cls._split_items(key_start, cap)
+            t = cls._makespan(cand[0], n_sm)
+            if best is None or t < best[0]:
+                best = (t, cand)
+        return best[1]
 
     @staticmethod
     def _check_modes(keep, nq):

@@ -208,7 +208,7 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
     void *ptr = nullptr;
     st = plan_alloc(p, &ptr, 2 * (size_t)elems);
     if (!st) {
-      p->mixed.adig = static_cast<__nv_bfloat16 *>(ptr);
+      p->mixed.adig = static_cast<__half *>(ptr);
       double amax = 0.0;
       const double *tv = static_cast<const double *>(desc->table_data);
       const int64_t ntv = (int64_t)d.n_tables * d.n_entries * (d.table_cplx ? 2 : 1);

@@ -1,5 +1,5 @@
-// Mixed-precision list-1 evaluation on the tensor cores (tcgen05, BF16 digits,
-// exact FP32 partial products, FP64 final sums).
+// Mixed-precision list-1 evaluation on the tensor cores (tcgen05, FP16 digits,
+// exact FP32 partial products, exact integer sums, one rounding to FP64).
 //
 // Formulation.  For a target box T and right-hand side r,
 //   y[T, t, r] = sum over list-1 pairs (T, S) with key k = (table level, case)
@@ -10,18 +10,21 @@
 // (M = 128 rows, N = target points of a column chunk, K = source points in
 // chunks of <= 64).
 //
-// Exactness (an Ozaki-type split).  A (the blocks, per plan) and x' (per call)
-// are written in fixed point against a global power-of-two scale and split
-// into ND = 5 signed 8-bit digits, each held exactly in BF16.  A product of
-// one digit pair over K <= 64 is an integer below 64*255^2 < 2^22, exact in the
-// FP32 accumulator.  Digit pairs (i, j) of weight 2^(-8(i+j)) with i + j <= 4
-// (the leading 32 bits) get their own TMEM accumulator, re-initialised per key
-// chunk and read after every key chunk into int32 registers (one FADD with
-// 1.5 * 2^23 turns the exact float into its integer bits); pairs with
-// i + j = 5, 6 accumulate across keys in FP32 TMEM (their rounding is below
-// 2^-40 of the result).  The integer diagonals and the two FP32 tails are
-// combined in FP64 once per output.
-#include <cuda_bf16.h>
+// Exactness (an Ozaki-type split).  The table blocks (per plan) and x' (per
+// call) are written in fixed point against per-plan / per-rhs power-of-two
+// scales: table values as 40-bit magnitudes, densities as 39-bit magnitudes,
+// each split into 5 base-256 digits carrying the value's sign (|digit| <= 255,
+// the densities' top digit <= 127), held exactly in FP16.  Densities are
+// stored as bytes (sign in bit 7 of the top digit) and expanded to FP16 in
+// shared memory.  A product of one digit pair summed over K <= 64 source
+// points is an integer below 2^22, exact in the FP32 accumulator; the pairs
+// of one diagonal i + j <= 4 together stay below 2^24.  Those diagonals (the
+// leading 32 bits) get their own TMEM accumulator, re-initialised per K round
+// and read after every round into int64 registers (one FADD with 1.5 * 2^23
+// turns the exact d = 2 float into its integer bits); diagonals i + j = 5, 6
+// accumulate across rounds in FP32 TMEM (their rounding is below 2^-40 of the
+// result).  Each output's sum is then one exact integer, rounded once to FP64.
+#include <cuda_fp16.h>
 
 #include "vl1_internal.cuh"
 #include "vl1_mixed.cuh"
@@ -36,25 +39,25 @@ constexpr int kMagicBits = 0x4B400000;
 
 // ----------------------------------------------------------------- helpers
 
-// |v| as a fixed-point integer m with v = sign * 2^(e - 40) * m, m < 2^40,
-// rounded to nearest (ties to even); digits are the five base-256 digits of
-// m.  Integer arithmetic on the IEEE-754 fields only: it equals
-// round(ldexp(|v|, 40 - e)) without touching the FP64 pipe, which is narrow
-// on this GPU.
-__device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits]) {
+// |v| as a fixed-point integer m with |v| = 2^(e - BITS) * m, m < 2^BITS,
+// rounded to nearest (ties to even), from the IEEE-754 fields with integer
+// arithmetic only: it equals round(ldexp(|v|, BITS - e)) without touching the
+// FP64 pipe, which is narrow on this GPU.
+template <int BITS>
+__device__ __forceinline__ unsigned long long fixed_magnitude(double v, int e) {
   const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(v));
   const unsigned long long mag = bits & 0x7FFFFFFFFFFFFFFFull;
   const int ef = (int)(mag >> 52);
   // |v| = M * 2^ev
   const unsigned long long M = ef ? ((mag & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : mag;
   const int ev = ef ? ef - 1075 : -1074;
-  const long long sh = (long long)ev + kFixedBits - (long long)e;
+  const long long sh = (long long)ev + BITS - (long long)e;
   unsigned long long m;
   if (M == 0) {
     m = 0;
   } else if (sh >= 0) {
-    // saturates when |v| is not below 2^e (m >= 2^40 after the shift)
-    m = (sh > kFixedBits || M >= (1ull << (kFixedBits - sh))) ? (1ull << kFixedBits) : (M << sh);
+    // saturates when |v| is not below 2^e (m >= 2^BITS after the shift)
+    m = (sh > BITS || M >= (1ull << (BITS - sh))) ? (1ull << BITS) : (M << sh);
   } else if (sh < -63) {
     m = 0;
   } else {
@@ -64,13 +67,32 @@ __device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits
     const unsigned long long half = 1ull << (k - 1);
     m = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
   }
-  if (m >= (1ull << kFixedBits)) m = (1ull << kFixedBits) - 1;  // v at the scale bound
-  const int sgn = (bits >> 63) ? -1 : 1;
+  if (m >= (1ull << BITS)) m = (1ull << BITS) - 1;  // v at the scale bound
+  return m;
+}
+
+// table digits: v = sign * 2^(e - 40) * m, digits the five base-256 digits
+// of m, each carrying the sign of v (|digit| <= 255)
+__device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits]) {
+  const unsigned long long m = fixed_magnitude<kFixedBits>(v, e);
+  const int sgn = __double_as_longlong(v) < 0 ? -1 : 1;
 #pragma unroll
   for (int i = 0; i < kDigits; ++i) {
     const int shift = kFixedBits - kDigitBits * (i + 1);
     dig[i] = sgn * (int)((m >> shift) & 0xFF);
   }
+}
+
+// density digit bytes: v = sign * 2^(e - 39) * m, m < 2^39; byte 0 holds
+// the sign (bit 7) and the top 7 bits of m, bytes 1..4 the following
+// base-256 digits of m (magnitudes)
+__device__ __forceinline__ void density_digit_bytes(double v, int e, uint8_t (&byt)[kDigits]) {
+  const unsigned long long m = fixed_magnitude<kXFixedBits>(v, e);
+  const unsigned sgn = __double_as_longlong(v) < 0 ? 0x80u : 0u;
+  byt[0] = (uint8_t)(sgn | (unsigned)((m >> (kXFixedBits - 7)) & 0x7F));
+#pragma unroll
+  for (int i = 1; i < kDigits; ++i)
+    byt[i] = (uint8_t)((m >> (kXFixedBits - 7 - kDigitBits * i)) & 0xFF);
 }
 
 // exponent e with |v| < 2^e, as frexp returns it (-1074 for v == 0), from the
@@ -86,7 +108,7 @@ __device__ __forceinline__ int scale_exponent(double v) {
 
 // ------------------------------------------------- plan: A digit operands
 
-__global__ void build_adig_kernel(DevDesc d, MixedGeom g, __nv_bfloat16 *adig, int a_exp) {
+__global__ void build_adig_kernel(DevDesc d, MixedGeom g, __half *adig, int a_exp) {
   // element (key, kchunk, digit, n, k) of [key][kchunk][digit][NP][KC]
   // (swizzled K-major order inside each [NP][KC] tile, as in shared memory)
   const int64_t per_tile = (int64_t)g.np * g.kc;
@@ -116,7 +138,7 @@ __global__ void build_adig_kernel(DevDesc d, MixedGeom g, __nv_bfloat16 *adig, i
     fixed_digits(v, a_exp, dig);
     const int64_t tile = ((int64_t)key * g.n_kc + kc) * kDigits + digit;
     const uint32_t off = tc::kmajor_swizzled_offset(n, k, g.kc);  // bytes
-    adig[tile * per_tile + off / 2] = __int2bfloat16_rn(dig[digit]);
+    adig[tile * per_tile + off / 2] = __int2half_rn(dig[digit]);
   }
 }
 
@@ -180,21 +202,21 @@ __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const doubl
       if (s_max[r] > -1074) atomicMax(x_exp + r, s_max[r]);
 }
 
-// x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bf16 (kp * 5
-// values), so that the digits of one pipeline unit are kc-wide row pieces at
-// column (kchunk * 5 + digit) * kc; source points sit at their mode id.
+// x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bytes (kp * 5),
+// so that the digits of one pipeline unit are one contiguous 5 * kc-byte
+// piece at byte kchunk * 5 * kc; source points sit at their mode id.
 __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
-                                int nrhs, const int *x_exp, __nv_bfloat16 *xdig, int kp,
-                                int kc, vl1_status *st) {
+                                int nrhs, const int *x_exp, uint8_t *xdig, int kp, int kc,
+                                vl1_status *st) {
   const int64_t n = (int64_t)nboxes * nrhs;
-  const int row_elems = kp * kDigits;
+  const int row_bytes = kp * kDigits;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
        idx += warps) {
     const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-    __nv_bfloat16 *row = xdig + idx * row_elems;
-    for (int k = lane * 8; k < row_elems; k += 32 * 8)
+    uint8_t *row = xdig + idx * row_bytes;
+    for (int k = lane * 16; k < row_bytes; k += 32 * 16)
       *reinterpret_cast<uint4 *>(row + k) = make_uint4(0u, 0u, 0u, 0u);
     __syncwarp();
     int cnt = tr.src_counts[b];
@@ -212,11 +234,11 @@ __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double 
         report(st, VL1_E_LAYOUT, b, -1 - s);
         continue;
       }
-      int dig[kDigits];
-      fixed_digits(sc * c[s], e, dig);
+      uint8_t byt[kDigits];
+      density_digit_bytes(sc * c[s], e, byt);
       const int base = (m / kc) * kDigits * kc + (m % kc);
 #pragma unroll
-      for (int i = 0; i < kDigits; ++i) row[base + i * kc] = __int2bfloat16_rn(dig[i]);
+      for (int i = 0; i < kDigits; ++i) row[base + i * kc] = byt[i];
     }
   }
 }
@@ -268,6 +290,32 @@ __global__ void disp_target_kernel(DevDesc d, TreeDev tr, int nrhs, const double
   }
 }
 
+// v * 2^k rounded once to FP64 (nearest, ties to even), with integer
+// operations only while the result is a normal number
+__device__ __forceinline__ double scaled_i64_to_double(long long v, int k) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long mag =
+      v < 0 ? (unsigned long long)(-(v + 1)) + 1ull : (unsigned long long)v;
+  const int lz = __clzll((long long)mag);
+  const unsigned long long m = mag << lz;   // leading one at bit 63
+  unsigned long long frac = m >> 11;        // 53 significant bits
+  const unsigned long long rem = m & 0x7FFull;
+  int ex = 63 - lz + k;                     // v * 2^k = (m / 2^63) * 2^ex
+  if (rem > 0x400ull || (rem == 0x400ull && (frac & 1ull))) {
+    ++frac;
+    if (frac == (1ull << 53)) {
+      frac >>= 1;
+      ++ex;
+    }
+  }
+  const int biased = ex + 1023;
+  if (biased >= 1 && biased <= 2046)
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)biased << 52) |
+                                            (frac & 0xFFFFFFFFFFFFFull)));
+  return ldexp((double)v, k);   // subnormal or overflowing results
+}
+
 // ---------------------------------------------------------- main kernel
 
 struct MixedParams {
@@ -275,9 +323,9 @@ struct MixedParams {
   MixedGeom g;
   int nrhs;
   vl1_mixed_schedule sched;
-  const __nv_bfloat16 *xdig;   // density digit rows [n_xrows][kp * 5]
+  const uint8_t *xdig;   // density digit bytes [n_xrows][kp * 5]
   int32_t n_xrows;
-  const __nv_bfloat16 *adig;
+  const __half *adig;
   const int *x_exp;
   int a_exp;
   const double *disp;  // [n_tgt_boxes * nrhs] (x2 complex) or nullptr
@@ -290,12 +338,12 @@ struct MixedParams {
 
 // Warp roles of mixed_kernel (warp index w):
 //   w <  8      producers: per pipeline unit, warp w gathers the density digit
-//               pieces of tile rows 16w .. 16w+15 with cp.async (consecutive
-//               lanes on consecutive 16-byte pieces of a row's 5 * kc digits,
-//               zero-filled for rows without a source box); each lane's
-//               copies arrive on full[stage] when they land.  Eight warps keep
-//               enough 16-byte requests in flight to cover the L2 latency of
-//               these scattered rows.
+//               bytes of tile rows 16w .. 16w+15 with cp.async (consecutive
+//               lanes on consecutive 16-byte pieces of a row's 5 * kc bytes,
+//               zero-filled for rows without a source box) into a staging
+//               ring, then expands them to FP16 digit planes in the stage and
+//               arrives on full[stage].  Eight warps keep enough requests in
+//               flight to cover the L2 latency of these scattered rows.
 //   w == 8      table loader (one lane): the five table digit tiles of the
 //               unit's key by bulk copies (TMA), counted on full[stage]
 //   w == 9      tensor-core issuer (one lane)
@@ -309,6 +357,7 @@ struct MixedParams {
 // multiplies density digit i by several table digits j at once; its output
 // column blocks land on consecutive diagonals i + j.
 constexpr int kStages = 3;
+constexpr int kStgDepth = 2;         // byte staging ring per producer warp
 constexpr uint32_t kExactCols = 3;   // accumulators per buffer
 constexpr int kProducerWarps = 8;
 constexpr int kRowsPerProducer = 128 / kProducerWarps;
@@ -423,8 +472,8 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      // producer lanes (cp.async arrivals) + the table copies' expect_tx
-      tc::mbar_init(&bars.full[s], 32 * kProducerWarps + 1);
+      // one arrival per producer warp + the table copies' expect_tx
+      tc::mbar_init(&bars.full[s], kProducerWarps + 1);
       tc::mbar_init(&bars.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -445,9 +494,17 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
 
   if (warp < kProducerWarps) {
     // ------------------------------------------------------------ producers
-    constexpr int NC16 = KC / 8;               // 16-byte pieces per digit row
-    constexpr int PPR = kDigits * NC16;        // pieces per row and unit
-    const int64_t row_elems = (int64_t)p.g.kp * kDigits;
+    // Per unit: gather the byte digits of this warp's 16 rows (5 * KC bytes
+    // per row, cp.async into a kStgDepth-deep staging ring), then, kStgDepth
+    // - 1 units behind, expand that unit's bytes to FP16 digit planes in the
+    // unit's pipeline stage.
+    constexpr int RB = kDigits * KC;           // bytes per row and unit
+    constexpr int PPR = RB / 16;               // 16-byte pieces per row and unit
+    constexpr int NH = KC / 16;                // 16-value halves per digit row
+    constexpr int LOOK = kStgDepth - 1;        // units gathered ahead of the expansion
+    const int64_t row_bytes = (int64_t)p.g.kp * kDigits;
+    uint8_t *stg = smem + (size_t)kStages * STAGE_BYTES +
+                   (size_t)warp * kStgDepth * kRowsPerProducer * RB;
     // lanes < kRowsPerProducer hold the source row of tile row my_row
     const int my_row = kRowsPerProducer * warp + (lane % kRowsPerProducer);
     // key id and this lane's source row, fetched one key ahead
@@ -456,6 +513,65 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
       nkey = p.sched.key_ids[k0];
       nxr = p.sched.key_xrow[(int64_t)k0 * 128 + my_row];
     }
+    // expand the staged bytes of unit v into stage v % kStages
+    auto expand = [&](int v) -> bool {
+      const int s = v % kStages;
+      const int use = v / kStages;
+      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) return false;
+      const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
+      uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
+      const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
+      for (int t = lane; t < kRowsPerProducer * NH; t += 32) {
+        const int rl = t / NH, h = t - (t / NH) * NH;
+        const uint8_t *src = sb + rl * RB + h * 16;
+        const uint4 top = *reinterpret_cast<const uint4 *>(src);
+        const uint32_t tw[4] = {top.x, top.y, top.z, top.w};
+        // sign masks of the FP16 pairs (values 4q + 0/1 and 4q + 2/3): the
+        // sign of a value is bit 7 of its top digit byte
+        uint32_t sg[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          sg[2 * q] = ((tw[q] << 8) & 0x8000u) | ((tw[q] << 16) & 0x80000000u);
+          sg[2 * q + 1] = ((tw[q] >> 8) & 0x8000u) | (tw[q] & 0x80000000u);
+        }
+        const int row = kRowsPerProducer * warp + rl;
+#pragma unroll
+        for (int dg = 0; dg < kDigits; ++dg) {
+          uint32_t w[4];
+          if (dg == 0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) w[q] = tw[q] & 0x7F7F7F7Fu;
+          } else {
+            const uint4 x4 = *reinterpret_cast<const uint4 *>(src + dg * KC);
+            w[0] = x4.x;
+            w[1] = x4.y;
+            w[2] = x4.z;
+            w[3] = x4.w;
+          }
+          // bytes (b0, b1) -> FP16 pair (1024 + b0, 1024 + b1) -> minus 1024:
+          // exact, two values per packed subtraction
+          uint32_t o[8];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            uint32_t lo = __byte_perm(w[q], 0x64646464u, 0x4140u);
+            uint32_t hi = __byte_perm(w[q], 0x64646464u, 0x4342u);
+            __half2 hlo = __hsub2(*reinterpret_cast<__half2 *>(&lo), k1024);
+            __half2 hhi = __hsub2(*reinterpret_cast<__half2 *>(&hi), k1024);
+            o[2 * q] = *reinterpret_cast<uint32_t *>(&hlo) | sg[2 * q];
+            o[2 * q + 1] = *reinterpret_cast<uint32_t *>(&hhi) | sg[2 * q + 1];
+          }
+          uint8_t *pl = xs + dg * XBYTES;
+          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16, KC)) =
+              make_uint4(o[0], o[1], o[2], o[3]);
+          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16 + 8, KC)) =
+              make_uint4(o[4], o[5], o[6], o[7]);
+        }
+      }
+      tc::fence_proxy_async_smem();   // generic writes -> tensor-core reads
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars.full[s]);
+      return true;
+    };
     int u = 0;
     bool aborted = false;
     for (int kidx = k0; kidx < k1 && !aborted; ++kidx) {
@@ -474,37 +590,34 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
         xr_lane = -1;
       }
       for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
-        const int s = u % kStages;
-        const int use = u / kStages;
-        if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) {
-          aborted = true;
-          break;
-        }
-        uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
-        // piece pc = it * 32 + lane of the warp's kRowsPerProducer * PPR
-        // pieces: row pc / PPR, piece q = pc % PPR = digit * NC16 + 16-byte column
-        int rl = lane / PPR, q = lane % PPR;
-        const int64_t col0 = (int64_t)kc * kDigits * KC;
-#pragma unroll 2
-        for (int it = 0; it < kRowsPerProducer * PPR / 32; ++it) {
+        // gather unit u: piece pc of the warp's rows -> row pc / PPR, piece pc % PPR
+        uint8_t *sb = stg + (u % kStgDepth) * kRowsPerProducer * RB;
+#pragma unroll
+        for (int it = 0; it < (kRowsPerProducer * PPR + 31) / 32; ++it) {
+          const int pc = it * 32 + lane;
+          const int rl = min(pc / PPR, kRowsPerProducer - 1), q = pc - (pc / PPR) * PPR;
           const int xr = __shfl_sync(0xffffffffu, xr_lane, rl);
-          const int dg = q / NC16, c = q - dg * NC16;
-          uint8_t *dst = xs + dg * XBYTES +
-                         tc::kmajor_swizzled_offset(kRowsPerProducer * warp + rl, c * 8, KC);
-          const bool have = xr >= 0;
-          const __nv_bfloat16 *src =
-              p.xdig + (have ? (int64_t)xr * row_elems + col0 + q * 8 : 0);
-          tc::cp_async16_zfill(dst, src, have ? 16u : 0u);
-          q += 32 % PPR;
-          rl += 32 / PPR;
-          if (q >= PPR) {
-            q -= PPR;
-            ++rl;
+          if (pc < kRowsPerProducer * PPR) {
+            const bool have = xr >= 0;
+            const uint8_t *src =
+                p.xdig + (have ? (int64_t)xr * row_bytes + (int64_t)kc * RB + q * 16 : 0);
+            tc::cp_async16_zfill(sb + rl * RB + q * 16, src, have ? 16u : 0u);
           }
         }
-        tc::cp_async_arrive_noinc(&bars.full[s]);
+        tc::cp_async_commit();
+        if (u >= LOOK) {
+          tc::cp_async_wait_group<LOOK>();   // unit u - LOOK landed (this lane's pieces)
+          __syncwarp();
+          if (!expand(u - LOOK)) {
+            aborted = true;
+            break;
+          }
+        }
       }
     }
+    tc::cp_async_wait_all();
+    __syncwarp();
+    for (int v = u - LOOK < 0 ? 0 : u - LOOK; v < u && !aborted; ++v) aborted = !expand(v);
   } else if (warp == kLoaderWarp) {
     // ---------------------------------------------------------- table loader
     if (lane == 0) {
@@ -573,7 +686,7 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
                                           : (g == 3 && u == 0 && kk == 0);
               const uint64_t ad = xd + (((uint32_t)(gr.i - 1) * XBYTES + kk * 32u) >> 4);
               const uint64_t bd = adsc + (((uint32_t)(gr.j0 - 1) * ABYTES + kk * 32u) >> 4);
-              tc::mma_bf16(col, ad, bd, tc::idesc_bf16_f32(128, NCH * gr.nb), first ? 0u : 1u);
+              tc::mma_f16(col, ad, bd, tc::idesc_f16_f32(128, NCH * gr.nb), first ? 0u : 1u);
             }
           }
           tc::mma_commit(&bars.empty[s]);   // stage free once these products finish
@@ -622,58 +735,71 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
 #pragma unroll
       for (int c = 0; c < 16; ++c) acc[c] += (long long)__float2int_rn(__uint_as_float(r16[c]));
     }
-    // ---- park the exact sums (one int64 per output, units of 2^(e-32)) and
-    // the FP32 tails (units of 2^(e-40)) in the idle pipeline buffers
+    // ---- park one int64 per output: the sum of digit products in units of
+    // 2^32 (integer diagonals 2..4, weights 2^64..2^48, shifted by 16, plus
+    // the FP32 tails d5, d6 of weights 2^40, 2^32 rounded to that unit)
     if (ok && !s_abort) {
-      long long *s_comb = reinterpret_cast<long long *>(smem);
-      float *s_tail = reinterpret_cast<float *>(s_comb + 128 * NCH);
+      long long *s_tot = reinterpret_cast<long long *>(smem);
       const uint32_t col = tbase + lane_off + kExactCols * NCH + cb * RC;
 #pragma unroll
-      for (int c = 0; c < 16; ++c) s_comb[row * NCH + cb * RC + c] = acc[c];
-      uint32_t r16[16];
-      float tl[16];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) tl[c] = 0.0f;
+      for (int c = 0; c < 16; ++c) acc[c] <<= 16;
       if (n_rounds > 0) {
-        tc::tmem_ld16(col, r16);
+        uint32_t r16[16];
+        tc::tmem_ld16(col, r16);                 // d5, weight 2^40
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) tl[c] = __uint_as_float(r16[c]);
-        tc::tmem_ld16(col + NCH, r16);
+        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]) * 256.0f);
+        tc::tmem_ld16(col + NCH, r16);           // d6, weight 2^32
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) tl[c] += __uint_as_float(r16[c]) * (1.0f / 256.0f);
+        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]));
       }
 #pragma unroll
-      for (int c = 0; c < 16; ++c) s_tail[row * NCH + cb * RC + c] = tl[c];
+      for (int c = 0; c < 16; ++c) s_tot[row * NCH + cb * RC + c] = acc[c];
     }
   }
 
-  // ---- all warps: FP64 combination and coalesced writes (a row's outputs
-  // are the consecutive target points of one box).  A split tile's parts
-  // store their exact partial sums; the part that finishes last adds them in
-  // slot order (integers exactly, tails in FP64) and writes the results.
+  // ---- all warps: final values and coalesced writes (a row's outputs are
+  // the consecutive target points of one box).  A split tile's parts store
+  // their exact partial sums; the part that finishes last adds them (exactly,
+  // in int64) and writes the results.  The one rounding to FP64 is done with
+  // integer operations (the FP64 pipe is narrow on this GPU).
   tc::tc_fence_before();
   __syncthreads();
   __shared__ int s_last;
-  const long long *comb_src = reinterpret_cast<const long long *>(smem);
-  const float *tail_src = reinterpret_cast<const float *>(comb_src + 128 * NCH);
+  __shared__ long long s_obase[128];   // result index of the row's first target point
+  __shared__ int s_ocnt[128];          // target points of the row's box (0: empty row)
+  __shared__ int s_oexp[128];          // an output is (parked sum) * 2^s_oexp
+  if (tid < 128) {
+    const int v = s_rows[tid];
+    int cnt = 0, ex = 0;
+    long long ob = 0;
+    if (v >= 0) {
+      const int j = v / p.nrhs, r = v - (v / p.nrhs) * p.nrhs;
+      const int tbox = p.target_boxes[j];
+      cnt = min(p.tgt_counts[tbox], p.d.nq);
+      ob = (long long)r * p.n_particles + p.tgt_starts[tbox];
+      // table values are m_a 2^(a_exp - kFixedBits), densities
+      // m_x 2^(x_exp - kXFixedBits); the parked sums count units of 2^32 of
+      // m_a m_x
+      ex = p.a_exp + p.x_exp[r] - (kFixedBits + kXFixedBits) + 32;
+    }
+    s_obase[tid] = ob;
+    s_ocnt[tid] = cnt;
+    s_oexp[tid] = ex;
+  }
+  const long long *tot_src = reinterpret_cast<const long long *>(smem);
   bool write = !s_abort;
   const uint8_t *g_parts = nullptr;   // slot region of part 0 of a split tile
+  const int64_t slot_bytes = (int64_t)128 * NCH * 8;
+  const int64_t part_stride = (int64_t)gridDim.y * slot_bytes;
   if (item.split >= 0) {
-    const int64_t slot_bytes = (int64_t)128 * NCH * 12;
     uint8_t *base = static_cast<uint8_t *>(p.sched.split_partials) +
                     ((int64_t)(item.slot - item.part) * gridDim.y + chunk) * slot_bytes;
-    const int64_t part_stride = (int64_t)gridDim.y * slot_bytes;
     g_parts = base;
     if (!s_abort) {
-      long long *my_comb = reinterpret_cast<long long *>(base + item.part * part_stride);
-      float *my_tail = reinterpret_cast<float *>(base + item.part * part_stride +
-                                                 (int64_t)128 * NCH * 8);
-      for (int i = tid; i < 128 * NCH; i += blockDim.x) {
-        my_comb[i] = comb_src[i];
-        my_tail[i] = tail_src[i];
-      }
+      long long *mine = reinterpret_cast<long long *>(base + item.part * part_stride);
+      for (int i = tid; i < 128 * NCH; i += blockDim.x) mine[i] = tot_src[i];
     }
     __threadfence();
     __syncthreads();
@@ -684,45 +810,33 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
     __syncthreads();
     write = write && s_last;
     if (write) __threadfence();
+  } else {
+    __syncthreads();
   }
   if (write) {
     const bool oc = p.d.table_cplx;
-    const int ncols = oc ? 2 * p.d.nq : p.d.nq;
-    const int64_t part_stride_e = (int64_t)gridDim.y * 128 * NCH * 12;
     for (int it = tid; it < 128 * NCH; it += blockDim.x) {
       const int rw_ = it / NCH, cc = it - rw_ * NCH;
-      const int v = s_rows[rw_];
-      const int n = chunk * NCH + cc;
-      if (v < 0 || n >= ncols) continue;
-      const int j = v / p.nrhs, r = v - (v / p.nrhs) * p.nrhs;
-      const int tbox = p.target_boxes[j];
-      int t = n, part = 0;
-      if (oc && n >= p.d.nq) {
-        t = n - p.d.nq;
+      int t = chunk * NCH + cc, part = 0;
+      if (oc && t >= p.d.nq) {
+        t -= p.d.nq;
         part = 1;
       }
-      if (t >= min(p.tgt_counts[tbox], p.d.nq)) continue;
-      long long comb;
-      double tail;
+      if (t >= s_ocnt[rw_]) continue;   // also empty rows and padding columns
+      long long tot;
       if (item.split >= 0) {
-        comb = 0;
-        tail = 0.0;
-        for (int q = 0; q < item.nparts; ++q) {
-          const uint8_t *pb = g_parts + q * part_stride_e;
-          comb += __ldcg(reinterpret_cast<const long long *>(pb) + it);
-          tail += (double)__ldcg(reinterpret_cast<const float *>(pb + (int64_t)128 * NCH * 8) + it);
-        }
+        tot = 0;
+        for (int q = 0; q < item.nparts; ++q)
+          tot += __ldcg(reinterpret_cast<const long long *>(g_parts + q * part_stride) + it);
       } else {
-        comb = comb_src[it];
-        tail = (double)tail_src[it];
+        tot = tot_src[it];
       }
-      const int e = p.a_exp + p.x_exp[r];
-      double y = fma(tail, ldexp(1.0, e - 40), (double)comb * ldexp(1.0, e - 32));
+      double y = scaled_i64_to_double(tot, s_oexp[rw_]);
       if (p.disp) {
-        const int64_t di = (int64_t)j * p.nrhs + r;
+        const int64_t di = s_rows[rw_];   // j * nrhs + r
         y += oc ? p.disp[2 * di + part] : p.disp[di];
       }
-      const int64_t o = (int64_t)r * p.n_particles + p.tgt_starts[tbox] + t;
+      const int64_t o = s_obase[rw_] + t;
       if (oc)
         p.result[2 * o + part] = y;
       else
@@ -796,7 +910,7 @@ int64_t mixed_workspace_bytes(const vl1_plan *plan, int64_t nboxes, int64_t n_tg
   const int cv = plan->d.table_cplx ? 2 : 1;
   int64_t b = 0;
   b += ((int64_t)nrhs * 4 + 255) / 256 * 256;                   // x exponents
-  b += (nboxes * nrhs * g.kp * kDigits * 2 + 255) / 256 * 256;  // x digits
+  b += (nboxes * nrhs * g.kp * kDigits + 255) / 256 * 256;  // x digit bytes
   if (plan->d.disp_kind == VL1_DISP_LOG2D) {
     b += (nboxes * nrhs * cv * 8 + 255) / 256 * 256;            // per-box displacement
     b += (n_tgt_boxes * nrhs * cv * 8 + 255) / 256 * 256;       // per-target displacement
@@ -827,14 +941,14 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   int *x_exp = reinterpret_cast<int *>(w);
   const int64_t exp_bytes = ((int64_t)nrhs * 4 + 255) / 256 * 256;
   w += exp_bytes;
-  __nv_bfloat16 *xdig = reinterpret_cast<__nv_bfloat16 *>(w);
+  uint8_t *xdig = w;
   const int64_t n_xrows = nboxes * nrhs;
   if (n_xrows >= INT32_MAX) {
     set_error("mixed path: %lld density rows exceed the 32-bit row index",
               (long long)n_xrows);
     return VL1_E_UNSUPPORTED;
   }
-  w += (n_xrows * g.kp * kDigits * 2 + 255) / 256 * 256;
+  w += (n_xrows * g.kp * kDigits + 255) / 256 * 256;
   double *wbox = nullptr, *disp = nullptr;
   if (d.disp_kind == VL1_DISP_LOG2D) {
     wbox = reinterpret_cast<double *>(w);
@@ -876,8 +990,9 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.n_particles = tree.n_particles;
   mp.result = result;
   mp.st = plan->status;
-  const size_t pipe = (size_t)kStages * kDigits * (128 + g.nch) * g.kc * 2;
-  const size_t park = (size_t)128 * g.nch * 12;   // int64 sums + float tails
+  const size_t pipe = (size_t)kStages * kDigits * (128 + g.nch) * g.kc * 2 +
+                      (size_t)kProducerWarps * kStgDepth * kRowsPerProducer * kDigits * g.kc;
+  const size_t park = (size_t)128 * g.nch * 8;   // int64 sums
   const size_t smem = (pipe > park ? pipe : park) + 1024;
   dim3 grid(sched.n_items > 0 ? sched.n_items : sched.n_tiles, g.np / g.nch);
   const int threads = 32 * (kReadWarp0 + 4 * (g.nch / 16));

@@ -1,16 +1,17 @@
 // Declarations of the mixed-precision (tensor-core) list-1 path.
 #pragma once
 
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 #include "vl1.h"
 
 namespace vl1 {
 
-constexpr int kDigits = 5;         // signed 8-bit digits per operand
+constexpr int kDigits = 5;         // 8-bit digits per operand (held exactly in FP16)
 constexpr int kDigitBits = 8;
-constexpr int kFixedBits = kDigits * kDigitBits;  // 40-bit fixed point
+constexpr int kFixedBits = kDigits * kDigitBits;  // table: 40-bit fixed point
+constexpr int kXFixedBits = kFixedBits - 1;        // densities: 39 bits + sign
 
 // Operand geometry of one plan.
 struct MixedGeom {
@@ -24,7 +25,7 @@ struct MixedGeom {
 struct MixedPlan {
   MixedGeom geom;
   int a_exp;                // 2^a_exp > max |table value|
-  __nv_bfloat16 *adig;      // [key][kchunk][digit][np][kc], core-matrix K-major tiles
+  __half *adig;             // [key][kchunk][digit][np][kc] FP16 digits, swizzled K-major tiles
   int64_t adig_elems;
 };
 

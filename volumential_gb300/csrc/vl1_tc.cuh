@@ -110,6 +110,11 @@ __device__ __forceinline__ void cp_async_arrive_noinc(uint64_t *bar) {
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
+// wait until at most N of this thread's committed cp.async groups are pending
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
@@ -221,8 +226,16 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n) {
          | ((uint32_t)(m >> 4) << 24);      // M / 16
 }
 
-// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+// Instruction descriptor of kind::f16: F16 x F16 -> FP32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int m, int n) {
+  return (1u << 4)                          // D format: F32 (A, B format 0: F16)
+         | ((uint32_t)(n >> 3) << 17)       // N / 8
+         | ((uint32_t)(m >> 4) << 24);      // M / 16
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread (kind::f16: both
+// operands F16 or both BF16, as the instruction descriptor says)
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
                                          uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
