@@ -406,6 +406,14 @@ def reference_arm(args):
     return 0
 
 
+def tensor_executed(r, ms_per_step, bf16_peak):
+    g = r["geometry"]
+    flops = 2.0 * 15 * 128 * r["schedule"]["tile_keys"] * g["kp"] * g["np"]
+    tflops = flops / (ms_per_step / 1e3) / 1e12
+    return {"flops_per_step": flops, "tflops": tflops, "frac_of_bf16_peak": tflops / bf16_peak,
+            "note": "FP16 digit-pair MMAs (M=128 rows x N=np x K=kp) per tile key"}
+
+
 def gb300_main(args):
     world, rank, _ = dist_env()
     r = gpu_arm(args)
@@ -474,6 +482,10 @@ def gb300_main(args):
         "paths": {"plain_fp64": plain, "mixed": dict(mixed, rel_l2_vs_fp64=r["mixed_err"]),
                   "speedup_mixed_over_plain": plain["ms_per_step"] / mixed["ms_per_step"]},
         "mixed_schedule": r["schedule"], "mixed_geometry": r["geometry"],
+        # digit products the tensor pipe executes per step (15 FP16 digit
+        # pairs per source/target point pair of every tile row, padding
+        # included), next to the FP64-equivalent algorithmic flops above
+        "tensor_executed": tensor_executed(r, mixed["ms_per_step"], bf16),
         "clocks": r["clocks"],
         "gpu_launches": K * (1 if r["headline"] == "plain" else (3 if w.dim == 3 else 5)),
         "plan_device_bytes": r["plan_bytes"],
