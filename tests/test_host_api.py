@@ -396,3 +396,61 @@ def test_mixed_work_items_cover_every_key_once():
             assert len({t for _, _, t in ps}) == 1
             base = ps[0][1]
             assert [s for _, s, _ in ps] == list(range(base, base + len(ps)))
+
+
+def _tile_schedule_by_loop(keys, starts, lists, n_tb, K, nrhs):
+    """Straightforward per-tile restatement of the tile schedule (test only)."""
+    tb_of_pair = np.repeat(np.arange(n_tb), np.diff(starts))
+    mask = np.zeros((n_tb, K), dtype=bool)
+    mask[tb_of_pair, keys] = True
+    _, sig = np.unique(np.packbits(mask, axis=1), axis=0, return_inverse=True)
+    order = np.lexsort((np.arange(n_tb), sig.ravel()))
+    rows = (order[:, None] * nrhs + np.arange(nrhs)[None, :]).ravel()
+    n_tiles = (len(rows) + 127) // 128
+    tile_rows = np.full(n_tiles * 128, -1)
+    tile_rows[:len(rows)] = rows
+    tile_rows = tile_rows.reshape(n_tiles, 128)
+    src = {(int(tb_of_pair[p]), int(keys[p])): int(lists[p]) for p in range(len(keys))}
+    tiles = []
+    for t in range(n_tiles):
+        js = [int(v) // nrhs for v in tile_rows[t] if v >= 0]
+        tkeys = sorted({int(keys[p]) for j in set(js) for p in range(starts[j], starts[j + 1])})
+        xr = []
+        for k in tkeys:
+            row = []
+            for v in tile_rows[t]:
+                s_ = src.get((int(v) // nrhs, k)) if v >= 0 else None
+                row.append(-1 if s_ is None else s_ * nrhs + int(v) % nrhs)
+            xr.append(row)
+        tiles.append((tkeys, xr))
+    lpt = sorted(range(n_tiles), key=lambda t: -len(tiles[t][0]))
+    key_start, key_ids, xrow = [0], [], []
+    for t in lpt:
+        key_ids += tiles[t][0]
+        xrow += tiles[t][1]
+        key_start.append(len(key_ids))
+    return tile_rows[lpt], np.array(key_start), np.array(key_ids), np.array(xrow).reshape(-1, 128)
+
+
+@pytest.mark.parametrize("nrhs", [1, 3, 130])
+def test_tile_schedule_matches_per_tile_restatement(nrhs):
+    from volumential_gb300.batched import MixedSchedule
+
+    rng = np.random.default_rng(11 + nrhs)
+    n_tb, K = 300, 40
+    deg = rng.integers(0, 9, size=n_tb)
+    starts = np.concatenate([[0], np.cumsum(deg)])
+    keys = np.concatenate([rng.choice(K, size=d, replace=False) for d in deg]).astype(np.int64)
+    lists = rng.integers(0, 500, size=len(keys)).astype(np.int64)
+    got = MixedSchedule.tile_schedule(keys, starts, lists, n_tb, K, nrhs)
+    want = _tile_schedule_by_loop(keys, starts, lists, n_tb, K, nrhs)
+    for g, w in zip(got, want):
+        assert np.array_equal(np.asarray(g), np.asarray(w))
+
+
+def test_tile_schedule_rejects_two_sources_with_one_case():
+    from volumential_gb300.batched import MixedSchedule
+
+    starts = np.array([0, 2])
+    with pytest.raises(RuntimeError):
+        MixedSchedule.tile_schedule(np.array([3, 3]), starts, np.array([1, 2]), 1, 5, 1)

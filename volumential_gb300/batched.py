@@ -55,76 +55,19 @@ class MixedSchedule:
         lists = keep["lists"].cpu().numpy().astype(np.int64)
         self._check_modes(keep, plan.nq)
 
-        tb_of_pair = np.repeat(np.arange(n_tb, dtype=np.int64), np.diff(starts))
-        # target boxes ordered by key signature (bitmask of keys), then index
-        if n_tb:
-            mask = np.zeros((n_tb, n_keys_total), dtype=bool)
-            mask[tb_of_pair, keys] = True
-            packed = np.packbits(mask, axis=1)
-            _, sig = np.unique(packed, axis=0, return_inverse=True)
-            order = np.lexsort((np.arange(n_tb), sig.ravel()))
-        else:
-            order = np.zeros(0, dtype=np.int64)
-        rows = (order[:, None] * self.nrhs + np.arange(self.nrhs)[None, :]).ravel()
-        n_tiles = (len(rows) + ROWS_PER_TILE - 1) // ROWS_PER_TILE
-        tile_rows = np.full(n_tiles * ROWS_PER_TILE, -1, dtype=np.int64)
-        tile_rows[:len(rows)] = rows
-        tile_rows = tile_rows.reshape(n_tiles, ROWS_PER_TILE)
-
-        # (box, key) -> source box lookup
-        comb = tb_of_pair * n_keys_total + keys
-        srt = np.argsort(comb, kind="stable")
-        comb_sorted = comb[srt]
-        src_sorted = lists[srt]
-        if len(comb_sorted) > 1 and np.any(comb_sorted[1:] == comb_sorted[:-1]):
-            raise RuntimeError("a target box has two list-1 source boxes with the same case")
-
-        tile_key_ids = []
-        tile_key_xrow = []
-        for t in range(n_tiles):
-            tr_ = tile_rows[t]
-            valid = tr_ >= 0
-            js = np.where(valid, tr_ // self.nrhs, 0)
-            rs = np.where(valid, tr_ % self.nrhs, 0)
-            boxes = np.unique(js[valid])
-            pair_idx = np.concatenate([np.arange(starts[j], starts[j + 1]) for j in boxes]) \
-                if len(boxes) else np.zeros(0, dtype=np.int64)
-            tkeys = np.unique(keys[pair_idx])
-            xrs = []
-            for k in tkeys:
-                q = js * n_keys_total + k
-                pos = np.searchsorted(comb_sorted, q)
-                pos = np.minimum(pos, len(comb_sorted) - 1)
-                hit = valid & (comb_sorted[pos] == q)
-                s_box = src_sorted[pos]
-                xrs.append(np.where(hit, s_box * self.nrhs + rs, -1))
-            tile_key_ids.append(tkeys)
-            tile_key_xrow.append(xrs)
-
-        # longest tiles first: CTAs start in grid order, so the tiles with the
-        # most keys are not left for the last wave
-        lpt = np.argsort(-np.asarray([len(k) for k in tile_key_ids], dtype=np.int64),
-                         kind="stable")
-        tile_rows = tile_rows[lpt]
-        key_start = [0]
-        key_ids = []
-        key_xrow = []
-        for t in lpt:
-            key_ids.extend(int(k) for k in tile_key_ids[t])
-            key_xrow.extend(tile_key_xrow[t])
-            key_start.append(len(key_ids))
+        tile_rows, key_start, key_ids, xrow = self.tile_schedule(
+            keys, starts, lists, n_tb, n_keys_total, self.nrhs)
+        n_tiles = len(tile_rows)
 
         self.n_tiles = n_tiles
-        self.n_tile_keys = len(key_ids)
+        self.n_tile_keys = int(len(key_ids))
         self.mean_keys_per_tile = self.n_tile_keys / max(n_tiles, 1)
-        i32 = torch.int32
         self.tile_rows = torch.from_numpy(tile_rows.ravel().astype(np.int32)).to("cuda")
-        self.tile_key_start = torch.from_numpy(np.asarray(key_start, dtype=np.int32)).to("cuda")
-        self.key_ids = torch.from_numpy(np.asarray(key_ids, dtype=np.int32)
-                                        if key_ids else np.zeros(1, np.int32)).to("cuda")
-        self.key_xrow = torch.from_numpy(
-            np.concatenate(key_xrow).astype(np.int32) if key_xrow
-            else np.zeros(ROWS_PER_TILE, np.int32)).to("cuda")
+        self.tile_key_start = torch.from_numpy(key_start.astype(np.int32)).to("cuda")
+        self.key_ids = torch.from_numpy(key_ids.astype(np.int32) if len(key_ids)
+                                        else np.zeros(1, np.int32)).to("cuda")
+        self.key_xrow = torch.from_numpy(xrow.ravel() if len(key_ids)
+                                         else np.zeros(ROWS_PER_TILE, np.int32)).to("cuda")
         geo = plan.mixed_geometry()
         n_chunks = geo["np"] // geo["nch"]
         items, n_splits, n_slots = self._work_items(np.asarray(key_start, dtype=np.int64),
@@ -155,7 +98,74 @@ class MixedSchedule:
         if ws < 0:
             raise RuntimeError("vl1_mixed_workspace_bytes failed")
         self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
-        del i32
+
+    @staticmethod
+    def tile_schedule(keys, starts, lists, n_tb, n_keys_total, nrhs):
+        """Tiles of 128 (target box, rhs) rows and their (tile, key) entries.
+
+        Target boxes are ordered by key signature (the set of (table level,
+        case) keys of their list-1 pairs) so that a tile's rows share keys;
+        tiles are ordered by key count, longest first.  Returns ``tile_rows``
+        [n_tiles, 128] (row j * nrhs + r, or -1), ``key_start`` [n_tiles + 1],
+        ``key_ids`` [n_entries] and ``xrow`` [n_entries, 128] (density row
+        S * nrhs + r of the row's list-1 source box S for that key, or -1).
+        """
+        nnz = len(keys)
+        K = n_keys_total
+        tb_of_pair = np.repeat(np.arange(n_tb, dtype=np.int64), np.diff(starts))
+        # target boxes ordered by key signature (bitmask of keys), then index
+        if n_tb:
+            mask = np.zeros((n_tb, K), dtype=bool)
+            mask[tb_of_pair, keys] = True
+            packed = np.packbits(mask, axis=1)
+            _, sig = np.unique(packed, axis=0, return_inverse=True)
+            order = np.lexsort((np.arange(n_tb), sig.ravel()))
+        else:
+            order = np.zeros(0, dtype=np.int64)
+        n_rows = n_tb * nrhs
+        n_tiles = (n_rows + ROWS_PER_TILE - 1) // ROWS_PER_TILE
+        tile_rows = np.full(n_tiles * ROWS_PER_TILE, -1, dtype=np.int64)
+        tile_rows[:n_rows] = (order[:, None] * nrhs + np.arange(nrhs)[None, :]).ravel()
+        pos = np.empty(n_tb, dtype=np.int64)      # rank of each box in the row order
+        pos[order] = np.arange(n_tb, dtype=np.int64)
+
+        # (box, key) pairs must be unique: one list-1 source box per case
+        comb = tb_of_pair * K + keys
+        if len(comb) > 1:
+            cs = np.sort(comb)
+            if np.any(cs[1:] == cs[:-1]):
+                raise RuntimeError("a target box has two list-1 source boxes with the same case")
+
+        # (tile, key) entries: every tile that holds a row of a pair's target box
+        first_tile = (pos * nrhs) // ROWS_PER_TILE
+        span = (pos * nrhs + nrhs - 1) // ROWS_PER_TILE - first_tile + 1
+        sp = span[tb_of_pair]
+        rep = np.repeat(np.arange(nnz, dtype=np.int64), sp)
+        offs = np.arange(len(rep), dtype=np.int64) - np.repeat(np.cumsum(sp) - sp, sp)
+        codes = np.unique((first_tile[tb_of_pair][rep] + offs) * K + keys[rep])
+        ent_tile = codes // K
+        ent_key = codes % K
+        n_keys_per_tile = np.bincount(ent_tile, minlength=n_tiles)
+        # longest tiles first (CTAs start in grid order)
+        lpt = np.argsort(-n_keys_per_tile, kind="stable")
+        inv_lpt = np.empty(n_tiles, dtype=np.int64)
+        inv_lpt[lpt] = np.arange(n_tiles, dtype=np.int64)
+        new_tile = inv_lpt[ent_tile]
+        o2 = np.lexsort((ent_key, new_tile))
+        inv_o2 = np.empty(len(codes), dtype=np.int64)
+        inv_o2[o2] = np.arange(len(codes), dtype=np.int64)
+        key_ids = ent_key[o2]
+        key_start = np.concatenate([[0], np.cumsum(np.bincount(new_tile, minlength=n_tiles))])
+        tile_rows = tile_rows.reshape(n_tiles, ROWS_PER_TILE)[lpt]
+
+        # density row of every (entry, tile slot): source box * nrhs + rhs, or -1
+        xrow = np.full((len(codes), ROWS_PER_TILE), -1, dtype=np.int32)
+        base_pos = pos[tb_of_pair] * nrhs
+        for r in range(nrhs):
+            P = base_pos + r
+            e = inv_o2[np.searchsorted(codes, (P // ROWS_PER_TILE) * K + keys)]
+            xrow[e, P % ROWS_PER_TILE] = (lists * nrhs + r).astype(np.int32)
+        return tile_rows, key_start, key_ids, xrow
 
     # cost model of one work item in pipeline units of one key: CTA start-up
     # and result write-back, and the extra partial-sum traffic of a split part
