@@ -388,6 +388,19 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_addr(bar)) : "memory");
 }
 
+// A work item of a batch launch: one problem's tile (or key range of it) and
+// output column chunk.
+struct BatchItem {
+  int32_t problem, chunk;
+  vl1_mixed_item item;
+};
+struct BatchLaunch {
+  const MixedParams *probs;   // [n_problems]
+  const BatchItem *items;     // [n_items], launched in this order
+  int n_items;
+  int *queue;                 // next item to take; zero before the launch
+};
+
 // One group of MMAs: density digit i times the stacked table digits
 // j0 .. j0 + nb - 1, into nb consecutive diagonal blocks.
 struct MmaGroup {
@@ -399,9 +412,14 @@ __device__ constexpr MmaGroup kGroups[8] = {{1, 1, 3, 1}, {2, 1, 2, 1}, {3, 1, 1
                                             {1, 4, 2, 0}, {2, 3, 2, 0}, {3, 2, 2, 0},
                                             {4, 1, 2, 0}, {5, 1, 1, 0}};
 
-template <int NCH, int KC>
+// MULTI == false: one work item per CTA (blockIdx.x; column chunk blockIdx.y)
+// of the single problem p1.  MULTI == true: a persistent launch over the
+// items of several problems, each CTA taking the next item from bl.queue; the
+// item's problem parameters are copied to shared memory, and the pipeline
+// barriers keep their phases across items (CTA-wide unit / round counters).
+template <int NCH, int KC, bool MULTI>
 __global__ void __launch_bounds__(32 * (kReadWarp0 + 4 * (NCH / 16)), 1)
-mixed_kernel(const __grid_constant__ MixedParams p) {
+mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ BatchLaunch bl) {
   constexpr int RC = 16;                            // columns per readout warp
   constexpr int NREAD = 4 * (NCH / RC);             // readout warps
   // TMEM: [buffer 0: 3 x NCH][tail d5][tail d6][buffer 1: 3 x NCH]
@@ -418,58 +436,14 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
   __shared__ uint32_t tmem_base;
   __shared__ volatile int s_abort;
   __shared__ int s_rows[128];
+  __shared__ __align__(16) MixedParams s_p;   // MULTI: the current item's problem
+  __shared__ int s_next;
+  const MixedParams &p = MULTI ? s_p : p1;
 
-  const int chunk = blockIdx.y;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
 
-  // this CTA's work item: a tile, or a key range of a split tile
-  vl1_mixed_item item;
-  if (p.sched.n_items > 0) {
-    item = p.sched.items[blockIdx.x];
-  } else {
-    item.tile = blockIdx.x;
-    item.key_begin = p.sched.tile_key_start[blockIdx.x];
-    item.key_end = p.sched.tile_key_start[blockIdx.x + 1];
-    item.split = -1;
-    item.part = 0;
-    item.nparts = 1;
-    item.slot = -1;
-  }
-  const int tile = item.tile;
-  {
-    bool bad = tile < 0 || tile >= p.sched.n_tiles;
-    if (!bad) {
-      const int t0 = p.sched.tile_key_start[tile], t1 = p.sched.tile_key_start[tile + 1];
-      bad = item.key_begin < t0 || item.key_end > t1 || item.key_begin > item.key_end;
-    }
-    if (item.split >= 0)
-      bad = bad || item.split >= p.sched.n_splits || item.part < 0 ||
-            item.part >= item.nparts || item.slot - item.part < 0 ||
-            item.slot - item.part + item.nparts > p.sched.n_slots;
-    else
-      bad = bad || item.split != -1;
-    if (bad) {
-      if (tid == 0) report(p.st, VL1_E_ARG, blockIdx.x, -1);
-      return;   // uniform across the CTA, before any barrier or TMEM use
-    }
-  }
-
-  const int k0 = item.key_begin, k1 = item.key_end;
-  const int n_keys = k1 - k0;
-  const int upr = (p.g.kp < 64 ? p.g.kp : 64) / KC;   // units per round
-  const int rpk = (p.g.kp + 63) / 64;                  // rounds per key
-  const int n_rounds = n_keys * rpk;
-
-  if (tid < 128) {
-    int v = p.sched.tile_rows[(int64_t)tile * 128 + tid];
-    if (v >= (int64_t)p.n_tgt_boxes * p.nrhs) {
-      report(p.st, VL1_E_ARG, tile, tid);
-      v = -1;
-    }
-    s_rows[tid] = v;
-  }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
       // one arrival per producer warp + the table copies' expect_tx
@@ -491,6 +465,78 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tbase = tmem_base;
+
+  // pipeline units and K rounds this CTA has run in earlier items (stage and
+  // buffer phases continue across items)
+  int ubase = 0, rbase = 0;
+  for (int pass = 0;; ++pass) {
+  int wi;
+  if (MULTI) {
+    if (tid == 0) s_next = s_abort ? bl.n_items : atomicAdd(bl.queue, 1);
+    __syncthreads();
+    wi = s_next;
+    if (wi >= bl.n_items) break;
+    const uint64_t *src = reinterpret_cast<const uint64_t *>(bl.probs + bl.items[wi].problem);
+    for (int i = tid; i < (int)(sizeof(MixedParams) / 8); i += blockDim.x)
+      reinterpret_cast<uint64_t *>(&s_p)[i] = src[i];
+    __syncthreads();
+  } else {
+    if (pass > 0) break;
+    wi = blockIdx.x;
+  }
+  const int chunk = MULTI ? bl.items[wi].chunk : blockIdx.y;
+  const int n_chunks = p.g.np / NCH;
+
+  // this CTA's work item: a tile, or a key range of a split tile
+  vl1_mixed_item item;
+  if (MULTI) {
+    item = bl.items[wi].item;
+  } else if (p.sched.n_items > 0) {
+    item = p.sched.items[wi];
+  } else {
+    item.tile = wi;
+    item.key_begin = p.sched.tile_key_start[wi];
+    item.key_end = p.sched.tile_key_start[wi + 1];
+    item.split = -1;
+    item.part = 0;
+    item.nparts = 1;
+    item.slot = -1;
+  }
+  const int tile = item.tile;
+  {
+    bool bad = tile < 0 || tile >= p.sched.n_tiles || chunk < 0 || chunk >= n_chunks;
+    if (!bad) {
+      const int t0 = p.sched.tile_key_start[tile], t1 = p.sched.tile_key_start[tile + 1];
+      bad = item.key_begin < t0 || item.key_end > t1 || item.key_begin > item.key_end;
+    }
+    if (item.split >= 0)
+      bad = bad || item.split >= p.sched.n_splits || item.part < 0 ||
+            item.part >= item.nparts || item.slot - item.part < 0 ||
+            item.slot - item.part + item.nparts > p.sched.n_slots;
+    else
+      bad = bad || item.split != -1;
+    if (bad) {   // uniform across the CTA
+      if (tid == 0) report(p.st, VL1_E_ARG, wi, -1);
+      __syncthreads();
+      continue;
+    }
+  }
+
+  const int k0 = item.key_begin, k1 = item.key_end;
+  const int n_keys = k1 - k0;
+  const int upr = (p.g.kp < 64 ? p.g.kp : 64) / KC;   // units per round
+  const int rpk = (p.g.kp + 63) / 64;                  // rounds per key
+  const int n_rounds = n_keys * rpk;
+
+  if (tid < 128) {
+    int v = p.sched.tile_rows[(int64_t)tile * 128 + tid];
+    if (v >= (int64_t)p.n_tgt_boxes * p.nrhs) {
+      report(p.st, VL1_E_ARG, tile, tid);
+      v = -1;
+    }
+    s_rows[tid] = v;
+  }
+  __syncthreads();
 
   if (warp < kProducerWarps) {
     // ------------------------------------------------------------ producers
@@ -515,8 +561,8 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
     }
     // expand the staged bytes of unit v into stage v % kStages
     auto expand = [&](int v) -> bool {
-      const int s = v % kStages;
-      const int use = v / kStages;
+      const int s = (ubase + v) % kStages;
+      const int use = (ubase + v) / kStages;
       if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) return false;
       const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
@@ -629,8 +675,8 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
         if (kidx + 1 < k1) nkey = p.sched.key_ids[kidx + 1];
         if (key < 0 || key >= p.d.n_tables * p.d.n_cases) key = 0;   // reported by warp 0
         for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
-          const int s = u % kStages;
-          const int use = u / kStages;
+          const int s = (ubase + u) % kStages;
+          const int use = (ubase + u) / kStages;
           if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) {
             aborted = true;
             break;
@@ -654,16 +700,17 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
       int u = 0;
       bool aborted = false;
       for (int round = 0; round < n_rounds && !aborted; ++round) {
-        const int b = round & 1;
-        if (round >= 2 && !wait_or_abort(&bars.acce[b], ((round >> 1) - 1) & 1, &s_abort)) {
+        const int R = rbase + round;
+        const int b = R & 1;
+        if (R >= 2 && !wait_or_abort(&bars.acce[b], ((R >> 1) - 1) & 1, &s_abort)) {
           aborted = true;
           break;
         }
         tc::tc_fence_after();
         const uint32_t exact_col = tbase + (uint32_t)b * 5 * NCH;
         for (int iu = 0; iu < upr; ++iu, ++u) {
-          const int s = u % kStages;
-          if (!wait_or_abort(&bars.full[s], (u / kStages) & 1, &s_abort)) {
+          const int s = (ubase + u) % kStages;
+          if (!wait_or_abort(&bars.full[s], ((ubase + u) / kStages) & 1, &s_abort)) {
             aborted = true;
             break;
           }
@@ -708,8 +755,9 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
     for (int c = 0; c < RC; ++c) acc[c] = 0;
     bool ok = true;
     for (int round = 0; round < n_rounds; ++round) {
-      const int b = round & 1;
-      if (!wait_or_abort(&bars.accf[b], (round >> 1) & 1, &s_abort)) {
+      const int R = rbase + round;
+      const int b = R & 1;
+      if (!wait_or_abort(&bars.accf[b], (R >> 1) & 1, &s_abort)) {
         ok = false;
         break;
       }
@@ -792,10 +840,10 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
   bool write = !s_abort;
   const uint8_t *g_parts = nullptr;   // slot region of part 0 of a split tile
   const int64_t slot_bytes = (int64_t)128 * NCH * 8;
-  const int64_t part_stride = (int64_t)gridDim.y * slot_bytes;
+  const int64_t part_stride = (int64_t)n_chunks * slot_bytes;
   if (item.split >= 0) {
     uint8_t *base = static_cast<uint8_t *>(p.sched.split_partials) +
-                    ((int64_t)(item.slot - item.part) * gridDim.y + chunk) * slot_bytes;
+                    ((int64_t)(item.slot - item.part) * n_chunks + chunk) * slot_bytes;
     g_parts = base;
     if (!s_abort) {
       long long *mine = reinterpret_cast<long long *>(base + item.part * part_stride);
@@ -804,7 +852,7 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
     __threadfence();
     __syncthreads();
     if (tid == 0) {
-      const int done = atomicAdd(p.sched.split_counters + item.split * gridDim.y + chunk, 1);
+      const int done = atomicAdd(p.sched.split_counters + item.split * n_chunks + chunk, 1);
       s_last = done == item.nparts - 1;
     }
     __syncthreads();
@@ -843,21 +891,47 @@ mixed_kernel(const __grid_constant__ MixedParams p) {
         p.result[o] = y;
     }
     // the last part leaves the counter at zero for the next call
-    if (item.split >= 0 && tid == 0) p.sched.split_counters[item.split * gridDim.y + chunk] = 0;
+    if (item.split >= 0 && tid == 0) p.sched.split_counters[item.split * n_chunks + chunk] = 0;
   }
   __syncthreads();
   if (s_abort && tid == 0) report(p.st, VL1_E_TIMEOUT, tile, chunk);
+  ubase += n_rounds * upr;
+  rbase += n_rounds;
+  __syncthreads();
+  }   // work items
   if (warp == kMmaWarp) tc::tmem_dealloc(tbase, COLS);
 }
 
-template <int NCH, int KC>
-cudaError_t launch_mixed_kernel(dim3 grid, int threads, size_t smem, cudaStream_t s,
-                                const MixedParams &mp) {
-  cudaError_t e = cudaFuncSetAttribute(mixed_kernel<NCH, KC>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// the kernel instance for a column chunk width and K chunk (nullptr if none)
+const void *mixed_kernel_ptr(int nch, int kc, bool multi) {
+#define VL1_MK(N, K)                                                                   \
+  if (nch == N && kc == K)                                                             \
+    return multi ? reinterpret_cast<const void *>(&mixed_kernel<N, K, true>)          \
+                 : reinterpret_cast<const void *>(&mixed_kernel<N, K, false>);
+  VL1_MK(64, 32) VL1_MK(32, 32) VL1_MK(16, 32) VL1_MK(64, 16) VL1_MK(32, 16) VL1_MK(16, 16)
+#undef VL1_MK
+  return nullptr;
+}
+
+size_t mixed_smem_bytes(int nch, int kc) {
+  const size_t pipe = (size_t)kStages * kDigits * (128 + nch) * kc * 2 +
+                      (size_t)kProducerWarps * kStgDepth * kRowsPerProducer * kDigits * kc;
+  const size_t park = (size_t)128 * nch * 8;   // int64 sums
+  return (pipe > park ? pipe : park) + 1024;
+}
+
+int mixed_threads(int nch) { return 32 * (kReadWarp0 + 4 * (nch / 16)); }
+
+cudaError_t launch_mixed_kernel(int nch, int kc, bool multi, dim3 grid, cudaStream_t s,
+                                const MixedParams &mp, const BatchLaunch &bl) {
+  const void *fn = mixed_kernel_ptr(nch, kc, multi);
+  if (!fn) return cudaErrorInvalidValue;
+  const size_t smem = mixed_smem_bytes(nch, kc);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
   if (e != cudaSuccess) return e;
-  mixed_kernel<NCH, KC><<<grid, threads, smem, s>>>(mp);
-  return cudaGetLastError();
+  void *args[] = {const_cast<MixedParams *>(&mp), const_cast<BatchLaunch *>(&bl)};
+  return cudaLaunchKernel(fn, grid, dim3(mixed_threads(nch)), args, smem, s);
 }
 
 int grid_for(int64_t n, int threads) {
@@ -990,30 +1064,13 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.n_particles = tree.n_particles;
   mp.result = result;
   mp.st = plan->status;
-  const size_t pipe = (size_t)kStages * kDigits * (128 + g.nch) * g.kc * 2 +
-                      (size_t)kProducerWarps * kStgDepth * kRowsPerProducer * kDigits * g.kc;
-  const size_t park = (size_t)128 * g.nch * 8;   // int64 sums
-  const size_t smem = (pipe > park ? pipe : park) + 1024;
-  dim3 grid(sched.n_items > 0 ? sched.n_items : sched.n_tiles, g.np / g.nch);
-  const int threads = 32 * (kReadWarp0 + 4 * (g.nch / 16));
-  if (g.kc == 32) {
-    if (g.nch == 64)
-      e = launch_mixed_kernel<64, 32>(grid, threads, smem, s, mp);
-    else if (g.nch == 32)
-      e = launch_mixed_kernel<32, 32>(grid, threads, smem, s, mp);
-    else
-      e = launch_mixed_kernel<16, 32>(grid, threads, smem, s, mp);
-  } else if (g.kc == 16) {
-    if (g.nch == 64)
-      e = launch_mixed_kernel<64, 16>(grid, threads, smem, s, mp);
-    else if (g.nch == 32)
-      e = launch_mixed_kernel<32, 16>(grid, threads, smem, s, mp);
-    else
-      e = launch_mixed_kernel<16, 16>(grid, threads, smem, s, mp);
-  } else {
-    set_error("mixed path: unsupported K chunk %d", g.kc);
+  if (!mixed_kernel_ptr(g.nch, g.kc, false)) {
+    set_error("mixed path: unsupported column chunk %d / K chunk %d", g.nch, g.kc);
     return VL1_E_UNSUPPORTED;
   }
+  dim3 grid(sched.n_items > 0 ? sched.n_items : sched.n_tiles, g.np / g.nch);
+  BatchLaunch none{};
+  e = launch_mixed_kernel(g.nch, g.kc, false, grid, s, mp, none);
   return e == cudaSuccess ? VL1_OK : cuda_fail(e, "mixed_kernel launch");
 }
 
