@@ -210,6 +210,44 @@ int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,
                        int32_t nrhs, void *result, void *workspace,
                        int64_t workspace_bytes, void *stream);
 
+/* ---- Batches: many problems in one persistent launch -------------------
+ * A batch is a fixed set of problems (different trees, depths, q, rhs
+ * counts and plans) whose tensor-core evaluations run together: batched
+ * preparation kernels, then one persistent launch per kernel shape (column
+ * chunk width x K chunk) in which every CTA takes the next (problem, tile,
+ * column chunk) work item from a queue, longest first.  vl1_batch_create
+ * copies the schedules' work lists to the host, builds the combined list
+ * and allocates one device buffer (parameters, work list, per-problem
+ * workspaces); vl1_batch_eval then only enqueues memsets and kernels on
+ * `stream` (no allocation, no host synchronisation), so its calls can be
+ * recorded in a CUDA graph and replayed.  All pointers of the problems
+ * (tree arrays, schedules, coefficients, results) are device pointers that
+ * must stay valid and fixed for the life of the batch; every eval reads the
+ * current coefficients and overwrites the results.  Replaces the separate
+ * vl1_eval_mixed calls a caller would make per problem
+ * (expansion_wrangler_fpnd.py:3417-3442 per output kernel and tree). */
+typedef struct vl1_batch vl1_batch;
+
+typedef struct {
+  vl1_plan *plan;
+  const vl1_tree_view *tree;
+  const vl1_mixed_schedule *schedule;   /* built for this tree and nrhs */
+  const double *coefs;                  /* [nrhs][n_particles], device */
+  int32_t nrhs;
+  void *result;                         /* as for vl1_eval_mixed, device */
+} vl1_batch_problem;
+
+typedef struct {
+  int32_t ctas_per_launch;   /* persistent CTAs per kernel shape; 0: one per SM */
+} vl1_batch_options;
+
+int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem *problems,
+                         const vl1_batch_options *options, vl1_batch **out);
+int32_t vl1_batch_eval(vl1_batch *batch, void *stream);
+int32_t vl1_batch_destroy(vl1_batch *batch);
+/* Device bytes held by the batch (its own buffer; plans and schedules apart). */
+int64_t vl1_batch_device_bytes(const vl1_batch *batch);
+
 /* Size of the fixed scratch array used by vl1_eval_mixed_noalloc (32 MiB). */
 #define VL1_NOALLOC_SCRATCH_BYTES (32LL << 20)
 

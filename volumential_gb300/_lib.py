@@ -107,6 +107,15 @@ class MixedSchedule(C.Structure):
     ]
 
 
+class BatchProblem(C.Structure):
+    _fields_ = [("plan", C.c_void_p), ("tree", C.c_void_p), ("schedule", C.c_void_p),
+                ("coefs", C.c_void_p), ("nrhs", C.c_int32), ("result", C.c_void_p)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("ctas_per_launch", C.c_int32)]
+
+
 class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("count", C.c_int32),
                 ("detail0", C.c_int32), ("detail1", C.c_int32)]
@@ -130,6 +139,11 @@ SIGNATURES = {
     "vl1_eval_mixed": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
                                    C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,
                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "vl1_batch_create": (C.c_int32, [C.c_int32, C.POINTER(BatchProblem),
+                                     C.POINTER(BatchOptions), C.POINTER(C.c_void_p)]),
+    "vl1_batch_eval": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_batch_destroy": (C.c_int32, [C.c_void_p]),
+    "vl1_batch_device_bytes": (C.c_int64, [C.c_void_p]),
     "vl1_eval_mixed_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
                                            C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,
                                            C.c_void_p, C.c_void_p]),

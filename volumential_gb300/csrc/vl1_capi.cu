@@ -255,7 +255,9 @@ int64_t vl1_plan_device_bytes(const vl1_plan *plan) {
   return plan ? plan->device_bytes : 0;
 }
 
-static int32_t make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &tr) {
+}  // extern "C"
+
+int32_t vl1::make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &tr) {
   if (!t || t->n_target_boxes < 0) {
     set_error("invalid tree view");
     return VL1_E_ARG;
@@ -305,6 +307,8 @@ static int32_t make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &
   }
   return VL1_OK;
 }
+
+extern "C" {
 
 int32_t vl1_eval_fp64(vl1_plan *plan, const vl1_tree_view *tree, const void *coefs,
                       int32_t coef_type, int32_t nrhs, void *result, void *stream) {

@@ -65,6 +65,8 @@ namespace vl1 {
 
 void set_error(const char *fmt, ...);
 int32_t cuda_fail(cudaError_t e, const char *what);
+// vl1_tree_view -> TreeDev with host validation (vl1_capi.cu)
+int32_t make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &tr);
 
 // Launchers (stream-ordered, no host synchronisation).
 int32_t launch_expand_blocks(vl1_plan *plan, cudaStream_t s);

@@ -26,6 +26,9 @@
 // result).  Each output's sum is then one exact integer, rounded once to FP64.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "vl1_internal.cuh"
 #include "vl1_mixed.cuh"
 #include "vl1_tc.cuh"
@@ -165,9 +168,78 @@ __global__ void classify_pairs_kernel(DevDesc d, TreeDev tr, int32_t *keys, vl1_
 
 // Per-call preparation kernels: one warp per density row (source box b, rhs r).
 
-// max exponent of scaling * coefficient per rhs: warp maxima are combined
-// per block in shared memory (rhs < kExpSmem), then one global atomic per
-// block and rhs
+// one problem of a batch, as the preparation kernels see it
+struct PrepProblem {
+  DevDesc d;
+  TreeDev tr;
+  const double *coefs;
+  int nrhs;
+  int *x_exp;
+  uint8_t *xdig;
+  int kp, kc;
+  vl1_status *st;
+};
+// rows [row0, row0 + nrows) of one problem
+struct PrepTask {
+  int32_t problem;
+  int32_t nrows;
+  int64_t row0;
+};
+
+// warp-wide maximum exponent of scaling * coefficient over row idx = b * nrhs
+// + r (-1074 for an empty row); the same value in every lane
+__device__ __forceinline__ int row_exponent(const DevDesc &d, const TreeDev &tr,
+                                            const double *coefs, int nrhs, int64_t idx,
+                                            int lane) {
+  const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
+  const int cnt = min(tr.src_counts[b], d.nq);
+  int e = -1074;
+  if (cnt > 0) {
+    const double sc = box_scaling(d, tr, tr.levels[b]);
+    const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
+    for (int s = lane; s < cnt; s += 32) e = max(e, scale_exponent(sc * c[s]));
+  }
+  return __reduce_max_sync(0xffffffffu, e);
+}
+
+// x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bytes (kp * 5),
+// so that the digits of one pipeline unit are one contiguous 5 * kc-byte
+// piece at byte kchunk * 5 * kc; source points sit at their mode id.
+__device__ __forceinline__ void row_digits(const DevDesc &d, const TreeDev &tr,
+                                           const double *coefs, int nrhs, const int *x_exp,
+                                           uint8_t *xdig, int kp, int kc, vl1_status *st,
+                                           int64_t idx, int lane) {
+  const int row_bytes = kp * kDigits;
+  const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
+  uint8_t *row = xdig + idx * row_bytes;
+  for (int k = lane * 16; k < row_bytes; k += 32 * 16)
+    *reinterpret_cast<uint4 *>(row + k) = make_uint4(0u, 0u, 0u, 0u);
+  __syncwarp();
+  int cnt = tr.src_counts[b];
+  if (cnt <= 0) return;
+  if (cnt > d.nq) {
+    if (lane == 0) report(st, VL1_E_LAYOUT, b, cnt);
+    cnt = d.nq;
+  }
+  const double sc = box_scaling(d, tr, tr.levels[b]);
+  const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
+  const int e = x_exp[r];
+  for (int s = lane; s < cnt; s += 32) {
+    const int m = tr.smode[tr.src_starts[b] + s];
+    if (m < 0 || m >= d.nq) {
+      report(st, VL1_E_LAYOUT, b, -1 - s);
+      continue;
+    }
+    uint8_t byt[kDigits];
+    density_digit_bytes(sc * c[s], e, byt);
+    const int base = (m / kc) * kDigits * kc + (m % kc);
+#pragma unroll
+    for (int i = 0; i < kDigits; ++i) row[base + i * kc] = byt[i];
+  }
+}
+
+// max exponent per rhs: warp maxima are combined per block in shared memory
+// (rhs < kExpSmem), then one global atomic per block and rhs
 constexpr int kExpSmem = 256;
 __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
                                   int nrhs, int *x_exp) {
@@ -181,20 +253,8 @@ __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const doubl
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
        idx += warps) {
-    const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-    const int cnt = min(tr.src_counts[b], d.nq);
-    if (cnt <= 0) continue;
-    const double sc = box_scaling(d, tr, tr.levels[b]);
-    const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
-    int e = -1074;
-    for (int s = lane; s < cnt; s += 32) e = max(e, scale_exponent(sc * c[s]));
-    e = __reduce_max_sync(0xffffffffu, e);
-    if (lane == 0) {
-      if (use_smem)
-        atomicMax(s_max + r, e);
-      else
-        atomicMax(x_exp + r, e);
-    }
+    const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
+    if (lane == 0 && e > -1074) atomicMax((use_smem ? s_max : x_exp) + (int)(idx % nrhs), e);
   }
   __syncthreads();
   if (use_smem)
@@ -202,45 +262,47 @@ __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const doubl
       if (s_max[r] > -1074) atomicMax(x_exp + r, s_max[r]);
 }
 
-// x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bytes (kp * 5),
-// so that the digits of one pipeline unit are one contiguous 5 * kc-byte
-// piece at byte kchunk * 5 * kc; source points sit at their mode id.
 __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
                                 int nrhs, const int *x_exp, uint8_t *xdig, int kp, int kc,
                                 vl1_status *st) {
   const int64_t n = (int64_t)nboxes * nrhs;
-  const int row_bytes = kp * kDigits;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
-       idx += warps) {
-    const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-    uint8_t *row = xdig + idx * row_bytes;
-    for (int k = lane * 16; k < row_bytes; k += 32 * 16)
-      *reinterpret_cast<uint4 *>(row + k) = make_uint4(0u, 0u, 0u, 0u);
-    __syncwarp();
-    int cnt = tr.src_counts[b];
-    if (cnt <= 0) continue;
-    if (cnt > d.nq) {
-      if (lane == 0) report(st, VL1_E_LAYOUT, b, cnt);
-      cnt = d.nq;
-    }
-    const double sc = box_scaling(d, tr, tr.levels[b]);
-    const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
-    const int e = x_exp[r];
-    for (int s = lane; s < cnt; s += 32) {
-      const int m = tr.smode[tr.src_starts[b] + s];
-      if (m < 0 || m >= d.nq) {
-        report(st, VL1_E_LAYOUT, b, -1 - s);
-        continue;
-      }
-      uint8_t byt[kDigits];
-      density_digit_bytes(sc * c[s], e, byt);
-      const int base = (m / kc) * kDigits * kc + (m % kc);
-#pragma unroll
-      for (int i = 0; i < kDigits; ++i) row[base + i * kc] = byt[i];
-    }
+       idx += warps)
+    row_digits(d, tr, coefs, nrhs, x_exp, xdig, kp, kc, st, idx, lane);
+}
+
+// Batch versions: block i handles rows [row0, row0 + nrows) of one problem
+// (tasks built on the host), 8 warps striding over them.
+__global__ void x_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+  __shared__ int s_max[kExpSmem];
+  const PrepTask t = tasks[blockIdx.x];
+  const PrepProblem &P = probs[t.problem];
+  const int nrhs = P.nrhs;
+  const bool use_smem = nrhs <= kExpSmem;
+  if (use_smem)
+    for (int r = threadIdx.x; r < nrhs; r += blockDim.x) s_max[r] = -1074;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5) {
+    const int64_t idx = t.row0 + i;
+    const int e = row_exponent(P.d, P.tr, P.coefs, nrhs, idx, lane);
+    if (lane == 0 && e > -1074) atomicMax((use_smem ? s_max : P.x_exp) + (int)(idx % nrhs), e);
   }
+  __syncthreads();
+  if (use_smem)
+    for (int r = threadIdx.x; r < nrhs; r += blockDim.x)
+      if (s_max[r] > -1074) atomicMax(P.x_exp + r, s_max[r]);
+}
+
+__global__ void x_digits_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+  const PrepTask t = tasks[blockIdx.x];
+  const PrepProblem &P = probs[t.problem];
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5)
+    row_digits(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, P.xdig, P.kp, P.kc, P.st, t.row0 + i,
+               lane);
 }
 
 // 2D log displacement: w[b, r] = dispfac(b) * sum_s nmlz[lev(b), s] * coef
@@ -1075,3 +1137,328 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
 }
 
 }  // namespace vl1
+
+// --------------------------------------------------------------- batches
+
+namespace {
+
+constexpr int kRowsPerTask = 64;
+
+struct DispJob {   // 2D log displacement of one problem (per-problem launches)
+  vl1::DevDesc d;
+  vl1::TreeDev tr;
+  int nboxes, nrhs;
+  const double *coefs;
+  double *wbox, *disp;
+};
+
+struct BatchGroup {   // problems sharing one kernel shape: one persistent launch
+  int nch, kc;
+  int item0, n_items;
+  int grid;
+};
+
+int64_t round256(int64_t b) { return (b + 255) / 256 * 256; }
+
+}  // namespace
+
+struct vl1_batch {
+  int device = -1;
+  void *buf = nullptr;
+  int64_t bytes = 0;
+  int n_problems = 0;
+  void *d_probs = nullptr, *d_prep = nullptr, *d_tasks = nullptr, *d_items = nullptr;
+  int n_tasks = 0;
+  int *d_queue = nullptr;
+  int *x_exp_all = nullptr;
+  int64_t x_exp_bytes = 0;
+  std::vector<BatchGroup> groups;
+  std::vector<DispJob> disp;
+};
+
+using namespace vl1;
+
+extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem *problems,
+                                    const vl1_batch_options *options, vl1_batch **out) {
+  if (!out || n_problems < 1 || !problems) {
+    set_error("vl1_batch_create: no problems or null output");
+    return VL1_E_ARG;
+  }
+  *out = nullptr;
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  int n_sm = 0;
+  e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+
+  // ---- per problem: validation, parameters (workspace pointers set below)
+  std::vector<MixedParams> mps(n_problems);
+  std::vector<PrepProblem> preps(n_problems);
+  std::vector<int64_t> ws_need(n_problems), nrows(n_problems);
+  std::vector<std::vector<vl1_mixed_item>> items(n_problems);
+  for (int i = 0; i < n_problems; ++i) {
+    const vl1_batch_problem &q = problems[i];
+    if (!q.plan || !q.tree || !q.schedule || !q.coefs || !q.result || q.nrhs < 1) {
+      set_error("vl1_batch_create: problem %d has a null plan/tree/schedule/coefs/result "
+                "or nrhs < 1", i);
+      return VL1_E_ARG;
+    }
+    if (q.plan->device != dev) {
+      set_error("vl1_batch_create: problem %d's plan is on device %d, not the current %d", i,
+                q.plan->device, dev);
+      return VL1_E_ARG;
+    }
+    TreeDev tr;
+    int32_t st = make_tree(q.plan, q.tree, tr);
+    if (st) return st;
+    const vl1_mixed_schedule &sc = *q.schedule;
+    if (tr.nboxes < 1 || sc.n_tiles < 0 || sc.n_items < 0 ||
+        (sc.n_tiles > 0 && (!sc.tile_rows || !sc.tile_key_start || !sc.key_ids ||
+                            !sc.key_xrow)) ||
+        (sc.n_items > 0 && !sc.items) ||
+        reinterpret_cast<uintptr_t>(sc.key_xrow) % 16 != 0 ||
+        (sc.n_splits > 0 && (!sc.split_counters || !sc.split_partials))) {
+      set_error("vl1_batch_create: problem %d has an invalid tree or schedule", i);
+      return VL1_E_ARG;
+    }
+    const MixedGeom &g = q.plan->mixed.geom;
+    if (!mixed_kernel_ptr(g.nch, g.kc, true)) {
+      set_error("vl1_batch_create: problem %d: unsupported kernel shape", i);
+      return VL1_E_UNSUPPORTED;
+    }
+    nrows[i] = tr.nboxes * q.nrhs;
+    if (nrows[i] >= INT32_MAX) {
+      set_error("vl1_batch_create: problem %d has %lld density rows (32-bit row index)", i,
+                (long long)nrows[i]);
+      return VL1_E_UNSUPPORTED;
+    }
+    ws_need[i] = mixed_workspace_bytes(q.plan, tr.nboxes, tr.n_tgt_boxes, q.nrhs);
+    MixedParams &mp = mps[i];
+    mp = MixedParams{};
+    mp.d = q.plan->d;
+    mp.g = g;
+    mp.nrhs = q.nrhs;
+    mp.sched = sc;
+    mp.n_xrows = (int32_t)nrows[i];
+    mp.adig = q.plan->mixed.adig;
+    mp.a_exp = q.plan->mixed.a_exp;
+    mp.target_boxes = tr.target_boxes;
+    mp.tgt_starts = tr.tgt_starts;
+    mp.tgt_counts = tr.tgt_counts;
+    mp.n_tgt_boxes = tr.n_tgt_boxes;
+    mp.n_particles = tr.n_particles;
+    mp.result = static_cast<double *>(q.result);
+    mp.st = q.plan->status;
+    PrepProblem &pp = preps[i];
+    pp = PrepProblem{};
+    pp.d = q.plan->d;
+    pp.tr = tr;
+    pp.coefs = q.coefs;
+    pp.nrhs = q.nrhs;
+    pp.kp = g.kp;
+    pp.kc = g.kc;
+    pp.st = q.plan->status;
+    // the work list of this problem (host copy of the schedule's items)
+    if (sc.n_items > 0) {
+      items[i].resize(sc.n_items);
+      e = cudaMemcpy(items[i].data(), sc.items, sizeof(vl1_mixed_item) * sc.n_items,
+                     cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(schedule items)");
+    } else if (sc.n_tiles > 0) {
+      std::vector<int32_t> ks(sc.n_tiles + 1);
+      e = cudaMemcpy(ks.data(), sc.tile_key_start, sizeof(int32_t) * ks.size(),
+                     cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tile_key_start)");
+      for (int t = 0; t < sc.n_tiles; ++t)
+        items[i].push_back(vl1_mixed_item{t, ks[t], ks[t + 1], -1, 0, 1, -1, 0});
+    }
+  }
+
+  // ---- combined work list: one group per kernel shape, longest items first
+  struct Cand {
+    int64_t cost;
+    BatchItem it;
+  };
+  std::vector<BatchGroup> groups;
+  std::vector<BatchItem> all;
+  {
+    std::vector<std::pair<int, int>> shapes;
+    for (int i = 0; i < n_problems; ++i) {
+      const MixedGeom &g = problems[i].plan->mixed.geom;
+      std::pair<int, int> sh(g.nch, g.kc);
+      if (std::find(shapes.begin(), shapes.end(), sh) == shapes.end()) shapes.push_back(sh);
+    }
+    for (const auto &sh : shapes) {
+      std::vector<Cand> cands;
+      for (int i = 0; i < n_problems; ++i) {
+        const MixedGeom &g = problems[i].plan->mixed.geom;
+        if (g.nch != sh.first || g.kc != sh.second) continue;
+        for (const vl1_mixed_item &it : items[i])
+          for (int c = 0; c < g.np / g.nch; ++c)
+            cands.push_back(Cand{(int64_t)(it.key_end - it.key_begin) * g.n_kc + 2,
+                                 BatchItem{i, c, it}});
+      }
+      std::stable_sort(cands.begin(), cands.end(),
+                       [](const Cand &a, const Cand &b) { return a.cost > b.cost; });
+      BatchGroup bg;
+      bg.nch = sh.first;
+      bg.kc = sh.second;
+      bg.item0 = (int)all.size();
+      bg.n_items = (int)cands.size();
+      const int ctas = options && options->ctas_per_launch > 0 ? options->ctas_per_launch : n_sm;
+      bg.grid = bg.n_items < ctas ? bg.n_items : ctas;
+      for (const Cand &c : cands) all.push_back(c.it);
+      if (bg.n_items > 0) groups.push_back(bg);
+    }
+  }
+  std::vector<PrepTask> tasks;
+  for (int i = 0; i < n_problems; ++i)
+    for (int64_t r0 = 0; r0 < nrows[i]; r0 += kRowsPerTask)
+      tasks.push_back(PrepTask{i, (int32_t)std::min<int64_t>(kRowsPerTask, nrows[i] - r0), r0});
+
+  // ---- one device buffer: parameters, work list, queues, workspaces
+  int64_t off = 0;
+  const int64_t o_probs = off;
+  off += round256(sizeof(MixedParams) * n_problems);
+  const int64_t o_prep = off;
+  off += round256(sizeof(PrepProblem) * n_problems);
+  const int64_t o_tasks = off;
+  off += round256(sizeof(PrepTask) * (tasks.size() + 1));
+  const int64_t o_items = off;
+  off += round256(sizeof(BatchItem) * (all.size() + 1));
+  const int64_t o_queue = off;
+  off += round256(sizeof(int) * (groups.size() + 1));
+  const int64_t o_xexp = off;
+  std::vector<int64_t> o_exp(n_problems), o_ws(n_problems);
+  for (int i = 0; i < n_problems; ++i) {
+    o_exp[i] = off;
+    off += round256((int64_t)problems[i].nrhs * 4);
+  }
+  const int64_t xexp_bytes = off - o_xexp;
+  for (int i = 0; i < n_problems; ++i) {
+    o_ws[i] = off;
+    off += round256(ws_need[i]);
+  }
+  vl1_batch *b = new vl1_batch();
+  b->device = dev;
+  b->bytes = off;
+  b->n_problems = n_problems;
+  e = cudaMalloc(&b->buf, off);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_fail(e, "cudaMalloc(batch)");
+  }
+  uint8_t *base = static_cast<uint8_t *>(b->buf);
+  for (int i = 0; i < n_problems; ++i) {
+    const vl1_batch_problem &q = problems[i];
+    const MixedGeom &g = q.plan->mixed.geom;
+    const int cv = q.plan->d.table_cplx ? 2 : 1;
+    int *x_exp = reinterpret_cast<int *>(base + o_exp[i]);
+    uint8_t *w = base + o_ws[i];
+    // the workspace layout of launch_mixed: [x exponents][x digits][disp]
+    w += round256((int64_t)q.nrhs * 4);
+    uint8_t *xdig = w;
+    w += round256(nrows[i] * g.kp * kDigits);
+    double *wbox = nullptr, *disp = nullptr;
+    if (q.plan->d.disp_kind == VL1_DISP_LOG2D) {
+      wbox = reinterpret_cast<double *>(w);
+      w += round256(nrows[i] * cv * 8);
+      disp = reinterpret_cast<double *>(w);
+      b->disp.push_back(DispJob{q.plan->d, preps[i].tr, (int)preps[i].tr.nboxes, q.nrhs,
+                                q.coefs, wbox, disp});
+    }
+    mps[i].xdig = xdig;
+    mps[i].x_exp = x_exp;
+    mps[i].disp = disp;
+    preps[i].x_exp = x_exp;
+    preps[i].xdig = xdig;
+  }
+  b->d_probs = base + o_probs;
+  b->d_prep = base + o_prep;
+  b->d_tasks = base + o_tasks;
+  b->d_items = base + o_items;
+  b->n_tasks = (int)tasks.size();
+  b->d_queue = reinterpret_cast<int *>(base + o_queue);
+  b->x_exp_all = reinterpret_cast<int *>(base + o_xexp);
+  b->x_exp_bytes = xexp_bytes;
+  b->groups = groups;
+  struct Up {
+    void *dst;
+    const void *src;
+    size_t n;
+  } ups[] = {{b->d_probs, mps.data(), sizeof(MixedParams) * n_problems},
+             {b->d_prep, preps.data(), sizeof(PrepProblem) * n_problems},
+             {b->d_tasks, tasks.data(), sizeof(PrepTask) * tasks.size()},
+             {b->d_items, all.data(), sizeof(BatchItem) * all.size()}};
+  for (const Up &u : ups) {
+    if (!u.n) continue;
+    e = cudaMemcpy(u.dst, u.src, u.n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(b->buf);
+      delete b;
+      return cuda_fail(e, "cudaMemcpy(batch parameters)");
+    }
+  }
+  for (const BatchGroup &g : groups) {
+    e = cudaFuncSetAttribute(mixed_kernel_ptr(g.nch, g.kc, true),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)mixed_smem_bytes(g.nch, g.kc));
+    if (e != cudaSuccess) {
+      cudaFree(b->buf);
+      delete b;
+      return cuda_fail(e, "cudaFuncSetAttribute(batch kernel)");
+    }
+  }
+  *out = b;
+  return VL1_OK;
+}
+
+extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
+  if (!b) {
+    set_error("vl1_batch_eval: null batch");
+    return VL1_E_ARG;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(b->x_exp_all, 0x80, b->x_exp_bytes, s);   // -> very negative
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_queue, 0, sizeof(int) * b->groups.size(), s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(batch)");
+  if (b->n_tasks > 0) {
+    x_exponent_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
+        static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
+    x_digits_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
+        static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
+  }
+  for (const DispJob &j : b->disp) {
+    const int64_t nbr = (int64_t)j.nboxes * j.nrhs;
+    disp_box_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(j.d, j.tr, j.nboxes, j.coefs, j.nrhs,
+                                                      j.wbox);
+    disp_target_kernel<<<grid_for((int64_t)j.tr.n_tgt_boxes * j.nrhs, 256), 256, 0, s>>>(
+        j.d, j.tr, j.nrhs, j.wbox, j.disp);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "batch preparation launch");
+  const MixedParams unused{};
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+    const BatchGroup &g = b->groups[gi];
+    BatchLaunch bl;
+    bl.probs = static_cast<const MixedParams *>(b->d_probs);
+    bl.items = static_cast<const BatchItem *>(b->d_items) + g.item0;
+    bl.n_items = g.n_items;
+    bl.queue = b->d_queue + gi;
+    void *args[] = {const_cast<MixedParams *>(&unused), &bl};
+    e = cudaLaunchKernel(mixed_kernel_ptr(g.nch, g.kc, true), dim3(g.grid),
+                         dim3(mixed_threads(g.nch)), args, mixed_smem_bytes(g.nch, g.kc), s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch mixed_kernel launch");
+  }
+  return VL1_OK;
+}
+
+extern "C" int32_t vl1_batch_destroy(vl1_batch *b) {
+  if (!b) return VL1_OK;
+  cudaError_t e = b->buf ? cudaFree(b->buf) : cudaSuccess;
+  delete b;
+  return e == cudaSuccess ? VL1_OK : cuda_fail(e, "cudaFree(batch)");
+}
+
+extern "C" int64_t vl1_batch_device_bytes(const vl1_batch *b) { return b ? b->bytes : -1; }
