@@ -1,0 +1,235 @@
+"""Batches of list-1 problems evaluated together on the tensor cores.
+
+Many right-hand sides and many trees of uneven depth and quadrature order go
+through one set of launches: batched preparation kernels, then one persistent
+tensor-core launch per kernel shape in which every CTA takes the next
+(problem, tile, column chunk) work item from a queue, longest first.  The
+launches of one evaluation allocate nothing and do not synchronise the host,
+so :meth:`MixedBatch.capture` records them in a CUDA graph that
+:meth:`MixedBatch.replay` re-runs on the current coefficients.
+
+The reference evaluates one output kernel and tree per ``NearFieldFromCSR``
+call (``expansion_wrangler_fpnd.py:3417-3442``); a batch is the many-problem
+form of that call, with the same per-problem inputs and outputs.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib
+from .batched import get_schedule
+
+__all__ = ["BatchProblem", "MixedBatch", "autotune_batch", "problem_arrays"]
+
+TREE_KEYS = ("target_boxes", "neighbor_source_boxes_starts", "neighbor_source_boxes_lists",
+             "box_centers", "box_levels", "box_source_starts", "box_source_counts_nonchild",
+             "box_target_starts", "box_target_counts_nonchild", "source_mode_ids",
+             "target_point_ids")
+
+
+class BatchProblem:
+    """One problem of a batch: a plan, a tree view (device arrays kept alive
+    in ``keep``), device coefficients [nrhs, N] (float64) and the device
+    result buffer of the plan's output dtype."""
+
+    def __init__(self, plan, view, keep, coefs, out, nrhs):
+        self.plan, self.view, self.keep = plan, view, keep
+        self.coefs, self.out, self.nrhs = coefs, out, int(nrhs)
+
+
+def problem_arrays(workload, plan=None):
+    """(plan, view, keep) of a workload through the FPND wrangler's argument
+    assembly; ``plan`` reuses an existing plan of the same table set."""
+    from .expansion_wrangler_fpnd import (FPNDExpansionWrangler,
+                                          FPNDTreeIndependentDataForWrangler)
+    from .plan import as_device_tensor, tree_view_from_arrays
+
+    w = workload
+    ti = FPNDTreeIndependentDataForWrangler(target_kernels=[w.kernel])
+    dtype = np.complex128 if w.kernel.is_complex_valued else np.float64
+    wr = FPNDExpansionWrangler(ti, w.traversal, w.tables, dtype=dtype, quad_order=w.q)
+    tr = w.traversal
+    payload = wr.get_payload(w.kernel)
+    nf = wr.near_field_evaluator(w.kernel, payload)
+    kw = wr._near_field_kwargs(payload, tr.target_boxes, tr.neighbor_source_boxes_starts,
+                               tr.neighbor_source_boxes_lists, None)
+    if plan is None:
+        plan = nf.get_plan(
+            table_data_combined=kw["table_data_combined"],
+            mode_nmlz_combined=kw["mode_nmlz_combined"], case_indices=kw["case_indices"],
+            encoding_base=kw["encoding_base"], encoding_shift=kw["encoding_shift"],
+            table_root_extent=kw["table_root_extent"],
+            table_starting_level=kw["table_starting_level"],
+            **{n: kw[n] for n in kw if n.startswith("arithmetic_")})
+    view, keep = tree_view_from_arrays(root_extent=kw["root_extent"],
+                                       **{k: as_device_tensor(kw[k]) for k in TREE_KEYS})
+    return plan, view, keep
+
+
+class MixedBatch:
+    """A fixed set of problems evaluated by one ``vl1_batch_eval`` call.
+
+    ``max_keys_per_item`` caps the keys of one work item (long tiles are split
+    over several CTAs; ``None`` lets each problem's schedule choose);
+    ``ctas_per_launch`` sets the persistent CTAs per kernel shape (0: one per
+    SM).  Coefficient and result tensors are used in place: write new
+    densities into ``problem.coefs`` and call :meth:`eval` or :meth:`replay`.
+    """
+
+    def __init__(self, problems, *, max_keys_per_item=None, ctas_per_launch=0, stream=None):
+        import torch
+
+        self.problems = list(problems)
+        if not self.problems:
+            raise ValueError("a batch needs at least one problem")
+        self._lib = _lib.lib()
+        self.handle = None
+        sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        self.schedules = []
+        arr = (_lib.BatchProblem * len(self.problems))()
+        for i, p in enumerate(self.problems):
+            if p.coefs.dtype != torch.float64 or not p.coefs.is_contiguous():
+                raise TypeError("batch coefficients must be contiguous float64 tensors")
+            if p.coefs.numel() != p.nrhs * int(p.view.n_particles):
+                raise ValueError(f"problem {i}: coefficients must hold nrhs * N values")
+            sched = get_schedule(p.plan, p.view, p.keep, p.nrhs, sh, max_keys_per_item)
+            self.schedules.append(sched)
+            arr[i].plan = p.plan.handle
+            arr[i].tree = C.cast(C.pointer(p.view), C.c_void_p)
+            arr[i].schedule = C.cast(C.pointer(sched.c_struct), C.c_void_p)
+            arr[i].coefs = p.coefs.data_ptr()
+            arr[i].nrhs = p.nrhs
+            arr[i].result = p.out.data_ptr()
+        self._arr = arr
+        opt = _lib.BatchOptions(int(ctas_per_launch))
+        handle = C.c_void_p()
+        torch.cuda.current_stream().synchronize()
+        _lib.check(self._lib.vl1_batch_create(len(self.problems), arr, C.byref(opt),
+                                              C.byref(handle)), "vl1_batch_create")
+        self.handle = handle
+        self.graph = None
+        self.max_keys_per_item = max_keys_per_item
+        self.ctas_per_launch = int(ctas_per_launch)
+
+    @property
+    def device_bytes(self):
+        return int(self._lib.vl1_batch_device_bytes(self.handle))
+
+    def eval(self, stream=None):
+        import torch
+
+        sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _lib.check(self._lib.vl1_batch_eval(self.handle, C.c_void_p(sh)), "vl1_batch_eval")
+
+    def capture(self):
+        """Record one evaluation in a CUDA graph (after one plain run)."""
+        import torch
+
+        self.eval()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.eval(torch.cuda.current_stream().cuda_stream)
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            raise RuntimeError("capture() the batch first")
+        self.graph.replay()
+
+    def raise_on_status(self):
+        import torch
+
+        sh = torch.cuda.current_stream().cuda_stream
+        seen = set()
+        for p in self.problems:
+            if id(p.plan) not in seen:
+                seen.add(id(p.plan))
+                p.plan.raise_on_status(sh)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.graph = None
+            self._lib.vl1_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _time_batch(batch, reps):
+    import torch
+
+    batch.eval()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ts = []
+    for _ in range(reps):
+        ev[0].record()
+        batch.eval()
+        ev[1].record()
+        ev[1].synchronize()
+        ts.append(ev[0].elapsed_time(ev[1]))
+    return float(np.median(ts))
+
+
+_tuned: dict = {}
+
+
+def _signature(problems):
+    return tuple((int(p.view.n_target_boxes), int(p.keep["lists"].numel()), p.nrhs,
+                  int(p.plan.nq), id(p.plan)) for p in problems)
+
+
+def autotune_batch(problems, *, reps=3, divisors=(1, 2, 3, 4, 6, 8), verbose=False):
+    """Choose the work-item size of a batch by timing.
+
+    Candidates cap the keys of one work item at the mean (tile key, column
+    chunk) count per SM divided by each of ``divisors`` (smaller items balance
+    the persistent launch better, larger ones pay fewer start-ups); each
+    candidate batch is built and timed (median of ``reps`` evaluations, CUDA
+    events) and the fastest is returned with the timing table.  Choices are
+    cached per problem-set signature.
+    """
+    import torch
+
+    sig = _signature(problems)
+    if sig in _tuned:
+        cap = _tuned[sig]
+        return MixedBatch(problems, max_keys_per_item=cap), {"cached": cap}
+    stream = torch.cuda.current_stream().cuda_stream
+    n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    total_keys = 0
+    for p in problems:
+        s = get_schedule(p.plan, p.view, p.keep, p.nrhs, stream)
+        geo = p.plan.mixed_geometry()
+        total_keys += s.n_tile_keys * (geo["np"] // geo["nch"])
+    share = max(1, -(-total_keys // n_sm))
+    table = {}
+    best = None
+    for d in divisors:
+        cap = max(2, -(-share // d))
+        if cap in table:
+            continue
+        t0 = time.perf_counter()
+        b = MixedBatch(problems, max_keys_per_item=cap)
+        ms = _time_batch(b, reps)
+        table[cap] = {"ms": ms, "build_s": time.perf_counter() - t0}
+        if verbose:
+            print(f"autotune: cap {cap} keys -> {ms:.3f} ms")
+        if best is None or ms < best[0]:
+            if best is not None:
+                best[2].close()
+            best = (ms, cap, b)
+        else:
+            b.close()
+    _tuned[sig] = best[1]
+    return best[2], table
