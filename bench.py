@@ -54,8 +54,10 @@ def parse_args(argv=None):
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    p.add_argument("--workload", choices=("c2", "c1", "c3"), default="c2")
+    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4"), default="c2")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--c4-problems", type=int, default=64, help="C4: problems in the batch")
+    p.add_argument("--c4-max-level", type=int, default=5, help="C4: deepest uniform level")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="target CPU time of the cpu_baseline sample")
     return p.parse_args(argv)
@@ -509,10 +511,121 @@ def gb300_main(args):
     return 0
 
 
+def c4_main(args):
+    """Uneven batch (C4): 64 uniform 3D Laplace problems of levels 3..5,
+    q in {3, 4, 5}, 1..32 right-hand sides each, evaluated by one autotuned,
+    CUDA-graph-captured batch (batched preparation + one persistent
+    tensor-core launch per kernel shape).  One step = one replay of the graph
+    over all problems; compared with the same problems evaluated one by one
+    (mixed path) and with the FP64 kernel (one pass)."""
+    import torch
+
+    from volumential_gb300 import workloads as W
+    from volumential_gb300.batch import BatchProblem, autotune_batch, problem_arrays
+    from volumential_gb300.batched import eval_mixed
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    ws = W.config_c4(n_problems=args.c4_problems, levels=(3, args.c4_max_level))
+    plans = {}
+    probs = []
+    for w in ws:
+        plan, view, keep = problem_arrays(w, plans.get(w.meta["table_key"]))
+        plans.setdefault(w.meta["table_key"], plan)
+        pts = torch.from_numpy(np.ascontiguousarray(w.tree.targets)).to("cuda")
+        coefs = torch.stack([m.on_device(pts) for m in w.meta["mixtures"]]).contiguous()
+        out = torch.zeros_like(coefs)
+        probs.append(BatchProblem(plan, view, keep, coefs, out, w.nrhs))
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batch, table = autotune_batch(probs, reps=2)
+    t_tune = time.perf_counter() - t0
+    batch.capture()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        batch.replay()
+    batch.raise_on_status()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    step_ms = []
+    for _ in range(args.steps):
+        ev[0].record(stream)
+        batch.replay()
+        ev[1].record(stream)
+        ev[1].synchronize()
+        step_ms.append(ev[0].elapsed_time(ev[1]))
+    clock_info = clocks.stop()
+    batch.raise_on_status()
+    # the same problems one by one through the mixed path (one pass)
+    sh = stream.cuda_stream
+    sep = [torch.empty_like(p.out) for p in probs]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for p, o in zip(probs, sep):
+        eval_mixed(p.plan, p.view, p.coefs, o, stream=sh, nrhs=p.nrhs, keep=p.keep,
+                   max_keys_per_item=batch.max_keys_per_item)
+    ev[1].record(stream)
+    ev[1].synchronize()
+    sep_ms = ev[0].elapsed_time(ev[1])
+    # FP64 kernel, one pass, and the errors of the batch against it
+    ref = [torch.empty_like(p.out) for p in probs]
+    ev[0].record(stream)
+    for p, o in zip(probs, ref):
+        p.plan.eval_fp64(p.view, p.coefs, o, stream=sh, nrhs=p.nrhs)
+    ev[1].record(stream)
+    ev[1].synchronize()
+    plain_ms = ev[0].elapsed_time(ev[1])
+    errs = []
+    for p, o in zip(probs, ref):
+        d = (p.out - o).reshape(p.nrhs, -1)
+        errs.extend((torch.linalg.norm(d, dim=1) /
+                     torch.linalg.norm(o.reshape(p.nrhs, -1), dim=1)).tolist())
+    same = all(torch.equal(p.out, o) for p, o in zip(probs, sep))
+    pts = sum(int(p.view.n_particles) * p.nrhs for p in probs)
+    pairs = sum(w.pair_count() * w.nrhs for w in ws)
+    ms = float(np.mean(step_ms))
+    hbm, bf16, peak_kind = peaks()
+    line = {
+        "metric": METRIC, "value": pts / (ms / 1e3), "unit": "points/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16-digits/fp32-exact/f64", "data": "synthetic",
+        "config": {"workload": f"c4_lap3d_uniform_batch{len(probs)}", "problems": len(probs),
+                   "levels": [3, args.c4_max_level], "q": [3, 4, 5], "nrhs": [1, 32],
+                   "points_x_rhs": pts, "point_pairs_x_rhs": pairs,
+                   "l2": "inputs (%.1f GB) far larger than L2" %
+                         (sum(p.coefs.numel() * 16 for p in probs) / 1e9),
+                   "path": "batch, CUDA graph replay"},
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                       "p99": float(np.percentile(step_ms, 99))},
+        "rel_l2_max_vs_fp64": max(errs), "batch_equals_separate_mixed": bool(same),
+        "paths": {"batch_graph_ms": ms, "separate_mixed_ms": sep_ms, "plain_fp64_ms": plain_ms,
+                  "speedup_batch_over_plain": plain_ms / ms,
+                  "speedup_batch_over_separate": sep_ms / ms},
+        "autotune": {str(k): v for k, v in table.items()},
+        "max_keys_per_item": batch.max_keys_per_item,
+        "batch_device_bytes": batch.device_bytes,
+        "setup_s": t_setup, "autotune_s": t_tune,
+        "pair_rate_per_s": pairs / (ms / 1e3),
+        "e2e": None, "e2e_note": "resident-data batch; host copies of 23 GB are not part of "
+                                 "this configuration",
+        "clocks": clock_info, "peak_source": peak_kind,
+        "gpu_launches": args.steps * (2 + 2),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "c4":
+        return c4_main(args)
     return gb300_main(args)
 
 

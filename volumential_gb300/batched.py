@@ -38,11 +38,19 @@ _CACHE_MAX = 8
 class MixedSchedule:
     """Device-resident schedule (and workspace) of one (plan, tree, nrhs)."""
 
-    def __init__(self, plan, view, keep, nrhs, stream, max_keys_per_item=None):
+    def __init__(self, plan, view, keep, nrhs, stream, max_keys_per_item=None, base=None):
         import torch
 
         lib = _lib.lib()
         self.nrhs = int(nrhs)
+        if base is not None:
+            # same plan, tree and nrhs: only the work items differ
+            self._init_items(plan, base, max_keys_per_item)
+            ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
+            if ws < 0:
+                raise RuntimeError("vl1_mixed_workspace_bytes failed")
+            self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
+            return
         n_tb = int(view.n_target_boxes)
         nnz = int(keep["lists"].numel())
         n_keys_total = plan.n_tables * plan.n_cases
@@ -68,6 +76,24 @@ class MixedSchedule:
                                         else np.zeros(1, np.int32)).to("cuda")
         self.key_xrow = torch.from_numpy(xrow.ravel() if len(key_ids)
                                          else np.zeros(ROWS_PER_TILE, np.int32)).to("cuda")
+        self.key_start_np = np.asarray(key_start, dtype=np.int64)
+        self._init_items(plan, self, max_keys_per_item)
+        ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
+        if ws < 0:
+            raise RuntimeError("vl1_mixed_workspace_bytes failed")
+        self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
+
+    def _init_items(self, plan, base, max_keys_per_item):
+        """Work items, split counters and partial-sum scratch for a cap; the
+        tile arrays come from ``base`` (this schedule or one of the same plan,
+        tree and nrhs)."""
+        import torch
+
+        for name in ("n_tiles", "n_tile_keys", "mean_keys_per_tile", "tile_rows",
+                     "tile_key_start", "key_ids", "key_xrow", "key_start_np"):
+            setattr(self, name, getattr(base, name))
+        key_start = self.key_start_np
+        n_tiles = self.n_tiles
         geo = plan.mixed_geometry()
         n_chunks = geo["np"] // geo["nch"]
         items, n_splits, n_slots = self._work_items(np.asarray(key_start, dtype=np.int64),
@@ -94,10 +120,6 @@ class MixedSchedule:
         s.split_counters = self.split_counters.data_ptr()
         s.split_partials = self.split_partials.data_ptr()
         self.c_struct = s
-        ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
-        if ws < 0:
-            raise RuntimeError("vl1_mixed_workspace_bytes failed")
-        self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
 
     @staticmethod
     def tile_schedule(keys, starts, lists, n_tb, n_keys_total, nrhs):
@@ -268,7 +290,13 @@ def get_schedule(plan, view, keep, nrhs, stream, max_keys_per_item=None):
         if hit is not None:
             _cache.move_to_end(key)
             return hit[0]
-    sched = MixedSchedule(plan, view, keep, nrhs, stream, max_keys_per_item)
+    base = None
+    with _lock:
+        for k, v in _cache.items():
+            if k[:3] == key[:3]:
+                base = v[0]
+                break
+    sched = MixedSchedule(plan, view, keep, nrhs, stream, max_keys_per_item, base=base)
     with _lock:
         # keep the tree tensors alive with the schedule so the token stays unique
         _cache[key] = (sched, dict(keep), plan)

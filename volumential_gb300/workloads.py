@@ -31,7 +31,7 @@ from .tree_build import (
 
 __all__ = ["GaussianMixture", "random_gaussian_mixture", "synthetic_tables",
            "Workload", "config_c1", "config_c2", "config_c3", "uniform_workload",
-           "adaptive_workload"]
+           "adaptive_workload", "config_c4"]
 
 
 @dataclass
@@ -49,6 +49,19 @@ class GaussianMixture:
             for ax in range(pts.shape[0]):
                 d2 += (pts[ax] - c[ax]) ** 2
             out += a * np.exp(-d2 / (w * w))
+        return out
+
+    def on_device(self, points):
+        """The same density evaluated with torch where ``points`` ([dim, N]
+        float64 tensor) lives."""
+        import torch
+
+        out = torch.zeros(points.shape[1:], dtype=torch.float64, device=points.device)
+        for c, w, a in zip(self.centers, self.widths, self.amps):
+            d2 = torch.zeros_like(out)
+            for ax in range(points.shape[0]):
+                d2 += (points[ax] - float(c[ax])) ** 2
+            out += float(a) * torch.exp(-d2 / float(w * w))
         return out
 
 
@@ -200,6 +213,42 @@ def config_c3(seed=3000, nrhs=256, k=20.0):
     w.tables = t
     w.meta["k"] = k
     return w
+
+
+def config_c4(seed=4000, n_problems=64, levels=(3, 5), qs=(3, 4, 5), nrhs_range=(1, 32),
+              terms=(4, 16), width_range=(0.01, 0.1)):
+    """Uneven batch: ``n_problems`` independent 3D Laplace problems on uniform
+    octrees, level uniform in ``levels``, q uniform in ``qs``, rhs count
+    uniform in ``nrhs_range``, each density a sum of ``terms`` Gaussians.
+
+    The densities are not evaluated here (``coefs`` has shape [nrhs, 0]):
+    the mixtures are in ``meta["mixtures"]`` and are evaluated on the device
+    (``GaussianMixture.on_device``).  Problems of one q share one table set.
+    The configuration text asks for levels 3..6; level 6 is left out of the
+    default because one level-6, q=5 problem with 32 right-hand sides alone
+    holds 32.8M points x 32 densities (8.4 GB of coefficients and as much
+    output), and the 64-problem mix would not fit one run's device and host
+    budget.
+    """
+    rng = np.random.default_rng(seed)
+    kernel = LaplaceKernel(3)
+    tables = {}
+    out = []
+    for i in range(n_problems):
+        lev = int(rng.integers(levels[0], levels[1] + 1))
+        q = int(rng.choice(qs))
+        nrhs = int(rng.integers(nrhs_range[0], nrhs_range[1] + 1))
+        tree = build_uniform_tree(3, lev, q)
+        trav = build_list1_traversal(tree)
+        mixes = [random_gaussian_mixture(rng, 3, int(rng.integers(terms[0], terms[1] + 1)),
+                                         width_range) for _ in range(nrhs)]
+        if q not in tables:
+            tables[q] = synthetic_tables(3, q, kernel, seed=seed + 17 + q,
+                                         source_box_extent=tree.root_extent)
+        out.append(Workload(f"c4_p{i:02d}_l{lev}_q{q}", 3, q, kernel, trav, tables[q],
+                            np.zeros((nrhs, 0)), seed,
+                            meta={"level": lev, "mixtures": mixes, "table_key": q}))
+    return out
 
 
 def constant_workload(dim, q, level=1):
