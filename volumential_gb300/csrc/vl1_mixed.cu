@@ -174,7 +174,8 @@ struct PrepProblem {
   TreeDev tr;
   const double *coefs;
   int nrhs;
-  int *x_exp;
+  int *x_exp;     // per density row
+  int *ref_exp;   // per target row (target box index * nrhs + rhs)
   uint8_t *xdig;
   int kp, kc;
   vl1_status *st;
@@ -223,7 +224,7 @@ __device__ __forceinline__ void row_digits(const DevDesc &d, const TreeDev &tr,
   }
   const double sc = box_scaling(d, tr, tr.levels[b]);
   const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
-  const int e = x_exp[r];
+  const int e = x_exp[idx];
   for (int s = lane; s < cnt; s += 32) {
     const int m = tr.smode[tr.src_starts[b] + s];
     if (m < 0 || m >= d.nq) {
@@ -238,28 +239,38 @@ __device__ __forceinline__ void row_digits(const DevDesc &d, const TreeDev &tr,
   }
 }
 
-// max exponent per rhs: warp maxima are combined per block in shared memory
-// (rhs < kExpSmem), then one global atomic per block and rhs
-constexpr int kExpSmem = 256;
+// Scale exponents.  Every density row (source box, rhs) gets its own: the
+// exponent e with |scaling * coefficient| < 2^e over the box (-1074 for an
+// empty or zero row); its digits are fixed point against 2^e.  Every target
+// row (target box, rhs) gets the largest exponent of its list-1 source rows:
+// its sum is accumulated in units of that exponent, so the precision of an
+// output is relative to its own largest contribution.
 __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
                                   int nrhs, int *x_exp) {
-  __shared__ int s_max[kExpSmem];
-  const bool use_smem = nrhs <= kExpSmem;
-  if (use_smem)
-    for (int r = threadIdx.x; r < nrhs; r += blockDim.x) s_max[r] = -1074;
-  __syncthreads();
   const int64_t n = (int64_t)nboxes * nrhs;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
        idx += warps) {
     const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
-    if (lane == 0 && e > -1074) atomicMax((use_smem ? s_max : x_exp) + (int)(idx % nrhs), e);
+    if (lane == 0) x_exp[idx] = e;
   }
-  __syncthreads();
-  if (use_smem)
-    for (int r = threadIdx.x; r < nrhs; r += blockDim.x)
-      if (s_max[r] > -1074) atomicMax(x_exp + r, s_max[r]);
+}
+
+__device__ __forceinline__ int target_row_exponent(const TreeDev &tr, int nrhs,
+                                                   const int *x_exp, int64_t idx) {
+  const int tb = (int)(idx / nrhs), r = (int)(idx % nrhs);
+  int e = -1074;
+  for (int p = tr.starts[tb]; p < tr.starts[tb + 1]; ++p)
+    e = max(e, x_exp[(int64_t)tr.lists[p] * nrhs + r]);
+  return e;
+}
+
+__global__ void ref_exponent_kernel(TreeDev tr, int nrhs, const int *x_exp, int *ref_exp) {
+  const int64_t n = (int64_t)tr.n_tgt_boxes * nrhs;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    ref_exp[idx] = target_row_exponent(tr, nrhs, x_exp, idx);
 }
 
 __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
@@ -276,24 +287,22 @@ __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double 
 // Batch versions: block i handles rows [row0, row0 + nrows) of one problem
 // (tasks built on the host), 8 warps striding over them.
 __global__ void x_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
-  __shared__ int s_max[kExpSmem];
   const PrepTask t = tasks[blockIdx.x];
   const PrepProblem &P = probs[t.problem];
-  const int nrhs = P.nrhs;
-  const bool use_smem = nrhs <= kExpSmem;
-  if (use_smem)
-    for (int r = threadIdx.x; r < nrhs; r += blockDim.x) s_max[r] = -1074;
-  __syncthreads();
   const int lane = threadIdx.x & 31;
   for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5) {
     const int64_t idx = t.row0 + i;
-    const int e = row_exponent(P.d, P.tr, P.coefs, nrhs, idx, lane);
-    if (lane == 0 && e > -1074) atomicMax((use_smem ? s_max : P.x_exp) + (int)(idx % nrhs), e);
+    const int e = row_exponent(P.d, P.tr, P.coefs, P.nrhs, idx, lane);
+    if (lane == 0) P.x_exp[idx] = e;
   }
-  __syncthreads();
-  if (use_smem)
-    for (int r = threadIdx.x; r < nrhs; r += blockDim.x)
-      if (s_max[r] > -1074) atomicMax(P.x_exp + r, s_max[r]);
+}
+
+// target rows [row0, row0 + nrows) of one problem, one thread each
+__global__ void ref_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+  const PrepTask t = tasks[blockIdx.x];
+  const PrepProblem &P = probs[t.problem];
+  for (int i = threadIdx.x; i < t.nrows; i += blockDim.x)
+    P.ref_exp[t.row0 + i] = target_row_exponent(P.tr, P.nrhs, P.x_exp, t.row0 + i);
 }
 
 __global__ void x_digits_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
@@ -352,6 +361,13 @@ __global__ void disp_target_kernel(DevDesc d, TreeDev tr, int nrhs, const double
   }
 }
 
+// x * 2^n as an integer: a left shift, or an arithmetic right shift
+// (rounding down; 0 once the shift passes the width)
+__device__ __forceinline__ long long shift_units(long long x, int n) {
+  if (n >= 0) return x << n;
+  return n <= -63 ? 0 : (x >> -n);
+}
+
 // v * 2^k rounded once to FP64 (nearest, ties to even), with integer
 // operations only while the result is a normal number
 __device__ __forceinline__ double scaled_i64_to_double(long long v, int k) {
@@ -388,7 +404,8 @@ struct MixedParams {
   const uint8_t *xdig;   // density digit bytes [n_xrows][kp * 5]
   int32_t n_xrows;
   const __half *adig;
-  const int *x_exp;
+  const int *x_exp;     // per density row
+  const int *ref_exp;   // per target row
   int a_exp;
   const double *disp;  // [n_tgt_boxes * nrhs] (x2 complex) or nullptr
   const int32_t *target_boxes, *tgt_starts, *tgt_counts;
@@ -434,6 +451,7 @@ struct Barriers {
   uint64_t empty[kStages];
   uint64_t accf[2];
   uint64_t acce[2];
+  uint64_t tailf;   // the tail blocks of the last round have been read
 };
 
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t phase,
@@ -516,6 +534,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       tc::mbar_init(&bars.accf[b], 1);
       tc::mbar_init(&bars.acce[b], NREAD);
     }
+    tc::mbar_init(&bars.tailf, NREAD);
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -784,15 +803,35 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
           // descriptors advance by (byte offset >> 4) in their address field
           const uint64_t xd = tc::smem_desc_kmajor_swizzled(xa, ROW_BYTES);
           const uint64_t adsc = tc::smem_desc_kmajor_swizzled(xa + kDigits * XBYTES, ROW_BYTES);
+          // exact diagonals into the round buffer
 #pragma unroll
           for (int kk = 0; kk < KC / 16; ++kk) {
 #pragma unroll
-            for (int g = 0; g < 8; ++g) {
+            for (int g = 0; g < 3; ++g) {
               const MmaGroup gr = kGroups[g];
-              const uint32_t col = gr.exact ? exact_col + (uint32_t)(gr.i + gr.j0 - 2) * NCH
-                                            : tail_col + (uint32_t)(gr.i + gr.j0 - 5) * NCH;
-              const bool first = gr.exact ? (g == 0 && iu == 0 && kk == 0)
-                                          : (g == 3 && u == 0 && kk == 0);
+              const uint32_t col = exact_col + (uint32_t)(gr.i + gr.j0 - 2) * NCH;
+              const bool first = g == 0 && iu == 0 && kk == 0;
+              const uint64_t ad = xd + (((uint32_t)(gr.i - 1) * XBYTES + kk * 32u) >> 4);
+              const uint64_t bd = adsc + (((uint32_t)(gr.j0 - 1) * ABYTES + kk * 32u) >> 4);
+              tc::mma_f16(col, ad, bd, tc::idesc_f16_f32(128, NCH * gr.nb), first ? 0u : 1u);
+            }
+          }
+          // tails: read after every round, so the first tail product of a
+          // round waits until the previous round's tails have been read
+          if (iu == 0 && R >= 1) {
+            if (!wait_or_abort(&bars.tailf, (R - 1) & 1, &s_abort)) {
+              aborted = true;
+              break;
+            }
+            tc::tc_fence_after();
+          }
+#pragma unroll
+          for (int kk = 0; kk < KC / 16; ++kk) {
+#pragma unroll
+            for (int g = 3; g < 8; ++g) {
+              const MmaGroup gr = kGroups[g];
+              const uint32_t col = tail_col + (uint32_t)(gr.i + gr.j0 - 5) * NCH;
+              const bool first = g == 3 && iu == 0 && kk == 0;
               const uint64_t ad = xd + (((uint32_t)(gr.i - 1) * XBYTES + kk * 32u) >> 4);
               const uint64_t bd = adsc + (((uint32_t)(gr.j0 - 1) * ABYTES + kk * 32u) >> 4);
               tc::mma_f16(col, ad, bd, tc::idesc_f16_f32(128, NCH * gr.nb), first ? 0u : 1u);
@@ -811,59 +850,71 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     const int cb = rw >> 2;                // RC-column block
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     const int row = quad * 32 + lane;
-    // exact sum of the diagonals per output, units of 2^(e-32)
+    // Per output: the sum of digit products in units of 2^32 of m_a m_x at
+    // the row's reference exponent e_ref.  A round (one key: one source row
+    // per tile row) is exact at its source row's exponent e_s <= e_ref; its
+    // diagonals 2..4 (weights 2^64, 2^56, 2^48) and FP32 tails d5, d6
+    // (weights 2^40, 2^32, read after every round and rounded to integers)
+    // are shifted by their weight's bits minus (e_ref - e_s).
     long long acc[RC];
 #pragma unroll
     for (int c = 0; c < RC; ++c) acc[c] = 0;
+    const int v_row = s_rows[row];
+    const int e_ref = v_row >= 0 ? p.ref_exp[v_row] : 0;
     bool ok = true;
     for (int round = 0; round < n_rounds; ++round) {
       const int R = rbase + round;
       const int b = R & 1;
+      const int xr = p.sched.key_xrow[(int64_t)(k0 + round / rpk) * 128 + row];
+      const int e_src = xr >= 0 ? p.x_exp[xr] : e_ref;
+      const int sh = e_ref - e_src;   // >= 0: a source row is never above its target's reference
       if (!wait_or_abort(&bars.accf[b], (R >> 1) & 1, &s_abort)) {
         ok = false;
         break;
       }
       tc::tc_fence_after();
       const uint32_t col = tbase + lane_off + (uint32_t)b * 5 * NCH + cb * RC;
-      uint32_t r16[16];
-      int dsum[16];
-      tc::tmem_ld16(col, r16);               // i + j = 2: |x| < 2^22
-      tc::tmem_ld_wait();
+      const uint32_t tcol = tbase + lane_off + kExactCols * NCH + cb * RC;
 #pragma unroll
-      for (int c = 0; c < 16; ++c)
-        dsum[c] = __float_as_int(__uint_as_float(r16[c]) + kMagic) - kMagicBits;
-      tc::tmem_ld16(col + NCH, r16);         // i + j = 3: |x| < 2^23
-      tc::tmem_ld_wait();
+      for (int h = 0; h < RC / 8; ++h) {   // 8 columns at a time (register pressure)
+        uint32_t r8[8];
+        tc::tmem_ld8(col + h * 8, r8);               // i + j = 2: |x| < 2^22
+        tc::tmem_ld_wait();
 #pragma unroll
-      for (int c = 0; c < 16; ++c)
-        acc[c] += ((long long)dsum[c] << 16) + ((long long)__float2int_rn(__uint_as_float(r16[c])) << 8);
-      tc::tmem_ld16(col + 2 * NCH, r16);     // i + j = 4: |x| < 2^24
-      tc::tmem_ld_wait();
+        for (int c = 0; c < 8; ++c)
+          acc[h * 8 + c] += shift_units(
+              __float_as_int(__uint_as_float(r8[c]) + kMagic) - kMagicBits, 32 - sh);
+        tc::tmem_ld8(col + NCH + h * 8, r8);         // i + j = 3: |x| < 2^23
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          acc[h * 8 + c] += shift_units(__float2int_rn(__uint_as_float(r8[c])), 24 - sh);
+        tc::tmem_ld8(col + 2 * NCH + h * 8, r8);     // i + j = 4: |x| < 2^24
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          acc[h * 8 + c] += shift_units(__float2int_rn(__uint_as_float(r8[c])), 16 - sh);
+        tc::tmem_ld8(tcol + h * 8, r8);              // d5, weight 2^40
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          acc[h * 8 + c] += shift_units(__float2ll_rn(__uint_as_float(r8[c]) * 256.0f), -sh);
+        tc::tmem_ld8(tcol + NCH + h * 8, r8);        // d6, weight 2^32
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          acc[h * 8 + c] += shift_units(__float2ll_rn(__uint_as_float(r8[c])), -sh);
+      }
       tc::tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&bars.acce[b]);
-#pragma unroll
-      for (int c = 0; c < 16; ++c) acc[c] += (long long)__float2int_rn(__uint_as_float(r16[c]));
+      if (lane == 0) {
+        mbar_arrive(&bars.acce[b]);
+        mbar_arrive(&bars.tailf);
+      }
     }
-    // ---- park one int64 per output: the sum of digit products in units of
-    // 2^32 (integer diagonals 2..4, weights 2^64..2^48, shifted by 16, plus
-    // the FP32 tails d5, d6 of weights 2^40, 2^32 rounded to that unit)
+    // ---- park one int64 per output
     if (ok && !s_abort) {
       long long *s_tot = reinterpret_cast<long long *>(smem);
-      const uint32_t col = tbase + lane_off + kExactCols * NCH + cb * RC;
-#pragma unroll
-      for (int c = 0; c < 16; ++c) acc[c] <<= 16;
-      if (n_rounds > 0) {
-        uint32_t r16[16];
-        tc::tmem_ld16(col, r16);                 // d5, weight 2^40
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]) * 256.0f);
-        tc::tmem_ld16(col + NCH, r16);           // d6, weight 2^32
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]));
-      }
 #pragma unroll
       for (int c = 0; c < 16; ++c) s_tot[row * NCH + cb * RC + c] = acc[c];
     }
@@ -890,9 +941,9 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       cnt = min(p.tgt_counts[tbox], p.d.nq);
       ob = (long long)r * p.n_particles + p.tgt_starts[tbox];
       // table values are m_a 2^(a_exp - kFixedBits), densities
-      // m_x 2^(x_exp - kXFixedBits); the parked sums count units of 2^32 of
-      // m_a m_x
-      ex = p.a_exp + p.x_exp[r] - (kFixedBits + kXFixedBits) + 32;
+      // m_x 2^(e - kXFixedBits) with e the row's reference exponent; the
+      // parked sums count units of 2^32 of m_a m_x
+      ex = p.a_exp + p.ref_exp[v] - (kFixedBits + kXFixedBits) + 32;
     }
     s_obase[tid] = ob;
     s_ocnt[tid] = cnt;
@@ -1045,7 +1096,8 @@ int64_t mixed_workspace_bytes(const vl1_plan *plan, int64_t nboxes, int64_t n_tg
   const MixedGeom &g = plan->mixed.geom;
   const int cv = plan->d.table_cplx ? 2 : 1;
   int64_t b = 0;
-  b += ((int64_t)nrhs * 4 + 255) / 256 * 256;                   // x exponents
+  b += (nboxes * nrhs * 4 + 255) / 256 * 256;                    // density row exponents
+  b += (n_tgt_boxes * nrhs * 4 + 255) / 256 * 256;               // target row exponents
   b += (nboxes * nrhs * g.kp * kDigits + 255) / 256 * 256;  // x digit bytes
   if (plan->d.disp_kind == VL1_DISP_LOG2D) {
     b += (nboxes * nrhs * cv * 8 + 255) / 256 * 256;            // per-box displacement
@@ -1074,16 +1126,18 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
     return VL1_E_ARG;
   }
   uint8_t *w = static_cast<uint8_t *>(workspace);
-  int *x_exp = reinterpret_cast<int *>(w);
-  const int64_t exp_bytes = ((int64_t)nrhs * 4 + 255) / 256 * 256;
-  w += exp_bytes;
-  uint8_t *xdig = w;
   const int64_t n_xrows = nboxes * nrhs;
   if (n_xrows >= INT32_MAX) {
     set_error("mixed path: %lld density rows exceed the 32-bit row index",
               (long long)n_xrows);
     return VL1_E_UNSUPPORTED;
   }
+  const int64_t n_trows = (int64_t)tree.n_tgt_boxes * nrhs;
+  int *x_exp = reinterpret_cast<int *>(w);
+  w += (n_xrows * 4 + 255) / 256 * 256;
+  int *ref_exp = reinterpret_cast<int *>(w);
+  w += (n_trows * 4 + 255) / 256 * 256;
+  uint8_t *xdig = w;
   w += (n_xrows * g.kp * kDigits + 255) / 256 * 256;
   double *wbox = nullptr, *disp = nullptr;
   if (d.disp_kind == VL1_DISP_LOG2D) {
@@ -1091,11 +1145,11 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
     w += (nboxes * nrhs * cv * 8 + 255) / 256 * 256;
     disp = reinterpret_cast<double *>(w);
   }
-  cudaError_t e = cudaMemsetAsync(x_exp, 0x80, exp_bytes, s);  // large negative exponents
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(x_exp)");
-  const int64_t nbr = nboxes * nrhs;
-  x_exponent_kernel<<<grid_for(nbr * 32, 256) < 152 * 8 ? grid_for(nbr * 32, 256) : 152 * 8,
-                      256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs, x_exp);
+  cudaError_t e;
+  const int64_t nbr = n_xrows;
+  x_exponent_kernel<<<grid_for(nbr * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
+                                                           x_exp);
+  ref_exponent_kernel<<<grid_for(n_trows, 256), 256, 0, s>>>(tree, nrhs, x_exp, ref_exp);
   x_digits_kernel<<<grid_for(nbr * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
                                                          x_exp, xdig, g.kp, g.kc, plan->status);
   if (disp) {
@@ -1117,6 +1171,7 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.n_xrows = (int32_t)n_xrows;
   mp.adig = plan->mixed.adig;
   mp.x_exp = x_exp;
+  mp.ref_exp = ref_exp;
   mp.a_exp = plan->mixed.a_exp;
   mp.disp = disp;
   mp.target_boxes = tree.target_boxes;
@@ -1170,8 +1225,8 @@ struct vl1_batch {
   void *d_probs = nullptr, *d_prep = nullptr, *d_tasks = nullptr, *d_items = nullptr;
   int n_tasks = 0;
   int *d_queue = nullptr;
-  int *x_exp_all = nullptr;
-  int64_t x_exp_bytes = 0;
+  void *d_ttasks = nullptr;   // target-row tasks of the reference exponents
+  int n_ttasks = 0;
   std::vector<BatchGroup> groups;
   std::vector<DispJob> disp;
 };
@@ -1312,10 +1367,14 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
       if (bg.n_items > 0) groups.push_back(bg);
     }
   }
-  std::vector<PrepTask> tasks;
-  for (int i = 0; i < n_problems; ++i)
+  std::vector<PrepTask> tasks, ttasks;
+  for (int i = 0; i < n_problems; ++i) {
     for (int64_t r0 = 0; r0 < nrows[i]; r0 += kRowsPerTask)
       tasks.push_back(PrepTask{i, (int32_t)std::min<int64_t>(kRowsPerTask, nrows[i] - r0), r0});
+    const int64_t nt = (int64_t)preps[i].tr.n_tgt_boxes * problems[i].nrhs;
+    for (int64_t r0 = 0; r0 < nt; r0 += 256)
+      ttasks.push_back(PrepTask{i, (int32_t)std::min<int64_t>(256, nt - r0), r0});
+  }
 
   // ---- one device buffer: parameters, work list, queues, workspaces
   int64_t off = 0;
@@ -1329,13 +1388,9 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
   off += round256(sizeof(BatchItem) * (all.size() + 1));
   const int64_t o_queue = off;
   off += round256(sizeof(int) * (groups.size() + 1));
-  const int64_t o_xexp = off;
-  std::vector<int64_t> o_exp(n_problems), o_ws(n_problems);
-  for (int i = 0; i < n_problems; ++i) {
-    o_exp[i] = off;
-    off += round256((int64_t)problems[i].nrhs * 4);
-  }
-  const int64_t xexp_bytes = off - o_xexp;
+  const int64_t o_ttasks = off;
+  off += round256(sizeof(PrepTask) * (ttasks.size() + 1));
+  std::vector<int64_t> o_ws(n_problems);
   for (int i = 0; i < n_problems; ++i) {
     o_ws[i] = off;
     off += round256(ws_need[i]);
@@ -1354,10 +1409,13 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
     const vl1_batch_problem &q = problems[i];
     const MixedGeom &g = q.plan->mixed.geom;
     const int cv = q.plan->d.table_cplx ? 2 : 1;
-    int *x_exp = reinterpret_cast<int *>(base + o_exp[i]);
     uint8_t *w = base + o_ws[i];
-    // the workspace layout of launch_mixed: [x exponents][x digits][disp]
-    w += round256((int64_t)q.nrhs * 4);
+    // the workspace layout of launch_mixed: [row exponents][target row
+    // exponents][x digits][disp]
+    int *x_exp = reinterpret_cast<int *>(w);
+    w += round256(nrows[i] * 4);
+    int *ref_exp = reinterpret_cast<int *>(w);
+    w += round256((int64_t)preps[i].tr.n_tgt_boxes * q.nrhs * 4);
     uint8_t *xdig = w;
     w += round256(nrows[i] * g.kp * kDigits);
     double *wbox = nullptr, *disp = nullptr;
@@ -1370,8 +1428,10 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
     }
     mps[i].xdig = xdig;
     mps[i].x_exp = x_exp;
+    mps[i].ref_exp = ref_exp;
     mps[i].disp = disp;
     preps[i].x_exp = x_exp;
+    preps[i].ref_exp = ref_exp;
     preps[i].xdig = xdig;
   }
   b->d_probs = base + o_probs;
@@ -1380,8 +1440,8 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
   b->d_items = base + o_items;
   b->n_tasks = (int)tasks.size();
   b->d_queue = reinterpret_cast<int *>(base + o_queue);
-  b->x_exp_all = reinterpret_cast<int *>(base + o_xexp);
-  b->x_exp_bytes = xexp_bytes;
+  b->d_ttasks = base + o_ttasks;
+  b->n_ttasks = (int)ttasks.size();
   b->groups = groups;
   struct Up {
     void *dst;
@@ -1390,7 +1450,8 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
   } ups[] = {{b->d_probs, mps.data(), sizeof(MixedParams) * n_problems},
              {b->d_prep, preps.data(), sizeof(PrepProblem) * n_problems},
              {b->d_tasks, tasks.data(), sizeof(PrepTask) * tasks.size()},
-             {b->d_items, all.data(), sizeof(BatchItem) * all.size()}};
+             {b->d_items, all.data(), sizeof(BatchItem) * all.size()},
+             {b->d_ttasks, ttasks.data(), sizeof(PrepTask) * ttasks.size()}};
   for (const Up &u : ups) {
     if (!u.n) continue;
     e = cudaMemcpy(u.dst, u.src, u.n, cudaMemcpyHostToDevice);
@@ -1420,12 +1481,15 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
     return VL1_E_ARG;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(b->x_exp_all, 0x80, b->x_exp_bytes, s);   // -> very negative
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_queue, 0, sizeof(int) * b->groups.size(), s);
+  cudaError_t e = cudaMemsetAsync(b->d_queue, 0, sizeof(int) * b->groups.size(), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(batch)");
   if (b->n_tasks > 0) {
     x_exponent_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
         static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
+    if (b->n_ttasks > 0)
+      ref_exponent_batch_kernel<<<b->n_ttasks, 256, 0, s>>>(
+          static_cast<const PrepProblem *>(b->d_prep),
+          static_cast<const PrepTask *>(b->d_ttasks));
     x_digits_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
         static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
   }
