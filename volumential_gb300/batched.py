@@ -32,7 +32,7 @@ ROWS_PER_TILE = 128
 
 _cache: "collections.OrderedDict" = collections.OrderedDict()
 _lock = threading.Lock()
-_CACHE_MAX = 8
+_CACHE_MAX = 256
 
 
 class MixedSchedule:
