@@ -361,13 +361,6 @@ __global__ void disp_target_kernel(DevDesc d, TreeDev tr, int nrhs, const double
   }
 }
 
-// x * 2^n as an integer: a left shift, or an arithmetic right shift
-// (rounding down; 0 once the shift passes the width)
-__device__ __forceinline__ long long shift_units(long long x, int n) {
-  if (n >= 0) return x << n;
-  return n <= -63 ? 0 : (x >> -n);
-}
-
 // v * 2^k rounded once to FP64 (nearest, ties to even), with integer
 // operations only while the result is a normal number
 __device__ __forceinline__ double scaled_i64_to_double(long long v, int k) {
@@ -451,7 +444,6 @@ struct Barriers {
   uint64_t empty[kStages];
   uint64_t accf[2];
   uint64_t acce[2];
-  uint64_t tailf;   // the tail blocks of the last round have been read
 };
 
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t phase,
@@ -534,7 +526,6 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       tc::mbar_init(&bars.accf[b], 1);
       tc::mbar_init(&bars.acce[b], NREAD);
     }
-    tc::mbar_init(&bars.tailf, NREAD);
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -632,14 +623,26 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     const int64_t row_bytes = (int64_t)p.g.kp * kDigits;
     uint8_t *stg = smem + (size_t)kStages * STAGE_BYTES +
                    (size_t)warp * kStgDepth * kRowsPerProducer * RB;
-    // lanes < kRowsPerProducer hold the source row of tile row my_row
+    // lanes < kRowsPerProducer hold the source row of tile row my_row and
+    // the reference exponent of its target row
     const int my_row = kRowsPerProducer * warp + (lane % kRowsPerProducer);
-    // key id and this lane's source row, fetched one key ahead
-    int nkey = 0, nxr = -1;
+    int my_ref = 0;
+    {
+      const int v = s_rows[my_row];
+      if (v >= 0) my_ref = p.ref_exp[v];
+    }
+    // key id, this lane's source row and its exponent, fetched one key ahead
+    int nkey = 0, nxr = -1, nxe = 0;
     if (n_keys > 0) {
       nkey = p.sched.key_ids[k0];
       nxr = p.sched.key_xrow[(int64_t)k0 * 128 + my_row];
+      if (nxr >= 0 && nxr < p.n_xrows) nxe = p.x_exp[nxr];
     }
+    // right shift of the staged digits of units with even / odd index: a
+    // source row's digits are fixed point against its own exponent and are
+    // moved to the target row's reference exponent as they are expanded
+    static_assert(kStgDepth == 2, "one shift register per staging slot");
+    int sh_even = 0, sh_odd = 0;
     // expand the staged bytes of unit v into stage v % kStages
     auto expand = [&](int v) -> bool {
       const int s = (ubase + v) % kStages;
@@ -648,33 +651,68 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
       const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
-      for (int t = lane; t < kRowsPerProducer * NH; t += 32) {
+      constexpr int ITER = (kRowsPerProducer * NH + 31) / 32;
+      const int shv = (v & 1) ? sh_odd : sh_even;
+      int shr[ITER];
+#pragma unroll
+      for (int i = 0; i < ITER; ++i)
+        shr[i] = __shfl_sync(0xffffffffu, shv, min((lane + 32 * i) / NH, kRowsPerProducer - 1));
+#pragma unroll
+      for (int i = 0; i < ITER; ++i) {
+        const int t = lane + 32 * i;
+        if (t >= kRowsPerProducer * NH) break;
         const int rl = t / NH, h = t - (t / NH) * NH;
         const uint8_t *src = sb + rl * RB + h * 16;
-        const uint4 top = *reinterpret_cast<const uint4 *>(src);
-        const uint32_t tw[4] = {top.x, top.y, top.z, top.w};
+        // digit planes of 16 values, most significant first, 4 values per word
+        uint32_t m[kDigits][4];
+#pragma unroll
+        for (int dg = 0; dg < kDigits; ++dg) {
+          const uint4 x4 = *reinterpret_cast<const uint4 *>(src + dg * KC);
+          m[dg][0] = x4.x;
+          m[dg][1] = x4.y;
+          m[dg][2] = x4.z;
+          m[dg][3] = x4.w;
+        }
         // sign masks of the FP16 pairs (values 4q + 0/1 and 4q + 2/3): the
         // sign of a value is bit 7 of its top digit byte
         uint32_t sg[8];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          sg[2 * q] = ((tw[q] << 8) & 0x8000u) | ((tw[q] << 16) & 0x80000000u);
-          sg[2 * q + 1] = ((tw[q] >> 8) & 0x8000u) | (tw[q] & 0x80000000u);
+          const uint32_t tw = m[0][q];
+          sg[2 * q] = ((tw << 8) & 0x8000u) | ((tw << 16) & 0x80000000u);
+          sg[2 * q + 1] = ((tw >> 8) & 0x8000u) | (tw & 0x80000000u);
+          m[0][q] = tw & 0x7F7F7F7Fu;
+        }
+        // magnitude >> sh (truncating), four values per word: whole digits
+        // first, then the bit shift within bytes (per-byte masks keep the
+        // lanes of a word apart)
+        const int sh = shr[i];
+        if (sh != 0) {
+          const int a = sh >> 3, bsh = sh & 7;
+#pragma unroll
+          for (int st = 1; st <= 4; st <<= 1) {
+            if (a & st) {
+#pragma unroll
+              for (int dg = kDigits - 1; dg >= 0; --dg)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) m[dg][q] = dg >= st ? m[dg - st][q] : 0u;
+            }
+          }
+          if (bsh != 0) {
+            const uint32_t lo = 0x01010101u * (0xFFu >> bsh);
+#pragma unroll
+            for (int dg = kDigits - 1; dg >= 1; --dg)
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                m[dg][q] = ((m[dg][q] >> bsh) & lo) | ((m[dg - 1][q] << (8 - bsh)) & ~lo);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) m[0][q] = (m[0][q] >> bsh) & lo;
+          }
         }
         const int row = kRowsPerProducer * warp + rl;
 #pragma unroll
         for (int dg = 0; dg < kDigits; ++dg) {
-          uint32_t w[4];
-          if (dg == 0) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) w[q] = tw[q] & 0x7F7F7F7Fu;
-          } else {
-            const uint4 x4 = *reinterpret_cast<const uint4 *>(src + dg * KC);
-            w[0] = x4.x;
-            w[1] = x4.y;
-            w[2] = x4.z;
-            w[3] = x4.w;
-          }
+          const uint32_t *w = m[dg];
           // bytes (b0, b1) -> FP16 pair (1024 + b0, 1024 + b1) -> minus 1024:
           // exact, two values per packed subtraction
           uint32_t o[8];
@@ -703,9 +741,11 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     bool aborted = false;
     for (int kidx = k0; kidx < k1 && !aborted; ++kidx) {
       int key = nkey, xr_lane = nxr;
+      const int xe_lane = nxe;
       if (kidx + 1 < k1) {
         nkey = p.sched.key_ids[kidx + 1];
         nxr = p.sched.key_xrow[(int64_t)(kidx + 1) * 128 + my_row];
+        nxe = (nxr >= 0 && nxr < p.n_xrows) ? p.x_exp[nxr] : 0;
       }
       const bool key_ok = key >= 0 && key < p.d.n_tables * p.d.n_cases;
       if (!key_ok) {
@@ -716,7 +756,19 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         report(p.st, VL1_E_ARG, tile, my_row);
         xr_lane = -1;
       }
+      // a source row above its target row's reference exponent is not one
+      // of that row's list-1 sources
+      int sh_lane = my_ref - xe_lane;
+      if (lane < kRowsPerProducer && xr_lane >= 0 && sh_lane < 0) {
+        report(p.st, VL1_E_ARG, tile, my_row);
+        xr_lane = -1;
+      }
+      sh_lane = min(max(sh_lane, 0), kXFixedBits + 1);   // past the width: zero
       for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
+        if (u & 1)
+          sh_odd = sh_lane;
+        else
+          sh_even = sh_lane;
         // gather unit u: piece pc of the warp's rows -> row pc / PPR, piece pc % PPR
         uint8_t *sb = stg + (u % kStgDepth) * kRowsPerProducer * RB;
 #pragma unroll
@@ -803,35 +855,15 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
           // descriptors advance by (byte offset >> 4) in their address field
           const uint64_t xd = tc::smem_desc_kmajor_swizzled(xa, ROW_BYTES);
           const uint64_t adsc = tc::smem_desc_kmajor_swizzled(xa + kDigits * XBYTES, ROW_BYTES);
-          // exact diagonals into the round buffer
 #pragma unroll
           for (int kk = 0; kk < KC / 16; ++kk) {
 #pragma unroll
-            for (int g = 0; g < 3; ++g) {
+            for (int g = 0; g < 8; ++g) {
               const MmaGroup gr = kGroups[g];
-              const uint32_t col = exact_col + (uint32_t)(gr.i + gr.j0 - 2) * NCH;
-              const bool first = g == 0 && iu == 0 && kk == 0;
-              const uint64_t ad = xd + (((uint32_t)(gr.i - 1) * XBYTES + kk * 32u) >> 4);
-              const uint64_t bd = adsc + (((uint32_t)(gr.j0 - 1) * ABYTES + kk * 32u) >> 4);
-              tc::mma_f16(col, ad, bd, tc::idesc_f16_f32(128, NCH * gr.nb), first ? 0u : 1u);
-            }
-          }
-          // tails: read after every round, so the first tail product of a
-          // round waits until the previous round's tails have been read
-          if (iu == 0 && R >= 1) {
-            if (!wait_or_abort(&bars.tailf, (R - 1) & 1, &s_abort)) {
-              aborted = true;
-              break;
-            }
-            tc::tc_fence_after();
-          }
-#pragma unroll
-          for (int kk = 0; kk < KC / 16; ++kk) {
-#pragma unroll
-            for (int g = 3; g < 8; ++g) {
-              const MmaGroup gr = kGroups[g];
-              const uint32_t col = tail_col + (uint32_t)(gr.i + gr.j0 - 5) * NCH;
-              const bool first = g == 3 && iu == 0 && kk == 0;
+              const uint32_t col = gr.exact ? exact_col + (uint32_t)(gr.i + gr.j0 - 2) * NCH
+                                            : tail_col + (uint32_t)(gr.i + gr.j0 - 5) * NCH;
+              const bool first = gr.exact ? (g == 0 && iu == 0 && kk == 0)
+                                          : (g == 3 && u == 0 && kk == 0);
               const uint64_t ad = xd + (((uint32_t)(gr.i - 1) * XBYTES + kk * 32u) >> 4);
               const uint64_t bd = adsc + (((uint32_t)(gr.j0 - 1) * ABYTES + kk * 32u) >> 4);
               tc::mma_f16(col, ad, bd, tc::idesc_f16_f32(128, NCH * gr.nb), first ? 0u : 1u);
@@ -850,71 +882,59 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     const int cb = rw >> 2;                // RC-column block
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     const int row = quad * 32 + lane;
-    // Per output: the sum of digit products in units of 2^32 of m_a m_x at
-    // the row's reference exponent e_ref.  A round (one key: one source row
-    // per tile row) is exact at its source row's exponent e_s <= e_ref; its
-    // diagonals 2..4 (weights 2^64, 2^56, 2^48) and FP32 tails d5, d6
-    // (weights 2^40, 2^32, read after every round and rounded to integers)
-    // are shifted by their weight's bits minus (e_ref - e_s).
+    // exact sum of the diagonals per output, units of 2^(e-32)
     long long acc[RC];
 #pragma unroll
     for (int c = 0; c < RC; ++c) acc[c] = 0;
-    const int v_row = s_rows[row];
-    const int e_ref = v_row >= 0 ? p.ref_exp[v_row] : 0;
     bool ok = true;
     for (int round = 0; round < n_rounds; ++round) {
       const int R = rbase + round;
       const int b = R & 1;
-      const int xr = p.sched.key_xrow[(int64_t)(k0 + round / rpk) * 128 + row];
-      const int e_src = xr >= 0 ? p.x_exp[xr] : e_ref;
-      const int sh = e_ref - e_src;   // >= 0: a source row is never above its target's reference
       if (!wait_or_abort(&bars.accf[b], (R >> 1) & 1, &s_abort)) {
         ok = false;
         break;
       }
       tc::tc_fence_after();
       const uint32_t col = tbase + lane_off + (uint32_t)b * 5 * NCH + cb * RC;
-      const uint32_t tcol = tbase + lane_off + kExactCols * NCH + cb * RC;
+      uint32_t r16[16];
+      int dsum[16];
+      tc::tmem_ld16(col, r16);               // i + j = 2: |x| < 2^22
+      tc::tmem_ld_wait();
 #pragma unroll
-      for (int h = 0; h < RC / 8; ++h) {   // 8 columns at a time (register pressure)
-        uint32_t r8[8];
-        tc::tmem_ld8(col + h * 8, r8);               // i + j = 2: |x| < 2^22
-        tc::tmem_ld_wait();
+      for (int c = 0; c < 16; ++c)
+        dsum[c] = __float_as_int(__uint_as_float(r16[c]) + kMagic) - kMagicBits;
+      tc::tmem_ld16(col + NCH, r16);         // i + j = 3: |x| < 2^23
+      tc::tmem_ld_wait();
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-          acc[h * 8 + c] += shift_units(
-              __float_as_int(__uint_as_float(r8[c]) + kMagic) - kMagicBits, 32 - sh);
-        tc::tmem_ld8(col + NCH + h * 8, r8);         // i + j = 3: |x| < 2^23
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int c = 0; c < 8; ++c)
-          acc[h * 8 + c] += shift_units(__float2int_rn(__uint_as_float(r8[c])), 24 - sh);
-        tc::tmem_ld8(col + 2 * NCH + h * 8, r8);     // i + j = 4: |x| < 2^24
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int c = 0; c < 8; ++c)
-          acc[h * 8 + c] += shift_units(__float2int_rn(__uint_as_float(r8[c])), 16 - sh);
-        tc::tmem_ld8(tcol + h * 8, r8);              // d5, weight 2^40
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int c = 0; c < 8; ++c)
-          acc[h * 8 + c] += shift_units(__float2ll_rn(__uint_as_float(r8[c]) * 256.0f), -sh);
-        tc::tmem_ld8(tcol + NCH + h * 8, r8);        // d6, weight 2^32
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int c = 0; c < 8; ++c)
-          acc[h * 8 + c] += shift_units(__float2ll_rn(__uint_as_float(r8[c])), -sh);
-      }
+      for (int c = 0; c < 16; ++c)
+        acc[c] += ((long long)dsum[c] << 16) + ((long long)__float2int_rn(__uint_as_float(r16[c])) << 8);
+      tc::tmem_ld16(col + 2 * NCH, r16);     // i + j = 4: |x| < 2^24
+      tc::tmem_ld_wait();
       tc::tc_fence_before();
       __syncwarp();
-      if (lane == 0) {
-        mbar_arrive(&bars.acce[b]);
-        mbar_arrive(&bars.tailf);
-      }
+      if (lane == 0) mbar_arrive(&bars.acce[b]);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[c] += (long long)__float2int_rn(__uint_as_float(r16[c]));
     }
-    // ---- park one int64 per output
+    // ---- park one int64 per output: the sum of digit products in units of
+    // 2^32 (integer diagonals 2..4, weights 2^64..2^48, shifted by 16, plus
+    // the FP32 tails d5, d6 of weights 2^40, 2^32 rounded to that unit)
     if (ok && !s_abort) {
       long long *s_tot = reinterpret_cast<long long *>(smem);
+      const uint32_t col = tbase + lane_off + kExactCols * NCH + cb * RC;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[c] <<= 16;
+      if (n_rounds > 0) {
+        uint32_t r16[16];
+        tc::tmem_ld16(col, r16);                 // d5, weight 2^40
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]) * 256.0f);
+        tc::tmem_ld16(col + NCH, r16);           // d6, weight 2^32
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]));
+      }
 #pragma unroll
       for (int c = 0; c < 16; ++c) s_tot[row * NCH + cb * RC + c] = acc[c];
     }
