@@ -54,10 +54,16 @@ def parse_args(argv=None):
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4"), default="c2")
+    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5"), default="c2")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--c4-problems", type=int, default=64, help="C4: problems in the batch")
     p.add_argument("--c4-max-level", type=int, default=5, help="C4: deepest uniform level")
+    p.add_argument("--c5-requests", type=int, default=10000, help="C5: requests per run")
+    p.add_argument("--c5-budget-gb", type=float, default=64.0,
+                   help="C5: HBM budget of the resident plans, trees and schedules")
+    p.add_argument("--c5-step", type=int, default=256, help="C5: most requests per step")
+    p.add_argument("--c5-rates", default="0.25,0.5,0.75,0.9",
+                   help="C5: open-loop arrival rates as fractions of the closed-loop rate")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="target CPU time of the cpu_baseline sample")
     return p.parse_args(argv)
@@ -620,12 +626,147 @@ def c4_main(args):
     return 0
 
 
+def c5_main(args):
+    """Serving (C5): ``--c5-requests`` single-rhs requests over a seeded mix of
+    2D/3D Laplace and Helmholtz (k in 1..30) problems on uniform trees of
+    1k..500k points (q in {3,4,5}), resident under an HBM budget and served by
+    continuous batching (``volumential_gb300.serving``).  One step = one
+    closed-loop run of all requests (submitted at once, steps of up to
+    ``--c5-step`` requests, two in flight); then open-loop runs with Poisson
+    arrivals at fractions of the closed-loop rate give p50/p99 latency, and
+    the same requests one per step give the unbatched comparison."""
+    import torch
+
+    from volumential_gb300 import workloads as W
+    from volumential_gb300.serving import ServingEngine, latency_stats
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    probs, reqs, mixes = W.config_c5(n_requests=args.c5_requests)
+    ws = W.c5_workloads(probs)
+    t_host = time.perf_counter() - t0
+    eng = ServingEngine(hbm_budget_bytes=int(args.c5_budget_gb * (1 << 30)),
+                        step_capacity_bytes=4 << 30, max_step_requests=args.c5_step)
+    for key, w in ws.items():
+        eng.register(key, w, w.meta["table_key"], w.meta["tree_key"], w.meta["sched_key"])
+    t0 = time.perf_counter()
+    dens, outs = {}, {}
+    for key, w in ws.items():
+        eng.admit(key)
+        pts = torch.from_numpy(np.ascontiguousarray(w.tree.targets)).to("cuda")
+        dens[key] = [m.on_device(pts).contiguous() for m in mixes[key]]
+        outs[key] = torch.empty(w.n_points, dtype=torch.complex128
+                                if w.kernel.is_complex_valued else torch.float64,
+                                device="cuda")
+    torch.cuda.synchronize()
+    t_resident = time.perf_counter() - t0
+    n_points = sum(probs[k].n_points for k, _ in reqs)
+
+    def closed_loop():
+        for key, di in reqs:
+            eng.submit(key, dens[key][di], out=outs[key])
+        ta = time.perf_counter()
+        eng.drain()
+        torch.cuda.synchronize()
+        return time.perf_counter() - ta
+
+    for _ in range(args.warmup):
+        closed_loop()
+    eng.check_status()
+    clocks = ClockSampler(local)
+    clocks.start()
+    steps_before = eng.n_steps
+    runs = [closed_loop() for _ in range(args.steps)]
+    clock_info = clocks.stop()
+    n_batches = (eng.n_steps - steps_before) / max(args.steps, 1)
+    t_run = float(np.median(runs))
+    rate = len(reqs) / t_run
+    # open loop: Poisson arrivals at fractions of the closed-loop rate
+    sweep = {}
+    for frac in [float(x) for x in args.c5_rates.split(",") if x]:
+        arr = W.poisson_arrivals(len(reqs), frac * rate, seed=int(frac * 1000))
+        done, wall = eng.run([(float(t), k, dens[k][di], outs[k])
+                              for t, (k, di) in zip(arr, reqs)])
+        st = latency_stats(done)
+        st["offered_per_s"] = frac * rate
+        st["achieved_per_s"] = len(done) / wall
+        sweep[f"{frac:g}"] = st
+    # unbatched: one request per step, waiting for each
+    n_serial = min(len(reqs), 2000)
+    eng.max_step_requests = 1
+    ta = time.perf_counter()
+    for key, di in reqs[:n_serial]:
+        eng.submit(key, dens[key][di], out=outs[key])
+        eng.drain()
+    torch.cuda.synchronize()
+    serial_rate = n_serial / (time.perf_counter() - ta)
+    eng.max_step_requests = args.c5_step
+    # accuracy (vs the FP64 path) and alone-vs-mix identity on a sample
+    rng = np.random.default_rng(5)
+    sample = [reqs[i] for i in rng.choice(len(reqs), size=min(48, len(reqs)), replace=False)]
+    mix_reqs = [eng.submit(k, dens[k][di]) for k, di in sample]
+    for key, di in reqs[:200]:
+        eng.submit(key, dens[key][di], out=outs[key])
+    eng.drain()
+    errs, same = [], True
+    sh = torch.cuda.current_stream().cuda_stream
+    for q, (key, di) in zip(mix_reqs, sample):
+        alone = eng.submit(key, dens[key][di])
+        eng.drain()
+        same = same and torch.equal(alone.out, q.out)
+        plan, (view, keep), _ = eng.admit(key)
+        ref = torch.empty_like(q.out)
+        plan.eval_fp64(view, dens[key][di], ref, stream=sh, nrhs=1)
+        torch.cuda.synchronize()
+        errs.append(float(torch.linalg.norm(q.out - ref) / torch.linalg.norm(ref)))
+    eng.check_status()
+    hbm, bf16, peak_kind = peaks()
+    kinds = {}
+    for key, _ in reqs:
+        kk = f"{key[0]}d_{key[1]}"
+        kinds[kk] = kinds.get(kk, 0) + 1
+    line = {
+        "metric": METRIC, "value": n_points / t_run, "unit": "points/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_run * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16-digits/fp32-exact/f64", "data": "synthetic",
+        "config": {"workload": f"c5_serving_{len(reqs)}req", "requests": len(reqs),
+                   "problems": len(probs), "tables": len({p.table_key for p in probs.values()}),
+                   "trees": len({w.meta["tree_key"] for w in ws.values()}),
+                   "mix": kinds, "points_range": [1000, 500000], "q": [3, 4, 5],
+                   "helmholtz_k": [1, 30], "max_step_requests": args.c5_step,
+                   "l2": "resident densities %.1f GB, far larger than L2" %
+                         (sum(d.numel() * 8 for v in dens.values() for d in v) / 1e9),
+                   "path": "continuous batching (vl1_batch_update + vl1_batch_eval)"},
+        "solves_per_s": rate, "steps_per_run": n_batches,
+        "latency_ms": sweep.get("0.5", next(iter(sweep.values()), {})),
+        "open_loop": sweep,
+        "unbatched_solves_per_s": serial_rate,
+        "speedup_over_unbatched": rate / serial_rate,
+        "rel_l2_max_vs_fp64": max(errs), "same_alone_and_in_mix": bool(same),
+        "resident_bytes": eng.budget.used, "hbm_budget_bytes": eng.budget.budget,
+        "evictions": eng.budget.evictions,
+        "setup_s": {"host": t_host, "resident": t_resident},
+        "e2e": None, "e2e_note": "resident trees, tables and densities (the serving "
+                                 "configuration); results stay on the device",
+        "clocks": clock_info, "peak_source": peak_kind,
+        "gpu_launches": int(round(n_batches * 7)),
+    }
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         return reference_arm(args)
     if args.workload == "c4":
         return c4_main(args)
+    if args.workload == "c5":
+        return c5_main(args)
     return gb300_main(args)
 
 

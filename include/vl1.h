@@ -235,14 +235,31 @@ typedef struct {
   const double *coefs;                  /* [nrhs][n_particles], device */
   int32_t nrhs;
   void *result;                         /* as for vl1_eval_mixed, device */
+  const vl1_mixed_item *host_items;     /* optional host copy of schedule->items
+                                           (NULL: copied from the device) */
 } vl1_batch_problem;
 
 typedef struct {
   int32_t ctas_per_launch;   /* persistent CTAs per kernel shape; 0: one per SM */
+  int64_t capacity_bytes;    /* device buffer of at least this size, so that
+                                later vl1_batch_update calls fit (0: exact) */
 } vl1_batch_options;
 
+/* Two problems of one batch must not share a schedule that splits tiles
+ * (its split scratch): give each problem its own schedule instance. */
 int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem *problems,
                          const vl1_batch_options *options, vl1_batch **out);
+/* Replace the batch's problems (continuous batching: one call per serving
+ * step).  No device allocation: the new parameters, work list and
+ * workspaces must fit the batch's buffer (VL1_E_ARG otherwise); they are
+ * assembled on the host (from host_items where given) and uploaded with one
+ * asynchronous copy on `stream` from pinned staging owned by the batch.
+ * The next vl1_batch_eval must be ordered after it on the same stream; an
+ * update may wait (on the host) for the upload of the update before last.
+ * CUDA graphs recorded before an update replay the old problem set's
+ * launch shapes and must be recorded again. */
+int32_t vl1_batch_update(vl1_batch *batch, int32_t n_problems,
+                         const vl1_batch_problem *problems, void *stream);
 int32_t vl1_batch_eval(vl1_batch *batch, void *stream);
 int32_t vl1_batch_destroy(vl1_batch *batch);
 /* Device bytes held by the batch (its own buffer; plans and schedules apart). */

@@ -454,3 +454,51 @@ def test_tile_schedule_rejects_two_sources_with_one_case():
     starts = np.array([0, 2])
     with pytest.raises(RuntimeError):
         MixedSchedule.tile_schedule(np.array([3, 3]), starts, np.array([1, 2]), 1, 5, 1)
+
+
+# ---- serving: resident budget and the C5 mix (host logic) -----------------
+
+def test_resident_budget_evicts_idle_entries_oldest_first():
+    from volumential_gb300.serving import AdmissionError, ResidentBudget
+
+    released = []
+    b = ResidentBudget(100, release_fn=released.append)
+    b.admit("a", 40, lambda: "A")
+    b.admit("b", 40, lambda: "B")
+    b.get("a")                      # "a" is now the most recently used
+    b.admit("c", 40, lambda: "C")   # evicts "b", the least recently used
+    assert released == ["B"] and "a" in b and "c" in b and b.used == 80
+    b.pin("a")
+    b.pin("c")
+    with pytest.raises(AdmissionError):
+        b.admit("d", 40, lambda: "D")   # both residents busy
+    assert "d" not in b and b.used == 80
+    b.unpin("c")
+    b.admit("d", 40, lambda: "D")
+    assert released == ["B", "C"] and b.evictions == 2
+    with pytest.raises(AdmissionError):
+        b.admit("e", 101, lambda: "E")  # larger than the whole budget
+    b.resize("d", 10)
+    assert b.used == 50 and b.make_room(50) and not b.make_room(101)
+
+
+def test_c5_mix_follows_its_sampling_rules():
+    from volumential_gb300.workloads import _nearest_level, config_c5, poisson_arrivals
+
+    probs, reqs, mixes = config_c5(n_requests=400)
+    probs2, reqs2, _ = config_c5(n_requests=400)
+    assert reqs == reqs2 and sorted(probs) == sorted(probs2)
+    assert len(reqs) == 400 and set(k for k, _ in reqs) == set(probs)
+    dims = [k[0] for k, _ in reqs]
+    kerns = [k[1] for k, _ in reqs]
+    assert 0.4 < dims.count(2) / 400 < 0.6 and 0.4 < kerns.count("laplace") / 400 < 0.6
+    for key, p in probs.items():
+        assert p.n_points == (2 ** p.dim) ** p.level * p.q ** p.dim
+        assert p.q in (3, 4, 5)
+        assert (p.k == 0) == (p.kernel == "laplace") and 0 <= p.k <= 30
+        assert p.table_key == (p.dim, p.kernel, p.k, p.q)
+        assert len(mixes[key]) == 4
+    # nearest level in log: 2D q4 N=5000 -> level 4 (4096), 3D q3 N=3e5 -> 4 (110,592)
+    assert _nearest_level(2, 4, 5000) == 4 and _nearest_level(3, 3, 3e5) == 4
+    t = poisson_arrivals(20000, 1000.0, seed=1)
+    assert np.all(np.diff(t) > 0) and abs(t[-1] / 20000 - 1e-3) < 5e-5

@@ -109,11 +109,12 @@ class MixedSchedule(C.Structure):
 
 class BatchProblem(C.Structure):
     _fields_ = [("plan", C.c_void_p), ("tree", C.c_void_p), ("schedule", C.c_void_p),
-                ("coefs", C.c_void_p), ("nrhs", C.c_int32), ("result", C.c_void_p)]
+                ("coefs", C.c_void_p), ("nrhs", C.c_int32), ("result", C.c_void_p),
+                ("host_items", C.c_void_p)]
 
 
 class BatchOptions(C.Structure):
-    _fields_ = [("ctas_per_launch", C.c_int32)]
+    _fields_ = [("ctas_per_launch", C.c_int32), ("capacity_bytes", C.c_int64)]
 
 
 class Status(C.Structure):
@@ -142,6 +143,8 @@ SIGNATURES = {
     "vl1_batch_create": (C.c_int32, [C.c_int32, C.POINTER(BatchProblem),
                                      C.POINTER(BatchOptions), C.POINTER(C.c_void_p)]),
     "vl1_batch_eval": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_batch_update": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(BatchProblem),
+                                     C.c_void_p]),
     "vl1_batch_destroy": (C.c_int32, [C.c_void_p]),
     "vl1_batch_device_bytes": (C.c_int64, [C.c_void_p]),
     "vl1_eval_mixed_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),

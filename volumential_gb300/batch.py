@@ -23,7 +23,8 @@ import numpy as np
 from . import _lib
 from .batched import get_schedule
 
-__all__ = ["BatchProblem", "MixedBatch", "autotune_batch", "problem_arrays"]
+__all__ = ["BatchProblem", "MixedBatch", "autotune_batch", "plan_for", "problem_arrays",
+           "tree_arrays"]
 
 TREE_KEYS = ("target_boxes", "neighbor_source_boxes_starts", "neighbor_source_boxes_lists",
              "box_centers", "box_levels", "box_source_starts", "box_source_counts_nonchild",
@@ -41,12 +42,9 @@ class BatchProblem:
         self.coefs, self.out, self.nrhs = coefs, out, int(nrhs)
 
 
-def problem_arrays(workload, plan=None):
-    """(plan, view, keep) of a workload through the FPND wrangler's argument
-    assembly; ``plan`` reuses an existing plan of the same table set."""
+def _plan_kwargs(workload):
     from .expansion_wrangler_fpnd import (FPNDExpansionWrangler,
                                           FPNDTreeIndependentDataForWrangler)
-    from .plan import as_device_tensor, tree_view_from_arrays
 
     w = workload
     ti = FPNDTreeIndependentDataForWrangler(target_kernels=[w.kernel])
@@ -57,17 +55,66 @@ def problem_arrays(workload, plan=None):
     nf = wr.near_field_evaluator(w.kernel, payload)
     kw = wr._near_field_kwargs(payload, tr.target_boxes, tr.neighbor_source_boxes_starts,
                                tr.neighbor_source_boxes_lists, None)
+    return nf, kw
+
+
+def _plan_from(nf, kw, cache):
+    return nf.get_plan(
+        table_data_combined=kw["table_data_combined"],
+        mode_nmlz_combined=kw["mode_nmlz_combined"], case_indices=kw["case_indices"],
+        encoding_base=kw["encoding_base"], encoding_shift=kw["encoding_shift"],
+        table_root_extent=kw["table_root_extent"],
+        table_starting_level=kw["table_starting_level"], cache=cache,
+        **{n: kw[n] for n in kw if n.startswith("arithmetic_")})
+
+
+def _view_from(kw):
+    from .plan import as_device_tensor, tree_view_from_arrays
+
+    return tree_view_from_arrays(root_extent=kw["root_extent"],
+                                 **{k: as_device_tensor(kw[k]) for k in TREE_KEYS})
+
+
+def problem_arrays(workload, plan=None, cache=True):
+    """(plan, view, keep) of a workload through the FPND wrangler's argument
+    assembly; ``plan`` reuses an existing plan of the same table set;
+    ``cache=False`` makes a new plan owned by the caller (outside the
+    process-wide plan cache, which destroys its oldest plans)."""
+    nf, kw = _plan_kwargs(workload)
     if plan is None:
-        plan = nf.get_plan(
-            table_data_combined=kw["table_data_combined"],
-            mode_nmlz_combined=kw["mode_nmlz_combined"], case_indices=kw["case_indices"],
-            encoding_base=kw["encoding_base"], encoding_shift=kw["encoding_shift"],
-            table_root_extent=kw["table_root_extent"],
-            table_starting_level=kw["table_starting_level"],
-            **{n: kw[n] for n in kw if n.startswith("arithmetic_")})
-    view, keep = tree_view_from_arrays(root_extent=kw["root_extent"],
-                                       **{k: as_device_tensor(kw[k]) for k in TREE_KEYS})
+        plan = _plan_from(nf, kw, cache)
+    view, keep = _view_from(kw)
     return plan, view, keep
+
+
+def plan_for(workload, cache=True):
+    """The device plan of a workload's table set (as ``problem_arrays``)."""
+    nf, kw = _plan_kwargs(workload)
+    return _plan_from(nf, kw, cache)
+
+
+def tree_arrays(workload):
+    """(view, keep) of a workload's tree in the FPND wrangler's argument
+    layout (expansion_wrangler_fpnd.py:3402-3424: sources are the targets,
+    box-local mode ids), without building its tables' payload."""
+    from .expansion_wrangler_fpnd import (_compute_box_local_ids,
+                                          _validate_table_box_particle_layout)
+
+    w = workload
+    tree, tr = w.tree, w.traversal
+    nq = w.q ** w.dim
+    _validate_table_box_particle_layout(tree, tr.target_boxes, tr.neighbor_source_boxes_lists,
+                                        nq)
+    local = _compute_box_local_ids(tree, nq)
+    counts = np.asarray(tree.box_target_counts_nonchild).astype(np.int32)
+    kw = dict(target_boxes=tr.target_boxes,
+              neighbor_source_boxes_starts=tr.neighbor_source_boxes_starts,
+              neighbor_source_boxes_lists=tr.neighbor_source_boxes_lists,
+              box_centers=tree.box_centers, box_levels=tree.box_levels,
+              box_source_starts=tree.box_target_starts, box_source_counts_nonchild=counts,
+              box_target_starts=tree.box_target_starts, box_target_counts_nonchild=counts,
+              source_mode_ids=local, target_point_ids=local, root_extent=tree.root_extent)
+    return _view_from(kw)
 
 
 class MixedBatch:
@@ -104,8 +151,9 @@ class MixedBatch:
             arr[i].coefs = p.coefs.data_ptr()
             arr[i].nrhs = p.nrhs
             arr[i].result = p.out.data_ptr()
+            arr[i].host_items = sched.items_np.ctypes.data
         self._arr = arr
-        opt = _lib.BatchOptions(int(ctas_per_launch))
+        opt = _lib.BatchOptions(int(ctas_per_launch), 0)
         handle = C.c_void_p()
         torch.cuda.current_stream().synchronize()
         _lib.check(self._lib.vl1_batch_create(len(self.problems), arr, C.byref(opt),

@@ -38,18 +38,21 @@ _CACHE_MAX = 256
 class MixedSchedule:
     """Device-resident schedule (and workspace) of one (plan, tree, nrhs)."""
 
-    def __init__(self, plan, view, keep, nrhs, stream, max_keys_per_item=None, base=None):
+    def __init__(self, plan, view, keep, nrhs, stream, max_keys_per_item=None, base=None,
+                 workspace=True):
         import torch
 
         lib = _lib.lib()
         self.nrhs = int(nrhs)
+        self.workspace = None
         if base is not None:
             # same plan, tree and nrhs: only the work items differ
             self._init_items(plan, base, max_keys_per_item)
-            ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
-            if ws < 0:
-                raise RuntimeError("vl1_mixed_workspace_bytes failed")
-            self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
+            if workspace:
+                ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
+                if ws < 0:
+                    raise RuntimeError("vl1_mixed_workspace_bytes failed")
+                self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
             return
         n_tb = int(view.n_target_boxes)
         nnz = int(keep["lists"].numel())
@@ -78,10 +81,11 @@ class MixedSchedule:
                                          else np.zeros(ROWS_PER_TILE, np.int32)).to("cuda")
         self.key_start_np = np.asarray(key_start, dtype=np.int64)
         self._init_items(plan, self, max_keys_per_item)
-        ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
-        if ws < 0:
-            raise RuntimeError("vl1_mixed_workspace_bytes failed")
-        self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
+        if workspace:
+            ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
+            if ws < 0:
+                raise RuntimeError("vl1_mixed_workspace_bytes failed")
+            self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
 
     def _init_items(self, plan, base, max_keys_per_item):
         """Work items, split counters and partial-sum scratch for a cap; the
@@ -101,8 +105,10 @@ class MixedSchedule:
         self.n_items = len(items)
         self.n_splits = n_splits
         self.max_keys_per_item = int(max(1, max((it[2] - it[1] for it in items), default=1)))
-        self.items = torch.from_numpy(np.asarray(items, dtype=np.int32).reshape(-1, 8)
-                                      if items else np.zeros((1, 8), np.int32)).to("cuda")
+        # host copy (vl1_batch_problem.host_items) and device copy of the items
+        self.items_np = np.ascontiguousarray(np.asarray(items, dtype=np.int32).reshape(-1, 8)
+                                             if items else np.zeros((1, 8), np.int32))
+        self.items = torch.from_numpy(self.items_np).to("cuda")
         self.split_counters = torch.zeros(max(1, n_splits * n_chunks), dtype=torch.int32,
                                           device="cuda")
         self.split_partials = torch.empty(max(16, n_slots * ROWS_PER_TILE * geo["np"] * 8),

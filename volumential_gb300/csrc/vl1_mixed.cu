@@ -27,6 +27,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "vl1_internal.cuh"
@@ -177,6 +178,7 @@ struct PrepProblem {
   int *x_exp;     // per density row
   int *ref_exp;   // per target row (target box index * nrhs + rhs)
   uint8_t *xdig;
+  double *wbox, *disp;   // 2D log displacement scratch (nullptr: none)
   int kp, kc;
   vl1_status *st;
 };
@@ -316,49 +318,76 @@ __global__ void x_digits_batch_kernel(const PrepProblem *probs, const PrepTask *
 
 // 2D log displacement: w[b, r] = dispfac(b) * sum_s nmlz[lev(b), s] * coef
 // (complex when the normalizers are), then disp[tb, r] = sum over list 1.
+__device__ __forceinline__ void disp_box_row(const DevDesc &d, const TreeDev &tr,
+                                             const double *coefs, int nrhs, double *w,
+                                             int64_t idx) {
+  const int cv = d.table_cplx ? 2 : 1;
+  const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
+  double re = 0.0, im = 0.0;
+  int cnt = min(tr.src_counts[b], d.nq);
+  if (cnt > 0) {
+    const int lvl = tr.levels[b];
+    const double ext = level_extent(tr.root_extent, lvl);
+    const double f = __dmul_rn(__dmul_rn(d.disp_coef, pair_scaling(d, ext)),
+                               log(__ddiv_rn(ext, d.table_root_extent)));
+    const int lev = pair_table_level(d, lvl);
+    const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
+    for (int s = 0; s < cnt; ++s) {
+      const int64_t ni = (int64_t)lev * d.nq + s;
+      re += c[s] * (f * (d.table_cplx ? d.nmlz[2 * ni] : d.nmlz[ni]));
+      if (d.table_cplx) im += c[s] * (f * d.nmlz[2 * ni + 1]);
+    }
+  }
+  w[idx * cv] = re;
+  if (cv == 2) w[idx * cv + 1] = im;
+}
+
+__device__ __forceinline__ void disp_target_row(const DevDesc &d, const TreeDev &tr, int nrhs,
+                                                const double *w, double *disp, int64_t idx) {
+  const int cv = d.table_cplx ? 2 : 1;
+  const int tb = (int)(idx / nrhs), r = (int)(idx % nrhs);
+  double re = 0.0, im = 0.0;
+  for (int p = tr.starts[tb]; p < tr.starts[tb + 1]; ++p) {
+    const int64_t wi = ((int64_t)tr.lists[p] * nrhs + r) * cv;
+    re += w[wi];
+    if (cv == 2) im += w[wi + 1];
+  }
+  disp[idx * cv] = re;
+  if (cv == 2) disp[idx * cv + 1] = im;
+}
+
 __global__ void disp_box_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
                                 int nrhs, double *w) {
   const int64_t n = (int64_t)nboxes * nrhs;
-  const int cv = d.table_cplx ? 2 : 1;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-    double re = 0.0, im = 0.0;
-    int cnt = min(tr.src_counts[b], d.nq);
-    if (cnt > 0) {
-      const int lvl = tr.levels[b];
-      const double ext = level_extent(tr.root_extent, lvl);
-      const double f = __dmul_rn(__dmul_rn(d.disp_coef, pair_scaling(d, ext)),
-                                 log(__ddiv_rn(ext, d.table_root_extent)));
-      const int lev = pair_table_level(d, lvl);
-      const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
-      for (int s = 0; s < cnt; ++s) {
-        const int64_t ni = (int64_t)lev * d.nq + s;
-        re += c[s] * (f * (d.table_cplx ? d.nmlz[2 * ni] : d.nmlz[ni]));
-        if (d.table_cplx) im += c[s] * (f * d.nmlz[2 * ni + 1]);
-      }
-    }
-    w[idx * cv] = re;
-    if (cv == 2) w[idx * cv + 1] = im;
-  }
+       idx += (int64_t)gridDim.x * blockDim.x)
+    disp_box_row(d, tr, coefs, nrhs, w, idx);
 }
 
 __global__ void disp_target_kernel(DevDesc d, TreeDev tr, int nrhs, const double *w,
                                    double *disp) {
   const int64_t n = (int64_t)tr.n_tgt_boxes * nrhs;
-  const int cv = d.table_cplx ? 2 : 1;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int tb = (int)(idx / nrhs), r = (int)(idx % nrhs);
-    double re = 0.0, im = 0.0;
-    for (int p = tr.starts[tb]; p < tr.starts[tb + 1]; ++p) {
-      const int64_t wi = ((int64_t)tr.lists[p] * nrhs + r) * cv;
-      re += w[wi];
-      if (cv == 2) im += w[wi + 1];
-    }
-    disp[idx * cv] = re;
-    if (cv == 2) disp[idx * cv + 1] = im;
-  }
+       idx += (int64_t)gridDim.x * blockDim.x)
+    disp_target_row(d, tr, nrhs, w, disp, idx);
+}
+
+// batch versions over the density-row and target-row task lists (problems
+// without a displacement return at once)
+__global__ void disp_box_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+  const PrepTask t = tasks[blockIdx.x];
+  const PrepProblem &P = probs[t.problem];
+  if (!P.wbox) return;
+  for (int i = threadIdx.x; i < t.nrows; i += blockDim.x)
+    disp_box_row(P.d, P.tr, P.coefs, P.nrhs, P.wbox, t.row0 + i);
+}
+
+__global__ void disp_target_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+  const PrepTask t = tasks[blockIdx.x];
+  const PrepProblem &P = probs[t.problem];
+  if (!P.disp) return;
+  for (int i = threadIdx.x; i < t.nrows; i += blockDim.x)
+    disp_target_row(P.d, P.tr, P.nrhs, P.wbox, P.disp, t.row0 + i);
 }
 
 // v * 2^k rounded once to FP64 (nearest, ties to even), with integer
@@ -1219,14 +1248,6 @@ namespace {
 
 constexpr int kRowsPerTask = 64;
 
-struct DispJob {   // 2D log displacement of one problem (per-problem launches)
-  vl1::DevDesc d;
-  vl1::TreeDev tr;
-  int nboxes, nrhs;
-  const double *coefs;
-  double *wbox, *disp;
-};
-
 struct BatchGroup {   // problems sharing one kernel shape: one persistent launch
   int nch, kc;
   int item0, n_items;
@@ -1241,6 +1262,8 @@ struct vl1_batch {
   int device = -1;
   void *buf = nullptr;
   int64_t bytes = 0;
+  int n_sm = 0;
+  int ctas = 0;   // persistent CTAs per kernel shape (0: one per SM)
   int n_problems = 0;
   void *d_probs = nullptr, *d_prep = nullptr, *d_tasks = nullptr, *d_items = nullptr;
   int n_tasks = 0;
@@ -1248,10 +1271,282 @@ struct vl1_batch {
   void *d_ttasks = nullptr;   // target-row tasks of the reference exponents
   int n_ttasks = 0;
   std::vector<BatchGroup> groups;
-  std::vector<DispJob> disp;
+  bool has_disp = false;
+  // pinned staging of vl1_batch_update (two, so that one can be refilled
+  // while the copy from the other is in flight)
+  void *pinned[2] = {nullptr, nullptr};
+  int64_t pinned_bytes[2] = {0, 0};
+  cudaEvent_t pinned_done[2] = {nullptr, nullptr};
+  bool pinned_used[2] = {false, false};
+  int flip = 0;
 };
 
 using namespace vl1;
+
+namespace {
+
+// Host assembly of one problem set: validated parameters, task and work
+// lists, and the layout of the batch buffer ([parameters][workspaces]).
+struct BatchLayout {
+  std::vector<MixedParams> mps;
+  std::vector<PrepProblem> preps;
+  std::vector<int64_t> ws_need, nrows;
+  std::vector<PrepTask> tasks, ttasks;
+  std::vector<BatchItem> all;
+  std::vector<BatchGroup> groups;
+  int64_t o_probs = 0, o_prep = 0, o_tasks = 0, o_items = 0, o_queue = 0, o_ttasks = 0;
+  int64_t param_bytes = 0;   // the parameter region [0, param_bytes)
+  std::vector<int64_t> o_ws;
+  int64_t total_bytes = 0;
+};
+
+int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t n_problems,
+                       const vl1_batch_problem *problems, BatchLayout &L) {
+  L = BatchLayout{};
+  L.mps.resize(n_problems);
+  L.preps.resize(n_problems);
+  L.ws_need.resize(n_problems);
+  L.nrows.resize(n_problems);
+  std::vector<std::vector<vl1_mixed_item>> items(n_problems);
+  cudaError_t e;
+  for (int i = 0; i < n_problems; ++i) {
+    const vl1_batch_problem &q = problems[i];
+    if (!q.plan || !q.tree || !q.schedule || !q.coefs || !q.result || q.nrhs < 1) {
+      set_error("%s: problem %d has a null plan/tree/schedule/coefs/result or nrhs < 1", who,
+                i);
+      return VL1_E_ARG;
+    }
+    if (q.plan->device != dev) {
+      set_error("%s: problem %d's plan is on device %d, not the current %d", who, i,
+                q.plan->device, dev);
+      return VL1_E_ARG;
+    }
+    TreeDev tr;
+    int32_t st = make_tree(q.plan, q.tree, tr);
+    if (st) return st;
+    const vl1_mixed_schedule &sc = *q.schedule;
+    if (tr.nboxes < 1 || sc.n_tiles < 0 || sc.n_items < 0 ||
+        (sc.n_tiles > 0 && (!sc.tile_rows || !sc.tile_key_start || !sc.key_ids ||
+                            !sc.key_xrow)) ||
+        (sc.n_items > 0 && !sc.items) ||
+        reinterpret_cast<uintptr_t>(sc.key_xrow) % 16 != 0 ||
+        (sc.n_splits > 0 && (!sc.split_counters || !sc.split_partials))) {
+      set_error("%s: problem %d has an invalid tree or schedule", who, i);
+      return VL1_E_ARG;
+    }
+    const MixedGeom &g = q.plan->mixed.geom;
+    if (!mixed_kernel_ptr(g.nch, g.kc, true)) {
+      set_error("%s: problem %d: unsupported kernel shape", who, i);
+      return VL1_E_UNSUPPORTED;
+    }
+    L.nrows[i] = tr.nboxes * q.nrhs;
+    if (L.nrows[i] >= INT32_MAX) {
+      set_error("%s: problem %d has %lld density rows (32-bit row index)", who, i,
+                (long long)L.nrows[i]);
+      return VL1_E_UNSUPPORTED;
+    }
+    L.ws_need[i] = mixed_workspace_bytes(q.plan, tr.nboxes, tr.n_tgt_boxes, q.nrhs);
+    MixedParams &mp = L.mps[i];
+    mp = MixedParams{};
+    mp.d = q.plan->d;
+    mp.g = g;
+    mp.nrhs = q.nrhs;
+    mp.sched = sc;
+    mp.n_xrows = (int32_t)L.nrows[i];
+    mp.adig = q.plan->mixed.adig;
+    mp.a_exp = q.plan->mixed.a_exp;
+    mp.target_boxes = tr.target_boxes;
+    mp.tgt_starts = tr.tgt_starts;
+    mp.tgt_counts = tr.tgt_counts;
+    mp.n_tgt_boxes = tr.n_tgt_boxes;
+    mp.n_particles = tr.n_particles;
+    mp.result = static_cast<double *>(q.result);
+    mp.st = q.plan->status;
+    PrepProblem &pp = L.preps[i];
+    pp = PrepProblem{};
+    pp.d = q.plan->d;
+    pp.tr = tr;
+    pp.coefs = q.coefs;
+    pp.nrhs = q.nrhs;
+    pp.kp = g.kp;
+    pp.kc = g.kc;
+    pp.st = q.plan->status;
+    // the work list of this problem: the caller's host copy of the
+    // schedule's items, else a copy from the device
+    if (sc.n_items > 0 && q.host_items) {
+      items[i].assign(q.host_items, q.host_items + sc.n_items);
+    } else if (sc.n_items > 0) {
+      items[i].resize(sc.n_items);
+      e = cudaMemcpy(items[i].data(), sc.items, sizeof(vl1_mixed_item) * sc.n_items,
+                     cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(schedule items)");
+    } else if (sc.n_tiles > 0) {
+      std::vector<int32_t> ks(sc.n_tiles + 1);
+      e = cudaMemcpy(ks.data(), sc.tile_key_start, sizeof(int32_t) * ks.size(),
+                     cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tile_key_start)");
+      for (int t = 0; t < sc.n_tiles; ++t)
+        items[i].push_back(vl1_mixed_item{t, ks[t], ks[t + 1], -1, 0, 1, -1, 0});
+    }
+    for (const vl1_mixed_item &it : items[i]) {
+      if (it.tile < 0 || it.tile >= sc.n_tiles || it.key_begin < 0 ||
+          it.key_end < it.key_begin || it.nparts < 1 || it.part < 0 ||
+          it.part >= it.nparts || it.split >= sc.n_splits ||
+          (it.split >= 0 && (it.slot < it.part || it.slot >= sc.n_slots))) {
+        set_error("%s: problem %d has an invalid work item", who, i);
+        return VL1_E_ARG;
+      }
+    }
+  }
+  // one program-wide check: two problems may not share split scratch
+  for (int i = 0; i < n_problems; ++i)
+    for (int j = i + 1; j < n_problems; ++j)
+      if (problems[i].schedule->n_splits > 0 &&
+          problems[i].schedule->split_counters == problems[j].schedule->split_counters) {
+        set_error("%s: problems %d and %d share split scratch (one schedule per problem)",
+                  who, i, j);
+        return VL1_E_ARG;
+      }
+
+  // ---- combined work list: one group per kernel shape, longest items first
+  struct Cand {
+    int64_t cost;
+    BatchItem it;
+  };
+  std::vector<std::pair<int, int>> shapes;
+  for (int i = 0; i < n_problems; ++i) {
+    const MixedGeom &g = problems[i].plan->mixed.geom;
+    std::pair<int, int> sh(g.nch, g.kc);
+    if (std::find(shapes.begin(), shapes.end(), sh) == shapes.end()) shapes.push_back(sh);
+  }
+  for (const auto &sh : shapes) {
+    std::vector<Cand> cands;
+    for (int i = 0; i < n_problems; ++i) {
+      const MixedGeom &g = problems[i].plan->mixed.geom;
+      if (g.nch != sh.first || g.kc != sh.second) continue;
+      for (const vl1_mixed_item &it : items[i])
+        for (int c = 0; c < g.np / g.nch; ++c)
+          cands.push_back(Cand{(int64_t)(it.key_end - it.key_begin) * g.n_kc + 2,
+                               BatchItem{i, c, it}});
+    }
+    std::stable_sort(cands.begin(), cands.end(),
+                     [](const Cand &a, const Cand &b) { return a.cost > b.cost; });
+    BatchGroup bg;
+    bg.nch = sh.first;
+    bg.kc = sh.second;
+    bg.item0 = (int)L.all.size();
+    bg.n_items = (int)cands.size();
+    const int ctas = ctas_opt > 0 ? ctas_opt : n_sm;
+    bg.grid = bg.n_items < ctas ? bg.n_items : ctas;
+    for (const Cand &c : cands) L.all.push_back(c.it);
+    if (bg.n_items > 0) L.groups.push_back(bg);
+  }
+  for (int i = 0; i < n_problems; ++i) {
+    for (int64_t r0 = 0; r0 < L.nrows[i]; r0 += kRowsPerTask)
+      L.tasks.push_back(
+          PrepTask{i, (int32_t)std::min<int64_t>(kRowsPerTask, L.nrows[i] - r0), r0});
+    const int64_t nt = (int64_t)L.preps[i].tr.n_tgt_boxes * problems[i].nrhs;
+    for (int64_t r0 = 0; r0 < nt; r0 += 256)
+      L.ttasks.push_back(PrepTask{i, (int32_t)std::min<int64_t>(256, nt - r0), r0});
+  }
+
+  // ---- layout: parameters, work list, queues, then the workspaces
+  int64_t off = 0;
+  L.o_probs = off;
+  off += round256(sizeof(MixedParams) * n_problems);
+  L.o_prep = off;
+  off += round256(sizeof(PrepProblem) * n_problems);
+  L.o_tasks = off;
+  off += round256(sizeof(PrepTask) * (L.tasks.size() + 1));
+  L.o_items = off;
+  off += round256(sizeof(BatchItem) * (L.all.size() + 1));
+  L.o_queue = off;
+  off += round256(sizeof(int) * (L.groups.size() + 1));
+  L.o_ttasks = off;
+  off += round256(sizeof(PrepTask) * (L.ttasks.size() + 1));
+  L.param_bytes = off;
+  L.o_ws.resize(n_problems);
+  for (int i = 0; i < n_problems; ++i) {
+    L.o_ws[i] = off;
+    off += round256(L.ws_need[i]);
+  }
+  L.total_bytes = off;
+  return VL1_OK;
+}
+
+// Point every problem at its workspace inside the buffer at `base` and make
+// the batch's launch lists; `host` receives the parameter region's bytes.
+void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems,
+                 std::vector<uint8_t> *host, uint8_t *host_ptr) {
+  uint8_t *base = static_cast<uint8_t *>(b->buf);
+  const int n_problems = (int)L.mps.size();
+  b->has_disp = false;
+  for (int i = 0; i < n_problems; ++i) {
+    const vl1_batch_problem &q = problems[i];
+    const MixedGeom &g = q.plan->mixed.geom;
+    const int cv = q.plan->d.table_cplx ? 2 : 1;
+    uint8_t *w = base + L.o_ws[i];
+    // the workspace layout of launch_mixed: [row exponents][target row
+    // exponents][x digits][disp]
+    int *x_exp = reinterpret_cast<int *>(w);
+    w += round256(L.nrows[i] * 4);
+    int *ref_exp = reinterpret_cast<int *>(w);
+    w += round256((int64_t)L.preps[i].tr.n_tgt_boxes * q.nrhs * 4);
+    uint8_t *xdig = w;
+    w += round256(L.nrows[i] * g.kp * kDigits);
+    double *wbox = nullptr, *disp = nullptr;
+    if (q.plan->d.disp_kind == VL1_DISP_LOG2D) {
+      wbox = reinterpret_cast<double *>(w);
+      w += round256(L.nrows[i] * cv * 8);
+      disp = reinterpret_cast<double *>(w);
+      b->has_disp = true;
+    }
+    L.mps[i].xdig = xdig;
+    L.mps[i].x_exp = x_exp;
+    L.mps[i].ref_exp = ref_exp;
+    L.mps[i].disp = disp;
+    L.preps[i].x_exp = x_exp;
+    L.preps[i].ref_exp = ref_exp;
+    L.preps[i].xdig = xdig;
+    L.preps[i].wbox = wbox;
+    L.preps[i].disp = disp;
+  }
+  b->n_problems = n_problems;
+  b->d_probs = base + L.o_probs;
+  b->d_prep = base + L.o_prep;
+  b->d_tasks = base + L.o_tasks;
+  b->d_items = base + L.o_items;
+  b->n_tasks = (int)L.tasks.size();
+  b->d_queue = reinterpret_cast<int *>(base + L.o_queue);
+  b->d_ttasks = base + L.o_ttasks;
+  b->n_ttasks = (int)L.ttasks.size();
+  b->groups = L.groups;
+  uint8_t *h = host_ptr;
+  if (host) {
+    host->assign(L.param_bytes, 0);
+    h = host->data();
+  }
+  auto put = [&](int64_t o, const void *src, size_t n) {
+    if (n) std::memcpy(h + o, src, n);
+  };
+  put(L.o_probs, L.mps.data(), sizeof(MixedParams) * L.mps.size());
+  put(L.o_prep, L.preps.data(), sizeof(PrepProblem) * L.preps.size());
+  put(L.o_tasks, L.tasks.data(), sizeof(PrepTask) * L.tasks.size());
+  put(L.o_items, L.all.data(), sizeof(BatchItem) * L.all.size());
+  put(L.o_ttasks, L.ttasks.data(), sizeof(PrepTask) * L.ttasks.size());
+}
+
+int32_t set_batch_smem(const std::vector<BatchGroup> &groups) {
+  for (const BatchGroup &g : groups) {
+    cudaError_t e = cudaFuncSetAttribute(mixed_kernel_ptr(g.nch, g.kc, true),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)mixed_smem_bytes(g.nch, g.kc));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batch kernel)");
+  }
+  return VL1_OK;
+}
+
+}  // namespace
 
 extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem *problems,
                                     const vl1_batch_options *options, vl1_batch **out) {
@@ -1266,233 +1561,88 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
   int n_sm = 0;
   e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
-
-  // ---- per problem: validation, parameters (workspace pointers set below)
-  std::vector<MixedParams> mps(n_problems);
-  std::vector<PrepProblem> preps(n_problems);
-  std::vector<int64_t> ws_need(n_problems), nrows(n_problems);
-  std::vector<std::vector<vl1_mixed_item>> items(n_problems);
-  for (int i = 0; i < n_problems; ++i) {
-    const vl1_batch_problem &q = problems[i];
-    if (!q.plan || !q.tree || !q.schedule || !q.coefs || !q.result || q.nrhs < 1) {
-      set_error("vl1_batch_create: problem %d has a null plan/tree/schedule/coefs/result "
-                "or nrhs < 1", i);
-      return VL1_E_ARG;
-    }
-    if (q.plan->device != dev) {
-      set_error("vl1_batch_create: problem %d's plan is on device %d, not the current %d", i,
-                q.plan->device, dev);
-      return VL1_E_ARG;
-    }
-    TreeDev tr;
-    int32_t st = make_tree(q.plan, q.tree, tr);
-    if (st) return st;
-    const vl1_mixed_schedule &sc = *q.schedule;
-    if (tr.nboxes < 1 || sc.n_tiles < 0 || sc.n_items < 0 ||
-        (sc.n_tiles > 0 && (!sc.tile_rows || !sc.tile_key_start || !sc.key_ids ||
-                            !sc.key_xrow)) ||
-        (sc.n_items > 0 && !sc.items) ||
-        reinterpret_cast<uintptr_t>(sc.key_xrow) % 16 != 0 ||
-        (sc.n_splits > 0 && (!sc.split_counters || !sc.split_partials))) {
-      set_error("vl1_batch_create: problem %d has an invalid tree or schedule", i);
-      return VL1_E_ARG;
-    }
-    const MixedGeom &g = q.plan->mixed.geom;
-    if (!mixed_kernel_ptr(g.nch, g.kc, true)) {
-      set_error("vl1_batch_create: problem %d: unsupported kernel shape", i);
-      return VL1_E_UNSUPPORTED;
-    }
-    nrows[i] = tr.nboxes * q.nrhs;
-    if (nrows[i] >= INT32_MAX) {
-      set_error("vl1_batch_create: problem %d has %lld density rows (32-bit row index)", i,
-                (long long)nrows[i]);
-      return VL1_E_UNSUPPORTED;
-    }
-    ws_need[i] = mixed_workspace_bytes(q.plan, tr.nboxes, tr.n_tgt_boxes, q.nrhs);
-    MixedParams &mp = mps[i];
-    mp = MixedParams{};
-    mp.d = q.plan->d;
-    mp.g = g;
-    mp.nrhs = q.nrhs;
-    mp.sched = sc;
-    mp.n_xrows = (int32_t)nrows[i];
-    mp.adig = q.plan->mixed.adig;
-    mp.a_exp = q.plan->mixed.a_exp;
-    mp.target_boxes = tr.target_boxes;
-    mp.tgt_starts = tr.tgt_starts;
-    mp.tgt_counts = tr.tgt_counts;
-    mp.n_tgt_boxes = tr.n_tgt_boxes;
-    mp.n_particles = tr.n_particles;
-    mp.result = static_cast<double *>(q.result);
-    mp.st = q.plan->status;
-    PrepProblem &pp = preps[i];
-    pp = PrepProblem{};
-    pp.d = q.plan->d;
-    pp.tr = tr;
-    pp.coefs = q.coefs;
-    pp.nrhs = q.nrhs;
-    pp.kp = g.kp;
-    pp.kc = g.kc;
-    pp.st = q.plan->status;
-    // the work list of this problem (host copy of the schedule's items)
-    if (sc.n_items > 0) {
-      items[i].resize(sc.n_items);
-      e = cudaMemcpy(items[i].data(), sc.items, sizeof(vl1_mixed_item) * sc.n_items,
-                     cudaMemcpyDeviceToHost);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(schedule items)");
-    } else if (sc.n_tiles > 0) {
-      std::vector<int32_t> ks(sc.n_tiles + 1);
-      e = cudaMemcpy(ks.data(), sc.tile_key_start, sizeof(int32_t) * ks.size(),
-                     cudaMemcpyDeviceToHost);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(tile_key_start)");
-      for (int t = 0; t < sc.n_tiles; ++t)
-        items[i].push_back(vl1_mixed_item{t, ks[t], ks[t + 1], -1, 0, 1, -1, 0});
-    }
-  }
-
-  // ---- combined work list: one group per kernel shape, longest items first
-  struct Cand {
-    int64_t cost;
-    BatchItem it;
-  };
-  std::vector<BatchGroup> groups;
-  std::vector<BatchItem> all;
-  {
-    std::vector<std::pair<int, int>> shapes;
-    for (int i = 0; i < n_problems; ++i) {
-      const MixedGeom &g = problems[i].plan->mixed.geom;
-      std::pair<int, int> sh(g.nch, g.kc);
-      if (std::find(shapes.begin(), shapes.end(), sh) == shapes.end()) shapes.push_back(sh);
-    }
-    for (const auto &sh : shapes) {
-      std::vector<Cand> cands;
-      for (int i = 0; i < n_problems; ++i) {
-        const MixedGeom &g = problems[i].plan->mixed.geom;
-        if (g.nch != sh.first || g.kc != sh.second) continue;
-        for (const vl1_mixed_item &it : items[i])
-          for (int c = 0; c < g.np / g.nch; ++c)
-            cands.push_back(Cand{(int64_t)(it.key_end - it.key_begin) * g.n_kc + 2,
-                                 BatchItem{i, c, it}});
-      }
-      std::stable_sort(cands.begin(), cands.end(),
-                       [](const Cand &a, const Cand &b) { return a.cost > b.cost; });
-      BatchGroup bg;
-      bg.nch = sh.first;
-      bg.kc = sh.second;
-      bg.item0 = (int)all.size();
-      bg.n_items = (int)cands.size();
-      const int ctas = options && options->ctas_per_launch > 0 ? options->ctas_per_launch : n_sm;
-      bg.grid = bg.n_items < ctas ? bg.n_items : ctas;
-      for (const Cand &c : cands) all.push_back(c.it);
-      if (bg.n_items > 0) groups.push_back(bg);
-    }
-  }
-  std::vector<PrepTask> tasks, ttasks;
-  for (int i = 0; i < n_problems; ++i) {
-    for (int64_t r0 = 0; r0 < nrows[i]; r0 += kRowsPerTask)
-      tasks.push_back(PrepTask{i, (int32_t)std::min<int64_t>(kRowsPerTask, nrows[i] - r0), r0});
-    const int64_t nt = (int64_t)preps[i].tr.n_tgt_boxes * problems[i].nrhs;
-    for (int64_t r0 = 0; r0 < nt; r0 += 256)
-      ttasks.push_back(PrepTask{i, (int32_t)std::min<int64_t>(256, nt - r0), r0});
-  }
-
-  // ---- one device buffer: parameters, work list, queues, workspaces
-  int64_t off = 0;
-  const int64_t o_probs = off;
-  off += round256(sizeof(MixedParams) * n_problems);
-  const int64_t o_prep = off;
-  off += round256(sizeof(PrepProblem) * n_problems);
-  const int64_t o_tasks = off;
-  off += round256(sizeof(PrepTask) * (tasks.size() + 1));
-  const int64_t o_items = off;
-  off += round256(sizeof(BatchItem) * (all.size() + 1));
-  const int64_t o_queue = off;
-  off += round256(sizeof(int) * (groups.size() + 1));
-  const int64_t o_ttasks = off;
-  off += round256(sizeof(PrepTask) * (ttasks.size() + 1));
-  std::vector<int64_t> o_ws(n_problems);
-  for (int i = 0; i < n_problems; ++i) {
-    o_ws[i] = off;
-    off += round256(ws_need[i]);
-  }
+  const int ctas = options && options->ctas_per_launch > 0 ? options->ctas_per_launch : 0;
+  const int64_t capacity = options && options->capacity_bytes > 0 ? options->capacity_bytes : 0;
+  BatchLayout L;
+  int32_t st = assemble_batch("vl1_batch_create", dev, n_sm, ctas, n_problems, problems, L);
+  if (st) return st;
   vl1_batch *b = new vl1_batch();
   b->device = dev;
-  b->bytes = off;
-  b->n_problems = n_problems;
-  e = cudaMalloc(&b->buf, off);
+  b->n_sm = n_sm;
+  b->ctas = ctas;
+  b->bytes = std::max(L.total_bytes, capacity);
+  e = cudaMalloc(&b->buf, b->bytes);
   if (e != cudaSuccess) {
     delete b;
     return cuda_fail(e, "cudaMalloc(batch)");
   }
-  uint8_t *base = static_cast<uint8_t *>(b->buf);
-  for (int i = 0; i < n_problems; ++i) {
-    const vl1_batch_problem &q = problems[i];
-    const MixedGeom &g = q.plan->mixed.geom;
-    const int cv = q.plan->d.table_cplx ? 2 : 1;
-    uint8_t *w = base + o_ws[i];
-    // the workspace layout of launch_mixed: [row exponents][target row
-    // exponents][x digits][disp]
-    int *x_exp = reinterpret_cast<int *>(w);
-    w += round256(nrows[i] * 4);
-    int *ref_exp = reinterpret_cast<int *>(w);
-    w += round256((int64_t)preps[i].tr.n_tgt_boxes * q.nrhs * 4);
-    uint8_t *xdig = w;
-    w += round256(nrows[i] * g.kp * kDigits);
-    double *wbox = nullptr, *disp = nullptr;
-    if (q.plan->d.disp_kind == VL1_DISP_LOG2D) {
-      wbox = reinterpret_cast<double *>(w);
-      w += round256(nrows[i] * cv * 8);
-      disp = reinterpret_cast<double *>(w);
-      b->disp.push_back(DispJob{q.plan->d, preps[i].tr, (int)preps[i].tr.nboxes, q.nrhs,
-                                q.coefs, wbox, disp});
-    }
-    mps[i].xdig = xdig;
-    mps[i].x_exp = x_exp;
-    mps[i].ref_exp = ref_exp;
-    mps[i].disp = disp;
-    preps[i].x_exp = x_exp;
-    preps[i].ref_exp = ref_exp;
-    preps[i].xdig = xdig;
+  std::vector<uint8_t> host;
+  place_batch(b, L, problems, &host, nullptr);
+  e = cudaMemcpy(b->buf, host.data(), host.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(b->buf);
+    delete b;
+    return cuda_fail(e, "cudaMemcpy(batch parameters)");
   }
-  b->d_probs = base + o_probs;
-  b->d_prep = base + o_prep;
-  b->d_tasks = base + o_tasks;
-  b->d_items = base + o_items;
-  b->n_tasks = (int)tasks.size();
-  b->d_queue = reinterpret_cast<int *>(base + o_queue);
-  b->d_ttasks = base + o_ttasks;
-  b->n_ttasks = (int)ttasks.size();
-  b->groups = groups;
-  struct Up {
-    void *dst;
-    const void *src;
-    size_t n;
-  } ups[] = {{b->d_probs, mps.data(), sizeof(MixedParams) * n_problems},
-             {b->d_prep, preps.data(), sizeof(PrepProblem) * n_problems},
-             {b->d_tasks, tasks.data(), sizeof(PrepTask) * tasks.size()},
-             {b->d_items, all.data(), sizeof(BatchItem) * all.size()},
-             {b->d_ttasks, ttasks.data(), sizeof(PrepTask) * ttasks.size()}};
-  for (const Up &u : ups) {
-    if (!u.n) continue;
-    e = cudaMemcpy(u.dst, u.src, u.n, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-      cudaFree(b->buf);
-      delete b;
-      return cuda_fail(e, "cudaMemcpy(batch parameters)");
-    }
-  }
-  for (const BatchGroup &g : groups) {
-    e = cudaFuncSetAttribute(mixed_kernel_ptr(g.nch, g.kc, true),
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)mixed_smem_bytes(g.nch, g.kc));
-    if (e != cudaSuccess) {
-      cudaFree(b->buf);
-      delete b;
-      return cuda_fail(e, "cudaFuncSetAttribute(batch kernel)");
-    }
+  st = set_batch_smem(b->groups);
+  if (st) {
+    cudaFree(b->buf);
+    delete b;
+    return st;
   }
   *out = b;
   return VL1_OK;
+}
+
+extern "C" int32_t vl1_batch_update(vl1_batch *b, int32_t n_problems,
+                                    const vl1_batch_problem *problems, void *stream) {
+  if (!b || n_problems < 1 || !problems) {
+    set_error("vl1_batch_update: null batch or no problems");
+    return VL1_E_ARG;
+  }
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev != b->device) {
+    set_error("vl1_batch_update: batch is on device %d, not the current %d", b->device, dev);
+    return VL1_E_ARG;
+  }
+  BatchLayout L;
+  int32_t st = assemble_batch("vl1_batch_update", dev, b->n_sm, b->ctas, n_problems, problems, L);
+  if (st) return st;
+  if (L.total_bytes > b->bytes) {
+    set_error("vl1_batch_update: the problems need %lld bytes, the batch holds %lld",
+              (long long)L.total_bytes, (long long)b->bytes);
+    return VL1_E_ARG;
+  }
+  // refill the staging buffer whose last copy is oldest
+  const int k = b->flip;
+  b->flip ^= 1;
+  if (b->pinned_used[k]) {
+    e = cudaEventSynchronize(b->pinned_done[k]);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventSynchronize(batch staging)");
+  }
+  if (!b->pinned_done[k]) {
+    e = cudaEventCreateWithFlags(&b->pinned_done[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate(batch staging)");
+  }
+  if (b->pinned_bytes[k] < L.param_bytes) {
+    if (b->pinned[k]) cudaFreeHost(b->pinned[k]);
+    b->pinned[k] = nullptr;
+    b->pinned_bytes[k] = 0;
+    const int64_t want = std::max<int64_t>(L.param_bytes * 2, 1 << 16);
+    e = cudaMallocHost(&b->pinned[k], want);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost(batch staging)");
+    b->pinned_bytes[k] = want;
+  }
+  place_batch(b, L, problems, nullptr, static_cast<uint8_t *>(b->pinned[k]));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  e = cudaMemcpyAsync(b->buf, b->pinned[k], L.param_bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(batch parameters)");
+  e = cudaEventRecord(b->pinned_done[k], s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord(batch staging)");
+  b->pinned_used[k] = true;
+  return set_batch_smem(b->groups);
 }
 
 extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
@@ -1513,12 +1663,13 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
     x_digits_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
         static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
   }
-  for (const DispJob &j : b->disp) {
-    const int64_t nbr = (int64_t)j.nboxes * j.nrhs;
-    disp_box_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(j.d, j.tr, j.nboxes, j.coefs, j.nrhs,
-                                                      j.wbox);
-    disp_target_kernel<<<grid_for((int64_t)j.tr.n_tgt_boxes * j.nrhs, 256), 256, 0, s>>>(
-        j.d, j.tr, j.nrhs, j.wbox, j.disp);
+  if (b->has_disp && b->n_tasks > 0) {
+    disp_box_batch_kernel<<<b->n_tasks, 64, 0, s>>>(static_cast<const PrepProblem *>(b->d_prep),
+                                                    static_cast<const PrepTask *>(b->d_tasks));
+    if (b->n_ttasks > 0)
+      disp_target_batch_kernel<<<b->n_ttasks, 256, 0, s>>>(
+          static_cast<const PrepProblem *>(b->d_prep),
+          static_cast<const PrepTask *>(b->d_ttasks));
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch preparation launch");
@@ -1540,6 +1691,11 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
 
 extern "C" int32_t vl1_batch_destroy(vl1_batch *b) {
   if (!b) return VL1_OK;
+  for (int k = 0; k < 2; ++k) {
+    if (b->pinned_used[k]) cudaEventSynchronize(b->pinned_done[k]);
+    if (b->pinned_done[k]) cudaEventDestroy(b->pinned_done[k]);
+    if (b->pinned[k]) cudaFreeHost(b->pinned[k]);
+  }
   cudaError_t e = b->buf ? cudaFree(b->buf) : cudaSuccess;
   delete b;
   return e == cudaSuccess ? VL1_OK : cuda_fail(e, "cudaFree(batch)");

@@ -477,9 +477,11 @@ class NearFieldFromCSR(NearFieldEvalBase):
                  arithmetic_case_orbit_ranks, arithmetic_case_axis_perm,
                  arithmetic_case_axis_sign, arithmetic_case_axis_group,
                  arithmetic_case_value_offsets, arithmetic_axis_sign_power,
-                 arithmetic_axis_direction_signs, arithmetic_direction_sign_axis):
-        """The device plan of this table payload (cached per payload identity)."""
-        from .plan import plan_cache_get
+                 arithmetic_axis_direction_signs, arithmetic_direction_sign_axis,
+                 cache=True):
+        """The device plan of this table payload (cached per payload identity;
+        ``cache=False``: a new plan owned by the caller)."""
+        from .plan import Plan, plan_cache_get
         policy = parse_policy(self.get_kernel_scaling_policy())
         key = (self.get_cache_key(), _array_token(table_data_combined),
                _array_token(mode_nmlz_combined), _array_token(case_indices),
@@ -488,7 +490,8 @@ class NearFieldFromCSR(NearFieldEvalBase):
                _array_token(arithmetic_case_value_offsets), int(encoding_base),
                float(encoding_shift), float(table_root_extent), int(table_starting_level),
                int(arithmetic_direction_sign_axis))
-        return plan_cache_get(
+        get = plan_cache_get if cache else (lambda _key, **kw: Plan(**kw))
+        return get(
             key, dim=self.dim, quad_order=self.quad_order, n_tables=self.n_tables,
             table_data=_to_numpy(table_data_combined), mode_nmlz=_to_numpy(mode_nmlz_combined),
             case_indices=_to_numpy(case_indices), encoding_base=int(encoding_base),

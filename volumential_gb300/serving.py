@@ -1,0 +1,425 @@
+"""Serving: continuous batching of list-1 requests on one GPU.
+
+A request is one right-hand side of one resident problem (a tree and a table
+set, e.g. "3D Helmholtz k=12, q=4, uniform level 3").  The engine keeps
+trees, plans (tables and tensor-core operands) and schedules resident in HBM
+under a byte budget, evicting the least recently used idle entries when a
+new one must be admitted.  Each step takes every pending request (up to a
+cap) into one batch: ``vl1_batch_update`` re-targets a persistent batch
+buffer to the step's problems without allocating, and ``vl1_batch_eval``
+runs the batched preparation kernels and one persistent tensor-core launch
+per kernel shape.  Two steps are kept in flight so that the host assembles
+step k+1 while the GPU runs step k.
+
+Each request is its own batch problem with its own schedule instance (the
+tile arrays are shared per resident entry), so its work items, and hence its
+result bits, do not depend on what else is in the step: a result is the same
+alone and in any mix.
+
+The reference evaluates one problem per ``NearFieldFromCSR`` call
+(``expansion_wrangler_fpnd.py:3417-3442``) with a blocking ``queue.finish()``
+(``list1.py:1481``); serving many small problems that way is launch- and
+synchronisation-bound.
+"""
+
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib
+from .batch import plan_for, tree_arrays
+from .batched import MixedSchedule
+
+__all__ = ["AdmissionError", "ResidentBudget", "Request", "ServingEngine", "latency_stats"]
+
+
+class AdmissionError(RuntimeError):
+    """A resident entry does not fit the HBM budget even after evicting
+    every idle entry."""
+
+
+def _tensor_bytes(obj):
+    import torch
+
+    if isinstance(obj, torch.Tensor):
+        return int(obj.numel() * obj.element_size())
+    if isinstance(obj, dict):
+        return sum(_tensor_bytes(v) for v in obj.values())
+    if isinstance(obj, (list, tuple)):
+        return sum(_tensor_bytes(v) for v in obj)
+    return 0
+
+
+class ResidentBudget:
+    """Byte accounting of resident entries with LRU eviction of idle ones.
+
+    ``admit(key, nbytes, build)`` makes ``key`` resident: entries not in use
+    (``pin`` count 0) are evicted oldest first until ``nbytes`` fits, then
+    ``build()`` is called and its value stored.  ``release_fn(value)`` frees
+    an evicted entry.  Host-only logic (tested without a GPU).
+    """
+
+    def __init__(self, budget_bytes, release_fn=None):
+        self.budget = int(budget_bytes)
+        self.used = 0
+        self.entries = collections.OrderedDict()   # key -> [value, nbytes, pins]
+        self.release_fn = release_fn
+        self.evictions = 0
+
+    def __contains__(self, key):
+        return key in self.entries
+
+    def get(self, key):
+        e = self.entries[key]
+        self.entries.move_to_end(key)
+        return e[0]
+
+    def pin(self, key):
+        self.entries[key][2] += 1
+
+    def unpin(self, key):
+        self.entries[key][2] -= 1
+
+    def _evict_for(self, nbytes):
+        for key in list(self.entries):
+            if self.used + nbytes <= self.budget:
+                break
+            value, nb, pins = self.entries[key]
+            if pins > 0:
+                continue
+            del self.entries[key]
+            self.used -= nb
+            self.evictions += 1
+            if self.release_fn:
+                self.release_fn(value)
+        return self.used + nbytes <= self.budget
+
+    def make_room(self, nbytes):
+        """Evict idle entries until ``nbytes`` more would fit; False if they
+        cannot."""
+        return int(nbytes) <= self.budget and self._evict_for(int(nbytes))
+
+    def admit(self, key, nbytes, build):
+        if key in self.entries:
+            return self.get(key)
+        nbytes = int(nbytes)
+        if nbytes > self.budget or not self._evict_for(nbytes):
+            raise AdmissionError(
+                f"{key!r} needs {nbytes} bytes; budget {self.budget}, in use {self.used} "
+                f"by entries that are busy")
+        value = build()
+        self.entries[key] = [value, nbytes, 0]
+        self.used += nbytes
+        return value
+
+    def resize(self, key, nbytes):
+        """Record the measured size of a resident entry (after building)."""
+        e = self.entries[key]
+        self.used += int(nbytes) - e[1]
+        e[1] = int(nbytes)
+
+
+class Request:
+    __slots__ = ("rid", "key", "coefs", "out", "arrival", "t_start", "t_done", "step",
+                 "slot")
+
+    def __init__(self, rid, key, coefs, out, arrival):
+        self.rid, self.key, self.coefs, self.out = rid, key, coefs, out
+        self.arrival = arrival
+        self.t_start = self.t_done = None
+        self.step = None
+        self.slot = None
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+class _Sched:
+    """A resident schedule base of one (tree, table level structure) and its
+    pool of per-request schedule instances."""
+
+    def __init__(self, key, tree_key, base, ws_bytes):
+        self.key, self.tree_key, self.base, self.ws_bytes = key, tree_key, base, ws_bytes
+        self.free = []
+        self.n_slots = 0
+
+
+class ServingEngine:
+    """Continuous batching over resident problems.
+
+    ``hbm_budget_bytes`` bounds the resident trees, plans and schedules
+    (``step_capacity_bytes`` more is held by the batch buffer);
+    ``max_step_requests`` caps the requests of one step.  ``register(key,
+    workload, table_key)`` declares a problem (built lazily, on its first
+    request or by ``admit``); plans are shared by problems with the same
+    ``table_key``.
+    """
+
+    def __init__(self, *, hbm_budget_bytes, step_capacity_bytes=1 << 30,
+                 max_step_requests=128, max_keys_per_item=None, max_inflight=2,
+                 stream=None):
+        import torch
+
+        self.torch = torch
+        self.lib = _lib.lib()
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        self.max_step_requests = int(max_step_requests)
+        self.step_capacity = int(step_capacity_bytes)
+        self.max_keys_per_item = max_keys_per_item
+        self.max_inflight = int(max_inflight)
+        self.specs = {}         # key -> (workload, table_key)
+        # resident entries share one budget: ("plan", table_key) -> Plan,
+        # ("tree", tree_key) -> (view, keep), ("sched", sched_key) -> _Sched;
+        # in-flight requests pin the three entries of their problem and a
+        # schedule pins its tree
+        self.budget = ResidentBudget(hbm_budget_bytes, release_fn=self._release)
+        self.pending = collections.deque()
+        self.inflight = collections.deque()   # (event, requests)
+        self.batch = None
+        self.n_steps = 0
+        self.step_sizes = []
+        self.cold_admissions = 0
+        self._next_rid = 0
+
+    # ---- residents -----------------------------------------------------
+
+    def register(self, key, workload, table_key, tree_key=None, sched_key=None):
+        """Declare problem ``key``: ``workload`` (tree, tables, kernel, q);
+        problems with the same ``table_key`` share a plan, with the same
+        ``tree_key`` a tree, and with the same ``sched_key`` (tree plus table
+        level structure and shape) a schedule."""
+        tree_key = key if tree_key is None else tree_key
+        sched_key = (tree_key, table_key) if sched_key is None else sched_key
+        self.specs[key] = (workload, table_key, tree_key, sched_key)
+
+    def _release(self, value):
+        if isinstance(value, _Sched):
+            self.budget.unpin(("tree", value.tree_key))
+            value.free.clear()
+        elif isinstance(value, tuple):   # (view, keep) of a tree
+            pass
+        else:
+            value.destroy()
+
+    def _entry(self, ekey, estimate, build, measure):
+        """Admit one entry: room for ``estimate`` bytes, ``build()``, then
+        the measured size."""
+        if ekey in self.budget:
+            return self.budget.get(ekey)
+        if not self.budget.make_room(estimate):
+            raise AdmissionError(f"{ekey!r}: no room in the HBM budget (entries busy)")
+        value = build()
+        try:
+            self.budget.admit(ekey, measure(value), lambda: value)
+        except AdmissionError:
+            self._release(value)
+            raise
+        self.cold_admissions += 1
+        return value
+
+    def admit(self, key):
+        """Make problem ``key`` resident: its plan, tree and schedule (each
+        built if needed, evicting idle entries to stay in the budget).
+        Returns (plan, (view, keep), _Sched)."""
+        workload, table_key, tree_key, sched_key = self.specs[key]
+        pkey, tkey, skey = ("plan", table_key), ("tree", tree_key), ("sched", sched_key)
+        # pin each entry as soon as it is resident so that admitting the
+        # next one cannot evict it
+        plan = self._entry(pkey, 1 << 20, lambda: plan_for(workload, cache=False),
+                           lambda pl: pl.device_bytes())
+        self.budget.pin(pkey)
+        try:
+            tree = self._entry(tkey, workload.tree.ntargets * 24,
+                               lambda: tree_arrays(workload), lambda t: _tensor_bytes(t[1]))
+            self.budget.pin(tkey)
+            try:
+                def build_sched():
+                    view, keep = tree
+                    base = MixedSchedule(plan, view, keep, 1, self.stream.cuda_stream,
+                                         self.max_keys_per_item, workspace=False)
+                    ws = int(self.lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), 1))
+                    self.budget.pin(tkey)   # held by the schedule while it is resident
+                    return _Sched(sched_key, tree_key, base, ws)
+
+                sched = self._entry(skey, workload.tree.ntargets * 4, build_sched,
+                                    lambda sc: _tensor_bytes(
+                                        [sc.base.tile_rows, sc.base.tile_key_start,
+                                         sc.base.key_ids, sc.base.key_xrow, sc.base.items,
+                                         sc.base.split_counters, sc.base.split_partials]))
+            finally:
+                self.budget.unpin(tkey)
+        finally:
+            self.budget.unpin(pkey)
+        return plan, tree, sched
+
+    def _pin_problem(self, key, delta):
+        _, table_key, tree_key, sched_key = self.specs[key]
+        for ek in (("plan", table_key), ("tree", tree_key), ("sched", sched_key)):
+            self.budget.entries[ek][2] += delta
+
+    def _slot(self, sched, plan, tree):
+        if sched.free:
+            return sched.free.pop()
+        sched.n_slots += 1
+        view, keep = tree
+        s = MixedSchedule(plan, view, keep, 1, self.stream.cuda_stream,
+                          self.max_keys_per_item, base=sched.base, workspace=False)
+        ek = ("sched", sched.key)
+        extra = _tensor_bytes([s.items, s.split_counters, s.split_partials])
+        self.budget.make_room(extra)   # best effort: the problem's own entries are pinned
+        self.budget.resize(ek, self.budget.entries[ek][1] + extra)
+        return s
+
+    # ---- requests ------------------------------------------------------
+
+    def submit(self, key, coefs, out=None, arrival=None):
+        """Queue one right-hand side ``coefs`` (CUDA float64 [N]) of problem
+        ``key``; ``out`` (optional) receives the result."""
+        torch = self.torch
+        if coefs.dtype != torch.float64 or not coefs.is_cuda or not coefs.is_contiguous():
+            raise TypeError("request densities must be contiguous CUDA float64 tensors")
+        req = Request(self._next_rid, key, coefs, out,
+                      time.perf_counter() if arrival is None else arrival)
+        self._next_rid += 1
+        self.pending.append(req)
+        return req
+
+    def _launch_step(self):
+        torch = self.torch
+        reqs, probs, need = [], [], 0
+        while self.pending and len(reqs) < self.max_step_requests:
+            req = self.pending[0]
+            plan, tree, sched = self.admit(req.key)
+            add = (sched.ws_bytes + 255) // 256 * 256 + 4096
+            if reqs and need + add > self.step_capacity // 2:
+                break
+            self.pending.popleft()
+            need += add
+            view, keep = tree
+            n_points = int(view.n_particles)
+            if req.coefs.numel() != n_points:
+                raise ValueError(f"request {req.rid}: {req.coefs.numel()} densities for a "
+                                 f"tree of {n_points} points")
+            if req.out is None:
+                req.out = torch.empty(n_points, dtype=torch.complex128 if plan.complex_table
+                                      else torch.float64, device="cuda")
+            self._pin_problem(req.key, 1)
+            req.slot = (sched, self._slot(sched, plan, tree))
+            reqs.append(req)
+            p = _lib.BatchProblem()
+            p.plan = plan.handle
+            p.tree = C.cast(C.pointer(view), C.c_void_p)
+            p.schedule = C.cast(C.pointer(req.slot[1].c_struct), C.c_void_p)
+            p.coefs = req.coefs.data_ptr()
+            p.nrhs = 1
+            p.result = req.out.data_ptr()
+            p.host_items = req.slot[1].items_np.ctypes.data
+            probs.append(p)
+        if not reqs:
+            return False
+        arr = (_lib.BatchProblem * len(probs))(*probs)
+        sh = C.c_void_p(self.stream.cuda_stream)
+        if self.batch is None:
+            opt = _lib.BatchOptions(0, self.step_capacity)
+            h = C.c_void_p()
+            _lib.check(self.lib.vl1_batch_create(len(probs), arr, C.byref(opt), C.byref(h)),
+                       "vl1_batch_create")
+            self.batch = h
+        else:
+            _lib.check(self.lib.vl1_batch_update(self.batch, len(probs), arr, sh),
+                       "vl1_batch_update")
+        now = time.perf_counter()
+        for q in reqs:
+            q.t_start = now
+            q.step = self.n_steps
+        _lib.check(self.lib.vl1_batch_eval(self.batch, sh), "vl1_batch_eval")
+        ev = torch.cuda.Event()
+        ev.record(self.stream)
+        self.inflight.append((ev, reqs, arr))
+        self.n_steps += 1
+        self.step_sizes.append(len(reqs))
+        return True
+
+    def _complete(self, reqs):
+        now = time.perf_counter()
+        for q in reqs:
+            q.t_done = now
+            sched, inst = q.slot
+            sched.free.append(inst)
+            q.slot = None
+            self._pin_problem(q.key, -1)
+
+    def poll(self):
+        """Retire finished steps; returns the requests completed."""
+        done = []
+        while self.inflight and self.inflight[0][0].query():
+            _, reqs, _ = self.inflight.popleft()
+            self._complete(reqs)
+            done.extend(reqs)
+        return done
+
+    def pump(self):
+        """One scheduling round: retire finished steps, launch one if there
+        is room in flight and requests are pending."""
+        done = self.poll()
+        if self.pending and len(self.inflight) < self.max_inflight:
+            self._launch_step()
+        return done
+
+    def drain(self):
+        out = []
+        while self.pending or self.inflight:
+            out.extend(self.pump())
+        return out
+
+    def check_status(self):
+        """Raise if any resident plan's device status word is set."""
+        for k, e in self.budget.entries.items():
+            if isinstance(k, tuple) and k and k[0] == "plan":
+                e[0].raise_on_status(self.stream.cuda_stream)
+
+    def run(self, arrivals):
+        """Drive the engine with ``arrivals``: (offset seconds, key, coefs[,
+        out]) sorted by time; requests enter the queue at their offset from
+        the start.  Returns the requests (with latencies) and the wall time."""
+        reqs = []
+        t0 = time.perf_counter()
+        i = 0
+        n = len(arrivals)
+        while i < n or self.pending or self.inflight:
+            now = time.perf_counter() - t0
+            while i < n and arrivals[i][0] <= now:
+                a = arrivals[i]
+                reqs.append(self.submit(a[1], a[2], out=a[3] if len(a) > 3 else None,
+                                        arrival=t0 + a[0]))
+                i += 1
+            self.pump()
+        self.torch.cuda.synchronize()
+        return reqs, time.perf_counter() - t0
+
+    def close(self):
+        while self.inflight:
+            self.inflight[0][0].synchronize()
+            self.poll()
+        if self.batch is not None:
+            self.lib.vl1_batch_destroy(self.batch)
+            self.batch = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def latency_stats(reqs):
+    lat = np.array([q.latency for q in reqs if q.latency is not None]) * 1e3
+    if lat.size == 0:
+        return {}
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "n": int(lat.size)}

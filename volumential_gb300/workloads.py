@@ -31,7 +31,7 @@ from .tree_build import (
 
 __all__ = ["GaussianMixture", "random_gaussian_mixture", "synthetic_tables",
            "Workload", "config_c1", "config_c2", "config_c3", "uniform_workload",
-           "adaptive_workload", "config_c4"]
+           "adaptive_workload", "config_c4", "config_c5", "C5Problem", "poisson_arrivals"]
 
 
 @dataclass
@@ -249,6 +249,107 @@ def config_c4(seed=4000, n_problems=64, levels=(3, 5), qs=(3, 4, 5), nrhs_range=
                             np.zeros((nrhs, 0)), seed,
                             meta={"level": lev, "mixtures": mixes, "table_key": q}))
     return out
+
+
+@dataclass
+class C5Problem:
+    """One resident problem of the serving mix: a uniform tree and a table
+    set.  ``table_key`` = (dim, kernel, k, q) is shared by the problems that
+    use the same tables (Helmholtz: one table per tree level)."""
+    key: tuple
+    dim: int
+    kernel: str          # "laplace" | "helmholtz"
+    k: int               # Helmholtz wave number (0 for Laplace)
+    q: int
+    level: int
+    table_key: tuple
+    n_points: int
+
+
+def _nearest_level(dim, q, n):
+    per = q ** dim
+    levels = np.arange(1, 10)
+    npts = (2 ** dim) ** levels * per
+    return int(levels[np.argmin(np.abs(np.log(npts / n)))])
+
+
+def config_c5(seed=5000, n_requests=10000, n_range=(1e3, 5e5), qs=(3, 4, 5), k_range=(1, 30),
+              densities_per_problem=4):
+    """Serving mix: ``n_requests`` single-rhs requests; dim 2 or 3 with equal
+    probability, Laplace or Helmholtz with equal probability (k uniform over
+    the integers of ``k_range``: tables are resident per (dim, kernel, q, k)),
+    N log-uniform in ``n_range`` realised as q uniform in ``qs`` and the
+    uniform level whose N = 2^(dim L) q^dim is nearest to N in log.
+
+    Returns (problems {key: C5Problem}, requests [(key, density index)],
+    density terms {key: [GaussianMixture]}): each problem has
+    ``densities_per_problem`` seeded Gaussian-sum densities (4..16 terms) and
+    each request picks one of them.
+    """
+    rng = np.random.default_rng(seed)
+    problems, reqs = {}, []
+    for _ in range(n_requests):
+        dim = 2 if rng.random() < 0.5 else 3
+        kern = "laplace" if rng.random() < 0.5 else "helmholtz"
+        k = int(rng.integers(k_range[0], k_range[1] + 1)) if kern == "helmholtz" else 0
+        n = float(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+        q = int(rng.choice(qs))
+        lev = _nearest_level(dim, q, n)
+        key = (dim, kern, k, q, lev)
+        if key not in problems:
+            problems[key] = C5Problem(key, dim, kern, k, q, lev, (dim, kern, k, q),
+                                      (2 ** dim) ** lev * q ** dim)
+        reqs.append((key, int(rng.integers(densities_per_problem))))
+    mixes = {}
+    for key in sorted(problems):
+        mixes[key] = [random_gaussian_mixture(rng, key[0], int(rng.integers(4, 17)),
+                                              (0.01, 0.1))
+                      for _ in range(densities_per_problem)]
+    return problems, reqs, mixes
+
+
+def c5_workloads(problems, seed=5000):
+    """Trees and table sets of the serving problems: {key: Workload}.  Laplace
+    uses one canonical table per (dim, q) with inferred scaling; Helmholtz one
+    table per tree level over the levels its (dim, q) problems use.  Problems
+    of one tree shape share the tree (``meta["tree_key"]``) and problems of
+    one tree and kernel share the table level structure
+    (``meta["sched_key"]``)."""
+    levels = {}
+    for p in problems.values():
+        lo, hi = levels.get((p.dim, p.q), (p.level, p.level))
+        levels[(p.dim, p.q)] = (min(lo, p.level), max(hi, p.level))
+    tables, trees = {}, {}
+    out = {}
+    for key in sorted(problems):
+        p = problems[key]
+        if p.table_key not in tables:
+            tseed = seed + 7919 * p.dim + 101 * p.q + p.k
+            if p.kernel == "laplace":
+                tables[p.table_key] = synthetic_tables(p.dim, p.q, LaplaceKernel(p.dim),
+                                                       seed=tseed, source_box_extent=1.0)
+            else:
+                lo, hi = levels[(p.dim, p.q)]
+                tables[p.table_key] = synthetic_tables(
+                    p.dim, p.q, HelmholtzKernel(p.dim), n_tables=hi - lo + 1, seed=tseed,
+                    source_box_extent=0.5 ** lo, complex_values=True)
+        tkey = (p.dim, p.q, p.level)
+        if tkey not in trees:
+            tree = build_uniform_tree(p.dim, p.level, p.q)
+            trees[tkey] = build_list1_traversal(tree)
+        trav = trees[tkey]
+        kernel = LaplaceKernel(p.dim) if p.kernel == "laplace" else HelmholtzKernel(p.dim)
+        out[key] = Workload(f"c5_{p.dim}d_{p.kernel}{p.k}_q{p.q}_l{p.level}", p.dim, p.q,
+                            kernel, trav, tables[p.table_key], np.zeros((1, 0)), seed,
+                            meta={"level": p.level, "table_key": p.table_key,
+                                  "tree_key": tkey, "sched_key": (tkey, p.kernel)})
+    return out
+
+
+def poisson_arrivals(n, rate, seed=0):
+    """Arrival offsets (seconds) of a Poisson process of ``rate`` per second."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
 
 
 def constant_workload(dim, q, level=1):
