@@ -677,9 +677,12 @@ def c5_main(args):
     clocks = ClockSampler(local)
     clocks.start()
     steps_before = eng.n_steps
+    host0, gpu0 = eng.host_s, eng.gpu_ms
     runs = [closed_loop() for _ in range(args.steps)]
     clock_info = clocks.stop()
     n_batches = (eng.n_steps - steps_before) / max(args.steps, 1)
+    host_frac = (eng.host_s - host0) / sum(runs)
+    gpu_frac = (eng.gpu_ms - gpu0) / 1e3 / sum(runs)
     t_run = float(np.median(runs))
     rate = len(reqs) / t_run
     # open loop: Poisson arrivals at fractions of the closed-loop rate
@@ -740,6 +743,8 @@ def c5_main(args):
                          (sum(d.numel() * 8 for v in dens.values() for d in v) / 1e9),
                    "path": "continuous batching (vl1_batch_update + vl1_batch_eval)"},
         "solves_per_s": rate, "steps_per_run": n_batches,
+        "closed_loop_time_shares": {"host_step_assembly": host_frac,
+                                    "gpu_steps": gpu_frac},
         "latency_ms": sweep.get("0.5", next(iter(sweep.values()), {})),
         "open_loop": sweep,
         "unbatched_solves_per_s": serial_rate,

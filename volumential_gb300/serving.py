@@ -185,6 +185,10 @@ class ServingEngine:
         self.step_sizes = []
         self.cold_admissions = 0
         self._next_rid = 0
+        # host seconds spent assembling and launching steps, and device
+        # milliseconds of the finished steps (CUDA events around each step)
+        self.host_s = 0.0
+        self.gpu_ms = 0.0
 
     # ---- residents -----------------------------------------------------
 
@@ -291,6 +295,7 @@ class ServingEngine:
 
     def _launch_step(self):
         torch = self.torch
+        t_host = time.perf_counter()
         reqs, probs, need = [], [], 0
         while self.pending and len(reqs) < self.max_step_requests:
             req = self.pending[0]
@@ -324,6 +329,8 @@ class ServingEngine:
             return False
         arr = (_lib.BatchProblem * len(probs))(*probs)
         sh = C.c_void_p(self.stream.cuda_stream)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev0.record(self.stream)
         if self.batch is None:
             opt = _lib.BatchOptions(0, self.step_capacity)
             h = C.c_void_p()
@@ -338,11 +345,12 @@ class ServingEngine:
             q.t_start = now
             q.step = self.n_steps
         _lib.check(self.lib.vl1_batch_eval(self.batch, sh), "vl1_batch_eval")
-        ev = torch.cuda.Event()
+        ev = torch.cuda.Event(enable_timing=True)
         ev.record(self.stream)
-        self.inflight.append((ev, reqs, arr))
+        self.inflight.append((ev, reqs, arr, ev0))
         self.n_steps += 1
         self.step_sizes.append(len(reqs))
+        self.host_s += time.perf_counter() - t_host
         return True
 
     def _complete(self, reqs):
@@ -358,7 +366,8 @@ class ServingEngine:
         """Retire finished steps; returns the requests completed."""
         done = []
         while self.inflight and self.inflight[0][0].query():
-            _, reqs, _ = self.inflight.popleft()
+            ev, reqs, _, ev0 = self.inflight.popleft()
+            self.gpu_ms += ev0.elapsed_time(ev)
             self._complete(reqs)
             done.extend(reqs)
         return done
