@@ -473,6 +473,7 @@ struct Barriers {
   uint64_t empty[kStages];
   uint64_t accf[2];
   uint64_t acce[2];
+  uint64_t stg[kProducerWarps][kStgDepth];   // producer staging slots
 };
 
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t phase,
@@ -555,6 +556,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       tc::mbar_init(&bars.accf[b], 1);
       tc::mbar_init(&bars.acce[b], NREAD);
     }
+    for (int w = 0; w < kProducerWarps; ++w)
+      for (int k = 0; k < kStgDepth; ++k) tc::mbar_init(&bars.stg[w][k], 1);
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -642,11 +645,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   if (warp < kProducerWarps) {
     // ------------------------------------------------------------ producers
     // Per unit: gather the byte digits of this warp's 16 rows (5 * KC bytes
-    // per row, cp.async into a kStgDepth-deep staging ring), then, kStgDepth
-    // - 1 units behind, expand that unit's bytes to FP16 digit planes in the
-    // unit's pipeline stage.
-    constexpr int RB = kDigits * KC;           // bytes per row and unit
-    constexpr int PPR = RB / 16;               // 16-byte pieces per row and unit
+    // per row: one bulk copy per present row into a kStgDepth-deep staging
+    // ring, completing on the slot's mbarrier), then, kStgDepth - 1 units
+    // behind, expand that unit's bytes to FP16 digit planes in the unit's
+    // pipeline stage.  Slots and barrier phases follow the CTA-wide unit
+    // count ubase + u, like the stages.
+    constexpr int RB = kDigits * KC;           // bytes per row and unit (multiple of 16)
     constexpr int NH = KC / 16;                // 16-value halves per digit row
     constexpr int LOOK = kStgDepth - 1;        // units gathered ahead of the expansion
     const int64_t row_bytes = (int64_t)p.g.kp * kDigits;
@@ -660,28 +664,38 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       const int v = s_rows[my_row];
       if (v >= 0) my_ref = p.ref_exp[v];
     }
-    // key id, this lane's source row and its exponent, fetched one key ahead
-    int nkey = 0, nxr = -1, nxe = 0;
+    // key id, this lane's source row and its exponent, fetched one key
+    // ahead; the source row two keys ahead, so that the exponent load never
+    // waits for the row load
+    int nkey = 0, nxr = -1, nxe = 0, nnxr = -1;
     if (n_keys > 0) {
       nkey = p.sched.key_ids[k0];
       nxr = p.sched.key_xrow[(int64_t)k0 * 128 + my_row];
       if (nxr >= 0 && nxr < p.n_xrows) nxe = p.x_exp[nxr];
     }
+    if (n_keys > 1) nnxr = p.sched.key_xrow[(int64_t)(k0 + 1) * 128 + my_row];
     // right shift of the staged digits of units with even / odd index: a
     // source row's digits are fixed point against its own exponent and are
     // moved to the target row's reference exponent as they are expanded
     static_assert(kStgDepth == 2, "one shift register per staging slot");
     int sh_even = 0, sh_odd = 0;
+    // rows of the staged units that have a source (bit rl: row rl of the warp)
+    unsigned pm_even = 0, pm_odd = 0;
     // expand the staged bytes of unit v into stage v % kStages
     auto expand = [&](int v) -> bool {
       const int s = (ubase + v) % kStages;
       const int use = (ubase + v) / kStages;
       if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) return false;
-      const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
+      const int gv = ubase + v;
+      // the unit's row copies have landed
+      if (!wait_or_abort(&bars.stg[warp][gv % kStgDepth], (gv / kStgDepth) & 1, &s_abort))
+        return false;
+      const uint8_t *sb = stg + (gv % kStgDepth) * kRowsPerProducer * RB;
+      const unsigned pmv = (gv & 1) ? pm_odd : pm_even;
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
       const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
       constexpr int ITER = (kRowsPerProducer * NH + 31) / 32;
-      const int shv = (v & 1) ? sh_odd : sh_even;
+      const int shv = (gv & 1) ? sh_odd : sh_even;
       int shr[ITER];
 #pragma unroll
       for (int i = 0; i < ITER; ++i)
@@ -692,11 +706,14 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         if (t >= kRowsPerProducer * NH) break;
         const int rl = t / NH, h = t - (t / NH) * NH;
         const uint8_t *src = sb + rl * RB + h * 16;
-        // digit planes of 16 values, most significant first, 4 values per word
+        // digit planes of 16 values, most significant first, 4 values per
+        // word (zero for rows without a source: nothing was copied there)
+        const bool present = (pmv >> rl) & 1u;
         uint32_t m[kDigits][4];
 #pragma unroll
         for (int dg = 0; dg < kDigits; ++dg) {
-          const uint4 x4 = *reinterpret_cast<const uint4 *>(src + dg * KC);
+          const uint4 x4 = present ? *reinterpret_cast<const uint4 *>(src + dg * KC)
+                                   : make_uint4(0u, 0u, 0u, 0u);
           m[dg][0] = x4.x;
           m[dg][1] = x4.y;
           m[dg][2] = x4.z;
@@ -768,14 +785,16 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     };
     int u = 0;
     bool aborted = false;
+    int ve = 0;   // next unit to expand
     for (int kidx = k0; kidx < k1 && !aborted; ++kidx) {
       int key = nkey, xr_lane = nxr;
       const int xe_lane = nxe;
       if (kidx + 1 < k1) {
         nkey = p.sched.key_ids[kidx + 1];
-        nxr = p.sched.key_xrow[(int64_t)(kidx + 1) * 128 + my_row];
+        nxr = nnxr;
         nxe = (nxr >= 0 && nxr < p.n_xrows) ? p.x_exp[nxr] : 0;
       }
+      if (kidx + 2 < k1) nnxr = p.sched.key_xrow[(int64_t)(kidx + 2) * 128 + my_row];
       const bool key_ok = key >= 0 && key < p.d.n_tables * p.d.n_cases;
       if (!key_ok) {
         if (warp == 0 && lane == 0) report(p.st, VL1_E_ARG, tile, kidx);
@@ -793,39 +812,46 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         xr_lane = -1;
       }
       sh_lane = min(max(sh_lane, 0), kXFixedBits + 1);   // past the width: zero
+      const bool have = lane < kRowsPerProducer && xr_lane >= 0;
+      const unsigned pres = __ballot_sync(0xffffffffu, have) & ((1u << kRowsPerProducer) - 1u);
       for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
-        if (u & 1)
+        const int gu = ubase + u;
+        if (gu & 1) {
           sh_odd = sh_lane;
-        else
+          pm_odd = pres;
+        } else {
           sh_even = sh_lane;
-        // gather unit u: piece pc of the warp's rows -> row pc / PPR, piece pc % PPR
-        uint8_t *sb = stg + (u % kStgDepth) * kRowsPerProducer * RB;
-#pragma unroll
-        for (int it = 0; it < (kRowsPerProducer * PPR + 31) / 32; ++it) {
-          const int pc = it * 32 + lane;
-          const int rl = min(pc / PPR, kRowsPerProducer - 1), q = pc - (pc / PPR) * PPR;
-          const int xr = __shfl_sync(0xffffffffu, xr_lane, rl);
-          if (pc < kRowsPerProducer * PPR) {
-            const bool have = xr >= 0;
-            const uint8_t *src =
-                p.xdig + (have ? (int64_t)xr * row_bytes + (int64_t)kc * RB + q * 16 : 0);
-            tc::cp_async16_zfill(sb + rl * RB + q * 16, src, have ? 16u : 0u);
-          }
+          pm_even = pres;
         }
-        tc::cp_async_commit();
-        if (u >= LOOK) {
-          tc::cp_async_wait_group<LOOK>();   // unit u - LOOK landed (this lane's pieces)
-          __syncwarp();
-          if (!expand(u - LOOK)) {
-            aborted = true;
-            break;
-          }
+        // gather unit u: one bulk copy per present row (the slot's last
+        // reads, by the expansion kStgDepth units back, were ordered before
+        // these async-proxy writes by that expansion's proxy fence)
+        uint8_t *sb = stg + (gu % kStgDepth) * kRowsPerProducer * RB;
+        uint64_t *sbar = &bars.stg[warp][gu % kStgDepth];
+        if (lane == 0) tc::mbar_arrive_expect_tx(sbar, (uint32_t)__popc(pres) * RB);
+        __syncwarp();
+        if (have)
+          tc::bulk_g2s(sb + lane * RB, p.xdig + (int64_t)xr_lane * row_bytes + (int64_t)kc * RB,
+                       RB, sbar);
+        if (u >= LOOK && !expand(u - LOOK)) {
+          aborted = true;
+          break;
         }
+        ve = u - LOOK + 1;
       }
     }
-    tc::cp_async_wait_all();
-    __syncwarp();
-    for (int v = u - LOOK < 0 ? 0 : u - LOOK; v < u && !aborted; ++v) aborted = !expand(v);
+    for (int v = ve; v < u && !aborted; ++v, ++ve) aborted = !expand(v);
+    if (aborted) {
+      // copies of units never expanded may still be in flight: wait for
+      // them (bounded) before the shared memory is released
+      for (int v = ve; v < u; ++v) {
+        const int gv = ubase + v;
+        for (uint32_t i = 0; i < kSleepPolls; ++i)
+          if (tc::mbar_try_wait_sleep(&bars.stg[warp][gv % kStgDepth], (gv / kStgDepth) & 1,
+                                      kSleepNs))
+            break;
+      }
+    }
   } else if (warp == kLoaderWarp) {
     // ---------------------------------------------------------- table loader
     if (lane == 0) {
