@@ -265,6 +265,14 @@ int32_t vl1_batch_destroy(vl1_batch *batch);
 /* Device bytes held by the batch (its own buffer; plans and schedules apart). */
 int64_t vl1_batch_device_bytes(const vl1_batch *batch);
 
+/* Measurement hook (no reference counterpart): while `begin` and `end` are
+ * set (cudaEvent_t handles, or NULL to stop), every vl1_eval_mixed and
+ * vl1_batch_eval records `begin` on its stream right before its tensor-core
+ * kernel launch(es) and `end` right after, so that a caller can time that
+ * kernel alone with cudaEventElapsedTime.  Process-wide; not for concurrent
+ * callers. */
+int32_t vl1_set_kernel_events(void *begin, void *end);
+
 /* Size of the fixed scratch array used by vl1_eval_mixed_noalloc (32 MiB). */
 #define VL1_NOALLOC_SCRATCH_BYTES (32LL << 20)
 

@@ -143,6 +143,7 @@ SIGNATURES = {
     "vl1_batch_create": (C.c_int32, [C.c_int32, C.POINTER(BatchProblem),
                                      C.POINTER(BatchOptions), C.POINTER(C.c_void_p)]),
     "vl1_batch_eval": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_set_kernel_events": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_batch_update": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(BatchProblem),
                                      C.c_void_p]),
     "vl1_batch_destroy": (C.c_int32, [C.c_void_p]),

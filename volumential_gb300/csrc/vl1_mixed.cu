@@ -473,7 +473,6 @@ struct Barriers {
   uint64_t empty[kStages];
   uint64_t accf[2];
   uint64_t acce[2];
-  uint64_t stg[kProducerWarps][kStgDepth];   // producer staging slots
 };
 
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t phase,
@@ -556,8 +555,6 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       tc::mbar_init(&bars.accf[b], 1);
       tc::mbar_init(&bars.acce[b], NREAD);
     }
-    for (int w = 0; w < kProducerWarps; ++w)
-      for (int k = 0; k < kStgDepth; ++k) tc::mbar_init(&bars.stg[w][k], 1);
     tc::fence_mbar_init();
     s_abort = 0;
   }
@@ -645,12 +642,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   if (warp < kProducerWarps) {
     // ------------------------------------------------------------ producers
     // Per unit: gather the byte digits of this warp's 16 rows (5 * KC bytes
-    // per row: one bulk copy per present row into a kStgDepth-deep staging
-    // ring, completing on the slot's mbarrier), then, kStgDepth - 1 units
-    // behind, expand that unit's bytes to FP16 digit planes in the unit's
-    // pipeline stage.  Slots and barrier phases follow the CTA-wide unit
-    // count ubase + u, like the stages.
-    constexpr int RB = kDigits * KC;           // bytes per row and unit (multiple of 16)
+    // per row, cp.async into a kStgDepth-deep staging ring), then, kStgDepth
+    // - 1 units behind, expand that unit's bytes to FP16 digit planes in the
+    // unit's pipeline stage.  (One bulk copy per row instead was measured
+    // slower: the copies queue behind each other in the copy engine.)
+    constexpr int RB = kDigits * KC;           // bytes per row and unit
+    constexpr int PPR = RB / 16;               // 16-byte pieces per row and unit
     constexpr int NH = KC / 16;                // 16-value halves per digit row
     constexpr int LOOK = kStgDepth - 1;        // units gathered ahead of the expansion
     const int64_t row_bytes = (int64_t)p.g.kp * kDigits;
@@ -679,23 +676,16 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     // moved to the target row's reference exponent as they are expanded
     static_assert(kStgDepth == 2, "one shift register per staging slot");
     int sh_even = 0, sh_odd = 0;
-    // rows of the staged units that have a source (bit rl: row rl of the warp)
-    unsigned pm_even = 0, pm_odd = 0;
     // expand the staged bytes of unit v into stage v % kStages
     auto expand = [&](int v) -> bool {
       const int s = (ubase + v) % kStages;
       const int use = (ubase + v) / kStages;
       if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) return false;
-      const int gv = ubase + v;
-      // the unit's row copies have landed
-      if (!wait_or_abort(&bars.stg[warp][gv % kStgDepth], (gv / kStgDepth) & 1, &s_abort))
-        return false;
-      const uint8_t *sb = stg + (gv % kStgDepth) * kRowsPerProducer * RB;
-      const unsigned pmv = (gv & 1) ? pm_odd : pm_even;
+      const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
       const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
       constexpr int ITER = (kRowsPerProducer * NH + 31) / 32;
-      const int shv = (gv & 1) ? sh_odd : sh_even;
+      const int shv = (v & 1) ? sh_odd : sh_even;
       int shr[ITER];
 #pragma unroll
       for (int i = 0; i < ITER; ++i)
@@ -706,14 +696,11 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         if (t >= kRowsPerProducer * NH) break;
         const int rl = t / NH, h = t - (t / NH) * NH;
         const uint8_t *src = sb + rl * RB + h * 16;
-        // digit planes of 16 values, most significant first, 4 values per
-        // word (zero for rows without a source: nothing was copied there)
-        const bool present = (pmv >> rl) & 1u;
+        // digit planes of 16 values, most significant first, 4 values per word
         uint32_t m[kDigits][4];
 #pragma unroll
         for (int dg = 0; dg < kDigits; ++dg) {
-          const uint4 x4 = present ? *reinterpret_cast<const uint4 *>(src + dg * KC)
-                                   : make_uint4(0u, 0u, 0u, 0u);
+          const uint4 x4 = *reinterpret_cast<const uint4 *>(src + dg * KC);
           m[dg][0] = x4.x;
           m[dg][1] = x4.y;
           m[dg][2] = x4.z;
@@ -785,7 +772,6 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     };
     int u = 0;
     bool aborted = false;
-    int ve = 0;   // next unit to expand
     for (int kidx = k0; kidx < k1 && !aborted; ++kidx) {
       int key = nkey, xr_lane = nxr;
       const int xe_lane = nxe;
@@ -812,46 +798,39 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         xr_lane = -1;
       }
       sh_lane = min(max(sh_lane, 0), kXFixedBits + 1);   // past the width: zero
-      const bool have = lane < kRowsPerProducer && xr_lane >= 0;
-      const unsigned pres = __ballot_sync(0xffffffffu, have) & ((1u << kRowsPerProducer) - 1u);
       for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
-        const int gu = ubase + u;
-        if (gu & 1) {
+        if (u & 1)
           sh_odd = sh_lane;
-          pm_odd = pres;
-        } else {
+        else
           sh_even = sh_lane;
-          pm_even = pres;
+        // gather unit u: piece pc of the warp's rows -> row pc / PPR, piece pc % PPR
+        uint8_t *sb = stg + (u % kStgDepth) * kRowsPerProducer * RB;
+#pragma unroll
+        for (int it = 0; it < (kRowsPerProducer * PPR + 31) / 32; ++it) {
+          const int pc = it * 32 + lane;
+          const int rl = min(pc / PPR, kRowsPerProducer - 1), q = pc - (pc / PPR) * PPR;
+          const int xr = __shfl_sync(0xffffffffu, xr_lane, rl);
+          if (pc < kRowsPerProducer * PPR) {
+            const bool have = xr >= 0;
+            const uint8_t *src =
+                p.xdig + (have ? (int64_t)xr * row_bytes + (int64_t)kc * RB + q * 16 : 0);
+            tc::cp_async16_zfill(sb + rl * RB + q * 16, src, have ? 16u : 0u);
+          }
         }
-        // gather unit u: one bulk copy per present row (the slot's last
-        // reads, by the expansion kStgDepth units back, were ordered before
-        // these async-proxy writes by that expansion's proxy fence)
-        uint8_t *sb = stg + (gu % kStgDepth) * kRowsPerProducer * RB;
-        uint64_t *sbar = &bars.stg[warp][gu % kStgDepth];
-        if (lane == 0) tc::mbar_arrive_expect_tx(sbar, (uint32_t)__popc(pres) * RB);
-        __syncwarp();
-        if (have)
-          tc::bulk_g2s(sb + lane * RB, p.xdig + (int64_t)xr_lane * row_bytes + (int64_t)kc * RB,
-                       RB, sbar);
-        if (u >= LOOK && !expand(u - LOOK)) {
-          aborted = true;
-          break;
-        }
-        ve = u - LOOK + 1;
-      }
-    }
-    for (int v = ve; v < u && !aborted; ++v, ++ve) aborted = !expand(v);
-    if (aborted) {
-      // copies of units never expanded may still be in flight: wait for
-      // them (bounded) before the shared memory is released
-      for (int v = ve; v < u; ++v) {
-        const int gv = ubase + v;
-        for (uint32_t i = 0; i < kSleepPolls; ++i)
-          if (tc::mbar_try_wait_sleep(&bars.stg[warp][gv % kStgDepth], (gv / kStgDepth) & 1,
-                                      kSleepNs))
+        tc::cp_async_commit();
+        if (u >= LOOK) {
+          tc::cp_async_wait_group<LOOK>();   // unit u - LOOK landed (this lane's pieces)
+          __syncwarp();
+          if (!expand(u - LOOK)) {
+            aborted = true;
             break;
+          }
+        }
       }
     }
+    tc::cp_async_wait_all();
+    __syncwarp();
+    for (int v = u - LOOK < 0 ? 0 : u - LOOK; v < u && !aborted; ++v) aborted = !expand(v);
   } else if (warp == kLoaderWarp) {
     // ---------------------------------------------------------- table loader
     if (lane == 0) {
@@ -1188,6 +1167,16 @@ int32_t launch_classify(vl1_plan *plan, const TreeDev &tree, int32_t *keys, cuda
   return e == cudaSuccess ? VL1_OK : cuda_fail(e, "classify_pairs_kernel launch");
 }
 
+// Measurement hook (vl1_set_kernel_events): events recorded on the call's
+// stream right before and after the tensor-core kernel launches.
+cudaEvent_t g_kernel_begin = nullptr, g_kernel_end = nullptr;
+
+int32_t record_kernel_event(cudaEvent_t ev, cudaStream_t s) {
+  if (!ev) return VL1_OK;
+  cudaError_t e = cudaEventRecord(ev, s);
+  return e == cudaSuccess ? VL1_OK : cuda_fail(e, "cudaEventRecord(kernel event)");
+}
+
 int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
                      const vl1_mixed_schedule &sched, const double *coefs, int nrhs,
                      double *result, void *workspace, int64_t ws_bytes, cudaStream_t s) {
@@ -1262,8 +1251,11 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   }
   dim3 grid(sched.n_items > 0 ? sched.n_items : sched.n_tiles, g.np / g.nch);
   BatchLaunch none{};
+  int32_t st = record_kernel_event(g_kernel_begin, s);
+  if (st) return st;
   e = launch_mixed_kernel(g.nch, g.kc, false, grid, s, mp, none);
-  return e == cudaSuccess ? VL1_OK : cuda_fail(e, "mixed_kernel launch");
+  if (e != cudaSuccess) return cuda_fail(e, "mixed_kernel launch");
+  return record_kernel_event(g_kernel_end, s);
 }
 
 }  // namespace vl1
@@ -1700,6 +1692,8 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch preparation launch");
   const MixedParams unused{};
+  int32_t st = record_kernel_event(g_kernel_begin, s);
+  if (st) return st;
   for (size_t gi = 0; gi < b->groups.size(); ++gi) {
     const BatchGroup &g = b->groups[gi];
     BatchLaunch bl;
@@ -1712,7 +1706,7 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
                          dim3(mixed_threads(g.nch)), args, mixed_smem_bytes(g.nch, g.kc), s);
     if (e != cudaSuccess) return cuda_fail(e, "batch mixed_kernel launch");
   }
-  return VL1_OK;
+  return record_kernel_event(g_kernel_end, s);
 }
 
 extern "C" int32_t vl1_batch_destroy(vl1_batch *b) {
@@ -1728,3 +1722,9 @@ extern "C" int32_t vl1_batch_destroy(vl1_batch *b) {
 }
 
 extern "C" int64_t vl1_batch_device_bytes(const vl1_batch *b) { return b ? b->bytes : -1; }
+
+extern "C" int32_t vl1_set_kernel_events(void *begin, void *end) {
+  vl1::g_kernel_begin = static_cast<cudaEvent_t>(begin);
+  vl1::g_kernel_end = static_cast<cudaEvent_t>(end);
+  return VL1_OK;
+}
