@@ -230,6 +230,7 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
             self._check_table_levels(kn, lst)
         self._payload_cache = collections.OrderedDict()
         self._payload_cache_max = 16
+        self._view_cache = collections.OrderedDict()
         self._layout_validated = set()
 
     # {{{ table bookkeeping (expansion_wrangler_fpnd.py:2414-2472)
@@ -416,12 +417,24 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                 **{n: kw[n] for n in kw if n.startswith("arithmetic_")})
             nf._check_single_table_levels(kw["neighbor_source_boxes_lists"],
                                           kw["box_levels"], kw["table_starting_level"])
-            view, keep = tree_view_from_arrays(**{n: kw[n] for n in (
-                "target_boxes", "neighbor_source_boxes_starts", "neighbor_source_boxes_lists",
-                "box_centers", "box_levels", "box_source_starts",
-                "box_source_counts_nonchild", "box_target_starts",
-                "box_target_counts_nonchild", "source_mode_ids", "target_point_ids",
-                "root_extent")})
+            # device tree arrays per (box lists, layout): repeated calls reuse
+            # them, and with them the cached tensor-core schedule
+            vkey = (id(target_boxes), id(neighbor_source_boxes_starts),
+                    id(neighbor_source_boxes_lists), int(payload["table_data_shapes"]
+                                                         ["n_q_points"]))
+            hit = self._view_cache.get(vkey)
+            if hit is None or hit[2] is not target_boxes:
+                view, keep = tree_view_from_arrays(**{n: kw[n] for n in (
+                    "target_boxes", "neighbor_source_boxes_starts",
+                    "neighbor_source_boxes_lists", "box_centers", "box_levels",
+                    "box_source_starts", "box_source_counts_nonchild", "box_target_starts",
+                    "box_target_counts_nonchild", "source_mode_ids", "target_point_ids",
+                    "root_extent")})
+                if len(self._view_cache) >= 4:
+                    self._view_cache.pop(next(iter(self._view_cache)))
+                self._view_cache[vkey] = (view, keep, target_boxes)
+            else:
+                view, keep = hit[0], hit[1]
             c = coefs
             if c.dtype not in (torch.float64, torch.complex128):
                 c = c.to(torch.complex128 if c.is_complex() else torch.float64)
@@ -441,7 +454,6 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
             plan.raise_on_status(stream)
             outs.append(out)
             events.append(evt)
-            del keep
         return outs, _TimingFuture(events)
 
     # {{{ reordering and bookkeeping of drive_volume_fmm
