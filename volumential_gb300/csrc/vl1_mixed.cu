@@ -457,8 +457,13 @@ struct MixedParams {
 // The table digit planes j = 1..5 of a stage are stacked along N, so one MMA
 // multiplies density digit i by several table digits j at once; its output
 // column blocks land on consecutive diagonals i + j.
+// Density planes of a stage: the exact digits X1, X2, X3 and, for the tails
+// only, R = X4 + X5 / 256 rounded to FP16 (11 significant bits: the density
+// keeps ~2^-35 of its row's reference scale in the tails, far below the
+// 2^-24 weight of the tails; the exact diagonals use X1..X3 only).
 constexpr int kStages = 3;
-constexpr int kStgDepth = 2;         // byte staging ring per producer warp
+constexpr int kXPlanes = 4;          // density planes per stage: X1, X2, X3, R
+constexpr int kStgDepth = 3;         // byte staging ring per producer warp
 constexpr uint32_t kExactCols = 3;   // accumulators per buffer
 constexpr int kProducerWarps = 8;
 constexpr int kRowsPerProducer = 128 / kProducerWarps;
@@ -508,10 +513,13 @@ struct MmaGroup {
   int i, j0, nb, exact;  // exact: into the round buffer (else the tail blocks)
 };
 // exact diagonals 2..4: (1; 1..3), (2; 1..2), (3; 1); tails 5..6:
-// (1; 4..5), (2; 3..4), (3; 2..3), (4; 1..2), (5; 1)
-__device__ constexpr MmaGroup kGroups[8] = {{1, 1, 3, 1}, {2, 1, 2, 1}, {3, 1, 1, 1},
-                                            {1, 4, 2, 0}, {2, 3, 2, 0}, {3, 2, 2, 0},
-                                            {4, 1, 2, 0}, {5, 1, 1, 0}};
+// (1; 4..5), (2; 3..4), (3; 2..3), (R; 1..2) with density plane 4 holding
+// R = X4 + X5 / 256: R A1 = X4 A1 + X5 A1 / 256 covers (4, 1) and (5, 1),
+// R A2 covers (4, 2) (plus the negligible (5, 2) / 256)
+constexpr int kGroupCount = 7;
+__device__ constexpr MmaGroup kGroups[kGroupCount] = {{1, 1, 3, 1}, {2, 1, 2, 1}, {3, 1, 1, 1},
+                                                      {1, 4, 2, 0}, {2, 3, 2, 0}, {3, 2, 2, 0},
+                                                      {4, 1, 2, 0}};
 
 // MULTI == false: one work item per CTA (blockIdx.x; column chunk blockIdx.y)
 // of the single problem p1.  MULTI == true: a persistent launch over the
@@ -527,7 +535,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   constexpr uint32_t COLS = NCH * 8 > 256 ? 512 : (NCH * 8 > 128 ? 256 : 128);
   constexpr uint32_t XBYTES = 128u * KC * 2u;      // one digit plane of the rows
   constexpr uint32_t ABYTES = (uint32_t)NCH * KC * 2u;   // one digit plane of the table
-  constexpr uint32_t STAGE_BYTES = kDigits * (XBYTES + ABYTES);
+  constexpr uint32_t STAGE_BYTES = kXPlanes * XBYTES + kDigits * ABYTES;
   constexpr uint32_t ROW_BYTES = KC * 2u;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // swizzle atoms need a 1024-byte aligned base (the launch adds 1 KiB slack)
@@ -674,8 +682,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     // right shift of the staged digits of units with even / odd index: a
     // source row's digits are fixed point against its own exponent and are
     // moved to the target row's reference exponent as they are expanded
-    static_assert(kStgDepth == 2, "one shift register per staging slot");
-    int sh_even = 0, sh_odd = 0;
+    static_assert(kStgDepth == 3, "one shift register per staging slot");
+    int sh_s0 = 0, sh_s1 = 0, sh_s2 = 0;
     // expand the staged bytes of unit v into stage v % kStages
     auto expand = [&](int v) -> bool {
       const int s = (ubase + v) % kStages;
@@ -685,7 +693,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
       const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
       constexpr int ITER = (kRowsPerProducer * NH + 31) / 32;
-      const int shv = (v & 1) ? sh_odd : sh_even;
+      const int vs = v % kStgDepth;
+      const int shv = vs == 0 ? sh_s0 : (vs == 1 ? sh_s1 : sh_s2);
       int shr[ITER];
 #pragma unroll
       for (int i = 0; i < ITER; ++i)
@@ -743,8 +752,32 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
           }
         }
         const int row = kRowsPerProducer * warp + rl;
+        // plane 3: R = X4 + X5 / 256 rounded to FP16.  (X4 << 8 | X5) / 256
+        // is exact in FP32 as 2^15 + v * 2^-8 - 2^15; one rounding to FP16.
+        {
+          uint32_t o[8];
 #pragma unroll
-        for (int dg = 0; dg < kDigits; ++dg) {
+          for (int q = 0; q < 4; ++q) {
+            const uint32_t v01 = __byte_perm(m[4][q], m[3][q], 0x5140u);
+            const uint32_t v23 = __byte_perm(m[4][q], m[3][q], 0x7362u);
+            const float f0 = __uint_as_float(0x47000000u | (v01 & 0xFFFFu)) - 32768.0f;
+            const float f1 = __uint_as_float(0x47000000u | (v01 >> 16)) - 32768.0f;
+            const float f2 = __uint_as_float(0x47000000u | (v23 & 0xFFFFu)) - 32768.0f;
+            const float f3 = __uint_as_float(0x47000000u | (v23 >> 16)) - 32768.0f;
+            __half2 h01 = __floats2half2_rn(f0, f1);
+            __half2 h23 = __floats2half2_rn(f2, f3);
+            o[2 * q] = *reinterpret_cast<uint32_t *>(&h01) | sg[2 * q];
+            o[2 * q + 1] = *reinterpret_cast<uint32_t *>(&h23) | sg[2 * q + 1];
+          }
+          uint8_t *pl = xs + 3 * XBYTES;
+          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16, KC)) =
+              make_uint4(o[0], o[1], o[2], o[3]);
+          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16 + 8, KC)) =
+              make_uint4(o[4], o[5], o[6], o[7]);
+        }
+        // planes 0..2: the exact digits X1, X2, X3
+#pragma unroll
+        for (int dg = 0; dg < 3; ++dg) {
           const uint32_t *w = m[dg];
           // bytes (b0, b1) -> FP16 pair (1024 + b0, 1024 + b1) -> minus 1024:
           // exact, two values per packed subtraction
@@ -799,10 +832,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       }
       sh_lane = min(max(sh_lane, 0), kXFixedBits + 1);   // past the width: zero
       for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
-        if (u & 1)
-          sh_odd = sh_lane;
-        else
-          sh_even = sh_lane;
+        {
+          const int us = u % kStgDepth;
+          sh_s0 = us == 0 ? sh_lane : sh_s0;
+          sh_s1 = us == 1 ? sh_lane : sh_s1;
+          sh_s2 = us == 2 ? sh_lane : sh_s2;
+        }
         // gather unit u: piece pc of the warp's rows -> row pc / PPR, piece pc % PPR
         uint8_t *sb = stg + (u % kStgDepth) * kRowsPerProducer * RB;
 #pragma unroll
@@ -848,7 +883,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
             aborted = true;
             break;
           }
-          uint8_t *as = smem + (size_t)s * STAGE_BYTES + kDigits * XBYTES;
+          uint8_t *as = smem + (size_t)s * STAGE_BYTES + kXPlanes * XBYTES;
           tc::mbar_arrive_expect_tx(&bars.full[s], kDigits * ABYTES);
           const int64_t base = (((int64_t)key * p.g.n_kc + kc) * kDigits) * p.g.np * KC +
                                (int64_t)chunk * NCH * KC;
@@ -888,11 +923,11 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
           const uint32_t xa = tc::smem_addr(smem + (size_t)s * STAGE_BYTES);
           // descriptors advance by (byte offset >> 4) in their address field
           const uint64_t xd = tc::smem_desc_kmajor_swizzled(xa, ROW_BYTES);
-          const uint64_t adsc = tc::smem_desc_kmajor_swizzled(xa + kDigits * XBYTES, ROW_BYTES);
+          const uint64_t adsc = tc::smem_desc_kmajor_swizzled(xa + kXPlanes * XBYTES, ROW_BYTES);
 #pragma unroll
           for (int kk = 0; kk < KC / 16; ++kk) {
 #pragma unroll
-            for (int g = 0; g < 8; ++g) {
+            for (int g = 0; g < kGroupCount; ++g) {
               const MmaGroup gr = kGroups[g];
               const uint32_t col = gr.exact ? exact_col + (uint32_t)(gr.i + gr.j0 - 2) * NCH
                                             : tail_col + (uint32_t)(gr.i + gr.j0 - 5) * NCH;
@@ -1081,7 +1116,7 @@ const void *mixed_kernel_ptr(int nch, int kc, bool multi) {
 }
 
 size_t mixed_smem_bytes(int nch, int kc) {
-  const size_t pipe = (size_t)kStages * kDigits * (128 + nch) * kc * 2 +
+  const size_t pipe = (size_t)kStages * (kXPlanes * 128 + kDigits * nch) * kc * 2 +
                       (size_t)kProducerWarps * kStgDepth * kRowsPerProducer * kDigits * kc;
   const size_t park = (size_t)128 * nch * 8;   // int64 sums
   return (pipe > park ? pipe : park) + 1024;
