@@ -20,6 +20,7 @@ from volumential_gb300.plan import as_device_tensor
 pytestmark = pytest.mark.gpu
 
 TOL_MIXED = 1e-9
+TOL_SPLIT = 2e-11
 
 
 def _run(torch, w, cap):
@@ -48,7 +49,9 @@ def test_split_adaptive_3d_matches_unsplit_and_oracle(cuda, cap):
     assert s0.n_splits == 0
     split, s1 = _run(torch, w, cap)
     assert s1.n_splits > 0 and s1.max_keys_per_item <= cap
-    assert rel_l2(split[0], whole[0]) <= 1e-12
+    # the FP32 tail sums (whose last density plane carries fractional bits)
+    # round differently over different key ranges; the exact parts agree
+    assert rel_l2(split[0], whole[0]) <= TOL_SPLIT
     prob = oracle_for_workload(w, LAP3)
     assert rel_l2(split[0], oracle_eval(prob, w, w.coefs[0])) <= TOL_MIXED
 
