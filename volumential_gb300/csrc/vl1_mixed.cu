@@ -474,7 +474,8 @@ constexpr uint32_t kSleepNs = 200000;      // longest sleep of one wait poll
 constexpr uint32_t kSleepPolls = 10000;    // polls before a wait gives up (~2 s)
 
 struct Barriers {
-  uint64_t full[kStages];
+  uint64_t xfull[kStages];   // the producer warps' density planes are in the stage
+  uint64_t afull[kStages];   // the table digit tiles have landed
   uint64_t empty[kStages];
   uint64_t accf[2];
   uint64_t acce[2];
@@ -555,8 +556,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      // one arrival per producer warp + the table copies' expect_tx
-      tc::mbar_init(&bars.full[s], kProducerWarps + 1);
+      tc::mbar_init(&bars.xfull[s], kProducerWarps);   // one arrival per producer warp
+      tc::mbar_init(&bars.afull[s], 1);                // the loader's expect_tx
       tc::mbar_init(&bars.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -800,7 +801,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       }
       tc::fence_proxy_async_smem();   // generic writes -> tensor-core reads
       __syncwarp();
-      if (lane == 0) mbar_arrive(&bars.full[s]);
+      if (lane == 0) mbar_arrive(&bars.xfull[s]);
       return true;
     };
     int u = 0;
@@ -884,13 +885,13 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
             break;
           }
           uint8_t *as = smem + (size_t)s * STAGE_BYTES + kXPlanes * XBYTES;
-          tc::mbar_arrive_expect_tx(&bars.full[s], kDigits * ABYTES);
+          tc::mbar_arrive_expect_tx(&bars.afull[s], kDigits * ABYTES);
           const int64_t base = (((int64_t)key * p.g.n_kc + kc) * kDigits) * p.g.np * KC +
                                (int64_t)chunk * NCH * KC;
 #pragma unroll
           for (int dg = 0; dg < kDigits; ++dg)
             tc::bulk_g2s(as + dg * ABYTES, p.adig + base + (int64_t)dg * p.g.np * KC, ABYTES,
-                         &bars.full[s]);
+                         &bars.afull[s]);
         }
       }
     }
@@ -912,7 +913,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         const uint32_t exact_col = tbase + (uint32_t)b * 5 * NCH;
         for (int iu = 0; iu < upr; ++iu, ++u) {
           const int s = (ubase + u) % kStages;
-          if (!wait_or_abort(&bars.full[s], ((ubase + u) / kStages) & 1, &s_abort)) {
+          const uint32_t ph = ((ubase + u) / kStages) & 1;
+          if (!wait_or_abort(&bars.afull[s], ph, &s_abort)) {
+            aborted = true;
+            break;
+          }
+          if (!wait_or_abort(&bars.xfull[s], ph, &s_abort)) {
             aborted = true;
             break;
           }
