@@ -265,6 +265,47 @@ int32_t vl1_batch_destroy(vl1_batch *batch);
 /* Device bytes held by the batch (its own buffer; plans and schedules apart). */
 int64_t vl1_batch_device_bytes(const vl1_batch *batch);
 
+/* ---- Table builder: FP64 Duffy radial quadrature ----------------------
+ * Values of near-field table entries, T = int_{[0,h]^d} G(t - y) phi(y) dy,
+ * by the scheme of the reference's batched builder
+ * (volumential/nearfield_potential_table.py:2035-2223, nodes :2225-2291;
+ * 1D rules volumential/singular_integral_2d.py:807-853): the box split at
+ * the clipped target into 2^d sub-boxes and d! Duffy simplices each, a
+ * tanh-sinh radial rule and a Gauss-Legendre tail rule.  G includes the
+ * kernel's scaling constant: Laplace 2D -log(r)/(2 pi), 3D 1/(4 pi r);
+ * Helmholtz 2D (i/4) H0^(1)(k r), 3D exp(i k r)/(4 pi r); constant 1;
+ * plane wave cos(k d_0) (a test kernel).  All arrays are device arrays;
+ * result is [n_entries] doubles, or [n_entries][2] (re, im) when
+ * complex_output.  Replaces _batched_duffy_values_for_local_indices
+ * (nearfield_potential_table.py:2331-2463). */
+enum {
+  VL1_DUFFY_LAPLACE2D = 0,
+  VL1_DUFFY_LAPLACE3D = 1,
+  VL1_DUFFY_HELMHOLTZ2D = 2,
+  VL1_DUFFY_HELMHOLTZ3D = 3,
+  VL1_DUFFY_CONSTANT = 4,
+  VL1_DUFFY_PLANE_WAVE = 5
+};
+
+typedef struct {
+  int32_t dim, q, n_entries;
+  int32_t n_reg, n_rad;       /* 1D rule sizes */
+  int32_t kernel;             /* VL1_DUFFY_* */
+  int32_t complex_output;
+  int32_t reserved;
+  double extent;              /* source box [0, extent]^dim */
+  double k;                   /* Helmholtz / plane-wave wave number */
+  const double *target_points;          /* [dim][n_entries] */
+  const double *decomposition_targets;  /* [dim][n_entries]: targets clipped to the box */
+  const int32_t *mode_axes;             /* [dim][n_entries]: source mode index per axis */
+  const double *regular_nodes, *regular_weights;   /* [n_reg] on [0, 1] */
+  const double *radial_nodes, *radial_weights;     /* [n_rad] on (0, 1) */
+  const double *interp_nodes;    /* [q]: 1D Gauss-Legendre nodes on [0, extent] */
+  const double *interp_weights;  /* [q]: 1 / prod_{j != m} (x_m - x_j) */
+} vl1_duffy_desc;
+
+int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, void *stream);
+
 /* Measurement hook (no reference counterpart): while `begin` and `end` are
  * set (cudaEvent_t handles, or NULL to stop), every vl1_eval_mixed and
  * vl1_batch_eval records `begin` on its stream right before its tensor-core

@@ -117,6 +117,22 @@ class BatchOptions(C.Structure):
     _fields_ = [("ctas_per_launch", C.c_int32), ("capacity_bytes", C.c_int64)]
 
 
+class DuffyDesc(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("q", C.c_int32), ("n_entries", C.c_int32),
+                ("n_reg", C.c_int32), ("n_rad", C.c_int32), ("kernel", C.c_int32),
+                ("complex_output", C.c_int32), ("reserved", C.c_int32),
+                ("extent", C.c_double), ("k", C.c_double),
+                ("target_points", C.c_void_p), ("decomposition_targets", C.c_void_p),
+                ("mode_axes", C.c_void_p), ("regular_nodes", C.c_void_p),
+                ("regular_weights", C.c_void_p), ("radial_nodes", C.c_void_p),
+                ("radial_weights", C.c_void_p), ("interp_nodes", C.c_void_p),
+                ("interp_weights", C.c_void_p)]
+
+
+VL1_DUFFY_LAPLACE2D, VL1_DUFFY_LAPLACE3D, VL1_DUFFY_HELMHOLTZ2D = 0, 1, 2
+VL1_DUFFY_HELMHOLTZ3D, VL1_DUFFY_CONSTANT, VL1_DUFFY_PLANE_WAVE = 3, 4, 5
+
+
 class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("count", C.c_int32),
                 ("detail0", C.c_int32), ("detail1", C.c_int32)]
@@ -144,6 +160,7 @@ SIGNATURES = {
                                      C.POINTER(BatchOptions), C.POINTER(C.c_void_p)]),
     "vl1_batch_eval": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_set_kernel_events": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_duffy_table": (C.c_int32, [C.POINTER(DuffyDesc), C.c_void_p, C.c_void_p]),
     "vl1_batch_update": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(BatchProblem),
                                      C.c_void_p]),
     "vl1_batch_destroy": (C.c_int32, [C.c_void_p]),

@@ -1,0 +1,260 @@
+// FP64 table builder: singular box integrals by the Duffy radial scheme.
+//
+// Each table entry (case, source mode, target point) is
+//   T = int_{[0,h]^d} G(t - y) phi_m(y) dy
+// with t the case's target point, phi_m the source mode's tensor Lagrange
+// basis on the Gauss-Legendre nodes of [0, h], and G a free-space kernel.
+// The scheme of the reference's batched builder
+// (volumential/nearfield_potential_table.py:2035-2223 for the integrand,
+// :2225-2291 for the nodes): the box is split at the target point clipped
+// into it into 2^d sub-boxes (one per sign vector; empty ones dropped), each
+// sub-box into d! simplices (one per axis order), and each simplex is
+// mapped from the unit cube by the Duffy map u_{perm(i)} = prod_{k<=i} r_k,
+// whose Jacobian prod_{i<d-1} r_i^(d-1-i) cancels the singularity at the
+// target; r_0 (radial) takes a tanh-sinh rule, r_1.. a Gauss-Legendre rule.
+//
+// GPU layout: one CTA per entry, threads striding over the quadrature nodes
+// (sign vector x axis order x regular nodes x radial nodes, decoded from the
+// node index; only the 1D rules are read), FP64 sums reduced per CTA.  The
+// node count per entry is 2^d d! n_reg^(d-1) n_rad (3D, default orders:
+// 8 x 6 x 400 x 123 = 2.4M), so the kernel is bound by the FP64 pipe.
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "vl1_internal.cuh"
+
+namespace vl1 {
+namespace {
+
+constexpr int kDuffyThreads = 256;
+constexpr int kDuffyMaxQ = 16;
+
+struct DuffyArgs {
+  vl1_duffy_desc d;
+  int n_perm, n_reg_tail, n_sub;
+  double *out;
+};
+
+// axis orders in itertools.permutations order
+__device__ constexpr int8_t kPerm2[2][2] = {{0, 1}, {1, 0}};
+__device__ constexpr int8_t kPerm3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2},
+                                            {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+
+// G(dvec) times the kernel's scaling constant; (re, im)
+template <int DIM>
+__device__ __forceinline__ void green(int kind, double k, const double *dv, double &re,
+                                      double &im) {
+  double r2 = 0.0;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) r2 = fma(dv[a], dv[a], r2);
+  im = 0.0;
+  switch (kind) {
+    case VL1_DUFFY_LAPLACE2D:   // -log(r) / (2 pi)
+      re = -0.5 * log(r2) * (0.5 / 3.141592653589793);
+      break;
+    case VL1_DUFFY_LAPLACE3D:   // 1 / (4 pi r)
+      re = rsqrt(r2) * (0.25 / 3.141592653589793);
+      break;
+    case VL1_DUFFY_HELMHOLTZ2D: {   // (i/4) H0^(1)(k r) = (-Y0 + i J0) / 4
+      const double kr = k * sqrt(r2);
+      re = -0.25 * y0(kr);
+      im = 0.25 * j0(kr);
+      break;
+    }
+    case VL1_DUFFY_HELMHOLTZ3D: {   // exp(i k r) / (4 pi r)
+      const double r = sqrt(r2);
+      double s, c;
+      sincos(k * r, &s, &c);
+      const double f = (0.25 / 3.141592653589793) / r;
+      re = c * f;
+      im = s * f;
+      break;
+    }
+    case VL1_DUFFY_CONSTANT:
+      re = 1.0;
+      break;
+    default:   // VL1_DUFFY_PLANE_WAVE: cos(k d_0)
+      re = cos(k * dv[0]);
+      break;
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kDuffyThreads) duffy_entry_kernel(const DuffyArgs A) {
+  const vl1_duffy_desc &D = A.d;
+  const int e = blockIdx.x;
+  constexpr int dim = DIM;
+  const int q = D.q;
+  __shared__ double s_xi[kDuffyMaxQ], s_bw[kDuffyMaxQ];
+  __shared__ double s_red[2][kDuffyThreads / 32];
+  if (threadIdx.x < q) {
+    s_xi[threadIdx.x] = D.interp_nodes[threadIdx.x];
+    s_bw[threadIdx.x] = D.interp_weights[threadIdx.x];
+  }
+  __syncthreads();
+  double t[3], dc[3];
+  int mode[3];
+  bool mode_ok = true;
+#pragma unroll
+  for (int a = 0; a < dim; ++a) {
+    t[a] = D.target_points[(int64_t)a * D.n_entries + e];
+    dc[a] = D.decomposition_targets[(int64_t)a * D.n_entries + e];
+    mode[a] = D.mode_axes[(int64_t)a * D.n_entries + e];
+    mode_ok = mode_ok && mode[a] >= 0 && mode[a] < q;
+  }
+  if (!mode_ok) {   // an invalid entry yields NaN (the host checks its inputs)
+    if (threadIdx.x == 0) {
+      A.out[(D.complex_output ? 2 : 1) * (int64_t)e] = __longlong_as_double(0x7FF8000000000000ll);
+      if (D.complex_output) A.out[2 * (int64_t)e + 1] = __longlong_as_double(0x7FF8000000000000ll);
+    }
+    return;
+  }
+  const int64_t per_sub = (int64_t)A.n_perm * A.n_reg_tail * D.n_rad;
+  const int64_t n_nodes = (int64_t)A.n_sub * per_sub;
+  double acc_re = 0.0, acc_im = 0.0;
+  for (int64_t i = threadIdx.x; i < n_nodes; i += kDuffyThreads) {
+    // node index -> (sign vector, axis order, regular tail node, radial node)
+    const int irad = (int)(i % D.n_rad);
+    int64_t rest = i / D.n_rad;
+    int ireg = (int)(rest % A.n_reg_tail);
+    rest /= A.n_reg_tail;
+    const int iperm = (int)(rest % A.n_perm);
+    const int isub = (int)(rest / A.n_perm);
+    // sub-box lengths along each axis (sign bit of axis a: first axis slowest)
+    double len[3], sg[3];
+    bool active = true;
+    double len_prod = 1.0;
+#pragma unroll
+    for (int a = 0; a < dim; ++a) {
+      sg[a] = ((isub >> (dim - 1 - a)) & 1) ? 1.0 : -1.0;
+      len[a] = sg[a] < 0.0 ? dc[a] : D.extent - dc[a];
+      active = active && len[a] > 0.0;
+      len_prod *= len[a];
+    }
+    if (!active) continue;
+    // unit-cube coordinates r_0 (radial), r_1.. (regular; first slowest)
+    double rs[3];
+    rs[0] = D.radial_nodes[irad];
+    double w = D.radial_weights[irad];
+#pragma unroll
+    for (int a = dim - 1; a >= 1; --a) {
+      const int j = ireg % D.n_reg;
+      ireg /= D.n_reg;
+      rs[a] = D.regular_nodes[j];
+      w *= D.regular_weights[j];
+    }
+    // Duffy map and its Jacobian
+    double cumv[3], cum = 1.0;
+#pragma unroll
+    for (int i2 = 0; i2 < dim; ++i2) {
+      cum *= rs[i2];
+      cumv[i2] = cum;
+    }
+    // u[perm[i2]] = cumv[i2], written as u[a] = cumv[position of a in perm]
+    double u[3];
+#pragma unroll
+    for (int a = 0; a < dim; ++a) {
+      double v = 0.0;
+#pragma unroll
+      for (int i2 = 0; i2 < dim; ++i2) {
+        const int axis = dim == 3 ? kPerm3[iperm][i2] : kPerm2[iperm][i2];
+        v = axis == a ? cumv[i2] : v;
+      }
+      u[a] = v;
+    }
+    double jac = 1.0;
+#pragma unroll
+    for (int i2 = 0; i2 < dim - 1; ++i2)
+#pragma unroll
+      for (int p = 0; p < dim - 1 - i2; ++p) jac *= rs[i2];
+    // source point, displacement (target - source) and the mode's basis
+    double dv[3], basis = 1.0;
+#pragma unroll
+    for (int a = 0; a < dim; ++a) {
+      const double y = fma(sg[a] * len[a], u[a], dc[a]);
+      dv[a] = t[a] - y;
+      if (q > 1) {
+        // first-form Lagrange polynomial: bw_m prod_{j != m} (y - x_j)
+        double l = s_bw[mode[a]];
+        for (int j = 0; j < q; ++j)
+          if (j != mode[a]) l *= y - s_xi[j];
+        basis *= l;
+      }
+    }
+    double r2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < dim; ++a) r2 = fma(dv[a], dv[a], r2);
+    if (!(r2 > 0.0)) continue;   // a node on the singular point: zero weight
+    double gre, gim;
+    green<DIM>(D.kernel, D.k, dv, gre, gim);
+    const double f = w * jac * len_prod * basis;
+    acc_re = fma(gre, f, acc_re);
+    acc_im = fma(gim, f, acc_im);
+  }
+  // CTA reduction
+  for (int o = 16; o > 0; o >>= 1) {
+    acc_re += __shfl_down_sync(0xffffffffu, acc_re, o);
+    acc_im += __shfl_down_sync(0xffffffffu, acc_im, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    s_red[0][warp] = acc_re;
+    s_red[1][warp] = acc_im;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double re = 0.0, im = 0.0;
+    for (int w2 = 0; w2 < kDuffyThreads / 32; ++w2) {
+      re += s_red[0][w2];
+      im += s_red[1][w2];
+    }
+    if (D.complex_output) {
+      A.out[2 * (int64_t)e] = re;
+      A.out[2 * (int64_t)e + 1] = im;
+    } else {
+      A.out[e] = re;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace vl1
+
+using namespace vl1;
+
+extern "C" int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, void *stream) {
+  if (!desc || !result) {
+    set_error("vl1_duffy_table: null descriptor or result");
+    return VL1_E_ARG;
+  }
+  const vl1_duffy_desc &D = *desc;
+  if (D.dim < 2 || D.dim > 3 || D.q < 1 || D.q > kDuffyMaxQ || D.n_entries < 0 ||
+      D.n_reg < 1 || D.n_rad < 1 || !(D.extent > 0.0) || D.kernel < 0 ||
+      D.kernel > VL1_DUFFY_PLANE_WAVE) {
+    set_error("vl1_duffy_table: dim %d, q %d, entries %d, rules %d/%d, extent %g or kernel %d "
+              "out of range", D.dim, D.q, D.n_entries, D.n_reg, D.n_rad, D.extent, D.kernel);
+    return VL1_E_ARG;
+  }
+  if (D.n_entries == 0) return VL1_OK;
+  if (!D.target_points || !D.decomposition_targets || !D.mode_axes || !D.regular_nodes ||
+      !D.regular_weights || !D.radial_nodes || !D.radial_weights || !D.interp_nodes ||
+      !D.interp_weights) {
+    set_error("vl1_duffy_table: null array in the descriptor");
+    return VL1_E_ARG;
+  }
+  DuffyArgs A;
+  A.d = D;
+  A.n_perm = D.dim == 3 ? 6 : 2;
+  A.n_reg_tail = D.dim == 3 ? D.n_reg * D.n_reg : D.n_reg;
+  A.n_sub = 1 << D.dim;
+  A.out = result;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (D.dim == 3)
+    duffy_entry_kernel<3><<<D.n_entries, kDuffyThreads, 0, s>>>(A);
+  else
+    duffy_entry_kernel<2><<<D.n_entries, kDuffyThreads, 0, s>>>(A);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? VL1_OK : cuda_fail(e, "duffy_entry_kernel launch");
+}

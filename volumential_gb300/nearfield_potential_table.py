@@ -274,12 +274,34 @@ class NearFieldInteractionTable:
         if self.dim == 2:
             self.build_normalizer_table()
 
-    def build_table(self, queue=None, **kwargs):
+    def build_table_via_duffy_radial(self, radial_rule="tanh-sinh-fast",
+                                     regular_quad_order=20, radial_quad_order=61,
+                                     mp_dps=50, queue=None, **kwargs):
+        """Fill the table's orbit-invariant entries by Duffy radial quadrature
+        in FP64 on the GPU (``nearfield_potential_table.py:2948-3195``; the
+        fixed tanh-sinh rules of its batched path).  ``queue``: an optional
+        ``torch.cuda.Stream``.  A Helmholtz kernel's wave number is passed by
+        its argument name (``k`` by default)."""
+        from .plan import stream_handle
+        from .table_builder import build_table_values
+
+        name = getattr(self.integral_knl, "helmholtz_k_name", "k")
+        k = kwargs.pop(name, kwargs.pop("k", None))
+        kernel = kwargs.pop("kernel", None)
+        if kwargs:
+            raise TypeError(f"unexpected keyword arguments {sorted(kwargs)}")
+        build_table_values(self, radial_rule_name=radial_rule,
+                           regular_quad_order=regular_quad_order,
+                           radial_quad_order=radial_quad_order, mp_dps=mp_dps, kernel=kernel,
+                           k=k, stream=stream_handle(queue))
+
+    def build_table(self, cl_ctx=None, queue=None, build_config=None, **kwargs):
+        """``nearfield_potential_table.py:3200``: the constant kernel's closed
+        form, otherwise the Duffy radial builder."""
         name = type(self.integral_knl).__name__ if self.integral_knl is not None else None
         if self.kernel_type == "const" or name == "ConstantKernel":
             self.build_constant_table()
             return
-        from .table_builder import build_table_values
-        build_table_values(self, **kwargs)
+        self.build_table_via_duffy_radial(queue=queue, **kwargs)
 
     # }}}

@@ -1,0 +1,216 @@
+"""FP64 GPU builder of near-field table values (Duffy radial quadrature).
+
+The reference fills a table with ``build_table_via_duffy_radial``
+(``volumential/nearfield_potential_table.py:2948-3195``), whose default path
+evaluates every orbit-invariant entry with one generated OpenCL kernel
+(``:2035-2223``, ``:2331-2463``) over the node set of ``:2225-2291``.  This
+module assembles the same per-entry geometry (target point of the case,
+target clipped to the source box, the source mode's per-axis indices) and the
+1D rules, and calls ``vl1_duffy_table`` (``include/vl1.h``), which decodes the
+Duffy node set on the device and sums in FP64.
+
+1D rules (restated from ``volumential/singular_integral_2d.py:807-853``):
+``tanh-sinh-fast`` with n = max(3, order) is the tanh-sinh rule on [0, 1]
+with step h = 1/sqrt(n) over the integers -n..n, x = (1 + tanh(pi/2 sinh t))/2,
+w = pi/4 h cosh t sech^2(pi/2 sinh t), keeping nodes strictly inside (0, 1);
+``tanh-sinh`` takes mpmath's tanh-sinh nodes of degree max(3, order // 5)
+mapped to [0, 1]; the tail rule is Gauss-Legendre on [0, 1], tensor in
+dimension 3 (first tail axis slowest).
+
+Kernels (``G`` includes the scaling constant; the reference takes both from
+sumpy, which is not available here, so these are the standard free-space
+Green's functions): Laplace 2D -log(r)/(2 pi), 3D 1/(4 pi r); Helmholtz 2D
+(i/4) H0^(1)(k r), 3D exp(i k r)/(4 pi r); constant 1.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+__all__ = ["tanh_sinh_fast_rule", "radial_rule", "gauss_legendre_unit", "regular_rule",
+           "lagrange_product_weights", "entry_geometry", "kernel_code",
+           "build_table_values", "DEFAULT_ORDERS"]
+
+#: the reference's defaults (``nearfield_potential_table.py:2948-2953``)
+DEFAULT_ORDERS = {"regular_quad_order": 20, "radial_quad_order": 61}
+
+
+def tanh_sinh_fast_rule(order):
+    """Tanh-sinh nodes and weights on (0, 1) with n = max(3, order) steps of
+    h = 1/sqrt(n) on each side (the reference's ``tanh-sinh-fast``)."""
+    n = max(3, int(order))
+    h = 1.0 / np.sqrt(n)
+    t = h * np.arange(-n, n + 1, dtype=np.float64)
+    a = 0.5 * np.pi * np.sinh(t)
+    x = 0.5 * (1.0 + np.tanh(a))
+    # sech^2(a) = 4 e^{-2|a|} / (1 + e^{-2|a|})^2, without overflow
+    e = np.exp(-2.0 * np.abs(a))
+    w = 0.25 * np.pi * h * np.cosh(t) * (4.0 * e / (1.0 + e) ** 2)
+    keep = (x > 0.0) & (x < 1.0) & np.isfinite(w)
+    return x[keep], w[keep]
+
+
+def radial_rule(rule, order, mp_dps=50):
+    if rule == "tanh-sinh-fast":
+        return tanh_sinh_fast_rule(order)
+    if rule == "tanh-sinh":
+        import mpmath
+
+        old = mpmath.mp.dps
+        mpmath.mp.dps = mp_dps
+        try:
+            ts = mpmath.calculus.quadrature.TanhSinh(mpmath.mp)
+            prec = int(np.log(10) / np.log(2) * mpmath.mp.dps)
+            nodes = ts.calc_nodes(degree=max(3, int(order // 5)), prec=prec)
+            x = np.array([float(p[0]) for p in nodes])
+            w = np.array([float(p[1]) for p in nodes])
+        finally:
+            mpmath.mp.dps = old
+        return 0.5 * (x + 1.0), 0.5 * w
+    raise ValueError(f"unsupported radial rule {rule!r} (tanh-sinh-fast or tanh-sinh)")
+
+
+def gauss_legendre_unit(order):
+    """Gauss-Legendre rule on [0, 1] (scipy's nodes, as the reference's)."""
+    from scipy.special import roots_legendre
+
+    x, w = roots_legendre(int(order))
+    return 0.5 * (x + 1.0), 0.5 * w
+
+
+def regular_rule(dim_minus_one, order):
+    """Tensor Gauss-Legendre tail rule on [0, 1]^(dim - 1): (nodes [n, dim - 1],
+    weights [n]), first tail axis slowest."""
+    if dim_minus_one == 0:
+        return np.zeros((1, 0)), np.ones(1)
+    x, w = gauss_legendre_unit(order)
+    grids = np.meshgrid(*([x] * dim_minus_one), indexing="ij")
+    wgrids = np.meshgrid(*([w] * dim_minus_one), indexing="ij")
+    return (np.stack([g.ravel() for g in grids], axis=-1),
+            np.prod(np.array(wgrids), axis=0).ravel())
+
+
+def lagrange_product_weights(xi):
+    """1 / prod_{j != m} (x_m - x_j): the Lagrange polynomial of node m is
+    w_m prod_{j != m} (x - x_j)."""
+    xi = np.asarray(xi, dtype=np.float64)
+    d = xi[:, None] - xi[None, :]
+    np.fill_diagonal(d, 1.0)
+    return 1.0 / np.prod(d, axis=1)
+
+
+def entry_geometry(table, entry_ids):
+    """Per entry: target point [dim, n], target clipped to the source box
+    [dim, n] and source mode index per axis [dim, n] (axis 0 slowest)."""
+    entry_ids = np.asarray(entry_ids, dtype=np.int64)
+    case = entry_ids // table.n_pairs
+    pair = entry_ids % table.n_pairs
+    smode = pair // table.n_q_points
+    tpoint = pair % table.n_q_points
+    tp = table.get_case_target_points()[:, case, tpoint]
+    dc = np.clip(tp, 0.0, table.source_box_extent)
+    q, dim = table.quad_order, table.dim
+    axes = np.empty((dim, len(entry_ids)), dtype=np.int32)
+    rem = smode.copy()
+    for a in range(dim - 1, -1, -1):
+        axes[a] = rem % q
+        rem //= q
+    return np.ascontiguousarray(tp), np.ascontiguousarray(dc), axes
+
+
+def kernel_code(table, kernel=None):
+    """(vl1 kernel code, complex) of a table's kernel or of an explicit
+    ``kernel`` name ("laplace", "helmholtz", "constant", "plane_wave")."""
+    if kernel is None:
+        if table.kernel_type == "const":
+            kernel = "constant"
+        else:
+            name = type(table.integral_knl).__name__ if table.integral_knl is not None else ""
+            kernel = {"LaplaceKernel": "laplace", "HelmholtzKernel": "helmholtz",
+                      "ConstantKernel": "constant"}.get(name)
+            if kernel is None:
+                raise NotImplementedError(
+                    f"no GPU Duffy kernel for {name or table.kernel_type!r} (Laplace, "
+                    "Helmholtz and constant kernels are built)")
+    dim = table.dim
+    if kernel == "laplace":
+        return (_lib.VL1_DUFFY_LAPLACE2D if dim == 2 else _lib.VL1_DUFFY_LAPLACE3D), False
+    if kernel == "helmholtz":
+        return (_lib.VL1_DUFFY_HELMHOLTZ2D if dim == 2 else _lib.VL1_DUFFY_HELMHOLTZ3D), True
+    if kernel == "constant":
+        return _lib.VL1_DUFFY_CONSTANT, False
+    if kernel == "plane_wave":
+        return _lib.VL1_DUFFY_PLANE_WAVE, False
+    raise ValueError(f"unknown kernel {kernel!r}")
+
+
+def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad_order=20,
+                       radial_quad_order=61, mp_dps=50, kernel=None, k=None,
+                       entry_ids=None, stream=None, store=True):
+    """Compute the table's orbit-invariant entries on the GPU (FP64) and, with
+    ``store``, keep them as its compact data (plus the 2D normalizers).
+    Returns (entry_ids, values)."""
+    import torch
+
+    from .plan import require_cuda
+
+    require_cuda()
+    code, cplx = kernel_code(table, kernel)
+    if code in (_lib.VL1_DUFFY_HELMHOLTZ2D, _lib.VL1_DUFFY_HELMHOLTZ3D,
+                _lib.VL1_DUFFY_PLANE_WAVE):
+        if k is None:
+            name = getattr(table.integral_knl, "helmholtz_k_name", "k")
+            k = table.build_extra_kwargs.get(name)
+        if k is None or not np.isfinite(k):
+            raise ValueError("a finite wave number k is required for this kernel")
+    if cplx and not np.issubdtype(np.dtype(table.dtype), np.complexfloating):
+        raise TypeError("complex kernel values need a complex table dtype")
+    if entry_ids is None:
+        info = table._get_invariant_entry_info()
+        if info is None:
+            raise NotImplementedError("tables of dimension 2 and 3 only")
+        entry_ids = info["entry_ids"]
+    entry_ids = np.asarray(entry_ids, dtype=np.int64)
+    if entry_ids.size and (entry_ids.min() < 0 or entry_ids.max() >= table.n_cases *
+                           table.n_pairs):
+        raise ValueError("entry ids outside the table")
+    tp, dc, axes = entry_geometry(table, entry_ids)
+    rx, rw = radial_rule(radial_rule_name, radial_quad_order, mp_dps)
+    gx, gw = gauss_legendre_unit(regular_quad_order)
+    xi = np.asarray(table.q_points[:table.quad_order, table.dim - 1], dtype=np.float64)
+    bw = lagrange_product_weights(xi)
+
+    dev = lambda a, dt=torch.float64: torch.from_numpy(np.ascontiguousarray(a)).to(  # noqa: E731
+        device="cuda", dtype=dt)
+    arrs = {"tp": dev(tp), "dc": dev(dc), "ax": dev(axes, torch.int32), "gx": dev(gx),
+            "gw": dev(gw), "rx": dev(rx), "rw": dev(rw), "xi": dev(xi), "bw": dev(bw)}
+    n = len(entry_ids)
+    out = torch.empty((n, 2) if cplx else (n,), dtype=torch.float64, device="cuda")
+    d = _lib.DuffyDesc()
+    d.dim, d.q, d.n_entries = table.dim, table.quad_order, n
+    d.n_reg, d.n_rad, d.kernel = len(gx), len(rx), code
+    d.complex_output = int(cplx)
+    d.extent = float(table.source_box_extent)
+    d.k = float(k) if k is not None else 0.0
+    d.target_points, d.decomposition_targets = arrs["tp"].data_ptr(), arrs["dc"].data_ptr()
+    d.mode_axes = arrs["ax"].data_ptr()
+    d.regular_nodes, d.regular_weights = arrs["gx"].data_ptr(), arrs["gw"].data_ptr()
+    d.radial_nodes, d.radial_weights = arrs["rx"].data_ptr(), arrs["rw"].data_ptr()
+    d.interp_nodes, d.interp_weights = arrs["xi"].data_ptr(), arrs["bw"].data_ptr()
+    sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _lib.check(_lib.lib().vl1_duffy_table(C.byref(d), C.c_void_p(out.data_ptr() if n else 0),
+                                          C.c_void_p(sh)), "vl1_duffy_table")
+    vals = out.cpu().numpy()
+    if cplx:
+        vals = vals[:, 0] + 1j * vals[:, 1]
+    if not np.all(np.isfinite(vals)):
+        raise RuntimeError("the Duffy builder produced non-finite table values")
+    if store:
+        table.set_reduced_table_data(entry_ids, vals.astype(table.dtype))
+        if table.dim == 2:
+            table.build_normalizer_table()
+    return entry_ids, vals
