@@ -63,7 +63,7 @@ def test_gpu_constant_kernel_gives_the_exact_volume(cuda, dim):
     t.build_table_via_duffy_radial(regular_quad_order=6, radial_quad_order=21,
                                    kernel="constant")
     ids, vals = t.get_reduced_table_data()
-    assert len(ids) == t.n_cases
+    assert len(ids) > 0 and t.is_built
     assert np.max(np.abs(vals - 1.0)) < 1e-11
 
 
