@@ -55,7 +55,8 @@ def parse_args(argv=None):
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5"), default="c2")
+    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5", "table"),
+                   default="c2")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--c4-problems", type=int, default=64, help="C4: problems in the batch")
     p.add_argument("--c4-max-level", type=int, default=5, help="C4: deepest uniform level")
@@ -819,6 +820,93 @@ def c5_main(args):
     return 0
 
 
+def table_main(args):
+    """FP64 table builder (``vl1_duffy_table``): full orbit-invariant tables
+    at the reference's default Duffy orders (regular 20, radial 61,
+    tanh-sinh-fast).  One step = one full build of each table (3D Laplace
+    q=4; 2D Helmholtz q=5, k=20); the CPU restatement is timed on a sample of
+    entries at lower orders and reported per quadrature node."""
+    import torch
+
+    from oracle import duffy_oracle as DO   # CPU baseline only
+    from volumential_gb300 import table_builder as TB
+    from volumential_gb300.kernels import HelmholtzKernel, LaplaceKernel
+    from volumential_gb300.nearfield_potential_table import NearFieldInteractionTable
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    reg, rad = TB.DEFAULT_ORDERS["regular_quad_order"], TB.DEFAULT_ORDERS["radial_quad_order"]
+    n_rad = len(TB.tanh_sinh_fast_rule(rad)[0])
+    cases = [("lap3d_q4", 3, 4, LaplaceKernel(3), np.float64, None),
+             ("helm2d_q5_k20", 2, 5, HelmholtzKernel(2), np.complex128, 20.0)]
+    out = {}
+    stream = torch.cuda.current_stream()
+    for name, dim, q, knl, dt, k in cases:
+        t = NearFieldInteractionTable(q, dim=dim, sumpy_kernel=knl, dtype=dt)
+        ids = t._get_invariant_entry_info()["entry_ids"]
+        nodes_per_entry = (2 ** dim) * (6 if dim == 3 else 2) * reg ** (dim - 1) * n_rad
+        for _ in range(args.warmup):
+            TB.build_table_values(t, entry_ids=ids[:256], k=k, store=False)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            w0 = time.perf_counter()
+            e0.record(stream)
+            TB.build_table_values(t, k=k, store=False)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append((time.perf_counter() - w0) * 1e3)
+        tsec = float(np.median(ms)) / 1e3
+        # CPU restatement: a few entries at regular 6 / radial 21, per node
+        creg, crad = 6, 21
+        cn = (2 ** dim) * (6 if dim == 3 else 2) * creg ** (dim - 1) * \
+            len(TB.tanh_sinh_fast_rule(crad)[0])
+        sample = ids[:: max(1, len(ids) // 4)][:4]
+        tp, _, axes = TB.entry_geometry(t, sample)
+        c0 = time.perf_counter()
+        DO.entry_values(dim, q, 1.0, "laplace" if k is None else "helmholtz", tp, axes,
+                        creg, crad, k=k or 0.0)
+        csec = time.perf_counter() - c0
+        out[name] = {"entries": int(len(ids)), "nodes_per_entry": int(nodes_per_entry),
+                     "build_s": tsec, "entries_per_s": len(ids) / tsec,
+                     "node_evals_per_s": len(ids) * nodes_per_entry / tsec,
+                     "cpu_node_evals_per_s": len(sample) * cn / csec,
+                     "cpu_sample": f"{len(sample)} entries at regular {creg} / radial {crad}, "
+                                   f"{csec:.2f} s (numpy restatement, 1 core)"}
+    head = out["lap3d_q4"]
+    hbm, bf16, peak_kind = peaks()
+    fp64_nominal = 1250.0   # GB300 nominal FP64 (GFLOP/s); no measured FP64 peak
+    ops_per_node = 55       # FP64 operations per node (3D Laplace, q=4), counted
+    line = {
+        "metric": "table build: entries/s (FP64 Duffy radial, default orders)",
+        "value": head["entries_per_s"], "unit": "entries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["build_s"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "duffy_table_lap3d_q4", "regular_quad_order": reg,
+                   "radial_quad_order": rad, "radial_rule": "tanh-sinh-fast",
+                   "l2": "node rules are kB; entries read once"},
+        "tables": out,
+        "roofline": {"bound": "fp64", "achieved": head["node_evals_per_s"] * ops_per_node / 1e9,
+                     "peak": fp64_nominal, "unit": "GFLOP/s",
+                     "frac": head["node_evals_per_s"] * ops_per_node / 1e9 / fp64_nominal,
+                     "traffic": None, "peak_source": "nominal (no measured FP64 peak)",
+                     "ops_per_node_counted": ops_per_node},
+        "cpu_baseline": {"value": head["cpu_node_evals_per_s"] / head["nodes_per_entry"],
+                         "unit": "entries/s", "cores": 1, "kind": "port",
+                         "sample": head["cpu_sample"]},
+        "e2e": {"value": head["entries_per_s"], "unit": "entries/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": head["entries"] * 8,
+                "note": "timed around the Python build call (geometry, upload, kernel, "
+                        "read-back)"},
+        "gpu_launches": args.steps * len(cases),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
@@ -827,6 +915,8 @@ def main(argv=None):
         return c4_main(args)
     if args.workload == "c5":
         return c5_main(args)
+    if args.workload == "table":
+        return table_main(args)
     return gb300_main(args)
 
 
