@@ -877,7 +877,10 @@ def table_main(args):
     head = out["lap3d_q4"]
     hbm, bf16, peak_kind = peaks()
     fp64_nominal = 1250.0   # GB300 nominal FP64 (GFLOP/s); no measured FP64 peak
-    ops_per_node = 55       # FP64 operations per node (3D Laplace, q=4), counted
+    # FP64 flops per enumerated node of the 3D Laplace q=4 build, DADD + DMUL +
+    # 2 DFMA thread instructions over the nodes of one launch (ncu counters,
+    # profiles/duffy_table_lap3d_q4.md); nodes of empty sub-boxes included
+    ops_per_node = 10.74
     line = {
         "metric": "table build: entries/s (FP64 Duffy radial, default orders)",
         "value": head["entries_per_s"], "unit": "entries/s", "n_gpus": world,
@@ -892,7 +895,7 @@ def table_main(args):
                      "peak": fp64_nominal, "unit": "GFLOP/s",
                      "frac": head["node_evals_per_s"] * ops_per_node / 1e9 / fp64_nominal,
                      "traffic": None, "peak_source": "nominal (no measured FP64 peak)",
-                     "ops_per_node_counted": ops_per_node},
+                     "fp64_flops_per_node_ncu": ops_per_node},
         "cpu_baseline": {"value": head["cpu_node_evals_per_s"] / head["nodes_per_entry"],
                          "unit": "entries/s", "cores": 1, "kind": "port",
                          "sample": head["cpu_sample"]},
