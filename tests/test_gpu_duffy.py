@@ -107,3 +107,24 @@ def test_list1_on_a_gpu_built_laplace_table(cuda):
     assert rel_l2(plain.cpu().numpy(), ref) <= 1e-12
     assert rel_l2(mixed.cpu().numpy(), ref) <= 1e-9
     plan.destroy()
+
+
+def test_table_manager_builds_on_a_miss_and_reloads(cuda, tmp_path):
+    from volumential_gb300.table_manager import NearFieldInteractionTableManager
+
+    db = str(tmp_path / "cache.sqlite")
+    with NearFieldInteractionTableManager(db, root_extent=1.0) as m:
+        t, recomputed = m.get_table(2, "Laplace", 2, source_box_level=1,
+                                    regular_quad_order=6, radial_quad_order=21)
+        assert recomputed and t.is_built
+        ids, vals = t.get_reduced_table_data()
+    with NearFieldInteractionTableManager(db, root_extent=1.0) as m:
+        t2, recomputed = m.get_table(2, "Laplace", 2, source_box_level=1)
+        assert not recomputed
+        ids2, vals2 = t2.get_reduced_table_data()
+    np.testing.assert_array_equal(ids, ids2)
+    np.testing.assert_array_equal(vals, vals2)
+    # the GPU values against the CPU restatement on a few entries
+    tp, _, axes = TB.entry_geometry(t, ids[:6])
+    ref = DO.entry_values(2, 2, 0.5, "laplace", tp, axes, 6, 21)
+    assert np.max(np.abs(vals[:6] - ref) / np.abs(ref)) <= 1e-12
