@@ -306,6 +306,28 @@ typedef struct {
 
 int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, void *stream);
 
+/* ---- Helmholtz split correction ---------------------------------------
+ * The split mode's list-1 remainder (volumential/expansion_wrangler_fpnd.py:
+ * 3491-3836, split order 1, series remainder kernel :212-332):
+ *   result[t] = sum over list-1 source points s (s != t when exclude_self)
+ *               of weights[s] * R(|x_t - x_s|),
+ *   2D: R(r) = c0 + sum_{n=1..N} (a_n log r + b_n) r^{2n},
+ *   3D: R(r) = sum_{n=1..N} c_n r^{n-1},
+ * coefficients [2][N + 1][2] (re, im): row 0 = (c0, a_1..a_N) in 2D or
+ * (unused, c_1..c_N) in 3D, row 1 = (unused, b_1..b_N).  Points are the tree's
+ * sources = targets (tree order, [dim][n_points]); the result is complex
+ * [n_points][2] and is overwritten for the target boxes' points. */
+typedef struct {
+  int32_t dim, n_points, n_terms, exclude_self, weights_complex, reserved;
+  const vl1_tree_view *tree;
+  const double *points;
+  const double *weights;
+  const double *coefficients;
+  double *result;
+} vl1_split_desc;
+
+int32_t vl1_split_correction(const vl1_split_desc *desc, void *stream);
+
 /* Measurement hook (no reference counterpart): while `begin` and `end` are
  * set (cudaEvent_t handles, or NULL to stop), every vl1_eval_mixed and
  * vl1_batch_eval records `begin` on its stream right before its tensor-core

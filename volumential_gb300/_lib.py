@@ -133,6 +133,14 @@ VL1_DUFFY_LAPLACE2D, VL1_DUFFY_LAPLACE3D, VL1_DUFFY_HELMHOLTZ2D = 0, 1, 2
 VL1_DUFFY_HELMHOLTZ3D, VL1_DUFFY_CONSTANT, VL1_DUFFY_PLANE_WAVE = 3, 4, 5
 
 
+class SplitDesc(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("n_points", C.c_int32), ("n_terms", C.c_int32),
+                ("exclude_self", C.c_int32), ("weights_complex", C.c_int32),
+                ("reserved", C.c_int32), ("tree", C.c_void_p), ("points", C.c_void_p),
+                ("weights", C.c_void_p), ("coefficients", C.c_void_p),
+                ("result", C.c_void_p)]
+
+
 class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("count", C.c_int32),
                 ("detail0", C.c_int32), ("detail1", C.c_int32)]
@@ -161,6 +169,7 @@ SIGNATURES = {
     "vl1_batch_eval": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_set_kernel_events": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_duffy_table": (C.c_int32, [C.POINTER(DuffyDesc), C.c_void_p, C.c_void_p]),
+    "vl1_split_correction": (C.c_int32, [C.POINTER(SplitDesc), C.c_void_p]),
     "vl1_batch_update": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(BatchProblem),
                                      C.c_void_p]),
     "vl1_batch_destroy": (C.c_int32, [C.c_void_p]),

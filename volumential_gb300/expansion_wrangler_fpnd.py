@@ -26,6 +26,7 @@ import math
 import numpy as np
 
 from .expansion_wrangler_interface import ExpansionWranglerInterface
+from .kernels import base_kernel
 from .list1 import NearFieldFromCSR
 from .orbit_arithmetic import metadata_nbytes
 
@@ -195,11 +196,9 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                  fmm_level_to_order=None, quad_order=None, potential_kind=1,
                  source_extra_kwargs=None, kernel_extra_kwargs=None,
                  self_extra_kwargs=None, list1_extra_kwargs=None, queue=None,
-                 helmholtz_split=False, **kwargs):
-        if helmholtz_split:
-            raise NotImplementedError(
-                "the Helmholtz split correction (online P2P remainder) is not part of "
-                "the GB300 list-1 path; use Helmholtz tables (fixed or per-level)")
+                 helmholtz_split=None, helmholtz_split_order=1,
+                 helmholtz_split_smooth_quad_order=None,
+                 helmholtz_split_order1_legacy_subtraction=False, **kwargs):
         self.tree_indep = tree_indep
         self.traversal = traversal
         self.tree = traversal.tree
@@ -211,7 +210,6 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
         self.kernel_extra_kwargs = kernel_extra_kwargs or {}
         self.self_extra_kwargs = self_extra_kwargs or {}
         self.list1_extra_kwargs = dict(list1_extra_kwargs or {})
-        self.helmholtz_split = False
 
         knames = [repr(k) for k in tree_indep.target_kernels]
         if isinstance(near_field_table, dict):
@@ -228,10 +226,96 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
         self.near_field_table = tables
         for kn, lst in tables.items():
             self._check_table_levels(kn, lst)
+        self._init_helmholtz_split(helmholtz_split, helmholtz_split_order,
+                                   helmholtz_split_smooth_quad_order,
+                                   helmholtz_split_order1_legacy_subtraction)
         self._payload_cache = collections.OrderedDict()
         self._payload_cache_max = 16
         self._view_cache = collections.OrderedDict()
         self._layout_validated = set()
+
+    # {{{ Helmholtz split mode (expansion_wrangler_fpnd.py:2482-2600, 3491-3836)
+
+    def _split_support(self):
+        """(supported, reason): every target kernel Helmholtz, every table
+        Laplace-backed."""
+        for k in self.tree_indep.target_kernels:
+            if type(base_kernel(k)).__name__ != "HelmholtzKernel":
+                return False, f"target kernel {k!r} is not a Helmholtz kernel"
+        for kn, lst in self.near_field_table.items():
+            for t in lst:
+                if type(t.integral_knl).__name__ != "LaplaceKernel":
+                    return False, f"the near-field table of {kn} is not Laplace-backed"
+        return True, ""
+
+    def _init_helmholtz_split(self, split, order, smooth_quad_order, legacy):
+        ok, reason = self._split_support()
+        if split is None:
+            split = ok
+        elif split and not ok:
+            raise RuntimeError(
+                "helmholtz_split requires Helmholtz target kernels and Laplace-backed "
+                f"near-field tables; {reason}")
+        self.helmholtz_split = bool(split)
+        self.helmholtz_split_order = int(order) if split else order
+        if self.helmholtz_split:
+            if int(order) != 1:
+                raise NotImplementedError("helmholtz_split_order > 1 (extra split-term "
+                                          "tables) is not built; use order 1")
+            if smooth_quad_order is not None:
+                raise NotImplementedError("helmholtz_split_smooth_quad_order (resampled "
+                                          "remainder sources) is not built")
+            if legacy:
+                raise NotImplementedError("the legacy order-1 subtraction is not built")
+
+    def _split_wave_number(self, out_kernel):
+        name = getattr(base_kernel(out_kernel), "helmholtz_k_name", "k")
+        if name not in self.kernel_extra_kwargs:
+            raise TypeError(f"missing kernel parameter {name!r} for "
+                            f"{out_kernel.__class__.__name__} while evaluating split remainder")
+        return complex(self.kernel_extra_kwargs[name])
+
+    def eval_direct_helmholtz_split_correction(self, target_boxes, neighbor_source_boxes_starts,
+                                               neighbor_source_boxes_lists, src_weights,
+                                               src_func=None):
+        """The split mode's list-1 remainder sum, one complex [N] array per
+        target kernel (``expansion_wrangler_fpnd.py:3491-3836``, order 1).
+        ``src_weights``: density x quadrature weight in tree order."""
+        import torch
+
+        from .helmholtz_split import max_neighbor_distance, series_terms, split_correction
+        from .plan import as_device_tensor, stream_handle, tree_view_from_arrays
+
+        if not self.helmholtz_split:
+            return self.output_zeros(), _TimingFuture([])
+        w = as_device_tensor(src_weights)
+        pts = torch.from_numpy(np.ascontiguousarray(_np(self.tree.sources),
+                                                    dtype=np.float64)).to("cuda")
+        out, events = [], []
+        r_max = max_neighbor_distance(self.tree)
+        for k in self.tree_indep.target_kernels:
+            kw = self._near_field_kwargs(self.get_payload(k), target_boxes,
+                                         neighbor_source_boxes_starts,
+                                         neighbor_source_boxes_lists, None)
+            view, keep = tree_view_from_arrays(**{n: kw[n] for n in (
+                "target_boxes", "neighbor_source_boxes_starts", "neighbor_source_boxes_lists",
+                "box_centers", "box_levels", "box_source_starts",
+                "box_source_counts_nonchild", "box_target_starts",
+                "box_target_counts_nonchild", "source_mode_ids", "target_point_ids",
+                "root_extent")})
+            wave = self._split_wave_number(k)
+            corr = split_correction(view, pts, w, wave, series_terms(self.tree.dimensions,
+                                                                     wave, r_max),
+                                    exclude_self=self.tree_indep.exclude_self,
+                                    stream=stream_handle(self.queue))
+            evt = torch.cuda.Event()
+            evt.record()
+            out.append(corr)
+            events.append(evt)
+            del keep
+        return out, _TimingFuture(events)
+
+    # }}}
 
     # {{{ table bookkeeping (expansion_wrangler_fpnd.py:2414-2472)
 
@@ -267,6 +351,10 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
         kname = repr(out_kernel)
         tables = tables or self.near_field_table[kname]
         eval_dtype = self.eval_dtype(out_kernel)
+        if getattr(self, "helmholtz_split", False):
+            # split mode: the Laplace tables' real values (the remainder sum
+            # adds the complex part)
+            eval_dtype = np.dtype(np.float64)
         key = (kname, tuple(id(t) for t in tables),
                tuple(int(np.asarray(t.data).ctypes.data) for t in tables),
                tuple(int(np.asarray(t.data).size) for t in tables), eval_dtype.str)
@@ -343,6 +431,18 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
     def near_field_evaluator(self, out_kernel, payload, list1_extra_kwargs=None):
         kw = dict(self.list1_extra_kwargs if list1_extra_kwargs is None
                   else list1_extra_kwargs)
+        if self.helmholtz_split:
+            # the Laplace-table part with the split scaling rules
+            # (expansion_wrangler_fpnd.py:4801-4833)
+            from .helmholtz_split import split_scaling_codes
+            from .kernels import LaplaceKernel
+
+            scaling, disp = split_scaling_codes(self.tree.dimensions)
+            kw.setdefault("kernel_scaling_code", scaling)
+            kw.setdefault("kernel_displacement_code", disp)
+            return NearFieldFromCSR(LaplaceKernel(self.tree.dimensions),
+                                    payload["table_data_shapes"],
+                                    potential_kind=self.potential_kind, **kw)
         return NearFieldFromCSR(out_kernel, payload["table_data_shapes"],
                                 potential_kind=self.potential_kind, **kw)
 
@@ -362,6 +462,13 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
         near_field = self.near_field_evaluator(out_kernel, payload, list1_extra_kwargs)
         kw = self._near_field_kwargs(payload, target_boxes, neighbor_source_boxes_starts,
                                      neighbor_source_boxes_lists, mode_coefs)
+        if self.helmholtz_split and out_pot.is_complex():
+            import torch
+
+            real = torch.zeros(out_pot.shape, dtype=torch.float64, device=out_pot.device)
+            res, evt = near_field(self.queue, result=real, **kw)
+            out_pot.copy_(res)
+            return out_pot, evt
         res, evt = near_field(self.queue, result=out_pot, **kw)
         return res, evt
 

@@ -1,0 +1,158 @@
+"""Helmholtz split mode: Laplace-table near field plus a list-1 remainder sum.
+
+The reference's default Helmholtz list-1 evaluation
+(``volumential/expansion_wrangler_fpnd.py:2482-2519, 3491-3836``) uses the
+Laplace table (scaled by the split rules of ``:4801-4833``) and adds, per
+target, the sum over list-1 source points of (density x quadrature weight)
+x R(r), with R = G_k - G_0 the smooth Helmholtz-minus-Laplace remainder.  For
+split order 1 (the default) R is the series of ``:212-332``:
+
+* 2D: R = c0 + sum_{n>=1} (a_n log r + b_n) r^{2n} with
+  c0 = i/4 - (log(k/2) + gamma) / (2 pi), s_n = (-1)^n (k^2/4)^n / (n!)^2,
+  a_n = -s_n / (2 pi), b_n = s_n ((H_n - log(k/2) - gamma) / (2 pi) + i/4);
+* 3D: R = sum_{n>=1} (i k)^n / (4 pi n!) r^{n-1}  ( = (e^{ikr} - 1) / (4 pi r) ),
+
+truncated at the term count of ``:4337-4378`` (tolerance 1e-16 at the largest
+list-1 distance, at most 96 terms, plus 2).  ``split_correction`` evaluates
+the sum on the GPU (``vl1_split_correction``).  Split orders above 1 (which
+move r^{2n} log r / odd-power terms into extra tables) are not built.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+
+__all__ = ["series_terms", "remainder_coefficients", "remainder_series",
+           "max_neighbor_distance", "split_scaling_codes", "split_correction"]
+
+_GAMMA = 0.5772156649015329   # Euler-Mascheroni
+
+
+def series_terms(dim, k, r_max, tol=1.0e-16, max_n=96):
+    """Number of series terms for |k| r <= |k| r_max."""
+    z = abs(complex(k)) * float(r_max)
+    if dim == 3:
+        if z == 0.0:
+            return 1
+        mag, n = z, 1
+        while n < max_n and mag > tol:
+            n += 1
+            mag *= z / n
+        return min(max_n, n + 2)
+    if dim != 2:
+        raise NotImplementedError("split remainder series supports only 2D/3D")
+    if z == 0.0:
+        return 1
+    q = 0.25 * z * z
+    mag, n = q, 1
+    scale = max(1.0, abs(math.log(max(r_max, 1.0e-300))),
+                abs(math.log(max(0.5 * abs(complex(k)), 1.0e-300))) + _GAMMA)
+    while n < max_n and mag * scale > tol:
+        n += 1
+        mag *= q / (n * n)
+    return min(max_n, n + 2)
+
+
+def remainder_coefficients(dim, k, n_terms):
+    """Coefficient array [2, n_terms + 1, 2] of ``vl1_split_correction``."""
+    k = complex(k)
+    out = np.zeros((2, n_terms + 1), dtype=np.complex128)
+    if dim == 2:
+        if k == 0:
+            return np.zeros((2, n_terms + 1, 2))
+        lk = np.log(0.5 * k) + _GAMMA
+        out[0, 0] = 0.25j - lk / (2 * np.pi)
+        harmonic = 0.0
+        for n in range(1, n_terms + 1):
+            harmonic += 1.0 / n
+            s_n = ((-1) ** n) * (k * k / 4.0) ** n / (math.factorial(n) ** 2)
+            out[0, n] = -s_n / (2 * np.pi)
+            out[1, n] = s_n * ((harmonic - lk) / (2 * np.pi) + 0.25j)
+    else:
+        for n in range(1, n_terms + 1):
+            out[0, n] = (1j * k) ** n / (4 * np.pi * math.factorial(n))
+    return np.ascontiguousarray(np.stack([out.real, out.imag], axis=-1))
+
+
+def remainder_series(dim, k, r, n_terms):
+    """R(r) from the truncated series (numpy, for checks)."""
+    c = remainder_coefficients(dim, k, n_terms)
+    c = c[..., 0] + 1j * c[..., 1]
+    r = np.asarray(r, dtype=np.float64)
+    if dim == 2:
+        x = r * r
+        with np.errstate(divide="ignore"):
+            lg = np.where(r > 1e-300, np.log(np.maximum(r, 1e-300)), 0.0)
+        out = np.full(r.shape, c[0, 0])
+        for n in range(1, n_terms + 1):
+            out = out + (c[0, n] * lg + c[1, n]) * x ** n
+        return out
+    out = np.zeros(r.shape, dtype=np.complex128)
+    for n in range(1, n_terms + 1):
+        out = out + c[0, n] * r ** (n - 1)
+    return out
+
+
+def max_neighbor_distance(tree):
+    """2 sqrt(dim) times the extent of the coarsest box holding sources
+    (``expansion_wrangler_fpnd.py:4325-4335``)."""
+    counts = np.asarray(tree.box_source_counts_nonchild)
+    levels = np.asarray(tree.box_levels)[: len(counts)]
+    active = levels[counts > 0]
+    if active.size == 0:
+        return 0.0
+    return float(2.0 * np.sqrt(tree.dimensions) * tree.root_extent * 0.5 ** int(active.min()))
+
+
+def split_scaling_codes(dim):
+    """list-1 kernel scaling and displacement codes of the split mode's
+    Laplace-table part (``expansion_wrangler_fpnd.py:4801-4833``, no
+    derivatives): scaling (h / h_0)^2 in 2D and 3D; the 2D log
+    displacement."""
+    scaling = "(sbox_extent * sbox_extent) / (table_root_extent * table_root_extent)"
+    if dim == 2:
+        disp = (f"-0.5 / {np.pi!r} * scaling * log(sbox_extent / table_root_extent) * "
+                "mode_nmlz[table_lev, sid]")
+    else:
+        disp = "0.0"
+    return scaling, disp
+
+
+def split_correction(tree_view, points, weights, k, n_terms, *, exclude_self=True,
+                     stream=None):
+    """The list-1 remainder sum on the GPU.
+
+    ``tree_view``: a ``vl1_tree_view`` (device arrays); ``points``: CUDA
+    float64 [dim, N] (tree order); ``weights``: CUDA float64 or complex128 [N]
+    (density x quadrature weight).  Returns CUDA complex128 [N] (zero for
+    points outside the target boxes)."""
+    import torch
+
+    dim = int(points.shape[0])
+    n = int(points.shape[1])
+    if weights.numel() != n:
+        raise ValueError("weights must have one value per point")
+    w = weights.contiguous()
+    wcplx = w.is_complex()
+    if wcplx:
+        w = torch.view_as_real(w.to(torch.complex128)).contiguous()
+    else:
+        w = w.to(torch.float64)
+    coef = torch.from_numpy(remainder_coefficients(dim, k, n_terms)).to("cuda")
+    out = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+    d = _lib.SplitDesc()
+    d.dim, d.n_points, d.n_terms = dim, n, int(n_terms)
+    d.exclude_self, d.weights_complex = int(bool(exclude_self)), int(wcplx)
+    d.tree = C.cast(C.pointer(tree_view), C.c_void_p)
+    pts = points.to(torch.float64).contiguous()
+    d.points, d.weights = pts.data_ptr(), w.data_ptr()
+    d.coefficients, d.result = coef.data_ptr(), out.data_ptr()
+    sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _lib.check(_lib.lib().vl1_split_correction(C.byref(d), C.c_void_p(sh)),
+               "vl1_split_correction")
+    return torch.view_as_complex(out)

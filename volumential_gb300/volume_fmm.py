@@ -14,7 +14,7 @@ Restates ``volumential/volume_fmm.py:677-1053`` for the list-1 path:
 
 A wrangler that offers ``eval_direct_batched`` evaluates all fields in one
 launch; the result is the same sum of per-field potentials.  Stages outside
-list 1 (far field, global direct evaluation, Helmholtz split correction,
+list 1 (far field, global direct evaluation,
 target interpolation) raise ``NotImplementedError``.
 """
 
@@ -138,8 +138,22 @@ def drive_volume_fmm(traversal, expansion_wrangler, src_weights, src_func,
         getattr(traversal, "level_start_source_parent_box_nrs", None),
         getattr(traversal, "source_parent_boxes", None), mpole_exps)
 
-    if getattr(wrangler, "helmholtz_split", False):
-        raise NotImplementedError("Helmholtz split correction is not implemented on GB300")
+    split = bool(getattr(wrangler, "helmholtz_split", False)) and \
+        hasattr(wrangler, "eval_direct_helmholtz_split_correction")
+
+    def split_correction(idx, field_pot):
+        """volume_fmm.py:999-1026: add the split mode's list-1 remainder."""
+        corr, _ = wrangler.eval_direct_helmholtz_split_correction(
+            traversal.target_boxes, traversal.neighbor_source_boxes_starts,
+            traversal.neighbor_source_boxes_lists, src_weights[idx], src_func=src_func[idx])
+        if _contains_nonfinite(corr):
+            raise RuntimeError("Helmholtz split list1 correction produced non-finite values "
+                               f"for field {idx}")
+        out = [p + c for p, c in zip(field_pot, corr)]
+        if _contains_nonfinite(out):
+            raise RuntimeError("combined list1 potential produced non-finite values after "
+                               f"Helmholtz split correction for field {idx}")
+        return out
 
     potentials = None
     batched = getattr(wrangler, "eval_direct_batched", None)
@@ -157,7 +171,11 @@ def drive_volume_fmm(traversal, expansion_wrangler, src_weights, src_func,
                 raise RuntimeError(
                     "table-based list1 evaluation produced non-finite values for "
                     f"field {idx}; check near-field table data integrity")
-        potentials = [p.sum(dim=0) for p in per_kernel]
+        if split:
+            fields = [split_correction(idx, [p[idx] for p in per_kernel]) for idx in range(ns)]
+            potentials = [sum(f[i] for f in fields) for i in range(len(per_kernel))]
+        else:
+            potentials = [p.sum(dim=0) for p in per_kernel]
     else:
         for idx, field in enumerate(src_func):
             field_pot, _ = wrangler.eval_direct(
@@ -167,6 +185,8 @@ def drive_volume_fmm(traversal, expansion_wrangler, src_weights, src_func,
                 raise RuntimeError(
                     "table-based list1 evaluation produced non-finite values for "
                     f"field {idx}; check near-field table data integrity")
+            if split:
+                field_pot = split_correction(idx, field_pot)
             potentials = field_pot if potentials is None else _add(potentials, field_pot)
 
     result = potentials
