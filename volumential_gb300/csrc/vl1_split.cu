@@ -92,8 +92,9 @@ __global__ void __launch_bounds__(kSplitThreads) split_remainder_kernel(const Sp
               pb_re = fma(pb_re, r2, s_coef[1][n][0]);
               pb_im = fma(pb_im, r2, s_coef[1][n][1]);
             }
-            // r <= 1e-300 drops the log term (its factor r^{2n} vanishes)
-            const double lg = r2 > 1e-600 ? 0.5 * log(r2) : 0.0;
+            // the log term is dropped at r = 0 (its factor r^{2n} vanishes;
+            // any nonzero r2 in FP64 has r far above 1e-300)
+            const double lg = r2 > 0.0 ? 0.5 * log(r2) : 0.0;
             re = s_coef[0][0][0] + r2 * fma(lg, pa_re, pb_re);
             im = s_coef[0][0][1] + r2 * fma(lg, pa_im, pb_im);
           } else {
