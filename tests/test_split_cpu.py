@@ -33,3 +33,12 @@ def test_series_term_counts():
     c = remainder_coefficients(3, 2.0, 4)
     assert c.shape == (2, 5, 2)
     np.testing.assert_allclose(c[0, 1], [0.0, 2.0 / (4 * np.pi)], rtol=1e-15)
+
+
+def test_max_neighbor_distance_follows_the_coarsest_active_box():
+    from volumential_gb300.helmholtz_split import max_neighbor_distance
+    from volumential_gb300.tree_build import build_uniform_tree
+
+    t = build_uniform_tree(2, 3, 2)
+    assert t.dimensions == 2
+    assert abs(max_neighbor_distance(t) - 2 * np.sqrt(2) * t.root_extent / 8) < 1e-15

@@ -77,6 +77,11 @@ class ParticleTree:
         return self.targets
 
     @property
+    def dimensions(self):
+        """boxtree's name of the dimension."""
+        return self.dim
+
+    @property
     def box_source_starts(self):
         return self.box_target_starts
 
