@@ -275,6 +275,15 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                             f"{out_kernel.__class__.__name__} while evaluating split remainder")
         return complex(self.kernel_extra_kwargs[name])
 
+    def _split_self_limit(self, k):
+        """lim_{r->0} (G_k - G_0): 2D i/4 - (log(k/2) + gamma)/(2 pi), 3D i k/(4 pi)."""
+        k = complex(k)
+        if self.tree.dimensions == 3:
+            return 1j * k / (4.0 * np.pi)
+        if k == 0:
+            return 0j
+        return 0.25j - (np.log(0.5 * k) + np.euler_gamma) / (2.0 * np.pi)
+
     def eval_direct_helmholtz_split_correction(self, target_boxes, neighbor_source_boxes_starts,
                                                neighbor_source_boxes_lists, src_weights,
                                                src_func=None):
@@ -304,10 +313,15 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                 "box_target_counts_nonchild", "source_mode_ids", "target_point_ids",
                 "root_extent")})
             wave = self._split_wave_number(k)
+            exclude = bool(self.tree_indep.exclude_self)
             corr = split_correction(view, pts, w, wave, series_terms(self.tree.dimensions,
                                                                      wave, r_max),
-                                    exclude_self=self.tree_indep.exclude_self,
-                                    stream=stream_handle(self.queue))
+                                    exclude_self=exclude, stream=stream_handle(self.queue))
+            if exclude:
+                # self pairs excluded from the sum: add back the finite r -> 0
+                # limit of the remainder per point (expansion_wrangler_fpnd.py:
+                # 3824-3833, 5293-5360)
+                corr = corr + w.to(torch.complex128) * self._split_self_limit(wave)
             evt = torch.cuda.Event()
             evt.record()
             out.append(corr)
