@@ -328,6 +328,30 @@ typedef struct {
 
 int32_t vl1_split_correction(const vl1_split_desc *desc, void *stream);
 
+/* ---- List-1 interaction lists on the device ----------------------------
+ * For every leaf (target box, ascending box id), the sorted distinct leaves
+ * touching it at its level, one level coarser or one level finer (boxtree's
+ * list 1, used at volumential/volume_fmm.py:984-989), as CSR.  Boxes are
+ * given by their level and integer coordinates at that level.  Needs
+ * vl1_list1_csr_workspace_bytes(n_leaves) of device workspace and
+ * lists_capacity >= the list-1 entry count (n_leaves x 110 always suffices in
+ * 3D, x 30 in 2D); *nnz (host) receives the entry count.  Synchronises the
+ * stream (the entry count is read back). */
+typedef struct {
+  int32_t dim, nboxes, n_leaves, max_level;
+  const uint8_t *box_levels;    /* [nboxes] */
+  const int32_t *box_coords;    /* [nboxes][dim] */
+  const int32_t *leaf_boxes;    /* [n_leaves], ascending */
+  int32_t *starts;              /* [n_leaves + 1] out */
+  int32_t *lists;               /* [lists_capacity] out */
+  int64_t lists_capacity;
+  void *workspace;
+  int64_t workspace_bytes;
+} vl1_csr_desc;
+
+int64_t vl1_list1_csr_workspace_bytes(int32_t n_leaves);
+int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *stream);
+
 /* Measurement hook (no reference counterpart): while `begin` and `end` are
  * set (cudaEvent_t handles, or NULL to stop), every vl1_eval_mixed and
  * vl1_batch_eval records `begin` on its stream right before its tensor-core

@@ -141,6 +141,15 @@ class SplitDesc(C.Structure):
                 ("result", C.c_void_p)]
 
 
+class CsrDesc(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("nboxes", C.c_int32), ("n_leaves", C.c_int32),
+                ("max_level", C.c_int32), ("box_levels", C.c_void_p),
+                ("box_coords", C.c_void_p), ("leaf_boxes", C.c_void_p),
+                ("starts", C.c_void_p), ("lists", C.c_void_p),
+                ("lists_capacity", C.c_int64), ("workspace", C.c_void_p),
+                ("workspace_bytes", C.c_int64)]
+
+
 class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("count", C.c_int32),
                 ("detail0", C.c_int32), ("detail1", C.c_int32)]
@@ -170,6 +179,8 @@ SIGNATURES = {
     "vl1_set_kernel_events": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_duffy_table": (C.c_int32, [C.POINTER(DuffyDesc), C.c_void_p, C.c_void_p]),
     "vl1_split_correction": (C.c_int32, [C.POINTER(SplitDesc), C.c_void_p]),
+    "vl1_list1_csr_workspace_bytes": (C.c_int64, [C.c_int32]),
+    "vl1_list1_csr": (C.c_int32, [C.POINTER(CsrDesc), C.POINTER(C.c_int64), C.c_void_p]),
     "vl1_batch_update": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(BatchProblem),
                                      C.c_void_p]),
     "vl1_batch_destroy": (C.c_int32, [C.c_void_p]),

@@ -1,0 +1,298 @@
+// List-1 CSR on the device: for every leaf (target box), the leaves that
+// touch it at its own level, one level coarser or one level finer (the
+// list-1 interaction list of a 2:1-balanced tree; the reference takes it from
+// boxtree's FMMTraversalBuilder, used at volumential/volume_fmm.py:984-989).
+//
+// Boxes are named by key = offset(level) + linear(coordinates at that level)
+// (offset(l) = sum_{j<l} 2^(d j), coordinates axis 0 most significant).
+// Leaves go into an open-addressed hash table (key -> box id); one thread per
+// target leaf enumerates the candidate positions, in the order and with the
+// validity rules of the host builder:
+//   same level: coords + delta, delta in {-1,0,1}^d (the leaf itself included);
+//   one coarser: (coords + delta) >> 1, unless that is the leaf's parent;
+//   one finer:   2 coords + delta, delta in {-1,0,1,2}^d minus {0,1}^d;
+// looks them up, and keeps the sorted distinct hits.  Count, exclusive scan
+// and fill are separate launches; the row order is ascending box id.
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "vl1_internal.cuh"
+
+namespace vl1 {
+namespace {
+
+constexpr int kMaxCand = 27 + 27 + 56;   // 3D: same + coarser + finer
+constexpr int kTreeThreads = 256;
+constexpr int kScanThreads = 1024;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  // MurmurHash3's 64-bit finaliser (public domain): spreads keys over the table
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+
+struct CsrArgs {
+  int dim, nboxes, n_leaves, max_level;
+  const uint8_t *levels;
+  const int32_t *coords;      // [nboxes][dim]
+  const int32_t *leaf_boxes;  // [n_leaves]
+  long long *hkeys;           // [cap], -1 empty
+  int32_t *hvals;             // [cap]
+  uint64_t cap_mask;
+  int32_t *counts;            // [n_leaves + 1]
+  int32_t *starts;            // [n_leaves + 1]
+  int32_t *lists;
+  int32_t *status;            // [1]: 0 ok, 1 table full, 2 bad input
+};
+
+__device__ __forceinline__ long long level_offset(int dim, int lev) {
+  long long o = 0;
+  for (int j = 0; j < lev; ++j) o += 1ll << (dim * j);
+  return o;
+}
+
+__device__ __forceinline__ long long box_key(int dim, int lev, const long long *c) {
+  long long k = 0;
+  for (int a = 0; a < dim; ++a) k = (k << lev) | c[a];
+  return level_offset(dim, lev) + k;
+}
+
+__global__ void hash_insert_kernel(const CsrArgs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n_leaves) return;
+  const int b = A.leaf_boxes[i];
+  if (b < 0 || b >= A.nboxes) {
+    atomicExch(A.status, 2);
+    return;
+  }
+  const int lev = A.levels[b];
+  long long c[3];
+  for (int a = 0; a < A.dim; ++a) c[a] = A.coords[(int64_t)b * A.dim + a];
+  const long long key = box_key(A.dim, lev, c);
+  uint64_t h = mix64((uint64_t)key) & A.cap_mask;
+  for (uint64_t probe = 0; probe <= A.cap_mask; ++probe) {
+    const long long prev =
+        atomicCAS(reinterpret_cast<unsigned long long *>(A.hkeys + h), (unsigned long long)-1ll,
+                  (unsigned long long)key);
+    if (prev == -1ll || prev == key) {
+      A.hvals[h] = b;
+      return;
+    }
+    h = (h + 1) & A.cap_mask;
+  }
+  atomicExch(A.status, 1);
+}
+
+__device__ __forceinline__ int hash_find(const CsrArgs &A, long long key) {
+  uint64_t h = mix64((uint64_t)key) & A.cap_mask;
+  for (uint64_t probe = 0; probe <= A.cap_mask; ++probe) {
+    const long long k = A.hkeys[h];
+    if (k == key) return A.hvals[h];
+    if (k == -1ll) return -1;
+    h = (h + 1) & A.cap_mask;
+  }
+  return -1;
+}
+
+// candidates of target leaf i, sorted and distinct; returns their number
+__device__ int leaf_candidates(const CsrArgs &A, int i, int *out) {
+  const int dim = A.dim;
+  const int b = A.leaf_boxes[i];
+  if (b < 0 || b >= A.nboxes) return 0;   // reported by the insert kernel
+  const int tl = A.levels[b];
+  long long tc[3];
+  for (int a = 0; a < dim; ++a) tc[a] = A.coords[(int64_t)b * dim + a];
+  int n = 0;
+  const int n3 = dim == 3 ? 27 : 9;
+  // same level (shift 0) and one coarser (shift 1)
+  for (int shift = 0; shift <= 1; ++shift) {
+    const int clev = tl - shift;
+    if (clev < 0) continue;
+    for (int di = 0; di < n3; ++di) {
+      long long pos[3], cp[3];
+      bool valid = true, parent = true;
+      int rem = di;
+      for (int a = dim - 1; a >= 0; --a) {
+        const int d = rem % 3 - 1;
+        rem /= 3;
+        pos[a] = tc[a] + d;
+        valid = valid && pos[a] >= 0 && pos[a] < (1ll << tl);
+      }
+      if (!valid) continue;
+      for (int a = 0; a < dim; ++a) {
+        cp[a] = pos[a] >> shift;
+        parent = parent && cp[a] == (tc[a] >> 1);
+      }
+      if (shift == 1 && parent) continue;   // the leaf's own ancestor
+      const int id = hash_find(A, box_key(dim, clev, cp));
+      if (id >= 0) out[n++] = id;
+    }
+  }
+  // one finer: 2 coords + delta, delta in {-1..2}^d outside {0,1}^d
+  if (tl + 1 <= A.max_level) {
+    const int n4 = dim == 3 ? 64 : 16;
+    for (int di = 0; di < n4; ++di) {
+      long long pos[3];
+      bool valid = true, inner = true;
+      int rem = di;
+      for (int a = dim - 1; a >= 0; --a) {
+        const int d = rem % 4 - 1;
+        rem /= 4;
+        pos[a] = 2 * tc[a] + d;
+        inner = inner && (d == 0 || d == 1);
+        valid = valid && pos[a] >= 0 && pos[a] < (1ll << (tl + 1));
+      }
+      if (inner || !valid) continue;
+      const int id = hash_find(A, box_key(dim, tl + 1, pos));
+      if (id >= 0) out[n++] = id;
+    }
+  }
+  // insertion sort and dedup
+  for (int x = 1; x < n; ++x) {
+    const int v = out[x];
+    int y = x - 1;
+    while (y >= 0 && out[y] > v) {
+      out[y + 1] = out[y];
+      --y;
+    }
+    out[y + 1] = v;
+  }
+  int m = 0;
+  for (int x = 0; x < n; ++x)
+    if (m == 0 || out[m - 1] != out[x]) out[m++] = out[x];
+  return m;
+}
+
+__global__ void csr_count_kernel(const CsrArgs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n_leaves) return;
+  int cand[kMaxCand];
+  A.counts[i] = leaf_candidates(A, i, cand);
+}
+
+// exclusive scan of counts[0..n) into starts[0..n] (one CTA: each thread scans
+// a contiguous slice, then the slice sums are scanned in shared memory)
+__global__ void csr_scan_kernel(const CsrArgs A) {
+  __shared__ long long s_part[kScanThreads];
+  const int n = A.n_leaves;
+  const int per = (n + kScanThreads - 1) / kScanThreads;
+  const int lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
+  long long sum = 0;
+  for (int i = lo; i < hi; ++i) sum += A.counts[i];
+  s_part[threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long run = 0;
+    for (int t = 0; t < kScanThreads; ++t) {
+      const long long v = s_part[t];
+      s_part[t] = run;
+      run += v;
+    }
+    if (run > 0x7fffffffll) atomicExch(A.status, 2);
+    A.starts[n] = (int32_t)run;
+  }
+  __syncthreads();
+  long long run = s_part[threadIdx.x];
+  for (int i = lo; i < hi; ++i) {
+    A.starts[i] = (int32_t)run;
+    run += A.counts[i];
+  }
+}
+
+__global__ void csr_fill_kernel(const CsrArgs A, int64_t capacity) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n_leaves) return;
+  int cand[kMaxCand];
+  const int m = leaf_candidates(A, i, cand);
+  const int64_t s = A.starts[i];
+  if (s + m > capacity) {
+    atomicExch(A.status, 1);
+    return;
+  }
+  for (int x = 0; x < m; ++x) A.lists[s + x] = cand[x];
+}
+
+}  // namespace
+}  // namespace vl1
+
+using namespace vl1;
+
+namespace {
+uint64_t table_capacity(int32_t n_leaves) {
+  uint64_t cap = 64;
+  while (cap < 2ull * (uint64_t)n_leaves) cap <<= 1;
+  return cap;
+}
+}  // namespace
+
+extern "C" int64_t vl1_list1_csr_workspace_bytes(int32_t n_leaves) {
+  if (n_leaves < 0) return -1;
+  const uint64_t cap = table_capacity(n_leaves);
+  return (int64_t)(cap * 8 + cap * 4 + ((uint64_t)n_leaves + 1) * 4 + 256);
+}
+
+extern "C" int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *stream) {
+  if (!desc || !nnz) {
+    set_error("vl1_list1_csr: null argument");
+    return VL1_E_ARG;
+  }
+  const vl1_csr_desc &D = *desc;
+  if ((D.dim != 2 && D.dim != 3) || D.nboxes < 1 || D.n_leaves < 1 || D.max_level < 0 ||
+      D.max_level > (D.dim == 3 ? 20 : 30) || !D.box_levels || !D.box_coords ||
+      !D.leaf_boxes || !D.starts || !D.lists || !D.workspace ||
+      D.workspace_bytes < vl1_list1_csr_workspace_bytes(D.n_leaves)) {
+    set_error("vl1_list1_csr: dim %d, %d boxes, %d leaves, max level %d or workspace "
+              "out of range", D.dim, D.nboxes, D.n_leaves, D.max_level);
+    return VL1_E_ARG;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const uint64_t cap = table_capacity(D.n_leaves);
+  uint8_t *w = static_cast<uint8_t *>(D.workspace);
+  CsrArgs A;
+  A.dim = D.dim;
+  A.nboxes = D.nboxes;
+  A.n_leaves = D.n_leaves;
+  A.max_level = D.max_level;
+  A.levels = D.box_levels;
+  A.coords = D.box_coords;
+  A.leaf_boxes = D.leaf_boxes;
+  A.hkeys = reinterpret_cast<long long *>(w);
+  A.hvals = reinterpret_cast<int32_t *>(w + cap * 8);
+  A.counts = reinterpret_cast<int32_t *>(w + cap * 12);
+  A.status = reinterpret_cast<int32_t *>(w + cap * 12 + ((uint64_t)D.n_leaves + 1) * 4);
+  A.cap_mask = cap - 1;
+  A.starts = D.starts;
+  A.lists = D.lists;
+  cudaError_t e = cudaMemsetAsync(A.hkeys, 0xFF, cap * 8, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(A.status, 0, 4, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(list-1 csr)");
+  const int grid = (D.n_leaves + kTreeThreads - 1) / kTreeThreads;
+  hash_insert_kernel<<<grid, kTreeThreads, 0, s>>>(A);
+  csr_count_kernel<<<grid, kTreeThreads, 0, s>>>(A);
+  csr_scan_kernel<<<1, kScanThreads, 0, s>>>(A);
+  csr_fill_kernel<<<grid, kTreeThreads, 0, s>>>(A, D.lists_capacity);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "list-1 csr launches");
+  int32_t host[2];
+  e = cudaMemcpyAsync(&host[0], A.status, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&host[1], D.starts + D.n_leaves, 4,
+                                            cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "list-1 csr read-back");
+  if (host[0] == 1) {
+    set_error("vl1_list1_csr: list capacity %lld too small", (long long)D.lists_capacity);
+    return VL1_E_ARG;
+  }
+  if (host[0] == 2) {
+    set_error("vl1_list1_csr: invalid leaf box id or more than 2^31 list entries");
+    return VL1_E_ARG;
+  }
+  *nnz = host[1];
+  return VL1_OK;
+}

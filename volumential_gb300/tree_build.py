@@ -354,3 +354,45 @@ def _lin_per_box(coords, levels):
     for a in range(coords.shape[1]):
         out = (out << levels) | coords[:, a]
     return out
+
+
+def build_list1_traversal_device(tree: ParticleTree, stream=None, as_numpy=True) -> Traversal:
+    """The list-1 CSR of ``tree`` computed on the GPU (``vl1_list1_csr``);
+    the same arrays as :func:`build_list1_traversal`.  ``as_numpy=False``
+    keeps the CSR as CUDA tensors."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib
+
+    dim = tree.dim
+    leaves = np.ascontiguousarray(tree.leaf_boxes, dtype=np.int32)
+    n_leaves = len(leaves)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to("cuda")  # noqa: E731
+    levels = dev(tree.box_levels.astype(np.uint8))
+    coords = dev(tree.box_coords.astype(np.int32))
+    lv = dev(leaves)
+    lib = _lib.lib()
+    ws = torch.empty(int(lib.vl1_list1_csr_workspace_bytes(n_leaves)), dtype=torch.uint8,
+                     device="cuda")
+    cap = n_leaves * (110 if dim == 3 else 30)
+    starts = torch.empty(n_leaves + 1, dtype=torch.int32, device="cuda")
+    lists = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+    d = _lib.CsrDesc()
+    d.dim, d.nboxes, d.n_leaves = dim, int(tree.nboxes), n_leaves
+    d.max_level = int(tree.box_levels.max())
+    d.box_levels, d.box_coords, d.leaf_boxes = levels.data_ptr(), coords.data_ptr(), lv.data_ptr()
+    d.starts, d.lists, d.lists_capacity = starts.data_ptr(), lists.data_ptr(), cap
+    d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
+    nnz = C.c_int64()
+    sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _lib.check(lib.vl1_list1_csr(C.byref(d), C.byref(nnz), C.c_void_p(sh)), "vl1_list1_csr")
+    lists = lists[: nnz.value]
+    if as_numpy:
+        return Traversal(tree=tree, target_boxes=leaves,
+                         neighbor_source_boxes_starts=starts.cpu().numpy(),
+                         neighbor_source_boxes_lists=lists.cpu().numpy())
+    return Traversal(tree=tree, target_boxes=lv, neighbor_source_boxes_starts=starts,
+                     neighbor_source_boxes_lists=lists)
+
