@@ -55,7 +55,7 @@ def parse_args(argv=None):
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5", "table"),
+    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5", "table", "csr"),
                    default="c2")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--c4-problems", type=int, default=64, help="C4: problems in the batch")
@@ -910,6 +910,66 @@ def table_main(args):
     return 0
 
 
+def csr_main(args):
+    """List-1 CSR on the GPU (``vl1_list1_csr``) against the host builder:
+    the C2 adaptive octree (23,087 leaves) and a uniform level-6 octree
+    (262,144 leaves).  One step = one device build (CUDA events; includes the
+    upload of the box arrays and the read-back of the entry count)."""
+    import torch
+
+    from volumential_gb300 import workloads as W
+    from volumential_gb300.tree_build import (
+        build_list1_traversal,
+        build_list1_traversal_device,
+        build_uniform_tree,
+    )
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    out = {}
+    for name, tree in (("c2_adaptive_octree", W.config_c2().tree),
+                       ("uniform_octree_l6", build_uniform_tree(3, 6, 2))):
+        t0 = time.perf_counter()
+        h = build_list1_traversal(tree)
+        host_s = time.perf_counter() - t0
+        for _ in range(args.warmup):
+            build_list1_traversal_device(tree, as_numpy=False)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            d = build_list1_traversal_device(tree, as_numpy=False)
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        same = bool(np.array_equal(h.neighbor_source_boxes_lists,
+                                   d.neighbor_source_boxes_lists.cpu().numpy()) and
+                    np.array_equal(h.neighbor_source_boxes_starts,
+                                   d.neighbor_source_boxes_starts.cpu().numpy()))
+        out[name] = {"leaves": int(len(tree.leaf_boxes)), "nnz": int(h.nnz),
+                     "device_ms": float(np.median(ms)), "host_s": host_s,
+                     "speedup": host_s * 1e3 / float(np.median(ms)), "equal_to_host": same}
+    head = out["uniform_octree_l6"]
+    line = {
+        "metric": "list-1 CSR build: target boxes/s", "value": head["leaves"] /
+        (head["device_ms"] / 1e3), "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["device_ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "list1_csr_uniform_octree_l6", "l2": "n/a (one build)"},
+        "trees": out,
+        "cpu_baseline": {"value": head["leaves"] / head["host_s"], "unit": "boxes/s",
+                         "cores": 1, "kind": "port",
+                         "sample": "the host builder (numpy) on the same tree"},
+        "e2e": {"value": head["leaves"] / (head["device_ms"] / 1e3), "unit": "boxes/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8},
+        "gpu_launches": args.steps * 4,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
@@ -920,6 +980,8 @@ def main(argv=None):
         return c5_main(args)
     if args.workload == "table":
         return table_main(args)
+    if args.workload == "csr":
+        return csr_main(args)
     return gb300_main(args)
 
 
