@@ -706,67 +706,64 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         if (t >= kRowsPerProducer * NH) break;
         const int rl = t / NH, h = t - (t / NH) * NH;
         const uint8_t *src = sb + rl * RB + h * 16;
-        // digit planes of 16 values, most significant first, 4 values per word
-        uint32_t m[kDigits][4];
-#pragma unroll
-        for (int dg = 0; dg < kDigits; ++dg) {
-          const uint4 x4 = *reinterpret_cast<const uint4 *>(src + dg * KC);
-          m[dg][0] = x4.x;
-          m[dg][1] = x4.y;
-          m[dg][2] = x4.z;
-          m[dg][3] = x4.w;
-        }
         // sign masks of the FP16 pairs (values 4q + 0/1 and 4q + 2/3): the
         // sign of a value is bit 7 of its top digit byte
+        const uint4 top = *reinterpret_cast<const uint4 *>(src);
+        const uint32_t tw4[4] = {top.x, top.y, top.z, top.w};
         uint32_t sg[8];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const uint32_t tw = m[0][q];
+          const uint32_t tw = tw4[q];
           sg[2 * q] = ((tw << 8) & 0x8000u) | ((tw << 16) & 0x80000000u);
           sg[2 * q + 1] = ((tw >> 8) & 0x8000u) | (tw & 0x80000000u);
-          m[0][q] = tw & 0x7F7F7F7Fu;
         }
-        // magnitude >> sh (truncating), four values per word: whole digits
-        // first, then the bit shift within bytes (per-byte masks keep the
-        // lanes of a word apart)
+        // digit planes of 16 values, most significant first, 4 values per
+        // word, with the magnitude shifted right by sh (truncating): whole
+        // digits by reading output plane dg from staged plane dg - sh/8 (the
+        // top plane without its sign bits; zero above it), then the bit shift
+        // within bytes (per-byte masks keep the values of a word apart)
         const int sh = shr[i];
-        if (sh != 0) {
-          const int a = sh >> 3, bsh = sh & 7;
+        const int a = sh >> 3, bsh = sh & 7;
+        uint32_t m[kDigits][4];
 #pragma unroll
-          for (int st = 1; st <= 4; st <<= 1) {
-            if (a & st) {
+        for (int dg = 0; dg < kDigits; ++dg) {
+          const int j = dg - a;
+          uint4 x4 = make_uint4(0u, 0u, 0u, 0u);
+          if (j >= 0) x4 = *reinterpret_cast<const uint4 *>(src + j * KC);
+          const uint32_t keep = j == 0 ? 0x7F7F7F7Fu : 0xFFFFFFFFu;
+          m[dg][0] = x4.x & keep;
+          m[dg][1] = x4.y & keep;
+          m[dg][2] = x4.z & keep;
+          m[dg][3] = x4.w & keep;
+        }
+        if (bsh != 0) {
+          const uint32_t lo = 0x01010101u * (0xFFu >> bsh);
 #pragma unroll
-              for (int dg = kDigits - 1; dg >= 0; --dg)
+          for (int dg = kDigits - 1; dg >= 1; --dg)
 #pragma unroll
-                for (int q = 0; q < 4; ++q) m[dg][q] = dg >= st ? m[dg - st][q] : 0u;
-            }
-          }
-          if (bsh != 0) {
-            const uint32_t lo = 0x01010101u * (0xFFu >> bsh);
+            for (int q = 0; q < 4; ++q)
+              m[dg][q] = ((m[dg][q] >> bsh) & lo) | ((m[dg - 1][q] << (8 - bsh)) & ~lo);
 #pragma unroll
-            for (int dg = kDigits - 1; dg >= 1; --dg)
-#pragma unroll
-              for (int q = 0; q < 4; ++q)
-                m[dg][q] = ((m[dg][q] >> bsh) & lo) | ((m[dg - 1][q] << (8 - bsh)) & ~lo);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) m[0][q] = (m[0][q] >> bsh) & lo;
-          }
+          for (int q = 0; q < 4; ++q) m[0][q] = (m[0][q] >> bsh) & lo;
         }
         const int row = kRowsPerProducer * warp + rl;
-        // plane 3: R = X4 + X5 / 256 rounded to FP16.  (X4 << 8 | X5) / 256
-        // is exact in FP32 as 2^15 + v * 2^-8 - 2^15; one rounding to FP16.
+        // plane 3: R = X4 + X5 / 256 rounded to FP16: X4 and X5 are exact in
+        // FP16 and X5 / 256 too, so one packed FMA rounds the exact sum once
         {
+          const __half2 k2m8 = __floats2half2_rn(1.0f / 256.0f, 1.0f / 256.0f);
           uint32_t o[8];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const uint32_t v01 = __byte_perm(m[4][q], m[3][q], 0x5140u);
-            const uint32_t v23 = __byte_perm(m[4][q], m[3][q], 0x7362u);
-            const float f0 = __uint_as_float(0x47000000u | (v01 & 0xFFFFu)) - 32768.0f;
-            const float f1 = __uint_as_float(0x47000000u | (v01 >> 16)) - 32768.0f;
-            const float f2 = __uint_as_float(0x47000000u | (v23 & 0xFFFFu)) - 32768.0f;
-            const float f3 = __uint_as_float(0x47000000u | (v23 >> 16)) - 32768.0f;
-            __half2 h01 = __floats2half2_rn(f0, f1);
-            __half2 h23 = __floats2half2_rn(f2, f3);
+            uint32_t a_lo = __byte_perm(m[3][q], 0x64646464u, 0x4140u);
+            uint32_t a_hi = __byte_perm(m[3][q], 0x64646464u, 0x4342u);
+            uint32_t b_lo = __byte_perm(m[4][q], 0x64646464u, 0x4140u);
+            uint32_t b_hi = __byte_perm(m[4][q], 0x64646464u, 0x4342u);
+            const __half2 x4lo = __hsub2(*reinterpret_cast<__half2 *>(&a_lo), k1024);
+            const __half2 x4hi = __hsub2(*reinterpret_cast<__half2 *>(&a_hi), k1024);
+            const __half2 x5lo = __hsub2(*reinterpret_cast<__half2 *>(&b_lo), k1024);
+            const __half2 x5hi = __hsub2(*reinterpret_cast<__half2 *>(&b_hi), k1024);
+            __half2 h01 = __hfma2(x5lo, k2m8, x4lo);
+            __half2 h23 = __hfma2(x5hi, k2m8, x4hi);
             o[2 * q] = *reinterpret_cast<uint32_t *>(&h01) | sg[2 * q];
             o[2 * q + 1] = *reinterpret_cast<uint32_t *>(&h23) | sg[2 * q + 1];
           }
