@@ -1264,7 +1264,7 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   if (e != cudaSuccess) return cuda_fail(e, "mixed preparation launch");
   if (sched.n_tiles == 0) return VL1_OK;
 
-  MixedParams mp;
+  vl1::MixedParams mp;
   mp.d = d;
   mp.g = g;
   mp.nrhs = nrhs;
@@ -1310,6 +1310,17 @@ struct BatchGroup {   // problems sharing one kernel shape: one persistent launc
   int grid;
 };
 
+// A problem large enough to fill the GPU on its own (two waves of CTAs or
+// more): launched with one work item per CTA, its parameters by value (the
+// persistent variant reads them from shared memory per item and is slower
+// per item).
+struct SoloLaunch {
+  int problem;
+  int nch, kc;
+  int grid_x, grid_y;
+  vl1::MixedParams mp;
+};
+
 int64_t round256(int64_t b) { return (b + 255) / 256 * 256; }
 
 }  // namespace
@@ -1327,6 +1338,7 @@ struct vl1_batch {
   void *d_ttasks = nullptr;   // target-row tasks of the reference exponents
   int n_ttasks = 0;
   std::vector<BatchGroup> groups;
+  std::vector<SoloLaunch> solos;
   bool has_disp = false;
   // pinned staging of vl1_batch_update (two, so that one can be refilled
   // while the copy from the other is in flight)
@@ -1350,6 +1362,7 @@ struct BatchLayout {
   std::vector<PrepTask> tasks, ttasks;
   std::vector<BatchItem> all;
   std::vector<BatchGroup> groups;
+  std::vector<SoloLaunch> solos;
   int64_t o_probs = 0, o_prep = 0, o_tasks = 0, o_items = 0, o_queue = 0, o_ttasks = 0;
   int64_t param_bytes = 0;   // the parameter region [0, param_bytes)
   std::vector<int64_t> o_ws;
@@ -1469,8 +1482,26 @@ int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t
     int64_t cost;
     BatchItem it;
   };
+  std::vector<char> solo(n_problems, 0);
+  for (int i = 0; i < n_problems; ++i) {
+    const vl1_mixed_schedule &sc = *problems[i].schedule;
+    const MixedGeom &g = problems[i].plan->mixed.geom;
+    const int64_t n_x = sc.n_items > 0 ? sc.n_items : sc.n_tiles;
+    const int64_t ctas = n_x * (g.np / g.nch);
+    if (ctas >= 2ll * n_sm && n_x < INT32_MAX && mixed_kernel_ptr(g.nch, g.kc, false)) {
+      solo[i] = 1;
+      SoloLaunch sl;
+      sl.problem = i;
+      sl.nch = g.nch;
+      sl.kc = g.kc;
+      sl.grid_x = (int)n_x;
+      sl.grid_y = g.np / g.nch;
+      L.solos.push_back(sl);
+    }
+  }
   std::vector<std::pair<int, int>> shapes;
   for (int i = 0; i < n_problems; ++i) {
+    if (solo[i]) continue;
     const MixedGeom &g = problems[i].plan->mixed.geom;
     std::pair<int, int> sh(g.nch, g.kc);
     if (std::find(shapes.begin(), shapes.end(), sh) == shapes.end()) shapes.push_back(sh);
@@ -1479,7 +1510,7 @@ int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t
     std::vector<Cand> cands;
     for (int i = 0; i < n_problems; ++i) {
       const MixedGeom &g = problems[i].plan->mixed.geom;
-      if (g.nch != sh.first || g.kc != sh.second) continue;
+      if (solo[i] || g.nch != sh.first || g.kc != sh.second) continue;
       for (const vl1_mixed_item &it : items[i])
         for (int c = 0; c < g.np / g.nch; ++c)
           cands.push_back(Cand{(int64_t)(it.key_end - it.key_begin) * g.n_kc + 2,
@@ -1567,6 +1598,8 @@ void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems
     L.preps[i].wbox = wbox;
     L.preps[i].disp = disp;
   }
+  b->solos = L.solos;
+  for (SoloLaunch &sl : b->solos) sl.mp = L.mps[sl.problem];
   b->n_problems = n_problems;
   b->d_probs = base + L.o_probs;
   b->d_prep = base + L.o_prep;
@@ -1592,11 +1625,18 @@ void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems
   put(L.o_ttasks, L.ttasks.data(), sizeof(PrepTask) * L.ttasks.size());
 }
 
-int32_t set_batch_smem(const std::vector<BatchGroup> &groups) {
+int32_t set_batch_smem(const std::vector<BatchGroup> &groups,
+                       const std::vector<SoloLaunch> &solos) {
   for (const BatchGroup &g : groups) {
     cudaError_t e = cudaFuncSetAttribute(mixed_kernel_ptr(g.nch, g.kc, true),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)mixed_smem_bytes(g.nch, g.kc));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batch kernel)");
+  }
+  for (const SoloLaunch &sl : solos) {
+    cudaError_t e = cudaFuncSetAttribute(mixed_kernel_ptr(sl.nch, sl.kc, false),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)mixed_smem_bytes(sl.nch, sl.kc));
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(batch kernel)");
   }
   return VL1_OK;
@@ -1640,7 +1680,7 @@ extern "C" int32_t vl1_batch_create(int32_t n_problems, const vl1_batch_problem 
     delete b;
     return cuda_fail(e, "cudaMemcpy(batch parameters)");
   }
-  st = set_batch_smem(b->groups);
+  st = set_batch_smem(b->groups, b->solos);
   if (st) {
     cudaFree(b->buf);
     delete b;
@@ -1698,7 +1738,7 @@ extern "C" int32_t vl1_batch_update(vl1_batch *b, int32_t n_problems,
   e = cudaEventRecord(b->pinned_done[k], s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord(batch staging)");
   b->pinned_used[k] = true;
-  return set_batch_smem(b->groups);
+  return set_batch_smem(b->groups, b->solos);
 }
 
 extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
@@ -1732,6 +1772,13 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
   const MixedParams unused{};
   int32_t st = record_kernel_event(g_kernel_begin, s);
   if (st) return st;
+  for (const SoloLaunch &sl : b->solos) {
+    const BatchLaunch none{};
+    void *args[] = {const_cast<MixedParams *>(&sl.mp), const_cast<BatchLaunch *>(&none)};
+    e = cudaLaunchKernel(mixed_kernel_ptr(sl.nch, sl.kc, false), dim3(sl.grid_x, sl.grid_y),
+                         dim3(mixed_threads(sl.nch)), args, mixed_smem_bytes(sl.nch, sl.kc), s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch mixed_kernel launch (one problem)");
+  }
   for (size_t gi = 0; gi < b->groups.size(); ++gi) {
     const BatchGroup &g = b->groups[gi];
     BatchLaunch bl;
