@@ -80,6 +80,26 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(value):
+    """The largest ``value`` over the ranks of the default process group (the
+    value itself without one): replicas report the slowest rank's time."""
+    import torch
+
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank, world, total_ms):
+    """Whole-job throughput of ``world`` replicas that each processed
+    ``units_per_rank`` units, timed by the slowest rank (``total_ms``)."""
+    return world * units_per_rank / (total_ms / 1e3)
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -279,11 +299,7 @@ def gpu_arm(args):
     for name, fn in (("plain", plain_step), ("mixed", mixed_step)):
         step_ms, kernel_ms = _timed_steps(torch, fn, flush, args.steps, stream,
                                           _lib.lib() if name == "mixed" else None)
-        total = float(sum(step_ms))
-        if world > 1:
-            t = torch.tensor([total], device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total = float(t.item())
+        total = max_over_ranks(float(sum(step_ms)))
         res[name] = {"step_ms": step_ms, "total_ms": total, "kernel_ms": kernel_ms}
     if world > 1:
         torch.distributed.barrier()
@@ -332,11 +348,7 @@ def gpu_arm(args):
             e2e_ms.append((time.perf_counter() - t1) * 1e3)
     finally:
         gc.enable()
-    e2e_total = float(sum(e2e_ms))
-    if world > 1:
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = max_over_ranks(float(sum(e2e_ms)))
     api_err = float(np.linalg.norm(host_out.numpy().reshape(nrhs, n) - yp) / np.linalg.norm(yp))
 
     return {
@@ -480,7 +492,7 @@ def gb300_main(args):
         step_ms = np.asarray(r["res"][name]["step_ms"])
         t = float(np.mean(step_ms)) / 1e3
         return {
-            "value": world * n * nrhs * K / (r["res"][name]["total_ms"] / 1e3),
+            "value": replica_rate(n * nrhs * K, world, r["res"][name]["total_ms"]),
             "ms_per_step": r["res"][name]["total_ms"] / K,
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
                            "p99": float(np.percentile(step_ms, 99))},
@@ -535,7 +547,7 @@ def gb300_main(args):
         "rel_l2_vs_fp64": r["mixed_err"] if r["headline"] == "mixed" else 0.0,
         "solves_per_s": 1e3 * nrhs / head["ms_per_step"],
         "latency_ms": head["latency_ms"],
-        "e2e": {"value": world * n * nrhs * K / (r["e2e_total_ms"] / 1e3), "unit": "points/s",
+        "e2e": {"value": replica_rate(n * nrhs * K, world, r["e2e_total_ms"]), "unit": "points/s",
                 "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
                 "latency_ms": {"p50": float(np.percentile(r["e2e_ms"], 50)),
                                "p99": float(np.percentile(r["e2e_ms"], 99))},
