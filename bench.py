@@ -309,7 +309,9 @@ def gpu_arm(args):
     ym = out_mixed.cpu().numpy().reshape(nrhs, n)
     mixed_err = max(float(np.linalg.norm(ym[r] - yp[r]) / np.linalg.norm(yp[r]))
                     for r in range(nrhs))
-    headline = "mixed" if mixed_err <= 1e-9 else "plain"
+    headline = "plain"
+    if mixed_err <= 1e-9 and res["mixed"]["total_ms"] < res["plain"]["total_ms"]:
+        headline = "mixed"   # the faster path within its tolerance
 
     # e2e through the public API: pinned host densities in, host potentials
     # out (one rhs: NearFieldFromCSR.__call__; many: the wrangler's batched
@@ -524,11 +526,15 @@ def gb300_main(args):
                      "kernel_share_of_step": kernel_s * 1e3 / head["ms_per_step"],
                      "algorithmic_tensor_flops": int(F_tc)})
     else:
-        # the FP64 kernel: its binding roof is the FP64 pipe; HBM reported
+        # the FP64 kernel: its binding roof is the FP64 pipe (2 flops per point
+        # pair per rhs; no measured FP64 peak exists for this machine, so the
+        # nominal 1,250 GFLOP/s); its HBM rate is in paths.plain_fp64
         kernel_s = head["ms_per_step"] / 1e3
-        t_hbm, t_tc = B / (hbm * 1e9), 0.0
-        roof = {"bound": "hbm", "achieved": B / kernel_s / 1e9, "peak": hbm,
-                "unit": "GB/s", "frac": B / kernel_s / 1e9 / hbm, "kernel": "plain_kernel"}
+        fp64_nominal = 1250.0
+        t_hbm, t_tc = B / (hbm * 1e9), F / (fp64_nominal * 1e9)
+        roof = {"bound": "fp64", "achieved": F / kernel_s / 1e9, "peak": fp64_nominal,
+                "unit": "GFLOP/s", "frac": F / kernel_s / 1e9 / fp64_nominal,
+                "kernel": "plain_kernel", "peak_note": "nominal FP64 (no measured peak)"}
     roof.update({"traffic": traffic, "peak_source": peak_kind, "algorithmic_bytes": int(B),
                  "algorithmic_flops_fp64eq": int(F),
                  "roof_time_us": 1e6 * max(t_hbm, t_tc)})
