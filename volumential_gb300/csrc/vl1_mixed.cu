@@ -207,38 +207,47 @@ __device__ __forceinline__ int row_exponent(const DevDesc &d, const TreeDev &tr,
 
 // x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bytes (kp * 5),
 // so that the digits of one pipeline unit are one contiguous 5 * kc-byte
-// piece at byte kchunk * 5 * kc; source points sit at their mode id.
+// piece at byte kchunk * 5 * kc; source points sit at their mode id.  One
+// warp per row: the row's exponent (written to x_exp), then its digit bytes
+// assembled in the warp's shared-memory slice `stage` (row_bytes, 16-byte
+// aligned) and written out with 16-byte stores.
 __device__ __forceinline__ void row_digits(const DevDesc &d, const TreeDev &tr,
-                                           const double *coefs, int nrhs, const int *x_exp,
+                                           const double *coefs, int nrhs, int *x_exp,
                                            uint8_t *xdig, int kp, int kc, vl1_status *st,
-                                           int64_t idx, int lane) {
+                                           int64_t idx, int lane, uint8_t *stage) {
   const int row_bytes = kp * kDigits;
   const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-  uint8_t *row = xdig + idx * row_bytes;
+  const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
+  if (lane == 0) x_exp[idx] = e;
   for (int k = lane * 16; k < row_bytes; k += 32 * 16)
-    *reinterpret_cast<uint4 *>(row + k) = make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(stage + k) = make_uint4(0u, 0u, 0u, 0u);
   __syncwarp();
   int cnt = tr.src_counts[b];
-  if (cnt <= 0) return;
   if (cnt > d.nq) {
     if (lane == 0) report(st, VL1_E_LAYOUT, b, cnt);
     cnt = d.nq;
   }
-  const double sc = box_scaling(d, tr, tr.levels[b]);
-  const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
-  const int e = x_exp[idx];
-  for (int s = lane; s < cnt; s += 32) {
-    const int m = tr.smode[tr.src_starts[b] + s];
-    if (m < 0 || m >= d.nq) {
-      report(st, VL1_E_LAYOUT, b, -1 - s);
-      continue;
-    }
-    uint8_t byt[kDigits];
-    density_digit_bytes(sc * c[s], e, byt);
-    const int base = (m / kc) * kDigits * kc + (m % kc);
+  if (cnt > 0) {
+    const double sc = box_scaling(d, tr, tr.levels[b]);
+    const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
+    for (int s = lane; s < cnt; s += 32) {
+      const int m = tr.smode[tr.src_starts[b] + s];
+      if (m < 0 || m >= d.nq) {
+        report(st, VL1_E_LAYOUT, b, -1 - s);
+        continue;
+      }
+      uint8_t byt[kDigits];
+      density_digit_bytes(sc * c[s], e, byt);
+      const int base = (m / kc) * kDigits * kc + (m % kc);
 #pragma unroll
-    for (int i = 0; i < kDigits; ++i) row[base + i * kc] = byt[i];
+      for (int i = 0; i < kDigits; ++i) stage[base + i * kc] = byt[i];
+    }
   }
+  __syncwarp();
+  uint8_t *row = xdig + idx * row_bytes;
+  for (int k = lane * 16; k < row_bytes; k += 32 * 16)
+    *reinterpret_cast<uint4 *>(row + k) = *reinterpret_cast<const uint4 *>(stage + k);
+  __syncwarp();
 }
 
 // Scale exponents.  Every density row (source box, rhs) gets its own: the
@@ -247,18 +256,6 @@ __device__ __forceinline__ void row_digits(const DevDesc &d, const TreeDev &tr,
 // row (target box, rhs) gets the largest exponent of its list-1 source rows:
 // its sum is accumulated in units of that exponent, so the precision of an
 // output is relative to its own largest contribution.
-__global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
-                                  int nrhs, int *x_exp) {
-  const int64_t n = (int64_t)nboxes * nrhs;
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
-       idx += warps) {
-    const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
-    if (lane == 0) x_exp[idx] = e;
-  }
-}
-
 __device__ __forceinline__ int target_row_exponent(const TreeDev &tr, int nrhs,
                                                    const int *x_exp, int64_t idx) {
   const int tb = (int)(idx / nrhs), r = (int)(idx % nrhs);
@@ -275,31 +272,23 @@ __global__ void ref_exponent_kernel(TreeDev tr, int nrhs, const int *x_exp, int 
     ref_exp[idx] = target_row_exponent(tr, nrhs, x_exp, idx);
 }
 
+// dynamic shared memory: (blockDim.x / 32) x kp * 5 bytes (kp <= 1024 modes,
+// a multiple of 16, so every warp's slice and row stays 16-byte aligned)
 __global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
-                                int nrhs, const int *x_exp, uint8_t *xdig, int kp, int kc,
+                                int nrhs, int *x_exp, uint8_t *xdig, int kp, int kc,
                                 vl1_status *st) {
+  extern __shared__ __align__(16) uint8_t s_stage[];
   const int64_t n = (int64_t)nboxes * nrhs;
   const int lane = threadIdx.x & 31;
+  uint8_t *stage = s_stage + (threadIdx.x >> 5) * kp * kDigits;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
        idx += warps)
-    row_digits(d, tr, coefs, nrhs, x_exp, xdig, kp, kc, st, idx, lane);
+    row_digits(d, tr, coefs, nrhs, x_exp, xdig, kp, kc, st, idx, lane, stage);
 }
 
 // Batch versions: block i handles rows [row0, row0 + nrows) of one problem
-// (tasks built on the host), 8 warps striding over them.
-__global__ void x_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
-  const PrepTask t = tasks[blockIdx.x];
-  const PrepProblem &P = probs[t.problem];
-  const int lane = threadIdx.x & 31;
-  for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5) {
-    const int64_t idx = t.row0 + i;
-    const int e = row_exponent(P.d, P.tr, P.coefs, P.nrhs, idx, lane);
-    if (lane == 0) P.x_exp[idx] = e;
-  }
-}
-
-// target rows [row0, row0 + nrows) of one problem, one thread each
+// (tasks built on the host).  Target rows: one thread each.
 __global__ void ref_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
   const PrepTask t = tasks[blockIdx.x];
   const PrepProblem &P = probs[t.problem];
@@ -307,13 +296,18 @@ __global__ void ref_exponent_batch_kernel(const PrepProblem *probs, const PrepTa
     P.ref_exp[t.row0 + i] = target_row_exponent(P.tr, P.nrhs, P.x_exp, t.row0 + i);
 }
 
-__global__ void x_digits_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+// Density rows: 8 warps striding over them.  Dynamic shared memory:
+// (blockDim.x / 32) x (largest kp) * 5 bytes, at most 8 x 1024 x 5 = 40 KB.
+__global__ void x_digits_batch_kernel(const PrepProblem *probs, const PrepTask *tasks,
+                                      int max_row_bytes) {
+  extern __shared__ __align__(16) uint8_t s_stage[];
   const PrepTask t = tasks[blockIdx.x];
   const PrepProblem &P = probs[t.problem];
   const int lane = threadIdx.x & 31;
+  uint8_t *stage = s_stage + (threadIdx.x >> 5) * max_row_bytes;
   for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5)
     row_digits(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, P.xdig, P.kp, P.kc, P.st, t.row0 + i,
-               lane);
+               lane, stage);
 }
 
 // 2D log displacement: w[b, r] = dispfac(b) * sum_s nmlz[lev(b), s] * coef
@@ -1249,11 +1243,10 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   }
   cudaError_t e;
   const int64_t nbr = n_xrows;
-  x_exponent_kernel<<<grid_for(nbr * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
-                                                           x_exp);
+  // row exponents and digits in one pass, then the target rows' references
+  x_digits_kernel<<<grid_for(nbr * 32, 256), 256, 8 * g.kp * kDigits, s>>>(
+      d, tree, (int)nboxes, coefs, nrhs, x_exp, xdig, g.kp, g.kc, plan->status);
   ref_exponent_kernel<<<grid_for(n_trows, 256), 256, 0, s>>>(tree, nrhs, x_exp, ref_exp);
-  x_digits_kernel<<<grid_for(nbr * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
-                                                         x_exp, xdig, g.kp, g.kc, plan->status);
   if (disp) {
     disp_box_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
                                                       wbox);
@@ -1340,6 +1333,7 @@ struct vl1_batch {
   std::vector<BatchGroup> groups;
   std::vector<SoloLaunch> solos;
   bool has_disp = false;
+  int max_row_bytes = 16;   // largest kp * 5 of the problems (digit staging)
   // pinned staging of vl1_batch_update (two, so that one can be refilled
   // while the copy from the other is in flight)
   void *pinned[2] = {nullptr, nullptr};
@@ -1568,6 +1562,7 @@ void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems
   uint8_t *base = static_cast<uint8_t *>(b->buf);
   const int n_problems = (int)L.mps.size();
   b->has_disp = false;
+  b->max_row_bytes = 16;
   for (int i = 0; i < n_problems; ++i) {
     const vl1_batch_problem &q = problems[i];
     const MixedGeom &g = q.plan->mixed.geom;
@@ -1595,6 +1590,7 @@ void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems
     L.preps[i].x_exp = x_exp;
     L.preps[i].ref_exp = ref_exp;
     L.preps[i].xdig = xdig;
+    b->max_row_bytes = std::max(b->max_row_bytes, g.kp * kDigits);
     L.preps[i].wbox = wbox;
     L.preps[i].disp = disp;
   }
@@ -1750,14 +1746,13 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
   cudaError_t e = cudaMemsetAsync(b->d_queue, 0, sizeof(int) * b->groups.size(), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(batch)");
   if (b->n_tasks > 0) {
-    x_exponent_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
-        static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
+    x_digits_batch_kernel<<<b->n_tasks, 256, 8 * b->max_row_bytes, s>>>(
+        static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks),
+        b->max_row_bytes);
     if (b->n_ttasks > 0)
       ref_exponent_batch_kernel<<<b->n_ttasks, 256, 0, s>>>(
           static_cast<const PrepProblem *>(b->d_prep),
           static_cast<const PrepTask *>(b->d_ttasks));
-    x_digits_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
-        static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
   }
   if (b->has_disp && b->n_tasks > 0) {
     disp_box_batch_kernel<<<b->n_tasks, 64, 0, s>>>(static_cast<const PrepProblem *>(b->d_prep),
