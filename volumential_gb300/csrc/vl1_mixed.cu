@@ -532,6 +532,9 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   constexpr uint32_t ABYTES = (uint32_t)NCH * KC * 2u;   // one digit plane of the table
   constexpr uint32_t STAGE_BYTES = kXPlanes * XBYTES + kDigits * ABYTES;
   constexpr uint32_t ROW_BYTES = KC * 2u;
+  // parked int64 sums: rows padded by one value, so that the 32 lanes of a
+  // readout warp (32 rows) store one column into distinct banks
+  constexpr int PARK_STRIDE = NCH + 1;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // swizzle atoms need a 1024-byte aligned base (the launch adds 1 KiB slack)
   uint8_t *smem = reinterpret_cast<uint8_t *>(
@@ -1002,7 +1005,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]));
       }
 #pragma unroll
-      for (int c = 0; c < 16; ++c) s_tot[row * NCH + cb * RC + c] = acc[c];
+      for (int c = 0; c < 16; ++c) s_tot[row * PARK_STRIDE + cb * RC + c] = acc[c];
     }
   }
 
@@ -1046,7 +1049,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     g_parts = base;
     if (!s_abort) {
       long long *mine = reinterpret_cast<long long *>(base + item.part * part_stride);
-      for (int i = tid; i < 128 * NCH; i += blockDim.x) mine[i] = tot_src[i];
+      for (int i = tid; i < 128 * NCH; i += blockDim.x)
+        mine[i] = tot_src[(i / NCH) * PARK_STRIDE + i % NCH];
     }
     __threadfence();
     __syncthreads();
@@ -1076,7 +1080,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         for (int q = 0; q < item.nparts; ++q)
           tot += __ldcg(reinterpret_cast<const long long *>(g_parts + q * part_stride) + it);
       } else {
-        tot = tot_src[it];
+        tot = tot_src[rw_ * PARK_STRIDE + cc];
       }
       double y = scaled_i64_to_double(tot, s_oexp[rw_]);
       if (p.disp) {
@@ -1115,7 +1119,7 @@ const void *mixed_kernel_ptr(int nch, int kc, bool multi) {
 size_t mixed_smem_bytes(int nch, int kc) {
   const size_t pipe = (size_t)kStages * (kXPlanes * 128 + kDigits * nch) * kc * 2 +
                       (size_t)kProducerWarps * kStgDepth * kRowsPerProducer * kDigits * kc;
-  const size_t park = (size_t)128 * nch * 8;   // int64 sums
+  const size_t park = (size_t)128 * (nch + 1) * 8;   // int64 sums, padded rows
   return (pipe > park ? pipe : park) + 1024;
 }
 
