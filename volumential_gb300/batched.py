@@ -195,10 +195,16 @@ class MixedSchedule:
             xrow[e, P % ROWS_PER_TILE] = (lists * nrhs + r).astype(np.int32)
         return tile_rows, key_start, key_ids, xrow
 
-    # cost model of one work item in pipeline units of one key: CTA start-up
-    # and result write-back, and the extra partial-sum traffic of a split part
-    ITEM_OVERHEAD_KEYS = 3.0
-    SPLIT_OVERHEAD_KEYS = 1.0
+    # cost model of one work item in units of one key's pipeline time: CTA
+    # start-up, pipeline drain and result write-back; the partial-sum write
+    # of a split part; the sum over the parts that the last part of a split
+    # tile reads back (fitted to measured launches of a 3D q = 4 tree over
+    # caps 12 .. 100000: within ~4 %)
+    ITEM_OVERHEAD_KEYS = 4.0
+    SPLIT_OVERHEAD_KEYS = 1.5
+    LAST_PART_KEYS = 2.0
+    # candidate caps, as fractions of one SM's share of all keys
+    CAP_FRACTIONS = (1.5, 1.25, 1.0, 0.85, 0.75, 0.67, 0.6, 0.5, 0.4, 0.33, 0.25, 0.2, 0.17)
 
     @staticmethod
     def _split_items(key_start, cap):
@@ -230,8 +236,10 @@ class MixedSchedule:
 
         slots = [0.0] * n_sm
         for it in items:
-            cost = (it[2] - it[1]) + cls.ITEM_OVERHEAD_KEYS + \
-                (cls.SPLIT_OVERHEAD_KEYS if it[3] >= 0 else 0.0)
+            cost = (it[2] - it[1]) + cls.ITEM_OVERHEAD_KEYS
+            if it[3] >= 0:
+                cost += cls.SPLIT_OVERHEAD_KEYS + (cls.LAST_PART_KEYS if it[4] == it[5] - 1
+                                                   else 0.0)
             heapq.heapreplace(slots, slots[0] + cost)
         return max(slots)
 
@@ -240,7 +248,7 @@ class MixedSchedule:
         """Work items (one CTA each): whole tiles, and tiles with more than a
         cap of keys split into nearly equal key ranges, ordered longest first
         (CTAs start in grid order).  Without an explicit cap, the cap among
-        one SM's share of all keys and its 1/2 .. 1/6 with the shortest
+        ``CAP_FRACTIONS`` of one SM's share of all keys with the shortest
         modelled finish time is taken."""
         total = int(key_start[-1])
         if max_keys_per_item is not None:
@@ -252,8 +260,8 @@ class MixedSchedule:
                 .multi_processor_count
         share = max(1, -(-total // max(1, n_sm)))
         best = None
-        for div in (1, 2, 3, 4, 5, 6):
-            cap = max(4, -(-share // div))
+        for f in cls.CAP_FRACTIONS:
+            cap = max(4, int(np.ceil(share * f)))
             cand = cls._split_items(key_start, cap)
             t = cls._makespan(cand[0], n_sm)
             if best is None or t < best[0]:

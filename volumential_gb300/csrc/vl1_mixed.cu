@@ -410,6 +410,30 @@ __device__ __forceinline__ double scaled_i64_to_double(long long v, int k) {
   return ldexp((double)v, k);   // subnormal or overflowing results
 }
 
+// round(x * 2^s) to the nearest int64 (ties to even) with integer operations
+// (64-bit conversions run on the narrow FP64 side of this GPU); |x| * 2^s
+// must stay below 2^62, which the FP32 tail accumulators do by far
+__device__ __forceinline__ long long f32_scaled_to_i64(float x, int s) {
+  const uint32_t b = __float_as_uint(x);
+  const int e = (int)((b >> 23) & 0xFFu);
+  if (e == 0) return 0;   // zero or subnormal: rounds to 0
+  const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+  const int sh = e - 150 + s;   // |x| * 2^s = m * 2^sh
+  long long q;
+  if (sh >= 0) {
+    q = m << sh;
+  } else if (sh < -25) {
+    q = 0;                      // below 1/4
+  } else {
+    const int k = -sh;
+    q = m >> k;
+    const long long rem = m & ((1ll << k) - 1);
+    const long long half = 1ll << (k - 1);
+    q += (rem > half || (rem == half && (q & 1))) ? 1 : 0;
+  }
+  return (b >> 31) ? -q : q;
+}
+
 // ---------------------------------------------------------- main kernel
 
 struct MixedParams {
@@ -998,11 +1022,11 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         tc::tmem_ld16(col, r16);                 // d5, weight 2^40
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]) * 256.0f);
+        for (int c = 0; c < 16; ++c) acc[c] += f32_scaled_to_i64(__uint_as_float(r16[c]), 8);
         tc::tmem_ld16(col + NCH, r16);           // d6, weight 2^32
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] += __float2ll_rn(__uint_as_float(r16[c]));
+        for (int c = 0; c < 16; ++c) acc[c] += f32_scaled_to_i64(__uint_as_float(r16[c]), 0);
       }
 #pragma unroll
       for (int c = 0; c < 16; ++c) s_tot[row * PARK_STRIDE + cb * RC + c] = acc[c];
@@ -1066,32 +1090,45 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   }
   if (write) {
     const bool oc = p.d.table_cplx;
-    for (int it = tid; it < 128 * NCH; it += blockDim.x) {
-      const int rw_ = it / NCH, cc = it - rw_ * NCH;
-      int t = chunk * NCH + cc, part = 0;
-      if (oc && t >= p.d.nq) {
-        t -= p.d.nq;
-        part = 1;
+    // BATCH outputs per thread and pass: their loads (parked sums, or the
+    // parts of a split tile from L2) are issued before any conversion
+    constexpr int BATCH = 4;
+    for (int it0 = tid; it0 < 128 * NCH; it0 += BATCH * (int)blockDim.x) {
+      long long tot[BATCH];
+#pragma unroll
+      for (int bi = 0; bi < BATCH; ++bi) {
+        const int it = it0 + bi * (int)blockDim.x;
+        tot[bi] = 0;
+        if (it >= 128 * NCH) continue;
+        if (item.split >= 0) {
+          for (int q = 0; q < item.nparts; ++q)
+            tot[bi] += __ldcg(reinterpret_cast<const long long *>(g_parts + q * part_stride) + it);
+        } else {
+          tot[bi] = tot_src[(it / NCH) * PARK_STRIDE + it % NCH];
+        }
       }
-      if (t >= s_ocnt[rw_]) continue;   // also empty rows and padding columns
-      long long tot;
-      if (item.split >= 0) {
-        tot = 0;
-        for (int q = 0; q < item.nparts; ++q)
-          tot += __ldcg(reinterpret_cast<const long long *>(g_parts + q * part_stride) + it);
-      } else {
-        tot = tot_src[rw_ * PARK_STRIDE + cc];
+#pragma unroll
+      for (int bi = 0; bi < BATCH; ++bi) {
+        const int it = it0 + bi * (int)blockDim.x;
+        if (it >= 128 * NCH) continue;
+        const int rw_ = it / NCH, cc = it - rw_ * NCH;
+        int t = chunk * NCH + cc, part = 0;
+        if (oc && t >= p.d.nq) {
+          t -= p.d.nq;
+          part = 1;
+        }
+        if (t >= s_ocnt[rw_]) continue;   // also empty rows and padding columns
+        double y = scaled_i64_to_double(tot[bi], s_oexp[rw_]);
+        if (p.disp) {
+          const int64_t di = s_rows[rw_];   // j * nrhs + r
+          y += oc ? p.disp[2 * di + part] : p.disp[di];
+        }
+        const int64_t o = s_obase[rw_] + t;
+        if (oc)
+          p.result[2 * o + part] = y;
+        else
+          p.result[o] = y;
       }
-      double y = scaled_i64_to_double(tot, s_oexp[rw_]);
-      if (p.disp) {
-        const int64_t di = s_rows[rw_];   // j * nrhs + r
-        y += oc ? p.disp[2 * di + part] : p.disp[di];
-      }
-      const int64_t o = s_obase[rw_] + t;
-      if (oc)
-        p.result[2 * o + part] = y;
-      else
-        p.result[o] = y;
     }
     // the last part leaves the counter at zero for the next call
     if (item.split >= 0 && tid == 0) p.sched.split_counters[item.split * n_chunks + chunk] = 0;
