@@ -906,10 +906,15 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
           tc::mbar_arrive_expect_tx(&bars.afull[s], kDigits * ABYTES);
           const int64_t base = (((int64_t)key * p.g.n_kc + kc) * kDigits) * p.g.np * KC +
                                (int64_t)chunk * NCH * KC;
+          if (n_chunks == 1) {
+            // one column chunk: the five digit tiles are contiguous
+            tc::bulk_g2s(as, p.adig + base, kDigits * ABYTES, &bars.afull[s]);
+          } else {
 #pragma unroll
-          for (int dg = 0; dg < kDigits; ++dg)
-            tc::bulk_g2s(as + dg * ABYTES, p.adig + base + (int64_t)dg * p.g.np * KC, ABYTES,
-                         &bars.afull[s]);
+            for (int dg = 0; dg < kDigits; ++dg)
+              tc::bulk_g2s(as + dg * ABYTES, p.adig + base + (int64_t)dg * p.g.np * KC, ABYTES,
+                           &bars.afull[s]);
+          }
         }
       }
     }
