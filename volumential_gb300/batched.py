@@ -100,8 +100,16 @@ class MixedSchedule:
         n_tiles = self.n_tiles
         geo = plan.mixed_geometry()
         n_chunks = geo["np"] // geo["nch"]
-        items, n_splits, n_slots = self._work_items(np.asarray(key_start, dtype=np.int64),
-                                                    max_keys_per_item)
+        # the work list depends only on the tiles and the cap: computed once
+        # per base schedule (further instances, e.g. a server's per-request
+        # slots, only allocate their own scratch)
+        if not hasattr(base, "_items_memo"):
+            base._items_memo = {}
+        memo = base._items_memo.get(max_keys_per_item)
+        if memo is None:
+            memo = self._work_items(np.asarray(key_start, dtype=np.int64), max_keys_per_item)
+            base._items_memo[max_keys_per_item] = memo
+        items, n_splits, n_slots = memo
         self.n_items = len(items)
         self.n_splits = n_splits
         self.max_keys_per_item = int(max(1, max((it[2] - it[1] for it in items), default=1)))
