@@ -472,6 +472,17 @@ class NearFieldFromCSR(NearFieldEvalBase):
             f"reconstruction kind {self.reconstruction_kind!r} has no GB300 kernel; "
             "only the arithmetic orbit reconstruction (scalar/signed) is supported")
 
+    def _policy_and_key(self):
+        """(parsed policy, cache key), recomputed only when ``extra_kwargs``
+        changes (both derive from the kernel, fixed at construction, and the
+        extra keyword arguments)."""
+        snap = repr(sorted(self.extra_kwargs.items(), key=lambda kv: kv[0]))
+        memo = getattr(self, "_policy_memo", None)
+        if memo is None or memo[0] != snap:
+            memo = (snap, parse_policy(self.get_kernel_scaling_policy()), self.get_cache_key())
+            self._policy_memo = memo
+        return memo[1], memo[2]
+
     def get_plan(self, *, table_data_combined, mode_nmlz_combined, case_indices,
                  encoding_base, encoding_shift, table_root_extent, table_starting_level,
                  arithmetic_case_orbit_ranks, arithmetic_case_axis_perm,
@@ -482,8 +493,8 @@ class NearFieldFromCSR(NearFieldEvalBase):
         """The device plan of this table payload (cached per payload identity;
         ``cache=False``: a new plan owned by the caller)."""
         from .plan import Plan, plan_cache_get
-        policy = parse_policy(self.get_kernel_scaling_policy())
-        key = (self.get_cache_key(), _array_token(table_data_combined),
+        policy, cache_key = self._policy_and_key()
+        key = (cache_key, _array_token(table_data_combined),
                _array_token(mode_nmlz_combined), _array_token(case_indices),
                _array_token(arithmetic_case_orbit_ranks), _array_token(arithmetic_case_axis_perm),
                _array_token(arithmetic_case_axis_sign), _array_token(arithmetic_case_axis_group),

@@ -24,12 +24,18 @@ _cache: "collections.OrderedDict" = collections.OrderedDict()
 _cache_lock = threading.Lock()
 
 
+_cuda_ok = False
+
+
 def require_cuda():
+    global _cuda_ok
     import torch
-    if not torch.cuda.is_available():
-        raise RuntimeError(
-            "volumential_gb300 evaluates list 1 on a CUDA device only; no CUDA "
-            "device is available (there is no CPU fallback)")
+    if not _cuda_ok:
+        if not torch.cuda.is_available():
+            raise RuntimeError(
+                "volumential_gb300 evaluates list 1 on a CUDA device only; no CUDA "
+                "device is available (there is no CPU fallback)")
+        _cuda_ok = True   # a device, once seen, stays (the query costs microseconds)
     return torch
 
 
@@ -63,12 +69,47 @@ def stream_handle(queue):
     raise TypeError("queue must be None or a torch.cuda.Stream")
 
 
-def tree_view_from_arrays(*, target_boxes, neighbor_source_boxes_starts,
-                          neighbor_source_boxes_lists, box_centers, box_levels,
-                          box_source_starts, box_source_counts_nonchild,
-                          box_target_starts, box_target_counts_nonchild,
-                          source_mode_ids, target_point_ids, root_extent):
-    """Build a ``vl1_tree_view`` from arrays; returns (view, tensors to keep alive)."""
+_views: "collections.OrderedDict" = collections.OrderedDict()
+_VIEW_CACHE_MAX = 8
+
+
+def tree_view_from_arrays(**arrays):
+    """Build a ``vl1_tree_view`` from arrays; returns (view, tensors to keep alive).
+
+    When every array is already a CUDA tensor of the kernel's dtype, the view
+    is cached per array identity (pointer, shape, dtype and in-place version
+    counter), so repeated calls over one tree skip the rebuild."""
+    torch = require_cuda()
+    key = None
+    tensors = [arrays[k] for k in _VIEW_ARGS]
+    if all(isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous() for t in tensors):
+        key = (tuple(_token(t) for t in tensors), float(arrays["root_extent"]))
+        hit = _views.get(key)
+        if hit is not None:
+            _views.move_to_end(key)
+            return hit
+    out = _tree_view_from_arrays(**arrays)
+    if key is not None and all(out[1][k] is t for k, t in zip(_VIEW_KEYS, tensors)):
+        _views[key] = out
+        while len(_views) > _VIEW_CACHE_MAX:
+            _views.popitem(last=False)
+    return out
+
+
+# the array arguments and their keep-dict names, in one order
+_VIEW_ARGS = ("target_boxes", "neighbor_source_boxes_starts", "neighbor_source_boxes_lists",
+              "box_centers", "box_levels", "box_source_starts", "box_source_counts_nonchild",
+              "box_target_starts", "box_target_counts_nonchild", "source_mode_ids",
+              "target_point_ids")
+_VIEW_KEYS = ("target_boxes", "starts", "lists", "centers", "levels", "src_starts",
+              "src_counts", "tgt_starts", "tgt_counts", "smode", "tmode")
+
+
+def _tree_view_from_arrays(*, target_boxes, neighbor_source_boxes_starts,
+                           neighbor_source_boxes_lists, box_centers, box_levels,
+                           box_source_starts, box_source_counts_nonchild,
+                           box_target_starts, box_target_counts_nonchild,
+                           source_mode_ids, target_point_ids, root_extent):
     torch = require_cuda()
     i32 = torch.int32
     keep = {
