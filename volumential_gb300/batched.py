@@ -1,7 +1,7 @@
 """Mixed-precision (tensor-core) list-1 evaluation: host side.
 
 ``eval_mixed`` runs ``vl1_eval_mixed`` (``include/vl1.h``): the list-1 sum of
-``volumential/list1.py:1050-1159`` computed from exact BF16 digit products on
+``volumential/list1.py:1050-1159`` computed from exact FP16 digit products on
 the tcgen05 tensor cores with FP64 final sums (relative error ~2^-40 of
 sum |table| |density|, see ``csrc/vl1_mixed.cu``).
 

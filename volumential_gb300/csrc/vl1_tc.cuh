@@ -197,7 +197,7 @@ __device__ __forceinline__ uint64_t smem_desc_kmajor_noswizzle(uint32_t saddr, u
 }
 
 // Shared-memory matrix descriptor, K-major, swizzled rows of `row_bytes`
-// (32, 64 or 128 bytes = 16, 32 or 64 bf16 along K).  Eight rows form one
+// (32, 64 or 128 bytes = 16, 32 or 64 16-bit values along K).  Eight rows form one
 // swizzle atom of 8 * row_bytes bytes (aligned to that size); the 16-byte
 // chunk c of row r sits at chunk c ^ (bits 7.. of the row's offset), as the
 // hardware applies it to absolute shared-memory addresses.
@@ -214,7 +214,7 @@ __device__ __forceinline__ uint64_t smem_desc_kmajor_swizzled(uint32_t saddr, ui
 }
 
 // Byte offset of element (row, k) in a K-major swizzled operand with `kc`
-// bf16 per row (row bytes 2*kc in {32, 64, 128}), relative to an atom-aligned
+// 16-bit values per row (row bytes 2*kc in {32, 64, 128}), relative to an atom-aligned
 // base.
 __host__ __device__ __forceinline__ uint32_t kmajor_swizzled_offset(uint32_t row, uint32_t k,
                                                                     uint32_t kc) {
@@ -262,7 +262,7 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
 }
 
 // Byte offset of element (row, k) in a K-major no-swizzle operand whose rows
-// hold `kpad` bf16 values: core matrix (row/8, k/8), row-in-core, k-in-core.
+// hold `kpad` 16-bit values: core matrix (row/8, k/8), row-in-core, k-in-core.
 __host__ __device__ __forceinline__ uint32_t kmajor_offset(uint32_t row, uint32_t k,
                                                            uint32_t kpad) {
   return (row >> 3) * (kpad >> 3) * 128u + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;

@@ -22,7 +22,7 @@ Differences from the reference that a caller can see:
   reported by the kernel through a status word and raised as exceptions,
   where the reference would read out of bounds;
 * ``list1_precision`` (an extra keyword, default ``"fp64"``) selects the plain
-  FP64 kernel or the tensor-core path (``"mixed"``: exact BF16 digit products,
+  FP64 kernel or the tensor-core path (``"mixed"``: exact FP16 digit products,
   FP64 sums, relative error ~2^-40 of sum |table| |density|).
 """
 
