@@ -86,3 +86,36 @@ def test_densities_near_the_bottom_of_fp64(cuda):
     mixed = _eval(w, coefs, "mixed")
     assert np.all(np.isfinite(mixed)) and np.max(np.abs(mixed)) > 0
     assert rel_l2(mixed, ref) <= 1e-9
+
+
+def test_tree_view_cache_follows_in_place_changes(cuda):
+    """Repeated calls over one set of CUDA tree tensors reuse the tree view;
+    an in-place change of any of them (its version counter) rebuilds and
+    revalidates it, so a bad index written into a cached tree still raises."""
+    import torch
+
+    from volumential_gb300.plan import tree_view_from_arrays
+
+    w = W.uniform_workload("edge_viewcache", 2, 2, 3, seed=9)
+    tr, tree = w.traversal, w.tree
+    local = tree.box_local_mode_ids()
+    dev = lambda a, dt=torch.int32: torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dt)
+    arrays = dict(
+        target_boxes=dev(tr.target_boxes), neighbor_source_boxes_starts=dev(tr.neighbor_source_boxes_starts),
+        neighbor_source_boxes_lists=dev(tr.neighbor_source_boxes_lists),
+        box_centers=dev(tree.box_centers, torch.float64), box_levels=dev(tree.box_levels, torch.uint8),
+        box_source_starts=dev(tree.box_target_starts),
+        box_source_counts_nonchild=dev(tree.box_target_counts_nonchild),
+        box_target_starts=dev(tree.box_target_starts),
+        box_target_counts_nonchild=dev(tree.box_target_counts_nonchild),
+        source_mode_ids=dev(local), target_point_ids=dev(local), root_extent=tree.root_extent)
+    v1, k1 = tree_view_from_arrays(**arrays)
+    v2, k2 = tree_view_from_arrays(**arrays)
+    assert v2 is v1 and k2 is k1
+    lists = arrays["neighbor_source_boxes_lists"]
+    lists[0] = lists[0]                      # same value, new version
+    v3, _ = tree_view_from_arrays(**arrays)
+    assert v3 is not v1
+    lists[0] = int(tree.box_levels.size) + 5  # a source box past the tree
+    with pytest.raises(ValueError):
+        tree_view_from_arrays(**arrays)

@@ -115,6 +115,21 @@ def test_custom_scaling_policy_documents_user_code():
         parse_policy(p)
 
 
+def test_policy_memo_follows_extra_kwargs():
+    """The per-call plan lookup reuses the parsed policy and cache key until
+    the evaluator's extra keyword arguments change."""
+    nf = NearFieldFromCSR(LaplaceKernel(3), SHAPES1)
+    pol, key = nf._policy_and_key()
+    assert key == nf.get_cache_key()
+    assert nf._policy_and_key()[1] is key          # memoised
+    nf.extra_kwargs["infer_kernel_scaling"] = not nf.extra_kwargs["infer_kernel_scaling"]
+    pol2, key2 = nf._policy_and_key()
+    assert key2 == nf.get_cache_key() and key2 != key
+    assert pol2 == parse_policy(nf.get_kernel_scaling_policy())
+    nf.extra_kwargs["list1_precision"] = "mixed"     # any change refreshes the memo
+    assert nf._policy_and_key()[1] == nf.get_cache_key()
+
+
 def test_laplace_2d_derivative_has_no_log_displacement():
     for knl in (AxisTargetDerivative(0, LaplaceKernel(2)),
                 AxisSourceDerivative(1, LaplaceKernel(2))):
