@@ -205,7 +205,7 @@ int32_t vl1_mixed_geometry(const vl1_plan *plan, int32_t *out5);
  * power-of-two scale (requantised to each target row's reference scale),
  * exact FP32 partial sums of digit products, exact int64 sums and one
  * rounding to FP64; the relative error is ~2^-35 of an output's largest
- * contribution (measured 4e-11 .. 3e-10 relative l2). */
+ * contribution (measured 4e-11 .. 3e-10 relative l2).
  * coefs: real [nrhs][n_particles] float64; result as in vl1_eval_fp64.
  * workspace: caller-provided device memory of vl1_mixed_workspace_bytes. */
 int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,
