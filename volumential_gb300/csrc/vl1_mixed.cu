@@ -217,30 +217,61 @@ __device__ __forceinline__ void row_digits(const DevDesc &d, const TreeDev &tr,
                                            int64_t idx, int lane, uint8_t *stage) {
   const int row_bytes = kp * kDigits;
   const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-  const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
-  if (lane == 0) x_exp[idx] = e;
-  for (int k = lane * 16; k < row_bytes; k += 32 * 16)
-    *reinterpret_cast<uint4 *>(stage + k) = make_uint4(0u, 0u, 0u, 0u);
-  __syncwarp();
   int cnt = tr.src_counts[b];
+  const int s0 = tr.src_starts[b];
+  const int lev = tr.levels[b];
   if (cnt > d.nq) {
     if (lane == 0) report(st, VL1_E_LAYOUT, b, cnt);
     cnt = d.nq;
   }
-  if (cnt > 0) {
-    const double sc = box_scaling(d, tr, tr.levels[b]);
-    const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
-    for (int s = lane; s < cnt; s += 32) {
-      const int m = tr.smode[tr.src_starts[b] + s];
+  for (int k = lane * 16; k < row_bytes; k += 32 * 16)
+    *reinterpret_cast<uint4 *>(stage + k) = make_uint4(0u, 0u, 0u, 0u);
+  if (cnt > 0 && cnt <= 64) {
+    // one pass (up to two values per lane): the scaled values, their mode
+    // ids and the row exponent are loaded / formed once
+    const double sc = box_scaling(d, tr, lev);
+    const double *c = coefs + (int64_t)r * tr.n_particles + s0;
+    const bool h0 = lane < cnt, h1 = lane + 32 < cnt;
+    const double v0 = h0 ? sc * c[lane] : 0.0, v1 = h1 ? sc * c[lane + 32] : 0.0;
+    const int m0 = h0 ? tr.smode[s0 + lane] : 0, m1 = h1 ? tr.smode[s0 + lane + 32] : 0;
+    int e = max(h0 ? scale_exponent(v0) : -1074, h1 ? scale_exponent(v1) : -1074);
+    e = __reduce_max_sync(0xffffffffu, e);
+    if (lane == 0) x_exp[idx] = e;
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const bool have = h ? h1 : h0;
+      const int m = h ? m1 : m0;
+      if (!have) continue;
       if (m < 0 || m >= d.nq) {
-        report(st, VL1_E_LAYOUT, b, -1 - s);
+        report(st, VL1_E_LAYOUT, b, -1 - (lane + 32 * h));
         continue;
       }
       uint8_t byt[kDigits];
-      density_digit_bytes(sc * c[s], e, byt);
+      density_digit_bytes(h ? v1 : v0, e, byt);
       const int base = (m / kc) * kDigits * kc + (m % kc);
 #pragma unroll
       for (int i = 0; i < kDigits; ++i) stage[base + i * kc] = byt[i];
+    }
+  } else {
+    const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
+    if (lane == 0) x_exp[idx] = e;
+    __syncwarp();
+    if (cnt > 0) {
+      const double sc = box_scaling(d, tr, lev);
+      const double *c = coefs + (int64_t)r * tr.n_particles + s0;
+      for (int s = lane; s < cnt; s += 32) {
+        const int m = tr.smode[s0 + s];
+        if (m < 0 || m >= d.nq) {
+          report(st, VL1_E_LAYOUT, b, -1 - s);
+          continue;
+        }
+        uint8_t byt[kDigits];
+        density_digit_bytes(sc * c[s], e, byt);
+        const int base = (m / kc) * kDigits * kc + (m % kc);
+#pragma unroll
+        for (int i = 0; i < kDigits; ++i) stage[base + i * kc] = byt[i];
+      }
     }
   }
   __syncwarp();
