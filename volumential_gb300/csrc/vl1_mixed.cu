@@ -305,9 +305,10 @@ __global__ void ref_exponent_kernel(TreeDev tr, int nrhs, const int *x_exp, int 
 
 // dynamic shared memory: (blockDim.x / 32) x kp * 5 bytes (kp <= 1024 modes,
 // a multiple of 16, so every warp's slice and row stays 16-byte aligned)
-__global__ void x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
-                                int nrhs, int *x_exp, uint8_t *xdig, int kp, int kc,
-                                vl1_status *st) {
+// (five blocks of 256 per SM: 46 registers, no spills)
+__global__ void __launch_bounds__(256, 5)
+    x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs, int nrhs,
+                    int *x_exp, uint8_t *xdig, int kp, int kc, vl1_status *st) {
   extern __shared__ __align__(16) uint8_t s_stage[];
   const int64_t n = (int64_t)nboxes * nrhs;
   const int lane = threadIdx.x & 31;
