@@ -55,7 +55,8 @@ def parse_args(argv=None):
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5", "table", "csr"),
+    p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5", "table", "csr",
+                                          "split"),
                    default="c2")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--c4-problems", type=int, default=64, help="C4: problems in the batch")
@@ -997,6 +998,90 @@ def csr_main(args):
     return 0
 
 
+def split_main(args):
+    """Helmholtz split correction (``vl1_split_correction``): the list-1 sum
+    of density x weight x R(r), R = G_k - G_0 by its series, over the C3 tree
+    (2D uniform level 6, q = 5, 102,400 points, k = 20).  One step = one
+    device sum (CUDA events); roofline: the FP64 pipe (per pair 8 flops per
+    series term for the two Horner sums, ~40 for the log and the complex
+    accumulation), nominal 1,250 GFLOP/s."""
+    import torch
+
+    from volumential_gb300 import workloads as W
+    from volumential_gb300.batch import tree_arrays
+    from volumential_gb300.helmholtz_split import (max_neighbor_distance, series_terms,
+                                                   split_correction)
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    k = 20.0
+    w = W.config_c3()
+    tree = w.tree
+    view, keep = tree_arrays(w)
+    rng = np.random.default_rng(7)
+    wts = torch.from_numpy(rng.standard_normal(tree.ntargets)).to("cuda")
+    pts = torch.from_numpy(np.ascontiguousarray(tree.targets)).to("cuda")
+    n_terms = series_terms(2, k, max_neighbor_distance(tree))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        out = split_correction(view, pts, wts, k, n_terms)
+    torch.cuda.synchronize()
+    ms = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = split_correction(view, pts, wts, k, n_terms)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    clock_info = clocks.stop()
+    t = float(np.median(ms)) / 1e3
+    pairs = w.pair_count()
+    flops = pairs * (8 * n_terms + 40)
+    # CPU restatement on a sample of target boxes (closed form, numpy)
+    from oracle import split_oracle as SO
+    tr = w.traversal
+    sel = np.arange(0, len(tr.target_boxes), max(1, len(tr.target_boxes) // 64))
+    st = tr.neighbor_source_boxes_starts
+    sub_starts = np.concatenate([[0], np.cumsum(st[sel + 1] - st[sel])])
+    sub_lists = np.concatenate([tr.neighbor_source_boxes_lists[st[i]:st[i + 1]] for i in sel])
+    ta = time.perf_counter()
+    ref = SO.split_sum(2, k, tree.targets, wts.cpu().numpy().astype(np.complex128),
+                       tr.target_boxes[sel], sub_starts, sub_lists, tree.box_target_starts,
+                       tree.box_target_counts_nonchild, exclude_self=True)
+    cpu_s = time.perf_counter() - ta
+    got = out.cpu().numpy()
+    mask = ref != 0
+    err = float(np.linalg.norm(got[mask] - ref[mask]) / np.linalg.norm(ref[mask]))
+    sub_pairs = sum(int(tree.box_target_counts_nonchild[tr.target_boxes[i]]) *
+                    int(tree.box_target_counts_nonchild[tr.neighbor_source_boxes_lists[j]])
+                    for i in sel for j in range(st[i], st[i + 1]))
+    line = {
+        "metric": "Helmholtz split correction: point pairs/s", "value": pairs / t,
+        "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "split_c3_tree_2d_k20", "points": int(tree.ntargets),
+                   "point_pairs": int(pairs), "series_terms": int(n_terms),
+                   "l2": "flushed between steps (256 MiB write)"},
+        "roofline": {"bound": "fp64", "achieved": flops / t / 1e9, "peak": 1250.0,
+                     "unit": "GFLOP/s", "frac": flops / t / 1e9 / 1250.0,
+                     "kernel": "split_remainder_kernel", "traffic": None,
+                     "peak_note": "nominal FP64 (no measured peak)"},
+        "rel_l2_vs_cpu_closed_form": err,
+        "cpu_baseline": {"value": sub_pairs / cpu_s, "unit": "pairs/s", "cores": 1,
+                         "kind": "port", "sample": f"{len(sel)} target boxes, closed form "
+                                                   "(numpy, oracle/split_oracle.py)"},
+        "e2e": None, "clocks": clock_info, "gpu_launches": args.steps,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
@@ -1005,6 +1090,8 @@ def main(argv=None):
         return c4_main(args)
     if args.workload == "c5":
         return c5_main(args)
+    if args.workload == "split":
+        return split_main(args)
     if args.workload == "table":
         return table_main(args)
     if args.workload == "csr":

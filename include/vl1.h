@@ -319,9 +319,13 @@ int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, void *stream
  * coefficients [2][N + 1][2] (re, im): row 0 = (c0, a_1..a_N) in 2D or
  * (unused, c_1..c_N) in 3D, row 1 = (unused, b_1..b_N).  Points are the tree's
  * sources = targets (tree order, [dim][n_points]); the result is complex
- * [n_points][2] and is overwritten for the target boxes' points. */
+ * [n_points][2] and is overwritten for the target boxes' points.
+ * flags: VL1_SPLIT_REAL_K when the wave number is real (the coefficients then
+ * have its structure: 2D a_n real and Im b_n = -(pi/2) a_n; 3D c_n real for
+ * even n and imaginary for odd n), which halves the series work. */
+#define VL1_SPLIT_REAL_K 1
 typedef struct {
-  int32_t dim, n_points, n_terms, exclude_self, weights_complex, reserved;
+  int32_t dim, n_points, n_terms, exclude_self, weights_complex, flags;
   const vl1_tree_view *tree;
   const double *points;
   const double *weights;

@@ -23,7 +23,10 @@ from volumential_gb300.volume_fmm import drive_volume_fmm
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("dim,level,q,k", [(2, 3, 3, 20.0), (3, 2, 2, 5.0 + 0.3j)])
+# real wave numbers take the kernel's two-sum form of the series, complex ones
+# the general four-sum form
+@pytest.mark.parametrize("dim,level,q,k", [(2, 3, 3, 20.0), (3, 2, 2, 5.0 + 0.3j),
+                                           (3, 2, 3, 7.0), (2, 3, 3, 12.0 + 0.5j)])
 @pytest.mark.parametrize("exclude_self", [True, False])
 def test_remainder_sum_matches_the_closed_form_restatement(cuda, dim, level, q, k,
                                                            exclude_self):

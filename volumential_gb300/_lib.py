@@ -131,12 +131,13 @@ class DuffyDesc(C.Structure):
 
 VL1_DUFFY_LAPLACE2D, VL1_DUFFY_LAPLACE3D, VL1_DUFFY_HELMHOLTZ2D = 0, 1, 2
 VL1_DUFFY_HELMHOLTZ3D, VL1_DUFFY_CONSTANT, VL1_DUFFY_PLANE_WAVE = 3, 4, 5
+VL1_SPLIT_REAL_K = 1
 
 
 class SplitDesc(C.Structure):
     _fields_ = [("dim", C.c_int32), ("n_points", C.c_int32), ("n_terms", C.c_int32),
                 ("exclude_self", C.c_int32), ("weights_complex", C.c_int32),
-                ("reserved", C.c_int32), ("tree", C.c_void_p), ("points", C.c_void_p),
+                ("flags", C.c_int32), ("tree", C.c_void_p), ("points", C.c_void_p),
                 ("weights", C.c_void_p), ("coefficients", C.c_void_p),
                 ("result", C.c_void_p)]
 

@@ -27,6 +27,11 @@ constexpr int kSplitMaxTerms = 128;
 
 struct SplitArgs {
   int dim, n_points, nmax, exclude_self, wcplx, n_tgt_boxes;
+  // 1: real wave number.  2D: the a_n are real and Im b_n = rho a_n, so two
+  // real Horner sums give R; 3D: c_n is real for even n and imaginary for
+  // odd n, so Re R and Im R are two Horner sums in r^2 over half the terms
+  int real_k;
+  double rho;
   const int32_t *target_boxes, *starts, *lists;
   const int32_t *src_starts, *src_counts, *tgt_starts, *tgt_counts;
   const double *points;    // [dim][n_points]
@@ -82,7 +87,26 @@ __global__ void __launch_bounds__(kSplitThreads) split_remainder_kernel(const Sp
             r2 = fma(d, d, r2);
           }
           double re, im;
-          if (DIM == 2) {
+          if (DIM == 2 && A.real_k) {
+            double pa = s_coef[0][A.nmax][0], pb = s_coef[1][A.nmax][0];
+            for (int n = A.nmax - 1; n >= 1; --n) {
+              pa = fma(pa, r2, s_coef[0][n][0]);
+              pb = fma(pb, r2, s_coef[1][n][0]);
+            }
+            const double lg = r2 > 0.0 ? 0.5 * log(r2) : 0.0;
+            re = s_coef[0][0][0] + r2 * fma(lg, pa, pb);
+            im = fma(A.rho * r2, pa, s_coef[0][0][1]);
+          } else if (DIM == 3 && A.real_k) {
+            const double r = sqrt(r2);
+            // Re R = r sum_{m>=1} c_{2m} r2^(m-1), Im R = sum_{m>=0} Im c_{2m+1} r2^m
+            const int me = A.nmax / 2, mo = (A.nmax - 1) / 2;
+            double pe = me >= 1 ? s_coef[0][2 * me][0] : 0.0;
+            for (int m = me - 1; m >= 1; --m) pe = fma(pe, r2, s_coef[0][2 * m][0]);
+            double po = s_coef[0][2 * mo + 1][1];
+            for (int m = mo - 1; m >= 0; --m) po = fma(po, r2, s_coef[0][2 * m + 1][1]);
+            re = r * pe;
+            im = po;
+          } else if (DIM == 2) {
             // Horner in x = r^2 for the log and power series (terms n >= 1)
             double pa_re = s_coef[0][A.nmax][0], pa_im = s_coef[0][A.nmax][1];
             double pb_re = s_coef[1][A.nmax][0], pb_im = s_coef[1][A.nmax][1];
@@ -152,6 +176,8 @@ extern "C" int32_t vl1_split_correction(const vl1_split_desc *desc, void *stream
   A.exclude_self = D.exclude_self;
   A.wcplx = D.weights_complex;
   A.n_tgt_boxes = T.n_target_boxes;
+  A.real_k = (D.flags & VL1_SPLIT_REAL_K) ? 1 : 0;
+  A.rho = -0.5 * 3.14159265358979323846;   // Im b_n / a_n for a real wave number
   A.target_boxes = T.target_boxes;
   A.starts = T.neighbor_source_boxes_starts;
   A.lists = T.neighbor_source_boxes_lists;

@@ -12,7 +12,8 @@
 //   one coarser: (coords + delta) >> 1, unless that is the leaf's parent;
 //   one finer:   2 coords + delta, delta in {-1,0,1,2}^d minus {0,1}^d;
 // looks them up, and keeps the sorted distinct hits.  Count, exclusive scan
-// and fill are separate launches; the row order is ascending box id.
+// (three launches over tiles of 4096 counts) and fill are separate launches;
+// the row order is ascending box id.
 
 #include <cuda_runtime.h>
 
@@ -26,6 +27,7 @@ namespace {
 constexpr int kMaxCand = 27 + 27 + 56;   // 3D: same + coarser + finer
 constexpr int kTreeThreads = 256;
 constexpr int kScanThreads = 1024;
+constexpr int kScanTile = 4 * kScanThreads;   // counts per scan block
 
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   // MurmurHash3's 64-bit finaliser (public domain): spreads keys over the table
@@ -46,6 +48,7 @@ struct CsrArgs {
   int32_t *hvals;             // [cap]
   uint64_t cap_mask;
   int32_t *counts;            // [n_leaves + 1]
+  long long *tile_sums;       // [n_leaves / kScanTile + 1]
   int32_t *starts;            // [n_leaves + 1]
   int32_t *lists;
   int32_t *status;            // [1]: 0 ok, 1 table full, 2 bad input
@@ -176,32 +179,85 @@ __global__ void csr_count_kernel(const CsrArgs A) {
   A.counts[i] = leaf_candidates(A, i, cand);
 }
 
-// exclusive scan of counts[0..n) into starts[0..n] (one CTA: each thread scans
-// a contiguous slice, then the slice sums are scanned in shared memory)
-__global__ void csr_scan_kernel(const CsrArgs A) {
-  __shared__ long long s_part[kScanThreads];
-  const int n = A.n_leaves;
-  const int per = (n + kScanThreads - 1) / kScanThreads;
-  const int lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
-  long long sum = 0;
-  for (int i = lo; i < hi; ++i) sum += A.counts[i];
-  s_part[threadIdx.x] = sum;
+// exclusive scan of counts[0..n) into starts[0..n] in three launches: the sum
+// of every tile of kScanTile counts, an exclusive scan of the tile sums (one
+// CTA), then each tile's scan from its offset.
+
+// inclusive block scan of one value per thread (warp shuffles, then the warp
+// totals in shared memory); `total` receives the block's sum
+__device__ __forceinline__ long long block_inclusive_scan(long long v, long long *s_warp,
+                                                         long long &total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  if (lane == 31) s_warp[wid] = v;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    long long run = 0;
-    for (int t = 0; t < kScanThreads; ++t) {
-      const long long v = s_part[t];
-      s_part[t] = run;
-      run += v;
+  if (wid == 0) {
+    long long w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
     }
-    if (run > 0x7fffffffll) atomicExch(A.status, 2);
-    A.starts[n] = (int32_t)run;
+    s_warp[lane] = w;   // inclusive warp-total prefix
   }
   __syncthreads();
-  long long run = s_part[threadIdx.x];
-  for (int i = lo; i < hi; ++i) {
-    A.starts[i] = (int32_t)run;
-    run += A.counts[i];
+  total = s_warp[(blockDim.x >> 5) - 1];
+  const long long add = wid > 0 ? s_warp[wid - 1] : 0;
+  __syncthreads();
+  return v + add;
+}
+
+__global__ void __launch_bounds__(kScanThreads) csr_tile_sum_kernel(const CsrArgs A) {
+  __shared__ long long s_warp[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + 4 * threadIdx.x;
+  long long v = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (base + j < A.n_leaves) v += A.counts[base + j];
+  long long total;
+  block_inclusive_scan(v, s_warp, total);
+  if (threadIdx.x == 0) A.tile_sums[blockIdx.x] = total;
+}
+
+// one CTA: exclusive scan of the n_tiles tile sums in place; starts[n] = total
+__global__ void __launch_bounds__(kScanThreads) csr_tile_scan_kernel(const CsrArgs A,
+                                                                     int n_tiles) {
+  __shared__ long long s_warp[32];
+  long long carry = 0;
+  for (int t0 = 0; t0 < n_tiles; t0 += kScanThreads) {
+    const int t = t0 + threadIdx.x;
+    const long long v = t < n_tiles ? A.tile_sums[t] : 0;
+    long long total;
+    const long long inc = block_inclusive_scan(v, s_warp, total);
+    if (t < n_tiles) A.tile_sums[t] = carry + inc - v;
+    carry += total;
+  }
+  if (threadIdx.x == 0) {
+    if (carry > 0x7fffffffll) atomicExch(A.status, 2);
+    A.starts[A.n_leaves] = (int32_t)carry;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) csr_tile_down_kernel(const CsrArgs A) {
+  __shared__ long long s_warp[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + 4 * threadIdx.x;
+  int c[4];
+  long long v = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    c[j] = base + j < A.n_leaves ? A.counts[base + j] : 0;
+    v += c[j];
+  }
+  long long total;
+  long long run = block_inclusive_scan(v, s_warp, total) - v + A.tile_sums[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (base + j < A.n_leaves) A.starts[base + j] = (int32_t)run;
+    run += c[j];
   }
 }
 
@@ -234,7 +290,8 @@ uint64_t table_capacity(int32_t n_leaves) {
 extern "C" int64_t vl1_list1_csr_workspace_bytes(int32_t n_leaves) {
   if (n_leaves < 0) return -1;
   const uint64_t cap = table_capacity(n_leaves);
-  return (int64_t)(cap * 8 + cap * 4 + ((uint64_t)n_leaves + 1) * 4 + 256);
+  const uint64_t n_tiles = ((uint64_t)n_leaves + kScanTile - 1) / kScanTile + 1;
+  return (int64_t)(cap * 8 + cap * 4 + ((uint64_t)n_leaves + 1) * 4 + 256 + n_tiles * 8);
 }
 
 extern "C" int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *stream) {
@@ -266,6 +323,9 @@ extern "C" int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *s
   A.hvals = reinterpret_cast<int32_t *>(w + cap * 8);
   A.counts = reinterpret_cast<int32_t *>(w + cap * 12);
   A.status = reinterpret_cast<int32_t *>(w + cap * 12 + ((uint64_t)D.n_leaves + 1) * 4);
+  // 8-byte aligned: the status word's 256-byte slot, then the tile sums
+  A.tile_sums = reinterpret_cast<long long *>(
+      w + ((cap * 12 + ((uint64_t)D.n_leaves + 1) * 4 + 256 + 7) & ~(uint64_t)7));
   A.cap_mask = cap - 1;
   A.starts = D.starts;
   A.lists = D.lists;
@@ -275,7 +335,10 @@ extern "C" int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *s
   const int grid = (D.n_leaves + kTreeThreads - 1) / kTreeThreads;
   hash_insert_kernel<<<grid, kTreeThreads, 0, s>>>(A);
   csr_count_kernel<<<grid, kTreeThreads, 0, s>>>(A);
-  csr_scan_kernel<<<1, kScanThreads, 0, s>>>(A);
+  const int n_tiles = (int)(((int64_t)D.n_leaves + kScanTile - 1) / kScanTile);
+  csr_tile_sum_kernel<<<n_tiles, kScanThreads, 0, s>>>(A);
+  csr_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(A, n_tiles);
+  csr_tile_down_kernel<<<n_tiles, kScanThreads, 0, s>>>(A);
   csr_fill_kernel<<<grid, kTreeThreads, 0, s>>>(A, D.lists_capacity);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "list-1 csr launches");

@@ -148,6 +148,8 @@ def split_correction(tree_view, points, weights, k, n_terms, *, exclude_self=Tru
     d = _lib.SplitDesc()
     d.dim, d.n_points, d.n_terms = dim, n, int(n_terms)
     d.exclude_self, d.weights_complex = int(bool(exclude_self)), int(wcplx)
+    # a real wave number: the kernel's two-sum form of the series
+    d.flags = _lib.VL1_SPLIT_REAL_K if complex(k).imag == 0.0 else 0
     d.tree = C.cast(C.pointer(tree_view), C.c_void_p)
     pts = points.to(torch.float64).contiguous()
     d.points, d.weights = pts.data_ptr(), w.data_ptr()
