@@ -1002,9 +1002,9 @@ def split_main(args):
     """Helmholtz split correction (``vl1_split_correction``): the list-1 sum
     of density x weight x R(r), R = G_k - G_0 by its series, over the C3 tree
     (2D uniform level 6, q = 5, 102,400 points, k = 20).  One step = one
-    device sum (CUDA events); roofline: the FP64 pipe (per pair 8 flops per
-    series term for the two Horner sums, ~40 for the log and the complex
-    accumulation), nominal 1,250 GFLOP/s."""
+    device sum (CUDA events); roofline: the FP64 pipe (per pair 4 flops per
+    series term for the two real Horner sums of a real wave number, ~40 for
+    the log and the complex accumulation), nominal 1,250 GFLOP/s."""
     import torch
 
     from volumential_gb300 import workloads as W
@@ -1040,7 +1040,7 @@ def split_main(args):
     clock_info = clocks.stop()
     t = float(np.median(ms)) / 1e3
     pairs = w.pair_count()
-    flops = pairs * (8 * n_terms + 40)
+    flops = pairs * (4 * n_terms + 40)
     # CPU restatement on a sample of target boxes (closed form, numpy)
     from oracle import split_oracle as SO
     tr = w.traversal
