@@ -28,19 +28,7 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-
-// As mbar_try_wait, but the thread may sleep (up to `hint_ns`) until the
+// Test the phase parity; the thread may sleep (up to `hint_ns`) until the
 // phase completes instead of returning at once; a sleeping warp takes no
 // issue slots from the warps doing work.
 __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t phase,
@@ -56,14 +44,6 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t phas
   return ok != 0;
 }
 
-// Wait for the given phase parity; gives up after `limit` polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase,
-                                                  uint32_t limit) {
-  for (uint32_t i = 0; i < limit; ++i)
-    if (mbar_try_wait(bar, phase)) return true;
-  return false;
-}
-
 // ------------------------------------------------------- bulk copy (1D TMA)
 // global -> shared, completion counted on `bar` (bytes, 16-byte multiples,
 // both addresses 16-byte aligned)
@@ -75,36 +55,12 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       : "memory");
 }
 
-// ------------------------------------------- row gather (2D TMA, gather4)
-// Four rows (r0..r3) of a 2D tensor, columns [col, col + box width), into
-// `dst` (four consecutive box rows, swizzled as the tensor map says, by the
-// absolute shared-memory address).  Rows outside the tensor read as zero and
-// still count their bytes on `bar`.  The box must be one row high.
-__device__ __forceinline__ void gather4_g2s(void *dst, const void *tmap, int col, int r0,
-                                            int r1, int r2, int r3, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes "
-      "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_addr(dst)),
-      "l"(tmap), "r"(col), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_addr(bar))
-      : "memory");
-}
-
 // ---------------------------------------------------- cp.async (16 bytes)
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
-               : "memory");
-}
 // 16 bytes, of which the first `src_bytes` (0 or 16) are read and the rest
 // zero-filled; with src_bytes == 0 nothing is read from `src`
 __device__ __forceinline__ void cp_async16_zfill(void *dst, const void *src, uint32_t src_bytes) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src),
                "r"(src_bytes)
-               : "memory");
-}
-// arrive on `bar` once every prior cp.async of this thread has completed
-// (the arrival is part of the barrier's initial count)
-__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t *bar) {
-  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar))
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() {
@@ -144,20 +100,6 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// 32 lanes x 32 consecutive 32-bit columns -> 32 registers per thread
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-        "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),
-        "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-        "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
 // 32 lanes x 16 consecutive 32-bit columns -> 16 registers per thread
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
@@ -168,34 +110,11 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
-// 32 lanes x 8 consecutive 32-bit columns -> 8 registers per thread
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-        "=r"(r[6]), "=r"(r[7])
-      : "r"(taddr));
-}
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // ------------------------------------------------------------------ MMA
-// Shared-memory matrix descriptor, K-major, no swizzle ("interleaved" core
-// matrices of 8 rows x 16 bytes stored as 128 contiguous bytes).
-//   lbo: byte distance between core matrices adjacent along K
-//   sbo: byte distance between core matrices adjacent along M/N
-__device__ __forceinline__ uint64_t smem_desc_kmajor_noswizzle(uint32_t saddr, uint32_t lbo,
-                                                               uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for the sm_100 family
-  // base offset 0, lbo mode 0, layout type 0 (no swizzle)
-  return d;
-}
-
 // Shared-memory matrix descriptor, K-major, swizzled rows of `row_bytes`
 // (32, 64 or 128 bytes = 16, 32 or 64 16-bit values along K).  Eight rows form one
 // swizzle atom of 8 * row_bytes bytes (aligned to that size); the 16-byte
@@ -225,15 +144,6 @@ __host__ __device__ __forceinline__ uint32_t kmajor_swizzled_offset(uint32_t row
   return (row >> 3) * 8u * row_bytes + (a & ~(mask << 4)) + (chunk << 4);
 }
 
-// Instruction descriptor of kind::f16: BF16 x BF16 -> FP32, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n) {
-  return (1u << 4)                          // D format: F32
-         | (1u << 7)                        // A format: BF16
-         | (1u << 10)                       // B format: BF16
-         | ((uint32_t)(n >> 3) << 17)       // N / 8
-         | ((uint32_t)(m >> 4) << 24);      // M / 16
-}
-
 // Instruction descriptor of kind::f16: F16 x F16 -> FP32, both K-major.
 __host__ __device__ constexpr uint32_t idesc_f16_f32(int m, int n) {
   return (1u << 4)                          // D format: F32 (A, B format 0: F16)
@@ -241,8 +151,8 @@ __host__ __device__ constexpr uint32_t idesc_f16_f32(int m, int n) {
          | ((uint32_t)(m >> 4) << 24);      // M / 16
 }
 
-// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread (kind::f16: both
-// operands F16 or both BF16, as the instruction descriptor says)
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread (kind::f16 with the
+// F16 x F16 instruction descriptor above)
 __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
                                          uint32_t idesc, uint32_t accumulate) {
   asm volatile(
@@ -259,13 +169,6 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
       ::"r"(smem_addr(bar))
       : "memory");
-}
-
-// Byte offset of element (row, k) in a K-major no-swizzle operand whose rows
-// hold `kpad` 16-bit values: core matrix (row/8, k/8), row-in-core, k-in-core.
-__host__ __device__ __forceinline__ uint32_t kmajor_offset(uint32_t row, uint32_t k,
-                                                           uint32_t kpad) {
-  return (row >> 3) * (kpad >> 3) * 128u + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
 }
 
 }  // namespace tc
