@@ -463,6 +463,38 @@ def test_tile_schedule_matches_per_tile_restatement(nrhs):
         assert np.array_equal(np.asarray(g), np.asarray(w))
 
 
+def test_work_item_cap_choice_equals_the_exhaustive_search():
+    """The cap search skips candidates whose lower bound cannot beat the best
+    so far and uses max(cost) when every item has its own slot; the chosen
+    work list is the one an exhaustive search over the candidates picks."""
+    import heapq
+
+    from volumential_gb300.batched import MixedSchedule as M
+
+    def finish(items, n_sm):
+        slots = [0.0] * n_sm
+        for it in items:
+            cost = (it[2] - it[1]) + M.ITEM_OVERHEAD_KEYS
+            if it[3] >= 0:
+                cost += M.SPLIT_OVERHEAD_KEYS + (M.LAST_PART_KEYS if it[4] == it[5] - 1 else 0)
+            heapq.heapreplace(slots, slots[0] + cost)
+        return max(slots)
+
+    rng = np.random.default_rng(21)
+    for _ in range(60):
+        nt = int(rng.integers(1, 300))
+        ks = np.concatenate([[0], np.cumsum(rng.integers(1, 80, size=nt))])
+        n_sm = int(rng.integers(1, 160))
+        share = max(1, -(-int(ks[-1]) // n_sm))
+        best = None
+        for f in M.CAP_FRACTIONS:
+            cand = M._split_items(ks, max(4, int(np.ceil(share * f))))
+            t = finish(cand[0], n_sm)
+            if best is None or t < best[0]:
+                best = (t, cand)
+        assert M._work_items(ks, None, n_sm=n_sm) == best[1]
+
+
 def test_tile_schedule_rejects_two_sources_with_one_case():
     from volumential_gb300.batched import MixedSchedule
 

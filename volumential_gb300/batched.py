@@ -242,6 +242,8 @@ class MixedSchedule:
         ``n_sm`` one-CTA-per-SM slots, launched in order."""
         import heapq
 
+        if len(items) <= n_sm:   # one item per slot
+            return cls._makespan_bound(items, n_sm) if items else 0.0
         slots = [0.0] * n_sm
         for it in items:
             cost = (it[2] - it[1]) + cls.ITEM_OVERHEAD_KEYS
@@ -268,13 +270,31 @@ class MixedSchedule:
                 .multi_processor_count
         share = max(1, -(-total // max(1, n_sm)))
         best = None
+        seen = set()
         for f in cls.CAP_FRACTIONS:
             cap = max(4, int(np.ceil(share * f)))
+            if cap in seen:
+                continue
+            seen.add(cap)
             cand = cls._split_items(key_start, cap)
+            if best is not None and cls._makespan_bound(cand[0], n_sm) > best[0]:
+                continue   # cannot finish sooner (nor tie) than the best so far
             t = cls._makespan(cand[0], n_sm)
             if best is None or t < best[0]:
                 best = (t, cand)
         return best[1]
+
+    @classmethod
+    def _makespan_bound(cls, items, n_sm):
+        """A lower bound of ``_makespan``: the longest item, and the mean load
+        per slot."""
+        if not items:
+            return 0.0
+        costs = [(it[2] - it[1]) + cls.ITEM_OVERHEAD_KEYS +
+                 ((cls.SPLIT_OVERHEAD_KEYS + (cls.LAST_PART_KEYS if it[4] == it[5] - 1
+                                              else 0.0)) if it[3] >= 0 else 0.0)
+                 for it in items]
+        return max(max(costs), sum(costs) / n_sm)
 
     @staticmethod
     def _check_modes(keep, nq):
