@@ -6,14 +6,16 @@
 // Boxes are named by key = offset(level) + linear(coordinates at that level)
 // (offset(l) = sum_{j<l} 2^(d j), coordinates axis 0 most significant).
 // Leaves go into an open-addressed hash table (key -> box id); one thread per
-// target leaf enumerates the candidate positions, in the order and with the
-// validity rules of the host builder:
+// target leaf enumerates the candidate positions with the validity rules of
+// the host builder:
 //   same level: coords + delta, delta in {-1,0,1}^d (the leaf itself included);
-//   one coarser: (coords + delta) >> 1, unless that is the leaf's parent;
+//   one coarser: (coords + delta) >> 1 for in-range coords + delta, unless
+//                that is the leaf's parent (each such cell once);
 //   one finer:   2 coords + delta, delta in {-1,0,1,2}^d minus {0,1}^d;
-// looks them up, and keeps the sorted distinct hits.  Count, exclusive scan
-// (three launches over tiles of 4096 counts) and fill are separate launches;
-// the row order is ascending box id.
+// and looks them up; the hits are distinct boxes, so the count pass only
+// counts and the fill pass sorts its row.  Count, exclusive scan (three
+// launches over tiles of 4096 counts) and fill are separate launches; the
+// row order is ascending box id.
 
 #include <cuda_runtime.h>
 
@@ -24,7 +26,7 @@
 namespace vl1 {
 namespace {
 
-constexpr int kMaxCand = 27 + 27 + 56;   // 3D: same + coarser + finer
+constexpr int kMaxCand = 27 + 8 + 56;   // 3D: same + coarser + finer
 constexpr int kTreeThreads = 256;
 constexpr int kScanThreads = 1024;
 constexpr int kScanTile = 4 * kScanThreads;   // counts per scan block
@@ -103,38 +105,72 @@ __device__ __forceinline__ int hash_find(const CsrArgs &A, long long key) {
   return -1;
 }
 
-// candidates of target leaf i, sorted and distinct; returns their number
-__device__ int leaf_candidates(const CsrArgs &A, int i, int *out) {
+// The list-1 boxes of target leaf i: the leaves at its own level at
+// coords + delta, delta in {-1,0,1}^d (itself included); the leaves one
+// level coarser that contain such a position, except its parent; the leaves
+// one level finer at 2 coords + delta, delta in {-1..2}^d outside {0,1}^d.
+// Every hit is a distinct box: the same-level and finer positions are
+// distinct, and the coarser cells are enumerated once each (per axis the
+// distinct values of (coords + delta) >> 1 over the in-range deltas, at
+// most two).  EMIT(id) is called per hit; returns the number of hits.
+template <class Emit>
+__device__ __forceinline__ int leaf_hits(const CsrArgs &A, int i, Emit emit) {
   const int dim = A.dim;
   const int b = A.leaf_boxes[i];
   if (b < 0 || b >= A.nboxes) return 0;   // reported by the insert kernel
   const int tl = A.levels[b];
   long long tc[3];
   for (int a = 0; a < dim; ++a) tc[a] = A.coords[(int64_t)b * dim + a];
+  const long long side = 1ll << tl;
   int n = 0;
+  // same level
   const int n3 = dim == 3 ? 27 : 9;
-  // same level (shift 0) and one coarser (shift 1)
-  for (int shift = 0; shift <= 1; ++shift) {
-    const int clev = tl - shift;
-    if (clev < 0) continue;
-    for (int di = 0; di < n3; ++di) {
-      long long pos[3], cp[3];
-      bool valid = true, parent = true;
-      int rem = di;
-      for (int a = dim - 1; a >= 0; --a) {
-        const int d = rem % 3 - 1;
-        rem /= 3;
-        pos[a] = tc[a] + d;
-        valid = valid && pos[a] >= 0 && pos[a] < (1ll << tl);
+  for (int di = 0; di < n3; ++di) {
+    long long pos[3];
+    bool valid = true;
+    int rem = di;
+    for (int a = dim - 1; a >= 0; --a) {
+      const int d = rem % 3 - 1;
+      rem /= 3;
+      pos[a] = tc[a] + d;
+      valid = valid && pos[a] >= 0 && pos[a] < side;
+    }
+    if (!valid) continue;
+    const int id = hash_find(A, box_key(dim, tl, pos));
+    if (id >= 0) {
+      emit(n, id);
+      ++n;
+    }
+  }
+  // one coarser: per axis the distinct parents of the in-range positions
+  if (tl >= 1) {
+    long long cv[3][2];
+    int nv[3];
+    for (int a = 0; a < dim; ++a) {
+      nv[a] = 0;
+      for (int d = -1; d <= 1; ++d) {
+        const long long p = tc[a] + d;
+        if (p < 0 || p >= side) continue;
+        const long long c = p >> 1;
+        if (nv[a] == 0 || cv[a][nv[a] - 1] != c) cv[a][nv[a]++] = c;   // ascending
       }
-      if (!valid) continue;
-      for (int a = 0; a < dim; ++a) {
-        cp[a] = pos[a] >> shift;
+    }
+    const int tot = dim == 3 ? nv[0] * nv[1] * nv[2] : nv[0] * nv[1];
+    for (int ci = 0; ci < tot; ++ci) {
+      long long cp[3];
+      bool parent = true;
+      int rem = ci;
+      for (int a = dim - 1; a >= 0; --a) {
+        cp[a] = cv[a][rem % nv[a]];
+        rem /= nv[a];
         parent = parent && cp[a] == (tc[a] >> 1);
       }
-      if (shift == 1 && parent) continue;   // the leaf's own ancestor
-      const int id = hash_find(A, box_key(dim, clev, cp));
-      if (id >= 0) out[n++] = id;
+      if (parent) continue;   // the leaf's own ancestor
+      const int id = hash_find(A, box_key(dim, tl - 1, cp));
+      if (id >= 0) {
+        emit(n, id);
+        ++n;
+      }
     }
   }
   // one finer: 2 coords + delta, delta in {-1..2}^d outside {0,1}^d
@@ -149,15 +185,23 @@ __device__ int leaf_candidates(const CsrArgs &A, int i, int *out) {
         rem /= 4;
         pos[a] = 2 * tc[a] + d;
         inner = inner && (d == 0 || d == 1);
-        valid = valid && pos[a] >= 0 && pos[a] < (1ll << (tl + 1));
+        valid = valid && pos[a] >= 0 && pos[a] < 2 * side;
       }
       if (inner || !valid) continue;
       const int id = hash_find(A, box_key(dim, tl + 1, pos));
-      if (id >= 0) out[n++] = id;
+      if (id >= 0) {
+        emit(n, id);
+        ++n;
+      }
     }
   }
-  // insertion sort and dedup
-  for (int x = 1; x < n; ++x) {
+  return n;
+}
+
+// candidates of target leaf i, sorted ascending; returns their number
+__device__ int leaf_candidates(const CsrArgs &A, int i, int *out) {
+  const int n = leaf_hits(A, i, [&](int k, int id) { out[k] = id; });
+  for (int x = 1; x < n; ++x) {   // insertion sort
     const int v = out[x];
     int y = x - 1;
     while (y >= 0 && out[y] > v) {
@@ -166,17 +210,13 @@ __device__ int leaf_candidates(const CsrArgs &A, int i, int *out) {
     }
     out[y + 1] = v;
   }
-  int m = 0;
-  for (int x = 0; x < n; ++x)
-    if (m == 0 || out[m - 1] != out[x]) out[m++] = out[x];
-  return m;
+  return n;
 }
 
 __global__ void csr_count_kernel(const CsrArgs A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.n_leaves) return;
-  int cand[kMaxCand];
-  A.counts[i] = leaf_candidates(A, i, cand);
+  A.counts[i] = leaf_hits(A, i, [](int, int) {});   // distinct hits: no sort needed
 }
 
 // exclusive scan of counts[0..n) into starts[0..n] in three launches: the sum
