@@ -84,15 +84,17 @@ def tree_view_from_arrays(**arrays):
     tensors = [arrays[k] for k in _VIEW_ARGS]
     if all(isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous() for t in tensors):
         key = (tuple(_token(t) for t in tensors), float(arrays["root_extent"]))
-        hit = _views.get(key)
-        if hit is not None:
-            _views.move_to_end(key)
-            return hit
+        with _cache_lock:
+            hit = _views.get(key)
+            if hit is not None:
+                _views.move_to_end(key)
+                return hit
     out = _tree_view_from_arrays(**arrays)
     if key is not None and all(out[1][k] is t for k, t in zip(_VIEW_KEYS, tensors)):
-        _views[key] = out
-        while len(_views) > _VIEW_CACHE_MAX:
-            _views.popitem(last=False)
+        with _cache_lock:
+            _views[key] = out
+            while len(_views) > _VIEW_CACHE_MAX:
+                _views.popitem(last=False)
     return out
 
 
