@@ -476,7 +476,10 @@ class NearFieldFromCSR(NearFieldEvalBase):
         """(parsed policy, cache key), recomputed only when ``extra_kwargs``
         changes (both derive from the kernel, fixed at construction, and the
         extra keyword arguments)."""
-        snap = repr(sorted(self.extra_kwargs.items(), key=lambda kv: kv[0]))
+        snap = tuple(sorted(
+            (k, v if isinstance(v, (str, int, float, bool, complex, type(None)))
+             else (type(v).__name__, id(v)))
+            for k, v in self.extra_kwargs.items()))
         memo = getattr(self, "_policy_memo", None)
         if memo is None or memo[0] != snap:
             memo = (snap, parse_policy(self.get_kernel_scaling_policy()), self.get_cache_key())
