@@ -549,3 +549,28 @@ def test_c5_mix_follows_its_sampling_rules():
     assert _nearest_level(2, 4, 5000) == 4 and _nearest_level(3, 3, 3e5) == 4
     t = poisson_arrivals(20000, 1000.0, seed=1)
     assert np.all(np.diff(t) > 0) and abs(t[-1] / 20000 - 1e-3) < 5e-5
+
+
+def test_header_constants_match_the_python_binding():
+    """Every enumerator and integer #define of include/vl1.h has the same value
+    in the ctypes binding (status codes, dtypes, policy and builder codes,
+    split flags, the no-alloc scratch size)."""
+    import os
+    import re
+
+    from volumential_gb300 import _lib
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    text = open(os.path.join(root, "include", "vl1.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    consts = {}
+    for body in re.findall(r"enum\s*\{(.*?)\}", text, flags=re.S):
+        for name, val in re.findall(r"(VL1_[A-Z0-9_]+)\s*=\s*([^,\s]+)", body):
+            consts[name] = int(val, 0)
+    for name, a, b in re.findall(r"#define\s+(VL1_[A-Z0-9_]+)\s+\((\d+)LL\s*<<\s*(\d+)\)", text):
+        consts[name] = int(a) << int(b)
+    for name, val in re.findall(r"#define\s+(VL1_[A-Z0-9_]+)\s+(\d+)\s*$", text, flags=re.M):
+        consts[name] = int(val)
+    assert len(consts) >= 28
+    for name, val in consts.items():
+        assert getattr(_lib, name) == val, name
