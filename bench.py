@@ -7,8 +7,9 @@
 Workload (default ``c2``): 3D Laplace volume potential, list-1 near field only,
 FP64, adaptive 2:1-balanced octree on [-0.5, 0.5]^3 refined where the density
 variation over a leaf exceeds 1e-3 (23,087 leaves, q=4, 1,477,568 points),
-density a sum of 16 seeded Gaussians; seeded synthetic tables in the
-reference's compact layout (the evaluation is linear in the table values).
+density a sum of 16 seeded Gaussians; the canonical 3D Laplace table built
+by Duffy quadrature in FP64 (the package's GPU builder at the reference's
+default orders, outside the timed region).
 
 One step = one list-1 evaluation of all target points for one right-hand side
 (the reference's ``near_field`` launch).  Between timed steps the L2 cache is
@@ -108,6 +109,28 @@ def peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), float(d.get("bf16_tflops", 1900.0)), "measured"
     return 6800.0, 1900.0, "fallback"
+
+
+def measured_fp64_gflops(n=4096, reps=5):
+    """FP64 peak of this GPU as cuBLAS DGEMM reaches it (2 n^3 flops per
+    call, best of ``reps``, CUDA events): the denominator of the FP64-pipe
+    roofline of the plain kernel, measured in the same run."""
+    import torch
+
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    c = a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b, c
+    return 2.0 * n ** 3 / best / 1e9
 
 
 class ClockSampler:
@@ -308,8 +331,9 @@ def gpu_arm(args):
     plan.raise_on_status(sh)
     yp = out_plain.cpu().numpy().reshape(nrhs, n)
     ym = out_mixed.cpu().numpy().reshape(nrhs, n)
-    mixed_err = max(float(np.linalg.norm(ym[r] - yp[r]) / np.linalg.norm(yp[r]))
-                    for r in range(nrhs))
+    mixed_errs = [float(np.linalg.norm(ym[r] - yp[r]) / np.linalg.norm(yp[r]))
+                  for r in range(nrhs)]
+    mixed_err = max(mixed_errs)
     headline = "plain"
     if mixed_err <= 1e-9 and res["mixed"]["total_ms"] < res["plain"]["total_ms"]:
         headline = "mixed"   # the faster path within its tolerance
@@ -360,7 +384,8 @@ def gpu_arm(args):
         "coef_complex": coef_complex, "h2d": int(host_in.numel() * host_in.element_size()),
         "d2h": int(host_out.numel() * host_out.element_size()),
         "plan_bytes": plan.device_bytes(), "world": world, "rank": rank,
-        "mixed_err": mixed_err, "api_err": api_err, "headline": headline,
+        "mixed_err": mixed_err, "mixed_errs": mixed_errs, "api_err": api_err,
+        "headline": headline, "fp64_gflops": measured_fp64_gflops(),
         "schedule": {"tiles": sched.n_tiles, "tile_keys": sched.n_tile_keys,
                      "mean_keys_per_tile": sched.mean_keys_per_tile,
                      "build_s": t_sched, "workspace_bytes": int(sched.workspace.numel())},
@@ -453,17 +478,40 @@ def reference_arm(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w.name, "points": w.n_points,
-                   "leaves": int(len(w.traversal.target_boxes)), "q": w.q,
-                   "dim": w.dim, "nrhs": 1, "cpu": cpu_model()},
+        "config": workload_config(w),
         "cpu_baseline": {"value": value, "unit": "points/s", "cores": nthreads,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": f"{sample}, {cpu_model()}",
+                         "nrhs_timed": 1},
         "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(w):
+    """The workload's description, shared by both arms' JSON lines."""
+    return {"workload": w.name, "dim": w.dim, "q": w.q, "nrhs": w.nrhs,
+            "points": w.n_points, "leaves": int(len(w.traversal.target_boxes)),
+            "list1_box_pairs": w.traversal.nnz, "point_pairs": w.pair_count(),
+            "tables": _table_source(w)}
+
+
+def _per_rhs(errs):
+    """Relative l2 error of every right-hand side (rounded) and its spread."""
+    e = np.asarray(errs, dtype=np.float64)
+    return {"n": int(e.size), "min": float(e.min()), "median": float(np.median(e)),
+            "max": float(e.max()), "values": [float(f"{x:.3g}") for x in e]}
+
+
+def _table_source(w):
+    if w.meta.get("tables") == "duffy":
+        t = w.tables[0]
+        return (f"FP64 Duffy quadrature on the GPU ({type(t.integral_knl).__name__}, "
+                f"q={t.quad_order}, source box extent {t.source_box_extent:g}, regular 20 / "
+                "radial 61 tanh-sinh-fast)")
+    return "seeded synthetic values in the compact layout"
 
 
 def tensor_executed(r, ms_per_step, bf16_peak):
@@ -486,10 +534,10 @@ def gb300_main(args):
                           coef_complex=r["coef_complex"],
                           table_bytes=16 if w.tables[0].dtype == np.complex128 else 8)
     P = w.pair_count()
-    F = (4 if r["out_complex"] else 2) * P * nrhs   # FP64-equivalent algorithmic flops
-    # the mixed path's algorithm: 15 FP16 digit products (2 flops each) per
-    # point pair and rhs, twice for complex outputs (padding not counted)
-    F_tc = (2 if r["out_complex"] else 1) * 2 * 15 * P * nrhs
+    # FP64-equivalent algorithmic flops: 2 per point pair and rhs, 4 for a
+    # complex table (digit slices of the tensor-core path not counted)
+    F = (4 if r["out_complex"] else 2) * P * nrhs
+    fp64_peak = r["fp64_gflops"]
 
     def path_summary(name):
         step_ms = np.asarray(r["res"][name]["step_ms"])
@@ -505,6 +553,10 @@ def gb300_main(args):
 
     plain = path_summary("plain")
     mixed = path_summary("mixed")
+    plain.update({"fp64_gflops": F / (plain["ms_per_step"] / 1e3) / 1e9,
+                  "fp64_peak_gflops_measured_dgemm": fp64_peak,
+                  "fp64_frac_of_measured_dgemm":
+                      F / (plain["ms_per_step"] / 1e3) / 1e9 / fp64_peak})
     head = mixed if r["headline"] == "mixed" else plain
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -514,31 +566,35 @@ def gb300_main(args):
     kms = r["res"]["mixed"]["kernel_ms"]
     if r["headline"] == "mixed" and kms:
         # the dominant kernel (mixed_kernel) timed alone with events the
-        # library records around its launch, inside the timed steps
+        # library records around its launch, inside the timed steps.
+        # T_roof = max(B / HBM, F / tensor peak), F the FP64-equivalent
+        # algorithmic flops; frac = T_roof / T_kernel
         kernel_s = float(np.mean(kms)) / 1e3
-        t_hbm, t_tc = B / (hbm * 1e9), F_tc / (bf16 * 1e12)
-        if t_tc >= t_hbm:
-            roof = {"bound": "tensor", "achieved": F_tc / kernel_s / 1e12, "peak": bf16,
-                    "unit": "TFLOP/s", "frac": F_tc / kernel_s / 1e12 / bf16}
+        t_hbm, t_pipe = B / (hbm * 1e9), F / (bf16 * 1e12)
+        if t_pipe >= t_hbm:
+            roof = {"bound": "tensor", "achieved": F / kernel_s / 1e12, "peak": bf16,
+                    "unit": "TFLOP/s"}
         else:
             roof = {"bound": "hbm", "achieved": B / kernel_s / 1e9, "peak": hbm,
-                    "unit": "GB/s", "frac": B / kernel_s / 1e9 / hbm}
-        roof.update({"kernel": "mixed_kernel", "kernel_ms": kernel_s * 1e3,
-                     "kernel_share_of_step": kernel_s * 1e3 / head["ms_per_step"],
-                     "algorithmic_tensor_flops": int(F_tc)})
+                    "unit": "GB/s"}
+        roof.update({"frac": max(t_hbm, t_pipe) / kernel_s, "kernel": "mixed_kernel",
+                     "kernel_ms": kernel_s * 1e3,
+                     "kernel_share_of_step": kernel_s * 1e3 / head["ms_per_step"]})
     else:
         # the FP64 kernel: its binding roof is the FP64 pipe (2 flops per point
-        # pair per rhs; no measured FP64 peak exists for this machine, so the
-        # nominal 1,250 GFLOP/s); its HBM rate is in paths.plain_fp64
+        # pair per rhs), against the DGEMM rate measured in this run
         kernel_s = head["ms_per_step"] / 1e3
-        fp64_nominal = 1250.0
-        t_hbm, t_tc = B / (hbm * 1e9), F / (fp64_nominal * 1e9)
-        roof = {"bound": "fp64", "achieved": F / kernel_s / 1e9, "peak": fp64_nominal,
-                "unit": "GFLOP/s", "frac": F / kernel_s / 1e9 / fp64_nominal,
-                "kernel": "plain_kernel", "peak_note": "nominal FP64 (no measured peak)"}
-    roof.update({"traffic": traffic, "peak_source": peak_kind, "algorithmic_bytes": int(B),
+        t_hbm, t_pipe = B / (hbm * 1e9), F / (fp64_peak * 1e9)
+        roof = {"bound": "fp64", "achieved": F / kernel_s / 1e9, "peak": fp64_peak,
+                "unit": "GFLOP/s", "frac": max(t_hbm, t_pipe) / kernel_s,
+                "kernel": "plain_kernel", "peak_note": "cuBLAS DGEMM measured in this run"}
+    roof.update({"traffic": traffic,
+                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu "
+                                   "capture of this kernel on this workload "
+                                   "(profiles/traffic.json), not measured in this run",
+                 "peak_source": peak_kind, "algorithmic_bytes": int(B),
                  "algorithmic_flops_fp64eq": int(F),
-                 "roof_time_us": 1e6 * max(t_hbm, t_tc)})
+                 "roof_time_us": 1e6 * max(t_hbm, t_pipe)})
 
     line = {
         "metric": METRIC, "value": head["value"], "unit": "points/s", "n_gpus": world,
@@ -546,12 +602,11 @@ def gb300_main(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp16-digits/fp32-exact/f64" if r["headline"] == "mixed" else "f64",
         "data": "synthetic",
-        "config": {"workload": w.name, "dim": w.dim, "q": w.q, "nrhs": nrhs,
-                   "points": n, "leaves": int(len(w.traversal.target_boxes)),
-                   "list1_box_pairs": w.traversal.nnz, "point_pairs": P,
-                   "path": r["headline"], "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": workload_config(w),
+        "path": r["headline"], "l2": "flushed between steps (256 MiB write)",
+        "parallelism": "replicas" if world > 1 else "single",
         "rel_l2_vs_fp64": r["mixed_err"] if r["headline"] == "mixed" else 0.0,
+        "rel_l2_per_rhs": _per_rhs(r["mixed_errs"]) if r["headline"] == "mixed" else None,
         "solves_per_s": 1e3 * nrhs / head["ms_per_step"],
         "latency_ms": head["latency_ms"],
         "e2e": {"value": replica_rate(n * nrhs * K, world, r["e2e_total_ms"]), "unit": "points/s",
@@ -904,10 +959,10 @@ def table_main(args):
                                    f"{csec:.2f} s (numpy restatement, 1 core)"}
     head = out["lap3d_q4"]
     hbm, bf16, peak_kind = peaks()
-    fp64_nominal = 1250.0   # GB300 nominal FP64 (GFLOP/s); no measured FP64 peak
-    # FP64 flops per enumerated node of the 3D Laplace q=4 build, DADD + DMUL +
-    # 2 DFMA thread instructions over the nodes of one launch (ncu counters,
-    # profiles/duffy_table_lap3d_q4.md); nodes of empty sub-boxes included
+    fp64_peak = measured_fp64_gflops()
+    # FP64 flops per enumerated node of the 3D Laplace q=4 build: DADD + DMUL +
+    # 2 x DFMA thread instructions of one launch (ncu counters) over its nodes,
+    # the nodes of empty sub-boxes included
     ops_per_node = 10.74
     line = {
         "metric": "table build: entries/s (FP64 Duffy radial, default orders)",
@@ -920,9 +975,9 @@ def table_main(args):
                    "l2": "node rules are kB; entries read once"},
         "tables": out,
         "roofline": {"bound": "fp64", "achieved": head["node_evals_per_s"] * ops_per_node / 1e9,
-                     "peak": fp64_nominal, "unit": "GFLOP/s",
-                     "frac": head["node_evals_per_s"] * ops_per_node / 1e9 / fp64_nominal,
-                     "traffic": None, "peak_source": "nominal (no measured FP64 peak)",
+                     "peak": fp64_peak, "unit": "GFLOP/s",
+                     "frac": head["node_evals_per_s"] * ops_per_node / 1e9 / fp64_peak,
+                     "traffic": None, "peak_source": "cuBLAS DGEMM measured in this run",
                      "fp64_flops_per_node_ncu": ops_per_node},
         "cpu_baseline": {"value": head["cpu_node_evals_per_s"] / head["nodes_per_entry"],
                          "unit": "entries/s", "cores": 1, "kind": "port",
@@ -955,7 +1010,7 @@ def csr_main(args):
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     out = {}
-    for name, tree in (("c2_adaptive_octree", W.config_c2().tree),
+    for name, tree in (("c2_adaptive_octree", W.config_c2(tables="synthetic").tree),
                        ("uniform_octree_l6", build_uniform_tree(3, 6, 2))):
         t0 = time.perf_counter()
         h = build_list1_traversal(tree)
@@ -1004,7 +1059,8 @@ def split_main(args):
     (2D uniform level 6, q = 5, 102,400 points, k = 20).  One step = one
     device sum (CUDA events); roofline: the FP64 pipe (per pair 4 flops per
     series term for the two real Horner sums of a real wave number, ~40 for
-    the log and the complex accumulation), nominal 1,250 GFLOP/s."""
+    the log and the complex accumulation) against the DGEMM rate measured in
+    the same run."""
     import torch
 
     from volumential_gb300 import workloads as W
@@ -1041,6 +1097,7 @@ def split_main(args):
     t = float(np.median(ms)) / 1e3
     pairs = w.pair_count()
     flops = pairs * (4 * n_terms + 40)
+    fp64_peak = measured_fp64_gflops()
     # CPU restatement on a sample of target boxes (closed form, numpy)
     from oracle import split_oracle as SO
     tr = w.traversal
@@ -1067,10 +1124,10 @@ def split_main(args):
         "config": {"workload": "split_c3_tree_2d_k20", "points": int(tree.ntargets),
                    "point_pairs": int(pairs), "series_terms": int(n_terms),
                    "l2": "flushed between steps (256 MiB write)"},
-        "roofline": {"bound": "fp64", "achieved": flops / t / 1e9, "peak": 1250.0,
-                     "unit": "GFLOP/s", "frac": flops / t / 1e9 / 1250.0,
+        "roofline": {"bound": "fp64", "achieved": flops / t / 1e9, "peak": fp64_peak,
+                     "unit": "GFLOP/s", "frac": flops / t / 1e9 / fp64_peak,
                      "kernel": "split_remainder_kernel", "traffic": None,
-                     "peak_note": "nominal FP64 (no measured peak)"},
+                     "peak_note": "cuBLAS DGEMM measured in this run"},
         "rel_l2_vs_cpu_closed_form": err,
         "cpu_baseline": {"value": sub_pairs / cpu_s, "unit": "pairs/s", "cores": 1,
                          "kind": "port", "sample": f"{len(sel)} target boxes, closed form "

@@ -367,6 +367,18 @@ int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *stream);
  * callers. */
 int32_t vl1_set_kernel_events(void *begin, void *end);
 
+/* Test hook (no reference counterpart): every wait of the tensor-core kernel
+ * on a pipeline barrier is bounded; a wait that runs out sets the launch's
+ * abort flag, the kernel lets its issued copies and MMAs complete, frees its
+ * TMEM, writes no results and reports VL1_E_TIMEOUT in the status word.
+ * poll_limit: polls (each up to 0.2 ms) before a wait gives up, 0 = the
+ * default (10,000, about 2 s).  withhold_arrival != 0: in the next launches,
+ * one producer warp of CTA (0, 0) does not signal its first pipeline unit,
+ * so that the issuer's wait on it runs out (a barrier that nothing
+ * completes; no fault).  Process-wide; vl1_test_set_wait_fault(0, 0) restores
+ * normal operation.  A schedule that timed out stays usable. */
+int32_t vl1_test_set_wait_fault(int32_t poll_limit, int32_t withhold_arrival);
+
 /* Size of the fixed scratch array used by vl1_eval_mixed_noalloc (32 MiB). */
 #define VL1_NOALLOC_SCRATCH_BYTES (32LL << 20)
 
@@ -381,9 +393,12 @@ int32_t vl1_set_kernel_events(void *begin, void *end);
  * than that (vl1_mixed_workspace_bytes) are rejected with VL1_E_ARG.  No
  * cudaMalloc, cudaFree or other allocating call is made.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race and must be serialised
- * by the caller.  The plan must belong to the current device. */
+ * device current, and a call looks it up again when the CUDA context current
+ * on the device is not the one of the last lookup (the address is bound to
+ * that context); make the first call in each context before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.  The plan must belong to the current
+ * device. */
 int32_t vl1_eval_mixed_noalloc(vl1_plan *plan, const vl1_tree_view *tree,
                                const vl1_mixed_schedule *schedule, const double *coefs,
                                int32_t nrhs, void *result, void *stream);

@@ -340,6 +340,52 @@ int vl1o_near_field(const vl1o_params *p, int n_tgt_boxes,
   return status;
 }
 
+/* Case id and table level of every list-1 pair (target box position tbox,
+ * list position k), computed with the expressions of the main loop above
+ * (list1.py:1084-1091 case encoding, :1086-1087 / :361-437 table level).
+ * case_ids[k] = -1 where the code falls outside the gallery. */
+int vl1o_classify_pairs(const vl1o_params *p, int n_tgt_boxes, const int32_t *target_boxes,
+                        const int32_t *nbr_starts, const int32_t *nbr_lists,
+                        int64_t aligned_nboxes, const double *box_centers,
+                        const uint8_t *box_levels, int32_t *case_ids,
+                        int32_t *table_levels) {
+  const int dim = p->dim;
+  int status = VL1O_OK;
+  for (int tbox = 0; tbox < n_tgt_boxes; ++tbox) {
+    const int target_box_id = target_boxes[tbox];
+    for (int k = nbr_starts[tbox]; k < nbr_starts[tbox + 1]; ++k) {
+      const int source_box_id = nbr_lists[k];
+      const int sbox_level = box_levels[source_box_id];
+      const double sbox_extent = p->root_extent * ipow2_inv(sbox_level);
+      int table_lev = 0;
+      if (p->table_level_per_level) {
+        int d = sbox_level - p->table_starting_level;
+        table_lev = sbox_level < p->table_starting_level
+                        ? 0
+                        : (d < p->n_tables ? d : p->n_tables - 1);
+      }
+      double vec = 0.0;
+      for (int d = 0; d < dim; ++d) {
+        double comp = (box_centers[d * aligned_nboxes + target_box_id] -
+                       box_centers[d * aligned_nboxes + source_box_id]) /
+                          sbox_extent * 4.0 +
+                      p->encoding_shift + p->case_encoding_bias;
+        vec = vec * (double)p->encoding_base + comp;
+      }
+      const int vec_id = (int)(vec + 0.5);
+      int case_id = -1;
+      if (vec_id >= 0 && vec_id < p->n_case_codes) case_id = (int)p->case_indices[vec_id];
+      if (case_id < 0 || case_id >= p->n_cases) {
+        case_id = -1;
+        status = VL1O_E_INVALID_CASE;
+      }
+      case_ids[k] = case_id;
+      table_levels[k] = table_lev;
+    }
+  }
+  return status;
+}
+
 /* Number of threads OpenMP would use (reported beside CPU timings). */
 int vl1o_max_threads(void) {
 #ifdef _OPENMP

@@ -73,6 +73,10 @@ def _load():
             C.c_void_p, C.c_int]
         lib.vl1o_full_map.restype = C.c_int
         lib.vl1o_full_map.argtypes = [C.POINTER(Params), C.c_void_p, C.c_void_p]
+        lib.vl1o_classify_pairs.restype = C.c_int
+        lib.vl1o_classify_pairs.argtypes = [
+            C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.vl1o_max_threads.restype = C.c_int
         _lib = lib
     return _lib
@@ -150,6 +154,24 @@ class OracleProblem:
         if st:
             raise RuntimeError(f"oracle full_map failed with status {st}")
         return rows, signs
+
+    def classify_pairs(self, *, target_boxes, neighbor_source_boxes_starts,
+                       neighbor_source_boxes_lists, box_centers, box_levels):
+        """(case ids, table levels) of every list-1 pair, in list order, with
+        the main loop's FP64 case encoding; case id -1 outside the gallery."""
+        lib = _load()
+        tb = _c(target_boxes, np.int32)
+        st_ = _c(neighbor_source_boxes_starts, np.int32)
+        ls = _c(neighbor_source_boxes_lists, np.int32)
+        bc = _c(box_centers, np.float64)
+        bl = _c(box_levels, np.uint8)
+        cases = np.empty(ls.size, dtype=np.int32)
+        levels = np.empty(ls.size, dtype=np.int32)
+        lib.vl1o_classify_pairs(C.byref(self.params), int(tb.size), tb.ctypes.data,
+                                st_.ctypes.data, ls.ctypes.data, int(bc.shape[1]),
+                                bc.ctypes.data, bl.ctypes.data, cases.ctypes.data,
+                                levels.ctypes.data)
+        return cases, levels
 
     def near_field(self, *, target_boxes, neighbor_source_boxes_starts,
                    neighbor_source_boxes_lists, box_centers, box_levels,

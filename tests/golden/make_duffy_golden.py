@@ -2,7 +2,7 @@
 
 Run where the reference source tree is mounted (read only):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_duffy_golden.py [/path/to/reference]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_duffy_golden.py /path/to/reference
 
 Imports by file path only numpy/scipy/mpmath modules of the reference:
 ``volumential/singular_integral_2d.py`` (the 1D rules
@@ -53,7 +53,9 @@ def green(kind, dim, k, *d):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the volumential source tree>")
+    ref = sys.argv[1]
     sq = load_ref(ref, "singular_integral_2d")
     lg = load_ref(ref, "lagrange")
     gal = load_ref(ref, "list1_gallery")

@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is mounted (read only):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [/path/to/reference]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/reference
 
 Only the reference modules that depend on numpy alone are imported (by file
 path, without importing the ``volumential`` package, whose ``__init__`` needs
@@ -358,7 +358,9 @@ def make_list1_case(name, gal, oa, *, dim, q, tree, n_tables, policy, complex_ta
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the volumential source tree>")
+    ref_root = sys.argv[1]
     gal = load_ref(ref_root, "list1_gallery")
     oa = load_ref(ref_root, "orbit_arithmetic")
 

@@ -2,7 +2,7 @@
 
 Run where the reference source tree is mounted (read only):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_table_cache_golden.py [/path/to/reference]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_table_cache_golden.py /path/to/reference
 
 ``volumential/table_manager.py`` imports sumpy and the ``volumential``
 package, which are absent here; this script executes the module from its
@@ -88,7 +88,9 @@ def seeded_table(dim, kernel_type, q, level, seed):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the volumential source tree>")
+    ref = sys.argv[1]
     tm = load_reference_table_manager(ref)
     from volumential_gb300.table_manager import NearFieldInteractionTableManager
 

@@ -48,5 +48,5 @@ def test_adaptive_trees(cuda, dim, tol, max_level):
 
 
 def test_c2_tree(cuda):
-    w = W.config_c2()
+    w = W.config_c2(tables="synthetic")
     _same(w.tree)

@@ -130,6 +130,25 @@ def test_policy_memo_follows_extra_kwargs():
     assert nf._policy_and_key()[1] == nf.get_cache_key()
 
 
+def test_policy_memo_keys_numpy_scalars_by_value_and_sees_in_place_changes():
+    import numpy as np
+
+    nf = NearFieldFromCSR(LaplaceKernel(3), SHAPES1)
+    nf.extra_kwargs["some_order"] = np.int64(3)
+    key = nf._policy_and_key()[1]
+    nf.extra_kwargs["some_order"] = np.int64(3)       # equal value, new object
+    assert nf._policy_and_key()[1] is key
+    nf.extra_kwargs["some_list"] = [1, 2]
+    snap = nf._policy_memo[0]
+    nf.extra_kwargs["some_list"].append(3)            # changed in place
+    nf._policy_and_key()
+    assert nf._policy_memo[0] != snap
+    obj = object()
+    nf.extra_kwargs["some_object"] = obj
+    nf._policy_and_key()
+    assert any(v is obj for v in nf._policy_memo[3])   # held: its id cannot be reused
+
+
 def test_laplace_2d_derivative_has_no_log_displacement():
     for knl in (AxisTargetDerivative(0, LaplaceKernel(2)),
                 AxisSourceDerivative(1, LaplaceKernel(2))):

@@ -15,8 +15,8 @@ import numpy as np
 
 from . import _build
 
-__all__ = ["lib", "PlanDesc", "TreeView", "MixedSchedule", "Status", "VL1Error", "check",
-           "STATUS_NAMES"]
+__all__ = ["lib", "PlanDesc", "TreeView", "MixedSchedule", "Status", "VL1Error",
+           "VL1TimeoutError", "check", "STATUS_NAMES"]
 
 VL1_OK = 0
 VL1_E_INVALID_CASE = 1
@@ -55,6 +55,11 @@ class VL1Error(RuntimeError):
     def __init__(self, code, message):
         super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
         self.code = code
+
+
+class VL1TimeoutError(VL1Error, TimeoutError):
+    """A bounded device wait gave up (``VL1_E_TIMEOUT``); the call wrote no
+    results and the device, the plan and the schedule stay usable."""
 
 
 class PlanDesc(C.Structure):
@@ -178,6 +183,7 @@ SIGNATURES = {
                                      C.POINTER(BatchOptions), C.POINTER(C.c_void_p)]),
     "vl1_batch_eval": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_set_kernel_events": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_test_set_wait_fault": (C.c_int32, [C.c_int32, C.c_int32]),
     "vl1_duffy_table": (C.c_int32, [C.POINTER(DuffyDesc), C.c_void_p, C.c_void_p]),
     "vl1_split_correction": (C.c_int32, [C.POINTER(SplitDesc), C.c_void_p]),
     "vl1_list1_csr_workspace_bytes": (C.c_int64, [C.c_int32]),

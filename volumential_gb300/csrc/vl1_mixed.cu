@@ -485,6 +485,12 @@ struct MixedParams {
   int64_t n_particles;
   double *result;
   vl1_status *st;
+  // bounded waits: polls before a wait gives up (0: kSleepPolls); test hook
+  // (vl1_test_set_wait_fault): when nonzero, producer warp 0 of CTA (0, 0)
+  // withholds its arrival for that CTA's first pipeline unit, so that the
+  // tensor-core issuer's wait runs out and the launch reports VL1_E_TIMEOUT
+  uint32_t poll_limit;
+  int32_t withhold_arrival;
 };
 
 // Warp roles of mixed_kernel (warp index w):
@@ -522,6 +528,9 @@ constexpr int kMmaWarp = 9;
 constexpr int kReadWarp0 = 10;
 constexpr uint32_t kSleepNs = 200000;      // longest sleep of one wait poll
 constexpr uint32_t kSleepPolls = 10000;    // polls before a wait gives up (~2 s)
+// split-tile counters: parts in the low 16 bits, aborted parts also in the
+// high bits (a tile has fewer than 2^16 parts)
+constexpr int kSplitPoison = 1 << 16;
 
 struct Barriers {
   uint64_t xfull[kStages];   // the producer warps' density planes are in the stage
@@ -529,15 +538,28 @@ struct Barriers {
   uint64_t empty[kStages];
   uint64_t accf[2];
   uint64_t acce[2];
+  uint64_t drain;            // after an abort: every issued MMA has completed
 };
 
+// Wait for `phase` of `bar`; gives up (returns false) when another role has
+// set the abort flag, or after `polls` polls (then it sets the flag itself).
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t phase,
-                                              volatile int *abort_flag) {
-  for (uint32_t i = 0; i < kSleepPolls; ++i) {
+                                              volatile int *abort_flag, uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i) {
     if (tc::mbar_try_wait_sleep(bar, phase, kSleepNs)) return true;
     if (*abort_flag) return false;
   }
   *abort_flag = 1;
+  return false;
+}
+
+// Wait for `phase` of `bar` regardless of the abort flag, at most `polls`
+// polls: used after an abort for operations already issued (bulk copies
+// into this CTA's shared memory, MMAs into its TMEM), which complete on
+// their own, before the CTA releases its TMEM and exits.
+__device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t phase, uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i)
+    if (tc::mbar_try_wait_sleep(bar, phase, kSleepNs)) return true;
   return false;
 }
 
@@ -556,6 +578,8 @@ struct BatchLaunch {
   const BatchItem *items;     // [n_items], launched in this order
   int n_items;
   int *queue;                 // next item to take; zero before the launch
+  uint32_t poll_limit;        // as MixedParams::poll_limit (persistent launches)
+  int32_t withhold_arrival;   // as MixedParams::withhold_arrival
 };
 
 // One group of MMAs: density digit i times the stacked table digits
@@ -606,8 +630,14 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
+  const uint32_t lim = MULTI ? bl.poll_limit : p1.poll_limit;
+  const uint32_t polls = lim ? lim : kSleepPolls;
+  // test hook: this CTA's producer warp 0 withholds its first arrival
+  const bool withhold = (MULTI ? bl.withhold_arrival : p1.withhold_arrival) != 0 &&
+                        blockIdx.x == 0 && blockIdx.y == 0;
 
   if (tid == 0) {
+    tc::mbar_init(&bars.drain, 1);
     for (int s = 0; s < kStages; ++s) {
       tc::mbar_init(&bars.xfull[s], kProducerWarps);   // one arrival per producer warp
       tc::mbar_init(&bars.afull[s], 1);                // the loader's expect_tx
@@ -674,7 +704,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     }
     if (item.split >= 0)
       bad = bad || item.split >= p.sched.n_splits || item.part < 0 ||
-            item.part >= item.nparts || item.slot - item.part < 0 ||
+            item.part >= item.nparts || item.nparts >= kSplitPoison ||
+            item.slot - item.part < 0 ||
             item.slot - item.part + item.nparts > p.sched.n_slots;
     else
       bad = bad || item.split != -1;
@@ -742,7 +773,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     auto expand = [&](int v) -> bool {
       const int s = (ubase + v) % kStages;
       const int use = (ubase + v) / kStages;
-      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) return false;
+      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, polls))
+        return false;
       const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
       const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
@@ -851,7 +883,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       }
       tc::fence_proxy_async_smem();   // generic writes -> tensor-core reads
       __syncwarp();
-      if (lane == 0) mbar_arrive(&bars.xfull[s]);
+      if (lane == 0 && !(withhold && warp == 0 && ubase + v == 0)) mbar_arrive(&bars.xfull[s]);
       return true;
     };
     int u = 0;
@@ -930,7 +962,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
           const int s = (ubase + u) % kStages;
           const int use = (ubase + u) / kStages;
-          if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort)) {
+          if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, polls)) {
             aborted = true;
             break;
           }
@@ -949,6 +981,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
           }
         }
       }
+      if (aborted || s_abort) {
+        // copies of the last (up to kStages) issued units may still be in
+        // flight into this CTA's stages: let them land before the CTA exits
+        for (int v = u - kStages < 0 ? 0 : u - kStages; v < u; ++v)
+          wait_bounded(&bars.afull[(ubase + v) % kStages], ((ubase + v) / kStages) & 1, polls);
+      }
     }
     __syncwarp();
   } else if (warp == kMmaWarp) {
@@ -960,7 +998,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       for (int round = 0; round < n_rounds && !aborted; ++round) {
         const int R = rbase + round;
         const int b = R & 1;
-        if (R >= 2 && !wait_or_abort(&bars.acce[b], ((R >> 1) - 1) & 1, &s_abort)) {
+        if (R >= 2 && !wait_or_abort(&bars.acce[b], ((R >> 1) - 1) & 1, &s_abort, polls)) {
           aborted = true;
           break;
         }
@@ -969,11 +1007,11 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         for (int iu = 0; iu < upr; ++iu, ++u) {
           const int s = (ubase + u) % kStages;
           const uint32_t ph = ((ubase + u) / kStages) & 1;
-          if (!wait_or_abort(&bars.afull[s], ph, &s_abort)) {
+          if (!wait_or_abort(&bars.afull[s], ph, &s_abort, polls)) {
             aborted = true;
             break;
           }
-          if (!wait_or_abort(&bars.xfull[s], ph, &s_abort)) {
+          if (!wait_or_abort(&bars.xfull[s], ph, &s_abort, polls)) {
             aborted = true;
             break;
           }
@@ -1003,6 +1041,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         }
         if (!aborted) tc::mma_commit(&bars.accf[b]);
       }
+      if (aborted || s_abort) {
+        // MMAs issued before the abort still write TMEM and read the stages:
+        // wait for all of them before the TMEM is released
+        tc::mma_commit(&bars.drain);
+        wait_bounded(&bars.drain, 0, polls);
+      }
     }
     __syncwarp();
   } else {
@@ -1020,7 +1064,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     for (int round = 0; round < n_rounds; ++round) {
       const int R = rbase + round;
       const int b = R & 1;
-      if (!wait_or_abort(&bars.accf[b], (R >> 1) & 1, &s_abort)) {
+      if (!wait_or_abort(&bars.accf[b], (R >> 1) & 1, &s_abort, polls)) {
         ok = false;
         break;
       }
@@ -1077,7 +1121,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   // integer operations (the FP64 pipe is narrow on this GPU).
   tc::tc_fence_before();
   __syncthreads();
-  __shared__ int s_last;
+  __shared__ int s_last, s_poison;
   __shared__ long long s_obase[128];   // result index of the row's first target point
   __shared__ int s_ocnt[128];          // target points of the row's box (0: empty row)
   __shared__ int s_oexp[128];          // an output is (parked sum) * 2^s_oexp
@@ -1116,11 +1160,17 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     __threadfence();
     __syncthreads();
     if (tid == 0) {
-      const int done = atomicAdd(p.sched.split_counters + item.split * n_chunks + chunk, 1);
-      s_last = done == item.nparts - 1;
+      // parts count in the low 16 bits; a part that aborted (and stored no
+      // partial sums) also adds to the high bits, so that the last part
+      // writes nothing for the tile
+      const int inc = s_abort ? kSplitPoison + 1 : 1;
+      const int done =
+          atomicAdd(p.sched.split_counters + item.split * n_chunks + chunk, inc) + inc;
+      s_last = (done & (kSplitPoison - 1)) == item.nparts;
+      s_poison = done >= kSplitPoison;
     }
     __syncthreads();
-    write = write && s_last;
+    write = write && s_last && !s_poison;
     if (write) __threadfence();
   } else {
     __syncthreads();
@@ -1167,11 +1217,29 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
           p.result[o] = y;
       }
     }
-    // the last part leaves the counter at zero for the next call
-    if (item.split >= 0 && tid == 0) p.sched.split_counters[item.split * n_chunks + chunk] = 0;
   }
+  // the last part leaves the counter at zero for the next call (also after
+  // an abort, so that a timed-out call does not spoil the schedule)
+  if (item.split >= 0 && tid == 0 && s_last)
+    p.sched.split_counters[item.split * n_chunks + chunk] = 0;
   __syncthreads();
-  if (s_abort && tid == 0) report(p.st, VL1_E_TIMEOUT, tile, chunk);
+  if (s_abort && tid == 0) {
+    report(p.st, VL1_E_TIMEOUT, tile, chunk);
+    if (MULTI) {
+      // the items this launch will no longer run still count their parts,
+      // so that every split counter ends at zero
+      for (;;) {
+        const int wj = atomicAdd(bl.queue, 1);
+        if (wj >= bl.n_items) break;
+        const BatchItem bj = bl.items[wj];
+        if (bj.item.split < 0) continue;
+        const MixedParams *pj = bl.probs + bj.problem;
+        int *ctr = pj->sched.split_counters + bj.item.split * (pj->g.np / NCH) + bj.chunk;
+        const int done = atomicAdd(ctr, kSplitPoison + 1) + kSplitPoison + 1;
+        if ((done & (kSplitPoison - 1)) == bj.item.nparts) *ctr = 0;
+      }
+    }
+  }
   ubase += n_rounds * upr;
   rbase += n_rounds;
   __syncthreads();
@@ -1281,6 +1349,11 @@ int32_t launch_classify(vl1_plan *plan, const TreeDev &tree, int32_t *keys, cuda
 // stream right before and after the tensor-core kernel launches.
 cudaEvent_t g_kernel_begin = nullptr, g_kernel_end = nullptr;
 
+// Test hook (vl1_test_set_wait_fault): poll limit of the kernel's bounded
+// waits (0: the default) and the withheld arrival of CTA (0, 0).
+uint32_t g_test_poll_limit = 0;
+int32_t g_test_withhold = 0;
+
 int32_t record_kernel_event(cudaEvent_t ev, cudaStream_t s) {
   if (!ev) return VL1_OK;
   cudaError_t e = cudaEventRecord(ev, s);
@@ -1354,6 +1427,8 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.n_particles = tree.n_particles;
   mp.result = result;
   mp.st = plan->status;
+  mp.poll_limit = g_test_poll_limit;
+  mp.withhold_arrival = g_test_withhold;
   if (!mixed_kernel_ptr(g.nch, g.kc, false)) {
     set_error("mixed path: unsupported column chunk %d / K chunk %d", g.nch, g.kc);
     return VL1_E_UNSUPPORTED;
@@ -1532,7 +1607,7 @@ int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t
     for (const vl1_mixed_item &it : items[i]) {
       if (it.tile < 0 || it.tile >= sc.n_tiles || it.key_begin < 0 ||
           it.key_end < it.key_begin || it.nparts < 1 || it.part < 0 ||
-          it.part >= it.nparts || it.split >= sc.n_splits ||
+          it.part >= it.nparts || it.nparts >= kSplitPoison || it.split >= sc.n_splits ||
           (it.split >= 0 && (it.slot < it.part || it.slot >= sc.n_slots))) {
         set_error("%s: problem %d has an invalid work item", who, i);
         return VL1_E_ARG;
@@ -1847,7 +1922,10 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
   if (st) return st;
   for (const SoloLaunch &sl : b->solos) {
     const BatchLaunch none{};
-    void *args[] = {const_cast<MixedParams *>(&sl.mp), const_cast<BatchLaunch *>(&none)};
+    MixedParams mp = sl.mp;
+    mp.poll_limit = g_test_poll_limit;
+    mp.withhold_arrival = g_test_withhold;
+    void *args[] = {&mp, const_cast<BatchLaunch *>(&none)};
     e = cudaLaunchKernel(mixed_kernel_ptr(sl.nch, sl.kc, false), dim3(sl.grid_x, sl.grid_y),
                          dim3(mixed_threads(sl.nch)), args, mixed_smem_bytes(sl.nch, sl.kc), s);
     if (e != cudaSuccess) return cuda_fail(e, "batch mixed_kernel launch (one problem)");
@@ -1859,6 +1937,8 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
     bl.items = static_cast<const BatchItem *>(b->d_items) + g.item0;
     bl.n_items = g.n_items;
     bl.queue = b->d_queue + gi;
+    bl.poll_limit = g_test_poll_limit;
+    bl.withhold_arrival = g_test_withhold;
     void *args[] = {const_cast<MixedParams *>(&unused), &bl};
     e = cudaLaunchKernel(mixed_kernel_ptr(g.nch, g.kc, true), dim3(g.grid),
                          dim3(mixed_threads(g.nch)), args, mixed_smem_bytes(g.nch, g.kc), s);
@@ -1880,6 +1960,16 @@ extern "C" int32_t vl1_batch_destroy(vl1_batch *b) {
 }
 
 extern "C" int64_t vl1_batch_device_bytes(const vl1_batch *b) { return b ? b->bytes : -1; }
+
+extern "C" int32_t vl1_test_set_wait_fault(int32_t poll_limit, int32_t withhold_arrival) {
+  if (poll_limit < 0) {
+    set_error("vl1_test_set_wait_fault: negative poll limit");
+    return VL1_E_ARG;
+  }
+  vl1::g_test_poll_limit = (uint32_t)poll_limit;
+  vl1::g_test_withhold = withhold_arrival != 0;
+  return VL1_OK;
+}
 
 extern "C" int32_t vl1_set_kernel_events(void *begin, void *end) {
   vl1::g_kernel_begin = static_cast<cudaEvent_t>(begin);

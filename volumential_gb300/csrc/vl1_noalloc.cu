@@ -13,12 +13,18 @@
 //
 // The array is a file-scope __device__ object of VL1_NOALLOC_SCRATCH_BYTES
 // bytes: every GPU on which the library's module is loaded holds it until the
-// process exits.  Its device address is looked up once per device, with that
-// device current, on the first call made on that device; that first call
-// should therefore come before any stream capture.  All calls share the one
-// array: calls whose work overlaps on the GPU (different streams, or
-// different host threads) race on it and must be serialised by the caller.
-// Each call re-initialises every scratch value it reads.
+// process exits.  Its device address is looked up on the first call made on a
+// device (with that device current), and again whenever the CUDA context
+// current on that device has changed since (a context the caller created
+// with the driver API, or the primary context re-created after
+// cudaDeviceReset): the address belongs to the context in which it was looked
+// up.  A first call in a context should therefore come before any stream
+// capture.  All calls share the one array: calls whose work overlaps on the
+// GPU (different streams, or different host threads) race on it and must be
+// serialised by the caller.  Each call re-initialises every scratch value it
+// reads.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "vl1_internal.cuh"
@@ -33,19 +39,42 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 std::mutex g_noalloc_mutex;
 void *g_noalloc_addr[kMaxDevices] = {};
+CUcontext g_noalloc_ctx[kMaxDevices] = {};
 
-// Device address of the scratch array on `dev` (the current device).
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+
+// The driver's cuCtxGetCurrent, found through the runtime (the library does
+// not link the driver library itself); nullptr when unavailable.
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
+// Device address of the scratch array on `dev` (the current device) in the
+// current context.
 int32_t noalloc_scratch_address(int dev, void **out) {
   if (dev < 0 || dev >= kMaxDevices) {
     set_error("device ordinal %d outside the supported range", dev);
     return VL1_E_ARG;
   }
+  CUcontext ctx = nullptr;
+  CtxGetCurrentFn get = ctx_get_current();
+  if (get && get(&ctx) != CUDA_SUCCESS) ctx = nullptr;
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[dev]) {
+  if (!g_noalloc_addr[dev] || !get || ctx != g_noalloc_ctx[dev]) {
     void *ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
     g_noalloc_addr[dev] = ptr;
+    g_noalloc_ctx[dev] = ctx;
   }
   *out = g_noalloc_addr[dev];
   return VL1_OK;

@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import logging
 import math
+import numbers
 import re
 from dataclasses import dataclass
 
@@ -37,6 +38,21 @@ import numpy as np
 
 from . import _lib
 from .kernels import base_kernel, kernel_class_name
+
+
+def _is_scalar(v):
+    return isinstance(v, (str, bytes, numbers.Number, np.generic, type(None)))
+
+
+def _memo_token(v):
+    """Key of one extra keyword argument in the policy memo."""
+    if isinstance(v, np.generic):
+        return (type(v).__name__, v.item())
+    if _is_scalar(v):
+        return v
+    if isinstance(v, (list, tuple, dict)):
+        return (type(v).__name__, repr(v))
+    return (type(v).__name__, id(v))
 
 logger = logging.getLogger(__name__)
 
@@ -475,14 +491,17 @@ class NearFieldFromCSR(NearFieldEvalBase):
     def _policy_and_key(self):
         """(parsed policy, cache key), recomputed only when ``extra_kwargs``
         changes (both derive from the kernel, fixed at construction, and the
-        extra keyword arguments)."""
-        snap = tuple(sorted(
-            (k, v if isinstance(v, (str, int, float, bool, complex, type(None)))
-             else (type(v).__name__, id(v)))
-            for k, v in self.extra_kwargs.items()))
+        extra keyword arguments).  Scalars (numpy scalars included) enter the
+        memo key by value, lists, tuples and dicts by their ``repr`` (so that
+        changes made in place are seen), other objects by identity; the memo
+        holds those objects, so that an identity cannot be reused while the
+        memo stands."""
+        snap = tuple(sorted((k, _memo_token(v)) for k, v in self.extra_kwargs.items()))
         memo = getattr(self, "_policy_memo", None)
         if memo is None or memo[0] != snap:
-            memo = (snap, parse_policy(self.get_kernel_scaling_policy()), self.get_cache_key())
+            held = [v for v in self.extra_kwargs.values() if not _is_scalar(v)]
+            memo = (snap, parse_policy(self.get_kernel_scaling_policy()), self.get_cache_key(),
+                    held)
             self._policy_memo = memo
         return memo[1], memo[2]
 

@@ -346,6 +346,11 @@ class Plan:
                 f"list1 case encoding produced {s.count} codes outside the interaction "
                 f"gallery (first at target box {s.detail0}, list position {s.detail1}); "
                 "the tree is not 2:1 balanced or box centres are inconsistent")
+        if s.code == _lib.VL1_E_TIMEOUT:
+            raise _lib.VL1TimeoutError(
+                s.code, f"a bounded device wait gave up in {s.count} work items (first: "
+                        f"tile {s.detail0}, column chunk {s.detail1}); no results were "
+                        "written")
         raise _lib.VL1Error(s.code, f"device status: {s.count} faults, first detail "
                                     f"({s.detail0}, {s.detail1})")
 

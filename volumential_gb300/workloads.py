@@ -7,11 +7,16 @@ of Gaussians ``a * exp(-|x - c|^2 / w^2)`` with seeded centres, log-uniform
 widths and N(0, 1) amplitudes).  This module builds them with
 ``numpy.random.default_rng(seed)``.
 
-Table values: the list-1 evaluation is linear in the table, so parity and
-throughput do not depend on the values.  ``synthetic_tables`` fills the compact
-(orbit-reduced) layout with seeded values of the magnitude of a Laplace table;
-``kernel_tables`` uses the FP64 GPU table builder when one is available for
-the kernel.
+Table values.  ``duffy_tables`` builds the tables the configurations name
+(Laplace, Helmholtz) with the package's FP64 GPU Duffy builder at the
+reference's default orders (regular 20, radial 61, tanh-sinh-fast;
+``nearfield_potential_table.py:2948-2953``); C1, C2 and C3 use them by default.
+``synthetic_tables`` fills the compact (orbit-reduced) layout with seeded
+N(0, 0.1) values instead: it needs no GPU and serves the host-side tests and
+the parity tests of the index arithmetic, which do not depend on the values.
+The mixed-precision path's error does depend on them (each table value is
+held to 2^-40 of the table's largest one), which is why the headline
+configurations run on the physical tables.
 """
 
 from __future__ import annotations
@@ -29,7 +34,8 @@ from .tree_build import (
     build_uniform_tree,
 )
 
-__all__ = ["GaussianMixture", "random_gaussian_mixture", "synthetic_tables",
+__all__ = ["GaussianMixture", "random_gaussian_mixture", "synthetic_tables", "duffy_tables",
+           "make_tables",
            "Workload", "config_c1", "config_c2", "config_c3", "uniform_workload",
            "adaptive_workload", "config_c4", "config_c5", "C5Problem", "poisson_arrivals"]
 
@@ -98,6 +104,53 @@ def synthetic_tables(dim, q, kernel, *, n_tables=1, seed=0, source_box_extent=1.
     return out
 
 
+#: (dim, q, kernel name, k, n_tables, extent, orders) -> built tables; a table
+#: set is built once per process (the 3D q = 5 Laplace table takes ~2 s)
+_DUFFY_CACHE: dict = {}
+
+
+def duffy_tables(dim, q, kernel, *, n_tables=1, source_box_extent=1.0, k=None,
+                 complex_values=False, regular_quad_order=20, radial_quad_order=61):
+    """Tables of ``kernel`` with values from the FP64 GPU Duffy builder.
+
+    Level ``l`` has source box extent ``source_box_extent / 2**l``; Helmholtz
+    needs the wave number ``k``.  Orders default to the reference's
+    (``nearfield_potential_table.py:2948-2953``).  Needs a CUDA device."""
+    kname = type(kernel).__name__
+    key = (dim, q, kname, None if k is None else float(k), n_tables,
+           float(source_box_extent), complex_values, regular_quad_order, radial_quad_order)
+    hit = _DUFFY_CACHE.get(key)
+    if hit is not None:
+        return list(hit)
+    out = []
+    for lev in range(n_tables):
+        t = NearFieldInteractionTable(
+            q, dim=dim, sumpy_kernel=kernel,
+            source_box_extent=source_box_extent * 0.5 ** lev,
+            dtype=np.complex128 if complex_values else np.float64)
+        kw = {} if k is None else {"k": float(k)}
+        t.build_table_via_duffy_radial(regular_quad_order=regular_quad_order,
+                                       radial_quad_order=radial_quad_order, **kw)
+        out.append(t)
+    _DUFFY_CACHE[key] = tuple(out)
+    return out
+
+
+def make_tables(source, dim, q, kernel, *, n_tables=1, seed=0, source_box_extent=1.0,
+                complex_values=False, k=None, orders=None):
+    """``source`` "duffy" (physical values, GPU builder) or "synthetic"
+    (seeded values, no GPU)."""
+    if source == "duffy":
+        return duffy_tables(dim, q, kernel, n_tables=n_tables,
+                            source_box_extent=source_box_extent, k=k,
+                            complex_values=complex_values, **(orders or {}))
+    if source == "synthetic":
+        return synthetic_tables(dim, q, kernel, n_tables=n_tables, seed=seed,
+                                source_box_extent=source_box_extent,
+                                complex_values=complex_values)
+    raise ValueError(f"table source must be 'duffy' or 'synthetic', got {source!r}")
+
+
 @dataclass
 class Workload:
     name: str
@@ -137,7 +190,9 @@ def _densities(rng, tree, nrhs, n_terms, width_range):
     for _ in range(nrhs):
         k = int(rng.integers(n_terms[0], n_terms[1] + 1)) if isinstance(n_terms, tuple) \
             else int(n_terms)
-        mix = random_gaussian_mixture(rng, tree.dim, k, width_range)
+        lo = float(np.min(tree.root_vertex))
+        mix = random_gaussian_mixture(rng, tree.dim, k, width_range, a=lo,
+                                      b=lo + float(tree.root_extent))
         mixes.append(mix)
         cols.append(mix(tree.targets))
     return np.stack(cols), mixes
@@ -145,22 +200,25 @@ def _densities(rng, tree, nrhs, n_terms, width_range):
 
 def uniform_workload(name, dim, level, q, *, kernel=None, nrhs=1, seed=0,
                      n_terms=8, width_range=(0.02, 0.1), n_tables=1,
-                     complex_table=False):
+                     complex_table=False, tables="synthetic", k=None, orders=None,
+                     a=-0.5, b=0.5):
+    """Uniform tree of ``level`` on [a, b]^dim; ``tables`` "synthetic" or
+    "duffy" (canonical tables at the root extent, ``n_tables`` levels)."""
     rng = np.random.default_rng(seed)
-    tree = build_uniform_tree(dim, level, q)
+    tree = build_uniform_tree(dim, level, q, a=a, b=b)
     trav = build_list1_traversal(tree)
     kernel = kernel or LaplaceKernel(dim)
     coefs, mixes = _densities(rng, tree, nrhs, n_terms, width_range)
-    tables = synthetic_tables(dim, q, kernel, n_tables=n_tables, seed=seed + 17,
-                              source_box_extent=tree.root_extent,
-                              complex_values=complex_table)
-    return Workload(name, dim, q, kernel, trav, tables, coefs, seed,
-                    meta={"level": level, "mixtures": mixes})
+    tabs = make_tables(tables, dim, q, kernel, n_tables=n_tables, seed=seed + 17,
+                       source_box_extent=tree.root_extent, complex_values=complex_table,
+                       k=k, orders=orders)
+    return Workload(name, dim, q, kernel, trav, tabs, coefs, seed,
+                    meta={"level": level, "mixtures": mixes, "tables": tables})
 
 
 def adaptive_workload(name, dim, q, *, tol, max_level, min_level=2, kernel=None,
                       nrhs=1, seed=0, n_terms=16, width_range=(0.01, 0.08),
-                      max_leaves=None):
+                      max_leaves=None, tables="synthetic", orders=None):
     """Adaptive tree refined where the density's variation over a leaf's
     nodes (max - min) exceeds ``tol``, then 2:1 balanced."""
     rng = np.random.default_rng(seed)
@@ -178,40 +236,47 @@ def adaptive_workload(name, dim, q, *, tol, max_level, min_level=2, kernel=None,
     for _ in range(nrhs - 1):
         m = random_gaussian_mixture(rng, dim, n_terms, width_range)
         cols.append(m(tree.targets))
-    tables = synthetic_tables(dim, q, kernel, seed=seed + 17,
-                              source_box_extent=tree.root_extent)
-    return Workload(name, dim, q, kernel, trav, tables, np.stack(cols), seed,
-                    meta={"tol": tol, "max_level": max_level, "mixture": mix})
+    tabs = make_tables(tables, dim, q, kernel, seed=seed + 17,
+                       source_box_extent=tree.root_extent, orders=orders)
+    return Workload(name, dim, q, kernel, trav, tabs, np.stack(cols), seed,
+                    meta={"tol": tol, "max_level": max_level, "mixture": mix,
+                          "tables": tables})
 
 
-def config_c1(seed=1000):
-    """2D Laplace, uniform level 5, q=4 (1024 leaves, 16,384 points), 1 RHS."""
+def config_c1(seed=1000, tables="duffy"):
+    """2D Laplace, uniform level 5, q=4 (1024 leaves, 16,384 points), 1 RHS;
+    canonical 2D Laplace table (level 0, root extent) built by Duffy
+    quadrature in FP64, inferred scaling and the log displacement."""
     return uniform_workload("c1_lap2d_uniform_l5_q4", 2, 5, 4, seed=seed, n_terms=8,
-                            width_range=(0.02, 0.1))
+                            width_range=(0.02, 0.1), tables=tables)
 
 
-def config_c2(seed=2006, tol=1e-3, max_level=6):
+def config_c2(seed=2006, tol=1e-3, max_level=6, tables="duffy"):
     """3D Laplace, adaptive 2:1-balanced octree, q=4, 16 Gaussians (w in
     [0.01, 0.08]), refined where the leaf variation (max - min of the density
     at the leaf's 64 nodes) exceeds ``tol``, leaves on levels 3..6.  With the
     default seed: 23,087 leaves, 1,477,568 points, 565,335 list-1 box pairs,
-    2.32e9 point pairs."""
+    2.32e9 point pairs.  Canonical 3D Laplace table (FP64 Duffy build),
+    scaling h_s^2 / h_0^2."""
     return adaptive_workload("c2_lap3d_adaptive_q4", 3, 4, tol=tol, max_level=max_level,
-                             seed=seed, n_terms=16, width_range=(0.01, 0.08))
+                             seed=seed, n_terms=16, width_range=(0.01, 0.08),
+                             tables=tables)
 
 
-def config_c3(seed=3000, nrhs=256, k=20.0):
-    """2D Helmholtz (k=20, fixed single complex table at level 6), uniform
-    level 6, q=5 (102,400 points), ``nrhs`` Gaussian-sum densities."""
-    w = uniform_workload("c3_helm2d_uniform_l6_q5", 2, 6, 5, seed=seed, nrhs=nrhs,
-                         n_terms=8, width_range=(0.02, 0.1),
+def config_c3(seed=3000, nrhs=256, k=20.0, tables="duffy", level=6):
+    """2D Helmholtz (k=20, fixed single complex table at the tree's level),
+    uniform level 6, q=5 (102,400 points), ``nrhs`` Gaussian-sum densities.
+    The table is the Helmholtz kernel's, built by Duffy quadrature in FP64 at
+    source box extent root / 2^level (``fixed_single_table``,
+    list1.py:406-420)."""
+    w = uniform_workload(f"c3_helm2d_uniform_l{level}_q5", 2, level, 5, seed=seed,
+                         nrhs=nrhs, n_terms=8, width_range=(0.02, 0.1),
                          kernel=HelmholtzKernel(2), complex_table=True)
-    # fixed single table built at the active source level (root extent / 64)
-    t = synthetic_tables(2, 5, w.kernel, seed=seed + 17,
-                         source_box_extent=w.tree.root_extent / 64.0,
-                         complex_values=True)
-    w.tables = t
+    w.tables = make_tables(tables, 2, 5, w.kernel, seed=seed + 17,
+                           source_box_extent=w.tree.root_extent / 2.0 ** level,
+                           complex_values=True, k=k)
     w.meta["k"] = k
+    w.meta["tables"] = tables
     return w
 
 
