@@ -190,6 +190,37 @@ int32_t vl1_eval_fp64(vl1_plan *plan, const vl1_tree_view *tree,
 int32_t vl1_classify_pairs(vl1_plan *plan, const vl1_tree_view *tree, int32_t *keys,
                            void *stream);
 
+/* Schedule of the mixed path built on the device (no reference counterpart:
+ * the reference recomputes every pair's case in its kernel and has no
+ * schedule; this replaces the host pass a first call on a new tree would
+ * otherwise wait for).  begin: classifies every list-1 pair with the
+ * reference's case encoding (list1.py:439-459, 1084-1091), checks that each
+ * box's source mode ids are distinct and in range, orders the target boxes by
+ * key signature (rarest keys most significant; a stable radix sort) and sizes
+ * the tiles of 128 rows, longest first; it synchronises the stream twice and
+ * allocates its own scratch.  nnz: the length of neighbor_source_boxes_lists.
+ * key_start: copies the tile key starts [n_tiles + 1] to host memory.
+ * fill: writes the arrays of vl1_mixed_schedule into caller-owned device
+ * memory: tile_rows [n_tiles * 128], tile_key_start [n_tiles + 1], key_ids
+ * [n_entries], key_xrow [n_entries * 128] (16-byte aligned).  Errors: a pair
+ * whose case is outside the gallery (VL1_E_INVALID_CASE), two source boxes of
+ * one target box with the same key (VL1_E_ARG), a source mode id out of range
+ * or repeated in a box (VL1_E_LAYOUT). */
+typedef struct vl1_schedule_builder vl1_schedule_builder;
+typedef struct {
+  int32_t n_tiles;
+  int64_t n_entries;
+} vl1_schedule_sizes;
+int32_t vl1_schedule_build_begin(vl1_plan *plan, const vl1_tree_view *tree, int64_t nnz,
+                                 int32_t nrhs, vl1_schedule_builder **out,
+                                 vl1_schedule_sizes *sizes, void *stream);
+int32_t vl1_schedule_build_key_start(const vl1_schedule_builder *builder,
+                                     int32_t *key_start_host);
+int32_t vl1_schedule_build_fill(vl1_schedule_builder *builder, int32_t *tile_rows,
+                                int32_t *tile_key_start, int32_t *key_ids, int32_t *key_xrow,
+                                void *stream);
+int32_t vl1_schedule_builder_destroy(vl1_schedule_builder *builder);
+
 /* Bytes of caller-provided device workspace vl1_eval_mixed needs. */
 int64_t vl1_mixed_workspace_bytes(const vl1_plan *plan, const vl1_tree_view *tree,
                                   int32_t nrhs);
@@ -200,12 +231,12 @@ int32_t vl1_mixed_geometry(const vl1_plan *plan, int32_t *out5);
 
 /* Mixed-precision list-1 evaluation on the tensor cores: the same sum as
  * vl1_eval_fp64 (list1.py:1050-1159) computed from exact FP16 digit products:
- * table values as 5 signed base-256 digits of a 40-bit fixed-point form,
+ * table values as 5 balanced base-256 digits of a 39-bit fixed-point form,
  * scaled densities as 39-bit fixed point against each density row's own
  * power-of-two scale (requantised to each target row's reference scale),
  * exact FP32 partial sums of digit products, exact int64 sums and one
  * rounding to FP64; the relative error is ~2^-35 of an output's largest
- * contribution (measured 4e-11 .. 3e-10 relative l2).
+ * contribution.
  * coefs: real [nrhs][n_particles] float64; result as in vl1_eval_fp64.
  * workspace: caller-provided device memory of vl1_mixed_workspace_bytes. */
 int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,

@@ -46,10 +46,11 @@ def _eval(lib, plan, view, sched, coefs, out, nrhs, stream):
 @pytest.mark.parametrize("cap", [None, 3])   # 3: tiles split over several CTAs
 def test_timeout_is_reported_and_the_next_call_is_correct(cuda, cap):
     torch = cuda
-    w = W.uniform_workload("timeout", 3, 2, 4, seed=71, nrhs=2)
+    w = W.uniform_workload("timeout", 3, 3, 4, seed=71, nrhs=2)   # 8 tiles
     plan, view, keep = plan_and_view(w)
     stream = torch.cuda.current_stream().cuda_stream
     sched = get_schedule(plan, view, keep, w.nrhs, stream, max_keys_per_item=cap)
+    assert sched.n_tiles > 1
     if cap is not None:
         assert sched.n_splits > 0
     coefs = as_device_tensor(np.ascontiguousarray(w.coefs))
@@ -79,8 +80,8 @@ def test_timeout_is_reported_and_the_next_call_is_correct(cuda, cap):
 
 def test_timeout_in_a_persistent_batch_launch(cuda):
     torch = cuda
-    ws = [W.uniform_workload("tb2", 2, 3, 4, seed=72, nrhs=2),
-          W.uniform_workload("tb3", 3, 2, 3, seed=73, nrhs=1)]
+    ws = [W.uniform_workload("tb2", 2, 4, 4, seed=72, nrhs=2),
+          W.uniform_workload("tb3", 3, 3, 3, seed=73, nrhs=1)]
     probs = []
     for w in ws:
         plan, view, keep = problem_arrays(w)

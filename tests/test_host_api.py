@@ -432,13 +432,50 @@ def test_mixed_work_items_cover_every_key_once():
             assert [s for _, s, _ in ps] == list(range(base, base + len(ps)))
 
 
+def _pack_rows_by_loop(mask, rows_per_tile):
+    """Plain-Python restatement of the greedy tile packing (test only)."""
+    sigs = {}
+    for b in range(mask.shape[0]):
+        sigs.setdefault(tuple(np.flatnonzero(mask[b])), []).append(b)
+    # signature order of np.unique over the packed little-endian words
+    def word_key(sig):
+        words = [0] * (-(-mask.shape[1] // 64))
+        for k in map(int, sig):
+            words[k // 64] |= 1 << (k % 64)
+        return tuple(words)
+    order_sigs = sorted(sigs, key=word_key)
+    groups = [list(sigs[g]) for g in order_sigs]
+    keysets = [set(g) for g in order_sigs]
+    out = []
+    while any(groups):
+        tile, space = set(), rows_per_tile
+        s_ = max(range(len(groups)), key=lambda i: (len(groups[i]), -i))
+        while True:
+            take = min(space, len(groups[s_]))
+            out += groups[s_][:take]
+            groups[s_] = groups[s_][take:]
+            space -= take
+            tile |= keysets[s_]
+            if space == 0 or not any(groups):
+                break
+            best = None
+            for i, g in enumerate(groups):
+                if not g:
+                    continue
+                score = len(keysets[i] - tile) / max(min(len(g), space), 1)
+                cand = (score, -len(g), i)
+                if best is None or cand < best:
+                    best = cand
+            s_ = best[2]
+    return np.array(out)
+
+
 def _tile_schedule_by_loop(keys, starts, lists, n_tb, K, nrhs):
     """Straightforward per-tile restatement of the tile schedule (test only)."""
     tb_of_pair = np.repeat(np.arange(n_tb), np.diff(starts))
     mask = np.zeros((n_tb, K), dtype=bool)
     mask[tb_of_pair, keys] = True
-    _, sig = np.unique(np.packbits(mask, axis=1), axis=0, return_inverse=True)
-    order = np.lexsort((np.arange(n_tb), sig.ravel()))
+    order = _pack_rows_by_loop(mask, max(1, 128 // nrhs))
     rows = (order[:, None] * nrhs + np.arange(nrhs)[None, :]).ravel()
     n_tiles = (len(rows) + 127) // 128
     tile_rows = np.full(n_tiles * 128, -1)
@@ -464,6 +501,27 @@ def _tile_schedule_by_loop(keys, starts, lists, n_tb, K, nrhs):
         xrow += tiles[t][1]
         key_start.append(len(key_ids))
     return tile_rows[lpt], np.array(key_start), np.array(key_ids), np.array(xrow).reshape(-1, 128)
+
+
+@pytest.mark.parametrize("K", [40, 139, 300])
+def test_pack_rows_matches_the_greedy_restatement_and_packs_tighter(K):
+    from volumential_gb300.batched import MixedSchedule
+
+    rng = np.random.default_rng(K)
+    n_tb = 700
+    # boxes drawn from a few dozen signatures, as on a tree
+    protos = [rng.choice(K, size=rng.integers(3, 12), replace=False) for _ in range(40)]
+    mask = np.zeros((n_tb, K), dtype=bool)
+    for b in range(n_tb):
+        mask[b, protos[rng.integers(len(protos))]] = True
+    got = MixedSchedule.pack_rows(mask, 128)
+    assert np.array_equal(np.sort(got), np.arange(n_tb))
+    assert np.array_equal(got, _pack_rows_by_loop(mask, 128))
+
+    def tile_keys(order):
+        return sum(mask[order[i:i + 128]].any(axis=0).sum() for i in range(0, n_tb, 128))
+    _, sig = np.unique(np.packbits(mask, axis=1), axis=0, return_inverse=True)
+    assert tile_keys(got) <= tile_keys(np.lexsort((np.arange(n_tb), sig.ravel())))
 
 
 @pytest.mark.parametrize("nrhs", [1, 3, 130])

@@ -156,6 +156,10 @@ class CsrDesc(C.Structure):
                 ("workspace_bytes", C.c_int64)]
 
 
+class ScheduleSizes(C.Structure):
+    _fields_ = [("n_tiles", C.c_int32), ("n_entries", C.c_int64)]
+
+
 class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("count", C.c_int32),
                 ("detail0", C.c_int32), ("detail1", C.c_int32)]
@@ -175,6 +179,13 @@ SIGNATURES = {
     "vl1_classify_pairs": (C.c_int32, [C.c_void_p, C.POINTER(TreeView), C.c_void_p,
                                        C.c_void_p]),
     "vl1_mixed_workspace_bytes": (C.c_int64, [C.c_void_p, C.POINTER(TreeView), C.c_int32]),
+    "vl1_schedule_build_begin": (C.c_int32, [C.c_void_p, C.POINTER(TreeView), C.c_int64,
+                                             C.c_int32, C.POINTER(C.c_void_p),
+                                             C.POINTER(ScheduleSizes), C.c_void_p]),
+    "vl1_schedule_build_key_start": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_schedule_build_fill": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]),
+    "vl1_schedule_builder_destroy": (C.c_int32, [C.c_void_p]),
     "vl1_mixed_geometry": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_eval_mixed": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
                                    C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,

@@ -47,6 +47,7 @@ struct TreeDev {
   double level_scale[32];
 };
 constexpr int kScaleLevels = 32;
+constexpr int kTileRows = 128;   // rows (target box, rhs) of a mixed-path tile
 
 }  // namespace vl1
 

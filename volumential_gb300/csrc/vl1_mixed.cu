@@ -11,19 +11,22 @@
 // chunks of <= 64).
 //
 // Exactness (an Ozaki-type split).  The table blocks (per plan) and x' (per
-// call) are written in fixed point against per-plan / per-rhs power-of-two
-// scales: table values as 40-bit magnitudes, densities as 39-bit magnitudes,
-// each split into 5 base-256 digits carrying the value's sign (|digit| <= 255,
-// the densities' top digit <= 127), held exactly in FP16.  Densities are
-// stored as bytes (sign in bit 7 of the top digit) and expanded to FP16 in
-// shared memory.  A product of one digit pair summed over K <= 64 source
-// points is an integer below 2^22, exact in the FP32 accumulator; the pairs
-// of one diagonal i + j <= 4 together stay below 2^24.  Those diagonals (the
+// call) are written in fixed point against per-plan / per-row power-of-two
+// scales, both as 39-bit magnitudes: the table in balanced base-256 digits
+// (|digit| <= 128, times the value's sign), the densities as a 7-bit top
+// digit and four base-256 digits carrying the value's sign (|digit| <= 127
+// for the top one, <= 255 for the others), all held exactly in FP16.
+// Densities are stored as bytes (sign in bit 7 of the top digit) and expanded
+// to FP16 in shared memory.  A diagonal i + j of digit products summed over
+// K <= 64 source points is an integer below 2^22 for i + j <= 3 and below
+// 2^24 for i + j = 4, exact in the FP32 accumulator.  Those diagonals (the
 // leading 32 bits) get their own TMEM accumulator, re-initialised per K round
-// and read after every round into int64 registers (one FADD with 1.5 * 2^23
-// turns the exact d = 2 float into its integer bits); diagonals i + j = 5, 6
-// accumulate across rounds in FP32 TMEM (their rounding is below 2^-40 of the
-// result).  Each output's sum is then one exact integer, rounded once to FP64.
+// and read after every round into int64 registers: one FADD with 1.5 * 2^23
+// turns an exact d <= 3 float into its integer bits, d = 4 takes a
+// conversion; diagonals i + j = 5, 6 accumulate across rounds in FP32 TMEM
+// (their rounding is below 2^-40 of the result); the products i + j >= 7 are
+// dropped, and with balanced table digits they are zero-mean.  Each output's
+// sum is then one exact integer, rounded once to FP64.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -75,16 +78,23 @@ __device__ __forceinline__ unsigned long long fixed_magnitude(double v, int e) {
   return m;
 }
 
-// table digits: v = sign * 2^(e - 40) * m, digits the five base-256 digits
-// of m, each carrying the sign of v (|digit| <= 255)
+// table digits: v = sign * 2^(e - 39) * m, m < 2^39, written in balanced
+// base 256: m = sum_i d_i 256^(4 - i) with d_1..d_4 in [-128, 128) and the top
+// digit d_0 in [0, 128], all multiplied by the sign of v (|digit| <= 128).
+// Balanced digits make every digit product that the truncated expansion
+// drops (i + j >= 7) zero-mean, so the dropped terms cancel instead of
+// adding up with the sign of the products, as sign-magnitude digits would.
 __device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits]) {
-  const unsigned long long m = fixed_magnitude<kFixedBits>(v, e);
+  long long r = (long long)fixed_magnitude<kFixedBits>(v, e);
   const int sgn = __double_as_longlong(v) < 0 ? -1 : 1;
 #pragma unroll
-  for (int i = 0; i < kDigits; ++i) {
-    const int shift = kFixedBits - kDigitBits * (i + 1);
-    dig[i] = sgn * (int)((m >> shift) & 0xFF);
+  for (int i = kDigits - 1; i >= 1; --i) {
+    int lo = (int)(r & 0xFF);
+    lo -= lo >= 128 ? 256 : 0;
+    dig[i] = sgn * lo;
+    r = (r - lo) >> kDigitBits;
   }
+  dig[0] = sgn * (int)r;   // m < 2^39: r <= 128
 }
 
 // density digit bytes: v = sign * 2^(e - 39) * m, m < 2^39; byte 0 holds
@@ -769,6 +779,11 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     // moved to the target row's reference exponent as they are expanded
     static_assert(kStgDepth == 3, "one shift register per staging slot");
     int sh_s0 = 0, sh_s1 = 0, sh_s2 = 0;
+    // bit (u % kStgDepth): none of this warp's rows has a source box in unit
+    // u (nothing gathered, zero planes); bit s of zero_stages: this warp's
+    // rows of stage s hold zero planes (the stages are overwritten by the
+    // parked sums at the end of an item, so the bits start clear per item)
+    uint32_t empty_bits = 0, zero_stages = 0;
     // expand the staged bytes of unit v into stage v % kStages
     auto expand = [&](int v) -> bool {
       const int s = (ubase + v) % kStages;
@@ -777,6 +792,25 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         return false;
       const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
+      if ((empty_bits >> (v % kStgDepth)) & 1u) {
+        // no source rows: zero planes (rows 16w .. 16w + 15 of a swizzled
+        // K-major plane are one contiguous block), written once per stage
+        if (!((zero_stages >> s) & 1u)) {
+          constexpr int BLK = kRowsPerProducer * (int)ROW_BYTES;
+#pragma unroll
+          for (int dg = 0; dg < kXPlanes; ++dg)
+            for (int o = lane * 16; o < BLK; o += 32 * 16)
+              *reinterpret_cast<uint4 *>(xs + dg * XBYTES + warp * BLK + o) =
+                  make_uint4(0u, 0u, 0u, 0u);
+          zero_stages |= 1u << s;
+        }
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0 && !(withhold && warp == 0 && ubase + v == 0))
+          mbar_arrive(&bars.xfull[s]);
+        return true;
+      }
+      zero_stages &= ~(1u << s);
       const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
       constexpr int ITER = (kRowsPerProducer * NH + 31) / 32;
       const int vs = v % kStgDepth;
@@ -914,17 +948,21 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         xr_lane = -1;
       }
       sh_lane = min(max(sh_lane, 0), kXFixedBits + 1);   // past the width: zero
+      const bool key_empty =
+          __ballot_sync(0xffffffffu, lane < kRowsPerProducer && xr_lane >= 0) == 0u;
       for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
         {
           const int us = u % kStgDepth;
           sh_s0 = us == 0 ? sh_lane : sh_s0;
           sh_s1 = us == 1 ? sh_lane : sh_s1;
           sh_s2 = us == 2 ? sh_lane : sh_s2;
+          empty_bits = (empty_bits & ~(1u << us)) | (key_empty ? 1u << us : 0u);
         }
         // gather unit u: piece pc of the warp's rows -> row pc / PPR, piece pc % PPR
         uint8_t *sb = stg + (u % kStgDepth) * kRowsPerProducer * RB;
 #pragma unroll
         for (int it = 0; it < (kRowsPerProducer * PPR + 31) / 32; ++it) {
+          if (key_empty) break;
           const int pc = it * 32 + lane;
           const int rl = min(pc / PPR, kRowsPerProducer - 1), q = pc - (pc / PPR) * PPR;
           const int xr = __shfl_sync(0xffffffffu, xr_lane, rl);
@@ -1056,11 +1094,14 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     const int cb = rw >> 2;                // RC-column block
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     const int row = quad * 32 + lane;
-    // exact sum of the diagonals per output, units of 2^(e-32)
-    long long acc[RC];
+    // exact sum of the diagonals per output, units of 2^(e-32); the d = 2
+    // and d = 3 terms enter as the raw bits of (d + 1.5 * 2^23), whose
+    // constant part is taken out once after the loop
+    unsigned long long acc[RC];
 #pragma unroll
     for (int c = 0; c < RC; ++c) acc[c] = 0;
     bool ok = true;
+    int rounds_read = 0;
     for (int round = 0; round < n_rounds; ++round) {
       const int R = rbase + round;
       const int b = R & 1;
@@ -1070,25 +1111,28 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       }
       tc::tc_fence_after();
       const uint32_t col = tbase + lane_off + (uint32_t)b * 5 * NCH + cb * RC;
-      uint32_t r16[16];
-      int dsum[16];
-      tc::tmem_ld16(col, r16);               // i + j = 2: |x| < 2^22
+      uint32_t r2[16], r3[16];
+      tc::tmem_ld16(col, r2);                // i + j = 2: |x| <= 127 * 128 * 64 < 2^20
+      tc::tmem_ld16(col + NCH, r3);          // i + j = 3: |x| < 3.2e6 < 2^22
       tc::tmem_ld_wait();
 #pragma unroll
-      for (int c = 0; c < 16; ++c)
-        dsum[c] = __float_as_int(__uint_as_float(r16[c]) + kMagic) - kMagicBits;
-      tc::tmem_ld16(col + NCH, r16);         // i + j = 3: |x| < 2^23
-      tc::tmem_ld_wait();
-#pragma unroll
-      for (int c = 0; c < 16; ++c)
-        acc[c] += ((long long)dsum[c] << 16) + ((long long)__float2int_rn(__uint_as_float(r16[c])) << 8);
-      tc::tmem_ld16(col + 2 * NCH, r16);     // i + j = 4: |x| < 2^24
+      for (int c = 0; c < 16; ++c) {
+        // 1.5 * 2^23 + x for |x| < 2^22 is exact, with the integer x in its
+        // low bits (raw bits kMagicBits + x); weights 2^16 and 2^8 of the
+        // d = 2 and d = 3 terms
+        const uint32_t b2 = __float_as_uint(__uint_as_float(r2[c]) + kMagic);
+        const uint32_t b3 = __float_as_uint(__uint_as_float(r3[c]) + kMagic);
+        acc[c] += (unsigned long long)b2 * 65536ull + (unsigned long long)b3 * 256ull;
+      }
+      tc::tmem_ld16(col + 2 * NCH, r2);      // i + j = 4: |x| < 5.3e6 < 2^24
       tc::tmem_ld_wait();
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&bars.acce[b]);
 #pragma unroll
-      for (int c = 0; c < 16; ++c) acc[c] += (long long)__float2int_rn(__uint_as_float(r16[c]));
+      for (int c = 0; c < 16; ++c)
+        acc[c] += (unsigned long long)(long long)__float2int_rn(__uint_as_float(r2[c]));
+      ++rounds_read;
     }
     // ---- park one int64 per output: the sum of digit products in units of
     // 2^32 (integer diagonals 2..4, weights 2^64..2^48, shifted by 16, plus
@@ -1096,21 +1140,28 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     if (ok && !s_abort) {
       long long *s_tot = reinterpret_cast<long long *>(smem);
       const uint32_t col = tbase + lane_off + kExactCols * NCH + cb * RC;
+      // the constant parts of the raw bits, (kMagicBits << 16) + (kMagicBits
+      // << 8) per round (modulo 2^64: the true sum fits an int64)
+      const unsigned long long magic_total =
+          (unsigned long long)rounds_read * ((unsigned long long)kMagicBits * 65792ull);
 #pragma unroll
-      for (int c = 0; c < 16; ++c) acc[c] <<= 16;
+      for (int c = 0; c < 16; ++c) acc[c] = (acc[c] - magic_total) << 16;
       if (n_rounds > 0) {
         uint32_t r16[16];
         tc::tmem_ld16(col, r16);                 // d5, weight 2^40
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] += f32_scaled_to_i64(__uint_as_float(r16[c]), 8);
+        for (int c = 0; c < 16; ++c)
+          acc[c] += (unsigned long long)f32_scaled_to_i64(__uint_as_float(r16[c]), 8);
         tc::tmem_ld16(col + NCH, r16);           // d6, weight 2^32
         tc::tmem_ld_wait();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] += f32_scaled_to_i64(__uint_as_float(r16[c]), 0);
+        for (int c = 0; c < 16; ++c)
+          acc[c] += (unsigned long long)f32_scaled_to_i64(__uint_as_float(r16[c]), 0);
       }
 #pragma unroll
-      for (int c = 0; c < 16; ++c) s_tot[row * PARK_STRIDE + cb * RC + c] = acc[c];
+      for (int c = 0; c < 16; ++c)
+        s_tot[row * PARK_STRIDE + cb * RC + c] = (long long)acc[c];
     }
   }
 

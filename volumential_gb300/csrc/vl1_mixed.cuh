@@ -10,8 +10,12 @@ namespace vl1 {
 
 constexpr int kDigits = 5;         // 8-bit digits per operand (held exactly in FP16)
 constexpr int kDigitBits = 8;
-constexpr int kFixedBits = kDigits * kDigitBits;  // table: 40-bit fixed point
-constexpr int kXFixedBits = kFixedBits - 1;        // densities: 39 bits + sign
+// Both operands are 39-bit fixed-point magnitudes (a 7-bit top digit and four
+// 8-bit digits) carrying the value's sign: with both top digits below 128, a
+// diagonal sum of digit products over K <= 64 source points stays below 2^22
+// for i + j <= 3, where one FP32 addition recovers its integer bits.
+constexpr int kFixedBits = kDigits * kDigitBits - 1;   // table: 39 bits + sign
+constexpr int kXFixedBits = kDigits * kDigitBits - 1;  // densities: 39 bits + sign
 
 // Operand geometry of one plan.
 struct MixedGeom {
