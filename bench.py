@@ -57,11 +57,11 @@ def parse_args(argv=None):
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     p.add_argument("--workload", choices=("c2", "c1", "c3", "c4", "c5", "table", "csr",
-                                          "split"),
+                                          "split", "tree"),
                    default="c2")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--c4-problems", type=int, default=64, help="C4: problems in the batch")
-    p.add_argument("--c4-max-level", type=int, default=5, help="C4: deepest uniform level")
+    p.add_argument("--c4-max-level", type=int, default=6, help="C4: deepest uniform level")
     p.add_argument("--c5-requests", type=int, default=10000, help="C5: requests per run")
     p.add_argument("--c5-budget-gb", type=float, default=64.0,
                    help="C5: HBM budget of the resident plans, trees and schedules")
@@ -381,17 +381,42 @@ def gpu_arm(args):
     e2e_total = max_over_ranks(float(sum(e2e_ms)))
     api_err = float(np.linalg.norm(host_out.numpy().reshape(nrhs, n) - yp) / np.linalg.norm(yp))
 
+    # e2e_cold: the same public call on a tree the library has not seen (new
+    # device arrays every step): tree validation, the schedule built on the
+    # device and its work items run inside the timed region; the caller's
+    # copy of its tree arrays does not (one rhs: NearFieldFromCSR.__call__)
+    cold = None
+    if nrhs == 1:
+        cold_ms = []
+        n_cold = max(3, min(args.steps, 10))
+        for i in range(n_cold + 1):
+            fresh = {k: kw[k].clone() for k in tree_keys}
+            cold_kw = dict(api_kw, **fresh)
+            flush.fill_(3.0)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            dev_in.copy_(host_in, non_blocking=True)
+            r_, _ = nf(None, result=dev_out, mode_coefs=dev_in, **cold_kw)
+            host_out.copy_(r_, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            if i > 0:   # the first cold call also loads the builder's kernels
+                cold_ms.append((time.perf_counter() - t1) * 1e3)
+            del fresh, cold_kw
+        cold = {"ms": cold_ms,
+                "err": float(np.linalg.norm(host_out.numpy().reshape(nrhs, n) - yp) /
+                             np.linalg.norm(yp))}
+
     return {
         "w": w, "res": res, "clocks": clock_info, "e2e_total_ms": e2e_total,
         "e2e_ms": e2e_ms, "out": yp[0], "out_complex": out_complex, "nrhs": nrhs,
         "coef_complex": coef_complex, "h2d": int(host_in.numel() * host_in.element_size()),
         "d2h": int(host_out.numel() * host_out.element_size()),
         "plan_bytes": plan.device_bytes(), "world": world, "rank": rank,
-        "mixed_err": mixed_err, "mixed_errs": mixed_errs, "api_err": api_err,
+        "mixed_err": mixed_err, "mixed_errs": mixed_errs, "api_err": api_err, "cold": cold,
         "headline": headline, "fp64_gflops": measured_fp64_gflops(),
         "schedule": {"tiles": sched.n_tiles, "tile_keys": sched.n_tile_keys,
                      "mean_keys_per_tile": sched.mean_keys_per_tile,
-                     "build_s": t_sched, "workspace_bytes": int(sched.workspace.numel())},
+                     "build_s": t_sched, "workspace_bytes": int(sched.workspace_bytes)},
         "geometry": plan.mixed_geometry(),
     }
 
@@ -491,6 +516,22 @@ def reference_arm(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _cold_summary(r, n, nrhs):
+    """e2e_cold of the JSON line: points/s of first calls on new trees."""
+    c = r.get("cold")
+    if not c:
+        return None
+    ms = np.asarray(c["ms"])
+    warm = float(np.mean(r["e2e_ms"]))
+    return {"value": n * nrhs / (float(np.mean(ms)) / 1e3), "unit": "points/s",
+            "latency_ms": {"p50": float(np.percentile(ms, 50)),
+                           "p99": float(np.percentile(ms, 99))},
+            "ratio_to_warm_e2e": float(np.mean(ms)) / warm, "steps": int(ms.size),
+            "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
+            "rel_l2_vs_fp64": c["err"], "schedule": "built on the device per call",
+            "api": "NearFieldFromCSR.__call__ on new device tree arrays each step"}
 
 
 def workload_config(w):
@@ -619,6 +660,7 @@ def gb300_main(args):
                 "rel_l2_vs_fp64": r["api_err"],
                 "api": "NearFieldFromCSR.__call__" if nrhs == 1
                        else "FPNDExpansionWrangler.eval_direct_batched"},
+        "e2e_cold": _cold_summary(r, n, nrhs),
         "roofline": roof,
         "paths": {"plain_fp64": plain, "mixed": dict(mixed, rel_l2_vs_fp64=r["mixed_err"]),
                   "speedup_mixed_over_plain": plain["ms_per_step"] / mixed["ms_per_step"]},
@@ -651,31 +693,44 @@ def gb300_main(args):
 
 
 def c4_main(args):
-    """Uneven batch (C4): 64 uniform 3D Laplace problems of levels 3..5,
-    q in {3, 4, 5}, 1..32 right-hand sides each, evaluated by one autotuned,
-    CUDA-graph-captured batch (batched preparation + one persistent
-    tensor-core launch per kernel shape).  One step = one replay of the graph
-    over all problems; compared with the same problems evaluated one by one
-    (mixed path) and with the FP64 kernel (one pass)."""
+    """Uneven batch (C4): 64 uniform 3D Laplace problems of levels 3..6,
+    q in {3, 4, 5}, 1..32 right-hand sides each (FP64 Duffy tables per q),
+    evaluated by one CUDA-graph-captured batch (batched preparation + one
+    persistent tensor-core launch per kernel shape, problems that fill the GPU
+    alone with their own launch) whose tile shapes and work-item size are
+    autotuned.  One step = one replay of the graph over all problems;
+    compared with the same problems evaluated one by one (mixed path, same
+    schedules) and with the FP64 kernel (one pass each), and the errors of
+    every (problem, rhs) against the FP64 results."""
+    import ctypes as C
+
     import torch
 
+    from volumential_gb300 import _lib
     from volumential_gb300 import workloads as W
-    from volumential_gb300.batch import BatchProblem, autotune_batch, problem_arrays
-    from volumential_gb300.batched import eval_mixed
+    from volumential_gb300.batch import BatchProblem, autotune_batch, plan_for, tree_arrays
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     t0 = time.perf_counter()
     ws = W.config_c4(n_problems=args.c4_problems, levels=(3, args.c4_max_level))
-    plans = {}
-    probs = []
+    t_host = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    plans, views, probs = {}, {}, []
     for w in ws:
-        plan, view, keep = problem_arrays(w, plans.get(w.meta["table_key"]))
-        plans.setdefault(w.meta["table_key"], plan)
+        if w.meta["table_key"] not in plans:
+            plans[w.meta["table_key"]] = plan_for(w)
+        if w.meta["tree_key"] not in views:      # one copy of a tree on the device
+            views[w.meta["tree_key"]] = tree_arrays(w)
+        view, keep = views[w.meta["tree_key"]]
         pts = torch.from_numpy(np.ascontiguousarray(w.tree.targets)).to("cuda")
-        coefs = torch.stack([m.on_device(pts) for m in w.meta["mixtures"]]).contiguous()
-        out = torch.zeros_like(coefs)
-        probs.append(BatchProblem(plan, view, keep, coefs, out, w.nrhs))
+        coefs = torch.empty((w.nrhs, w.n_points), dtype=torch.float64, device="cuda")
+        for r, m in enumerate(w.meta["mixtures"]):
+            coefs[r] = m.on_device(pts)
+        del pts
+        probs.append(BatchProblem(plans[w.meta["table_key"]], view, keep, coefs,
+                                  torch.zeros_like(coefs), w.nrhs))
+    torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
     t0 = time.perf_counter()
     batch, table = autotune_batch(probs, reps=2)
@@ -698,73 +753,83 @@ def c4_main(args):
         step_ms.append(ev[0].elapsed_time(ev[1]))
     clock_info = clocks.stop()
     batch.raise_on_status()
-    # the same problems one by one through the mixed path (one pass)
+    mem_peak = torch.cuda.max_memory_allocated()
+    # comparisons, one problem at a time into one shared scratch output and
+    # one shared workspace: (a) each problem alone through vl1_eval_mixed with
+    # the batch's schedule (bit-identical to the batch), (b) the FP64 kernel
     sh = stream.cuda_stream
-    sep = [torch.empty_like(p.out) for p in probs]
-    for p, o in zip(probs, sep):   # untimed: builds each problem's default schedule
-        eval_mixed(p.plan, p.view, p.coefs, o, stream=sh, nrhs=p.nrhs, keep=p.keep)
+    lib = _lib.lib()
+    tmp = torch.empty(max(p.out.numel() for p in probs), dtype=torch.float64, device="cuda")
+    wsp = torch.empty(max(sc.workspace_bytes for sc in batch.schedules), dtype=torch.uint8,
+                      device="cuda")
+
+    def separate(p, sc):
+        _lib.check(lib.vl1_eval_mixed(p.plan.handle, C.byref(p.view), C.byref(sc.c_struct),
+                                      p.coefs.data_ptr(), p.nrhs, tmp.data_ptr(),
+                                      wsp.data_ptr(), wsp.numel(), C.c_void_p(sh)),
+                   "vl1_eval_mixed")
+
+    for p, sc in zip(probs, batch.schedules):   # untimed pass (kernel loading)
+        separate(p, sc)
     torch.cuda.synchronize()
     ev[0].record(stream)
-    for p, o in zip(probs, sep):
-        # each call with its own default work split (the batch's cap is
-        # tuned for the combined work list); schedules built in a first pass
-        eval_mixed(p.plan, p.view, p.coefs, o, stream=sh, nrhs=p.nrhs, keep=p.keep)
+    for p, sc in zip(probs, batch.schedules):
+        separate(p, sc)
     ev[1].record(stream)
     ev[1].synchronize()
     sep_ms = ev[0].elapsed_time(ev[1])
-    # FP64 kernel, one pass, and the errors of the batch against it
-    ref = [torch.empty_like(p.out) for p in probs]
-    ev[0].record(stream)
-    for p, o in zip(probs, ref):
-        p.plan.eval_fp64(p.view, p.coefs, o, stream=sh, nrhs=p.nrhs)
-    ev[1].record(stream)
-    ev[1].synchronize()
-    plain_ms = ev[0].elapsed_time(ev[1])
-    errs = []
-    for p, o in zip(probs, ref):
-        d = (p.out - o).reshape(p.nrhs, -1)
-        errs.extend((torch.linalg.norm(d, dim=1) /
-                     torch.linalg.norm(o.reshape(p.nrhs, -1), dim=1)).tolist())
-    # the batch against the same problems one by one with the batch's work
-    # split (identical bits: the split decides the rounding of the tails)
-    for p, o in zip(probs, sep):
-        eval_mixed(p.plan, p.view, p.coefs, o, stream=sh, nrhs=p.nrhs, keep=p.keep,
-                   max_keys_per_item=batch.max_keys_per_item)
-    torch.cuda.synchronize()
-    same = all(torch.equal(p.out, o) for p, o in zip(probs, sep))
+    same = True
+    for p, sc in zip(probs, batch.schedules):
+        separate(p, sc)
+        same = same and torch.equal(tmp[:p.out.numel()].view_as(p.out), p.out)
+    plain_ms, errs = 0.0, []
+    for p in probs:
+        ev[0].record(stream)
+        p.plan.eval_fp64(p.view, p.coefs, tmp[:p.out.numel()], stream=sh, nrhs=p.nrhs)
+        ev[1].record(stream)
+        ev[1].synchronize()
+        plain_ms += ev[0].elapsed_time(ev[1])
+        ref = tmp[:p.out.numel()].view(p.nrhs, -1)
+        d = (p.out.view(p.nrhs, -1) - ref)
+        errs.extend((torch.linalg.norm(d, dim=1) / torch.linalg.norm(ref, dim=1)).tolist())
     pts = sum(int(p.view.n_particles) * p.nrhs for p in probs)
     pairs = sum(w.pair_count() * w.nrhs for w in ws)
     ms = float(np.mean(step_ms))
     hbm, bf16, peak_kind = peaks()
+    levels = [w.meta["level"] for w in ws]
     line = {
         "metric": METRIC, "value": pts / (ms / 1e3), "unit": "points/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp16-digits/fp32-exact/f64", "data": "synthetic",
         "config": {"workload": f"c4_lap3d_uniform_batch{len(probs)}", "problems": len(probs),
-                   "levels": [3, args.c4_max_level], "q": [3, 4, 5], "nrhs": [1, 32],
-                   "points_x_rhs": pts, "point_pairs_x_rhs": pairs,
+                   "levels": [3, args.c4_max_level],
+                   "problems_per_level": {str(l): levels.count(l)
+                                          for l in range(3, args.c4_max_level + 1)},
+                   "q": [3, 4, 5], "nrhs": [1, 32], "points_x_rhs": pts,
+                   "point_pairs_x_rhs": pairs, "tables": _table_source(ws[0]),
                    "l2": "inputs (%.1f GB) far larger than L2" %
-                         (sum(p.coefs.numel() * 16 for p in probs) / 1e9),
-                   "path": "batch, CUDA graph replay"},
+                         (sum(p.coefs.numel() * 8 for p in probs) / 1e9),
+                   "path": "batch, CUDA graph replay", "waves": 1},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
                        "p99": float(np.percentile(step_ms, 99))},
-        "rel_l2_max_vs_fp64": max(errs), "batch_equals_separate_mixed": bool(same),
+        "rel_l2_vs_fp64": {"max": max(errs), "median": float(np.median(errs)),
+                           "n": len(errs)},
+        "batch_equals_separate_mixed": bool(same),
         "paths": {"batch_graph_ms": ms, "separate_mixed_ms": sep_ms, "plain_fp64_ms": plain_ms,
                   "speedup_batch_over_plain": plain_ms / ms,
                   "speedup_batch_over_separate": sep_ms / ms},
-        "autotune": {str(k): v for k, v in table.items()},
-        "max_keys_per_item": batch.max_keys_per_item,
-        "batch_device_bytes": batch.device_bytes,
-        "setup_s": t_setup, "autotune_s": t_tune,
-        "pair_rate_per_s": pairs / (ms / 1e3),
-        "e2e": None, "e2e_note": "resident-data batch; host copies of 23 GB are not part of "
-                                 "this configuration",
+        "autotune": table,
+        "batch_device_bytes": batch.device_bytes, "device_bytes_peak": int(mem_peak),
+        "setup_s": {"host_trees_tables": t_host, "device_inputs": t_setup},
+        "autotune_s": t_tune, "pair_rate_per_s": pairs / (ms / 1e3),
+        "e2e": None, "e2e_note": "resident-data batch; host copies of the inputs are not "
+                                 "part of this configuration",
         "clocks": clock_info, "peak_source": peak_kind,
-        "gpu_launches": args.steps * (2 + 2),
+        "gpu_launches": args.steps * batch.kernel_launches,
     }
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line, default=str), flush=True)
     return 0
 
 
@@ -1056,6 +1121,83 @@ def csr_main(args):
     return 0
 
 
+def tree_main(args):
+    """Tree construction on the GPU (refinement criterion evaluated on the
+    device, ``vl1_tree_balance``, ``vl1_tree_build_*`` and the list-1 CSR,
+    ``vl1_list1_csr``) against the host builder, for the C2 octree: 3D, q=4,
+    refined where the variation of the 16-Gaussian density over a leaf's 64
+    nodes exceeds 1e-3, levels 2..6, 2:1 balanced.  One step = one device
+    build of the tree and its list 1 (CUDA events around the whole call)."""
+    import torch
+
+    from volumential_gb300 import workloads as W
+    from volumential_gb300.tree_build import (build_adaptive_tree,
+                                              build_adaptive_tree_device,
+                                              build_list1_traversal,
+                                              build_list1_traversal_device)
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(2006)
+    mix = W.random_gaussian_mixture(rng, 3, 16, (0.01, 0.08))
+
+    def refine_host(nodes):
+        v = mix(nodes)
+        return (v.max(axis=-1) - v.min(axis=-1)) > 1e-3
+
+    def refine_dev(nodes):
+        v = mix.on_device(nodes)
+        return (v.amax(dim=-1) - v.amin(dim=-1)) > 1e-3
+
+    t0 = time.perf_counter()
+    host = build_adaptive_tree(3, 4, refine_host, max_level=6, min_level=2)
+    hc = build_list1_traversal(host)
+    host_s = time.perf_counter() - t0
+
+    def dev_build():
+        t = build_adaptive_tree_device(3, 4, refine_dev, max_level=6, min_level=2,
+                                       as_numpy=False)
+        return t, build_list1_traversal_device(t, as_numpy=False)
+
+    for _ in range(max(1, args.warmup)):
+        dev_build()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        e0.record()
+        t, dc = dev_build()
+        e1.record()
+        e1.synchronize()
+        ms.append((time.perf_counter() - w0) * 1e3)
+    n_leaves = int(t.leaf_boxes.numel())
+    same = (n_leaves == len(host.leaf_boxes) and
+            np.array_equal(t.box_levels.cpu().numpy(), host.box_levels) and
+            np.array_equal(dc.neighbor_source_boxes_lists.cpu().numpy(),
+                           hc.neighbor_source_boxes_lists))
+    tms = float(np.median(ms))
+    line = {
+        "metric": "adaptive tree + list-1 build: leaves/s", "value": n_leaves / (tms / 1e3),
+        "unit": "leaves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64/int32", "data": "synthetic",
+        "config": {"workload": "tree_c2_adaptive_octree_q4", "leaves": n_leaves,
+                   "boxes": int(t.nboxes), "points": int(t.targets.shape[1]),
+                   "list1_box_pairs": int(dc.nnz), "l2": "n/a (one build)"},
+        "equal_to_host_build": bool(same),
+        "cpu_baseline": {"value": len(host.leaf_boxes) / host_s, "unit": "leaves/s",
+                         "cores": 1, "kind": "port",
+                         "sample": f"the host builder (numpy) on the same tree: {host_s:.2f} s"},
+        "e2e": {"value": n_leaves / (tms / 1e3), "unit": "leaves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0, "note": "wall time of the device build call"},
+        "gpu_launches": None,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def split_main(args):
     """Helmholtz split correction (``vl1_split_correction``): the list-1 sum
     of density x weight x R(r), R = G_k - G_0 by its series, over the C3 tree
@@ -1156,6 +1298,8 @@ def main(argv=None):
         return table_main(args)
     if args.workload == "csr":
         return csr_main(args)
+    if args.workload == "tree":
+        return tree_main(args)
     return gb300_main(args)
 
 

@@ -134,9 +134,12 @@ typedef struct {
  * has no list-1 pair of that key.
  * items: n_items work items, launched in this order (longest first balances
  * the GPU); n_items == 0 means one item per tile covering all its keys.
- * split_counters: n_splits * (output column chunks) int32, zero before the
- * first call; every call leaves them zero.  split_partials: n_slots *
- * (128 * padded output columns) * 8 bytes of scratch for split tiles.
+ * split_counters: n_splits * n_chunks int32, zero before the first call;
+ * every call leaves them zero.  split_partials: n_slots * (128 * padded
+ * output columns) * 8 bytes of scratch for split tiles.  n_chunks: the
+ * plan's output column chunks (padded output columns / columns per CTA) when
+ * the split scratch was sized; a call on a plan with another count is
+ * refused (VL1_E_ARG).
  * DEVICE pointers, caller owned; key_xrow 16-byte aligned. */
 typedef struct {
   int32_t n_tiles;
@@ -150,6 +153,7 @@ typedef struct {
   int32_t n_slots;
   int32_t *split_counters;
   void *split_partials;
+  int32_t n_chunks;
 } vl1_mixed_schedule;
 
 typedef struct {
@@ -221,6 +225,19 @@ int32_t vl1_schedule_build_fill(vl1_schedule_builder *builder, int32_t *tile_row
                                 void *stream);
 int32_t vl1_schedule_builder_destroy(vl1_schedule_builder *builder);
 
+/* Work items of a mixed-path schedule (host code, no device access; no
+ * reference counterpart).  Tiles with more keys than a cap are split into
+ * nearly equal key ranges; items are ordered longest first (ties keep tile
+ * order).  cap > 0: that cap; cap <= 0: the cap among 13 fractions of one
+ * SM's share of all keys whose modelled finish time on n_sm one-CTA-per-SM
+ * slots is shortest (per item 4 keys of start-up and drain, a split part 1.5
+ * more, the last part of a split tile 2 more).  key_start: host
+ * [n_tiles + 1]; items: host [capacity]; *n_items receives the count also
+ * when the capacity is too small (VL1_E_ARG). */
+int32_t vl1_mixed_work_items(const int32_t *key_start, int32_t n_tiles, int32_t cap,
+                             int32_t n_sm, vl1_mixed_item *items, int32_t capacity,
+                             int32_t *n_items, int32_t *n_splits, int32_t *n_slots);
+
 /* Bytes of caller-provided device workspace vl1_eval_mixed needs. */
 int64_t vl1_mixed_workspace_bytes(const vl1_plan *plan, const vl1_tree_view *tree,
                                   int32_t nrhs);
@@ -228,6 +245,14 @@ int64_t vl1_mixed_workspace_bytes(const vl1_plan *plan, const vl1_tree_view *tre
 /* Operand geometry of the mixed path: out[0..4] = padded source points, K
  * chunk, K chunks, padded output columns, output columns per CTA. */
 int32_t vl1_mixed_geometry(const vl1_plan *plan, int32_t *out5);
+
+/* Tile shape of the plan's tensor-core kernel (no reference counterpart; the
+ * reference's tuning point is its kernel choice, list1.py:1240-1258): K chunk
+ * kc (16 or 32 source points per pipeline unit) and output columns per CTA
+ * nch (16, 32 or 64).  Rebuilds the plan's digit operands; synchronises the
+ * device, so no evaluation with the plan may be in flight.  Schedules are
+ * tied to the column chunk count (vl1_mixed_schedule.n_chunks). */
+int32_t vl1_plan_set_mixed_geometry(vl1_plan *plan, int32_t kc, int32_t nch);
 
 /* Mixed-precision list-1 evaluation on the tensor cores: the same sum as
  * vl1_eval_fp64 (list1.py:1050-1159) computed from exact FP16 digit products:
@@ -298,6 +323,9 @@ int32_t vl1_batch_eval(vl1_batch *batch, void *stream);
 int32_t vl1_batch_destroy(vl1_batch *batch);
 /* Device bytes held by the batch (its own buffer; plans and schedules apart). */
 int64_t vl1_batch_device_bytes(const vl1_batch *batch);
+/* Kernels one vl1_batch_eval launches (preparation and tensor-core launches;
+ * its one memset not counted). */
+int32_t vl1_batch_kernel_launches(const vl1_batch *batch);
 
 /* ---- Table builder: FP64 Duffy radial quadrature ----------------------
  * Values of near-field table entries, T = int_{[0,h]^d} G(t - y) phi(y) dy,
@@ -390,6 +418,48 @@ typedef struct {
 int64_t vl1_list1_csr_workspace_bytes(int32_t n_leaves);
 int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *stream);
 
+/* ---- Box trees on the device -----------------------------------------
+ * 2:1 level restriction of a set of leaves (volumential/
+ * tree_interactive_build.py:202-432): a leaf at level L splits every leaf at
+ * a level below L - 1 that contains one of its same-level neighbour
+ * positions, until none does.  levels/coords: device arrays of `capacity`
+ * leaves ([capacity] uint8, [capacity][dim] int32 integer coordinates at the
+ * leaf's level), of which *n_leaves are set; on return they hold the
+ * balanced leaves (in no particular order) and *n_leaves their count
+ * (VL1_E_ARG when they need more than `capacity`).  Synchronises the stream
+ * once per pass and allocates its own scratch. */
+int32_t vl1_tree_balance(int32_t dim, int32_t *n_leaves, int32_t capacity, uint8_t *levels,
+                         int32_t *coords, void *stream);
+
+/* The particle tree of a set of leaves (the layout of
+ * build_particle_tree_from_box_tree, tree_interactive_build.py:1274-1441):
+ * boxes are the leaves and their ancestors, numbered level by level and
+ * lexicographically by integer coordinates inside a level; every leaf holds
+ * the q^dim tensor Gauss-Legendre nodes of its box (meshgrid "ij" order),
+ * leaves in box order.  begin: leaf_levels / leaf_coords are device arrays
+ * of n_leaves distinct leaves of one tree; root_vertex is a host [dim];
+ * sizes3 receives (nboxes, aligned_nboxes = nboxes rounded up to 32,
+ * max_level).  level_starts: host [max_level + 2] first box of each level.
+ * fill: ref_nodes host [dim][q^dim] and ref_weights host [q^dim] (the
+ * reference nodes on [-1, 1] and the products of their weights); device
+ * outputs box_levels [nboxes], box_coords [nboxes][dim], box_centers
+ * [dim][aligned_nboxes], box_is_leaf [nboxes], box_starts / box_counts
+ * [nboxes] (q^dim per leaf, 0 otherwise), leaf_boxes [n_leaves], targets
+ * [dim][n_leaves q^dim], weights [n_leaves q^dim] (weights of the reference
+ * rule times (extent / 2)^dim).  Synchronises the stream. */
+typedef struct vl1_tree_builder vl1_tree_builder;
+int32_t vl1_tree_build_begin(int32_t dim, int32_t q, int32_t n_leaves, const uint8_t *leaf_levels,
+                             const int32_t *leaf_coords, double root_extent,
+                             const double *root_vertex, vl1_tree_builder **out,
+                             int32_t *sizes3, void *stream);
+int32_t vl1_tree_build_level_starts(const vl1_tree_builder *builder, int32_t *out);
+int32_t vl1_tree_build_fill(vl1_tree_builder *builder, const double *ref_nodes,
+                            const double *ref_weights, uint8_t *box_levels, int32_t *box_coords,
+                            double *box_centers, uint8_t *box_is_leaf, int32_t *box_starts,
+                            int32_t *box_counts, int32_t *leaf_boxes, double *targets,
+                            double *weights, void *stream);
+int32_t vl1_tree_builder_destroy(vl1_tree_builder *builder);
+
 /* Measurement hook (no reference counterpart): while `begin` and `end` are
  * set (cudaEvent_t handles, or NULL to stop), every vl1_eval_mixed and
  * vl1_batch_eval records `begin` on its stream right before its tensor-core
@@ -399,16 +469,16 @@ int32_t vl1_list1_csr(const vl1_csr_desc *desc, int64_t *nnz, void *stream);
 int32_t vl1_set_kernel_events(void *begin, void *end);
 
 /* Test hook (no reference counterpart): every wait of the tensor-core kernel
- * on a pipeline barrier is bounded; a wait that runs out sets the launch's
- * abort flag, the kernel lets its issued copies and MMAs complete, frees its
- * TMEM, writes no results and reports VL1_E_TIMEOUT in the status word.
- * poll_limit: polls (each up to 0.2 ms) before a wait gives up, 0 = the
- * default (10,000, about 2 s).  withhold_arrival != 0: in the next launches,
- * one producer warp of CTA (0, 0) does not signal its first pipeline unit,
- * so that the issuer's wait on it runs out (a barrier that nothing
- * completes; no fault).  Process-wide; vl1_test_set_wait_fault(0, 0) restores
- * normal operation.  A schedule that timed out stays usable. */
-int32_t vl1_test_set_wait_fault(int32_t poll_limit, int32_t withhold_arrival);
+ * on a pipeline barrier is bounded in time; a wait that runs out sets the
+ * launch's abort flag, the kernel lets its issued copies and MMAs complete,
+ * frees its TMEM, writes no results and reports VL1_E_TIMEOUT in the status
+ * word.  wait_limit_us: microseconds before a wait gives up, 0 = the default
+ * (2 s).  withhold_arrival != 0: in the next launches, one producer warp of
+ * CTA (0, 0) does not signal its first pipeline unit, so that the issuer's
+ * wait on it runs out (a barrier that nothing completes; no fault).
+ * Process-wide; vl1_test_set_wait_fault(0, 0) restores normal operation.  A
+ * schedule that timed out stays usable. */
+int32_t vl1_test_set_wait_fault(int32_t wait_limit_us, int32_t withhold_arrival);
 
 /* Size of the fixed scratch array used by vl1_eval_mixed_noalloc (32 MiB). */
 #define VL1_NOALLOC_SCRATCH_BYTES (32LL << 20)

@@ -104,17 +104,68 @@ def test_batch_graph_replay_follows_the_coefficients(cuda):
     batch.close()
 
 
+def _default_shapes(probs):
+    return {id(p.plan): (p.plan, p.plan.mixed_geometry()) for p in probs}
+
+
+def _restore(saved):
+    for plan, geo in saved.values():
+        plan.set_mixed_geometry(geo["kc"], geo["nch"])
+
+
 def test_autotuned_batch_gives_the_same_results(cuda):
     torch = cuda
     ws = _workloads()[:3]
     probs = _problems(torch, ws)
-    batch, table = autotune_batch(probs, reps=1, divisors=(1, 4))
-    batch.eval()
-    batch.raise_on_status()
-    assert table
-    for (w, pol), p in zip(ws, probs):
-        prob = oracle_for_workload(w, pol)
-        got = p.out.cpu().numpy()
-        for r in range(w.nrhs):
-            assert rel_l2(got[r], oracle_eval(prob, w, w.coefs[r])) <= TOL_MIXED
-    batch.close()
+    saved = _default_shapes(probs)
+    try:
+        batch, table = autotune_batch(probs, reps=1, divisors=(1, 4))
+        batch.eval()
+        batch.raise_on_status()
+        # every plan's shapes were timed and one chosen
+        labels = {f"3d_q{q}" for q in (3, 4, 5)}
+        assert set(table["shapes"]) == labels
+        for rows in table["shapes"].values():
+            assert rows["chosen"] in rows and len(rows) >= 3
+        for (w, pol), p in zip(ws, probs):
+            prob = oracle_for_workload(w, pol)
+            got = p.out.cpu().numpy()
+            for r in range(w.nrhs):
+                assert rel_l2(got[r], oracle_eval(prob, w, w.coefs[r])) <= TOL_MIXED
+        batch.close()
+    finally:
+        _restore(saved)
+
+
+@pytest.mark.parametrize("kc,nch", [(16, 16), (16, 32), (16, 64), (32, 16), (32, 32),
+                                    (32, 64)])
+def test_every_tile_shape_matches_the_oracle(cuda, kc, nch):
+    """Each tensor-core kernel instance (K chunk x column chunk) on a 3D q=4
+    adaptive tree and a 2D complex-table problem, single calls and a batch."""
+    torch = cuda
+    ws = [(W.adaptive_workload("shape3", 3, 4, tol=3e-2, max_level=4, min_level=2, seed=67,
+                               nrhs=2), LAP3)]
+    h = W.uniform_workload("shape_h", 2, 3, 5, seed=68, kernel=HelmholtzKernel(2),
+                           complex_table=True, nrhs=1)
+    h.tables = W.synthetic_tables(2, 5, h.kernel, seed=9, complex_values=True,
+                                  source_box_extent=h.tree.root_extent / 8)
+    ws.append((h, FIXED))
+    probs = _problems(torch, ws)
+    saved = _default_shapes(probs)
+    try:
+        for p in probs:
+            p.plan.set_mixed_geometry(kc, nch)
+            assert (p.plan.mixed_geometry()["kc"], p.plan.mixed_geometry()["nch"]) == (kc, nch)
+        singles = _singles(torch, probs, None)
+        batch = MixedBatch(probs)
+        batch.eval()
+        batch.raise_on_status()
+        for (w, pol), p, single in zip(ws, probs, singles):
+            prob = oracle_for_workload(w, pol)
+            got = p.out.cpu().numpy()
+            assert np.array_equal(got, single)
+            for r in range(w.nrhs):
+                assert rel_l2(got[r], oracle_eval(prob, w, w.coefs[r])) <= TOL_MIXED
+        batch.close()
+    finally:
+        _restore(saved)

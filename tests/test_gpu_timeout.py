@@ -1,7 +1,7 @@
 """The bounded-wait failure path of the tensor-core kernel, without a GPU fault.
 
 Every wait of ``mixed_kernel`` on a pipeline barrier is bounded.  The test
-hook ``vl1_test_set_wait_fault`` shortens the bound and has one producer warp
+hook ``vl1_test_set_wait_fault`` shortens the bound (5 ms) and has one producer warp
 of the first CTA withhold its first arrival: a barrier that nothing
 completes, so the issuer's wait runs out.  The kernel must then let its
 issued copies and MMAs finish, free its TMEM, write no results for that CTA,
@@ -25,12 +25,12 @@ from volumential_gb300.plan import as_device_tensor
 pytestmark = pytest.mark.gpu
 
 TOL_MIXED = 1e-9
-POLLS = 40   # each poll sleeps up to 0.2 ms: a wait gives up within ~8 ms
+WAIT_LIMIT_US = 5000   # a wait gives up after 5 ms
 
 
 class _WaitFault:
     def __enter__(self):
-        _lib.check(_lib.lib().vl1_test_set_wait_fault(POLLS, 1), "vl1_test_set_wait_fault")
+        _lib.check(_lib.lib().vl1_test_set_wait_fault(WAIT_LIMIT_US, 1), "vl1_test_set_wait_fault")
 
     def __exit__(self, *exc):
         _lib.check(_lib.lib().vl1_test_set_wait_fault(0, 0), "vl1_test_set_wait_fault")

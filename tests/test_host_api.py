@@ -540,6 +540,30 @@ def test_tile_schedule_matches_per_tile_restatement(nrhs):
         assert np.array_equal(np.asarray(g), np.asarray(w))
 
 
+# restatement of the work-item cost model of vl1_mixed_work_items (test only)
+ITEM_OVERHEAD_KEYS, SPLIT_OVERHEAD_KEYS, LAST_PART_KEYS = 4.0, 1.5, 2.0
+CAP_FRACTIONS = (1.5, 1.25, 1.0, 0.85, 0.75, 0.67, 0.6, 0.5, 0.4, 0.33, 0.25, 0.2, 0.17)
+
+
+def _split_items(key_start, cap):
+    items, n_splits, n_slots = [], 0, 0
+    for t in range(len(key_start) - 1):
+        k0, k1 = int(key_start[t]), int(key_start[t + 1])
+        nk = k1 - k0
+        nparts = max(1, -(-nk // cap))
+        if nparts == 1:
+            items.append((t, k0, k1, -1, 0, 1, -1, 0))
+            continue
+        bounds = [k0 + (nk * i) // nparts for i in range(nparts + 1)]
+        for part in range(nparts):
+            items.append((t, bounds[part], bounds[part + 1], n_splits, part, nparts,
+                          n_slots + part, 0))
+        n_splits += 1
+        n_slots += nparts
+    items.sort(key=lambda it: -(it[2] - it[1]))
+    return items, n_splits, n_slots
+
+
 def test_work_item_cap_choice_equals_the_exhaustive_search():
     """The cap search skips candidates whose lower bound cannot beat the best
     so far and uses max(cost) when every item has its own slot; the chosen
@@ -551,9 +575,9 @@ def test_work_item_cap_choice_equals_the_exhaustive_search():
     def finish(items, n_sm):
         slots = [0.0] * n_sm
         for it in items:
-            cost = (it[2] - it[1]) + M.ITEM_OVERHEAD_KEYS
+            cost = (it[2] - it[1]) + ITEM_OVERHEAD_KEYS
             if it[3] >= 0:
-                cost += M.SPLIT_OVERHEAD_KEYS + (M.LAST_PART_KEYS if it[4] == it[5] - 1 else 0)
+                cost += SPLIT_OVERHEAD_KEYS + (LAST_PART_KEYS if it[4] == it[5] - 1 else 0)
             heapq.heapreplace(slots, slots[0] + cost)
         return max(slots)
 
@@ -564,12 +588,16 @@ def test_work_item_cap_choice_equals_the_exhaustive_search():
         n_sm = int(rng.integers(1, 160))
         share = max(1, -(-int(ks[-1]) // n_sm))
         best = None
-        for f in M.CAP_FRACTIONS:
-            cand = M._split_items(ks, max(4, int(np.ceil(share * f))))
+        for f in CAP_FRACTIONS:
+            cand = _split_items(ks, max(4, int(np.ceil(share * f))))
             t = finish(cand[0], n_sm)
             if best is None or t < best[0]:
                 best = (t, cand)
-        assert M._work_items(ks, None, n_sm=n_sm) == best[1]
+        def as_tuples(r):
+            return [tuple(int(v) for v in row) for row in r[0]], r[1], r[2]
+        assert as_tuples(M._work_items(ks, None, n_sm=n_sm)) == best[1]
+        cap = int(rng.integers(1, 60))
+        assert as_tuples(M._work_items(ks, cap, n_sm=n_sm)) == _split_items(ks, cap)
 
 
 def test_tile_schedule_rejects_two_sources_with_one_case():

@@ -109,6 +109,7 @@ class MixedSchedule(C.Structure):
         ("n_items", C.c_int32), ("items", C.c_void_p),
         ("n_splits", C.c_int32), ("n_slots", C.c_int32),
         ("split_counters", C.c_void_p), ("split_partials", C.c_void_p),
+        ("n_chunks", C.c_int32),
     ]
 
 
@@ -186,7 +187,11 @@ SIGNATURES = {
     "vl1_schedule_build_fill": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p]),
     "vl1_schedule_builder_destroy": (C.c_int32, [C.c_void_p]),
+    "vl1_mixed_work_items": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "vl1_mixed_geometry": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_plan_set_mixed_geometry": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
     "vl1_eval_mixed": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
                                    C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,
                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
@@ -198,11 +203,20 @@ SIGNATURES = {
     "vl1_duffy_table": (C.c_int32, [C.POINTER(DuffyDesc), C.c_void_p, C.c_void_p]),
     "vl1_split_correction": (C.c_int32, [C.POINTER(SplitDesc), C.c_void_p]),
     "vl1_list1_csr_workspace_bytes": (C.c_int64, [C.c_int32]),
+    "vl1_tree_balance": (C.c_int32, [C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]),
+    "vl1_tree_build_begin": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                         C.c_void_p, C.c_double, C.c_void_p,
+                                         C.POINTER(C.c_void_p), C.c_void_p, C.c_void_p]),
+    "vl1_tree_build_level_starts": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "vl1_tree_build_fill": (C.c_int32, [C.c_void_p] + [C.c_void_p] * 11 + [C.c_void_p]),
+    "vl1_tree_builder_destroy": (C.c_int32, [C.c_void_p]),
     "vl1_list1_csr": (C.c_int32, [C.POINTER(CsrDesc), C.POINTER(C.c_int64), C.c_void_p]),
     "vl1_batch_update": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(BatchProblem),
                                      C.c_void_p]),
     "vl1_batch_destroy": (C.c_int32, [C.c_void_p]),
     "vl1_batch_device_bytes": (C.c_int64, [C.c_void_p]),
+    "vl1_batch_kernel_launches": (C.c_int32, [C.c_void_p]),
     "vl1_eval_mixed_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(TreeView),
                                            C.POINTER(MixedSchedule), C.c_void_p, C.c_int32,
                                            C.c_void_p, C.c_void_p]),

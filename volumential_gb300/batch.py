@@ -21,7 +21,7 @@ import time
 import numpy as np
 
 from . import _lib
-from .batched import get_schedule
+from .batched import MixedSchedule, get_schedule
 
 __all__ = ["BatchProblem", "MixedBatch", "autotune_batch", "plan_for", "problem_arrays",
            "tree_arrays"]
@@ -138,12 +138,19 @@ class MixedBatch:
         sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         self.schedules = []
         arr = (_lib.BatchProblem * len(self.problems))()
+        used = set()
         for i, p in enumerate(self.problems):
             if p.coefs.dtype != torch.float64 or not p.coefs.is_contiguous():
                 raise TypeError("batch coefficients must be contiguous float64 tensors")
             if p.coefs.numel() != p.nrhs * int(p.view.n_particles):
                 raise ValueError(f"problem {i}: coefficients must hold nrhs * N values")
             sched = get_schedule(p.plan, p.view, p.keep, p.nrhs, sh, max_keys_per_item)
+            if id(sched) in used and sched.n_splits > 0:
+                # problems of one plan, tree and rhs count share the cached
+                # schedule; each needs its own split scratch
+                sched = MixedSchedule(p.plan, p.view, p.keep, p.nrhs, sh, max_keys_per_item,
+                                      base=sched, workspace=False)
+            used.add(id(sched))
             self.schedules.append(sched)
             arr[i].plan = p.plan.handle
             arr[i].tree = C.cast(C.pointer(p.view), C.c_void_p)
@@ -166,6 +173,11 @@ class MixedBatch:
     @property
     def device_bytes(self):
         return int(self._lib.vl1_batch_device_bytes(self.handle))
+
+    @property
+    def kernel_launches(self):
+        """Kernels one evaluation launches."""
+        return int(self._lib.vl1_batch_kernel_launches(self.handle))
 
     def eval(self, stream=None):
         import torch
@@ -237,40 +249,83 @@ def _signature(problems):
                   int(p.plan.nq), id(p.plan)) for p in problems)
 
 
-def autotune_batch(problems, *, reps=3, divisors=(1, 2, 3, 4, 6, 8), verbose=False):
-    """Choose the work-item size of a batch by timing.
+def _plan_label(plan):
+    return f"{plan.dim}d_q{plan.quad_order}" + ("_complex" if plan.complex_table else "")
 
-    Candidates cap the keys of one work item at the mean (tile key, column
-    chunk) count per SM divided by each of ``divisors`` (smaller items balance
-    the persistent launch better, larger ones pay fewer start-ups); each
-    candidate batch is built and timed (median of ``reps`` evaluations, CUDA
-    events) and the fastest is returned with the timing table.  Choices are
-    cached per problem-set signature.
+
+def autotune_batch(problems, *, reps=3, divisors=(1, 2, 3, 4, 6, 8), shapes=True,
+                   verbose=False):
+    """Choose the tile shapes and the work-item size of a batch by timing.
+
+    1. Tile shapes (when ``shapes``): for each plan of the batch in turn (the
+       others at their best so far), every shape it can take (K chunk of 16
+       or 32 source points per pipeline unit, 16, 32 or 64 output columns per
+       CTA; ``Plan.mixed_shapes``) is set and the batch built and timed; the
+       fastest shape is kept.
+    2. Work-item size: candidates cap the keys of one work item at the mean
+       (tile key, column chunk) count per SM divided by each of ``divisors``
+       (smaller items balance the persistent launch better, larger ones pay
+       fewer start-ups).
+    Every candidate batch is timed by the median of ``reps`` evaluations
+    (CUDA events).  Returns the fastest batch and the timing table; choices
+    are cached per problem-set signature.  (The reference's tuning point is
+    its kernel choice, ``list1.py:1240-1258``.)
     """
     import torch
 
     sig = _signature(problems)
+    plans = []
+    for p in problems:
+        if all(p.plan is not q for q in plans):
+            plans.append(p.plan)
     if sig in _tuned:
-        cap = _tuned[sig]
-        return MixedBatch(problems, max_keys_per_item=cap), {"cached": cap}
+        chosen, cap = _tuned[sig]
+        for pl in plans:
+            pl.set_mixed_geometry(*chosen[id(pl)])
+        return MixedBatch(problems, max_keys_per_item=cap), {"cached": True}
     stream = torch.cuda.current_stream().cuda_stream
     n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    total_keys = 0
-    for p in problems:
-        s = get_schedule(p.plan, p.view, p.keep, p.nrhs, stream)
-        geo = p.plan.mixed_geometry()
-        total_keys += s.n_tile_keys * (geo["np"] // geo["nch"])
-    share = max(1, -(-total_keys // n_sm))
-    table = {}
-    best = None
-    for d in divisors:
-        cap = max(2, -(-share // d))
-        if cap in table:
-            continue
+    table = {"shapes": {}, "caps": {}}
+
+    def timed(cap):
         t0 = time.perf_counter()
         b = MixedBatch(problems, max_keys_per_item=cap)
         ms = _time_batch(b, reps)
-        table[cap] = {"ms": ms, "build_s": time.perf_counter() - t0}
+        return b, ms, time.perf_counter() - t0
+
+    best_ms = None
+    if shapes:
+        for pl in plans:
+            label = _plan_label(pl)
+            geo = pl.mixed_geometry()
+            current = (geo["kc"], geo["nch"])
+            rows = {}
+            best_shape = current
+            for shape in pl.mixed_shapes():
+                pl.set_mixed_geometry(*shape)
+                b, ms, build_s = timed(None)
+                b.close()
+                rows[f"kc{shape[0]}_nch{shape[1]}"] = {"ms": ms, "build_s": build_s}
+                if verbose:
+                    print(f"autotune {label}: kc {shape[0]}, nch {shape[1]} -> {ms:.3f} ms")
+                if best_ms is None or ms < best_ms:
+                    best_ms, best_shape = ms, shape
+            pl.set_mixed_geometry(*best_shape)
+            rows["chosen"] = f"kc{best_shape[0]}_nch{best_shape[1]}"
+            table["shapes"][label] = rows
+    total_keys = 0
+    for p in problems:
+        sch = get_schedule(p.plan, p.view, p.keep, p.nrhs, stream)
+        geo = p.plan.mixed_geometry()
+        total_keys += sch.n_tile_keys * (geo["np"] // geo["nch"])
+    share = max(1, -(-total_keys // n_sm))
+    best = None
+    for d in (None,) + tuple(divisors):
+        cap = None if d is None else max(2, -(-share // d))
+        if str(cap) in table["caps"]:
+            continue
+        b, ms, build_s = timed(cap)
+        table["caps"][str(cap)] = {"ms": ms, "build_s": build_s}
         if verbose:
             print(f"autotune: cap {cap} keys -> {ms:.3f} ms")
         if best is None or ms < best[0]:
@@ -279,5 +334,12 @@ def autotune_batch(problems, *, reps=3, divisors=(1, 2, 3, 4, 6, 8), verbose=Fal
             best = (ms, cap, b)
         else:
             b.close()
-    _tuned[sig] = best[1]
+    chosen = {}
+    for pl in plans:
+        geo = pl.mixed_geometry()
+        chosen[id(pl)] = (geo["kc"], geo["nch"])
+    _tuned[sig] = (chosen, best[1])
+    table["chosen"] = {"shapes": {_plan_label(pl): f"kc{chosen[id(pl)][0]}_nch{chosen[id(pl)][1]}"
+                                  for pl in plans},
+                       "cap": best[1], "ms": best[0]}
     return best[2], table

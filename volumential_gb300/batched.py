@@ -53,16 +53,19 @@ class MixedSchedule:
 
         lib = _lib.lib()
         self.nrhs = int(nrhs)
-        self.workspace = None
+        self._workspace = None
         self.packing = packing if base is None else base.packing
+        # bytes of vl1_eval_mixed's workspace, allocated on first use
+        # (schedules of a batch use the batch's buffer instead)
+        self.workspace_bytes = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view),
+                                                                 self.nrhs))
+        if self.workspace_bytes < 0:
+            raise RuntimeError("vl1_mixed_workspace_bytes failed")
         if base is not None:
             # same plan, tree and nrhs: only the work items differ
             self._init_items(plan, base, max_keys_per_item)
             if workspace:
-                ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
-                if ws < 0:
-                    raise RuntimeError("vl1_mixed_workspace_bytes failed")
-                self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
+                _ = self.workspace
             return
         if packing == "device":
             self._build_on_device(plan, view, keep, stream)
@@ -72,10 +75,17 @@ class MixedSchedule:
             raise ValueError(f"packing must be 'device' or 'greedy', got {packing!r}")
         self._init_items(plan, self, max_keys_per_item)
         if workspace:
-            ws = int(lib.vl1_mixed_workspace_bytes(plan.handle, C.byref(view), self.nrhs))
-            if ws < 0:
-                raise RuntimeError("vl1_mixed_workspace_bytes failed")
-            self.workspace = torch.empty(ws, dtype=torch.uint8, device="cuda")
+            _ = self.workspace
+
+    @property
+    def workspace(self):
+        """Device workspace of ``vl1_eval_mixed`` (allocated on first use)."""
+        if self._workspace is None:
+            import torch
+
+            self._workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8,
+                                          device="cuda")
+        return self._workspace
 
     def _build_on_device(self, plan, view, keep, stream):
         import torch
@@ -169,10 +179,11 @@ class MixedSchedule:
         items, n_splits, n_slots = memo
         self.n_items = len(items)
         self.n_splits = n_splits
-        self.max_keys_per_item = int(max(1, max((it[2] - it[1] for it in items), default=1)))
+        self.max_keys_per_item = int(max(1, (items[:, 2] - items[:, 1]).max()
+                                         if len(items) else 1))
         # host copy (vl1_batch_problem.host_items) and device copy of the items
-        self.items_np = np.ascontiguousarray(np.asarray(items, dtype=np.int32).reshape(-1, 8)
-                                             if items else np.zeros((1, 8), np.int32))
+        self.items_np = np.ascontiguousarray(items if len(items)
+                                             else np.zeros((1, 8), np.int32))
         self.items = torch.from_numpy(self.items_np).to("cuda")
         self.split_counters = torch.zeros(max(1, n_splits * n_chunks), dtype=torch.int32,
                                           device="cuda")
@@ -190,6 +201,9 @@ class MixedSchedule:
         s.n_slots = n_slots
         s.split_counters = self.split_counters.data_ptr()
         s.split_partials = self.split_partials.data_ptr()
+        s.n_chunks = n_chunks
+        self.n_chunks = n_chunks
+        self.geometry = (geo["kc"], geo["nch"])
         self.c_struct = s
 
     @staticmethod
@@ -314,98 +328,30 @@ class MixedSchedule:
                 s_ = int(cand[np.argmax(rem[cand])])
         return out
 
-    # cost model of one work item in units of one key's pipeline time: CTA
-    # start-up, pipeline drain and result write-back; the partial-sum write
-    # of a split part; the sum over the parts that the last part of a split
-    # tile reads back (fitted to measured launches of a 3D q = 4 tree over
-    # caps 12 .. 100000: within ~4 %)
-    ITEM_OVERHEAD_KEYS = 4.0
-    SPLIT_OVERHEAD_KEYS = 1.5
-    LAST_PART_KEYS = 2.0
-    # candidate caps, as fractions of one SM's share of all keys
-    CAP_FRACTIONS = (1.5, 1.25, 1.0, 0.85, 0.75, 0.67, 0.6, 0.5, 0.4, 0.33, 0.25, 0.2, 0.17)
-
     @staticmethod
-    def _split_items(key_start, cap):
-        n_tiles = len(key_start) - 1
-        items = []
-        n_splits = 0
-        n_slots = 0
-        for t in range(n_tiles):
-            k0, k1 = int(key_start[t]), int(key_start[t + 1])
-            nk = k1 - k0
-            nparts = max(1, -(-nk // cap))
-            if nparts == 1:
-                items.append((t, k0, k1, -1, 0, 1, -1, 0))
-                continue
-            bounds = [k0 + (nk * i) // nparts for i in range(nparts + 1)]
-            for part in range(nparts):
-                items.append((t, bounds[part], bounds[part + 1], n_splits, part, nparts,
-                              n_slots + part, 0))
-            n_splits += 1
-            n_slots += nparts
-        items.sort(key=lambda it: -(it[2] - it[1]))   # stable: ties keep tile order
-        return items, n_splits, n_slots
-
-    @classmethod
-    def _makespan(cls, items, n_sm):
-        """Greedy list-scheduling finish time of ``items`` (in key units) on
-        ``n_sm`` one-CTA-per-SM slots, launched in order."""
-        import heapq
-
-        if len(items) <= n_sm:   # one item per slot
-            return cls._makespan_bound(items, n_sm) if items else 0.0
-        slots = [0.0] * n_sm
-        for it in items:
-            cost = (it[2] - it[1]) + cls.ITEM_OVERHEAD_KEYS
-            if it[3] >= 0:
-                cost += cls.SPLIT_OVERHEAD_KEYS + (cls.LAST_PART_KEYS if it[4] == it[5] - 1
-                                                   else 0.0)
-            heapq.heapreplace(slots, slots[0] + cost)
-        return max(slots)
-
-    @classmethod
-    def _work_items(cls, key_start, max_keys_per_item, n_sm=None):
+    def _work_items(key_start, max_keys_per_item, n_sm=None):
         """Work items (one CTA each): whole tiles, and tiles with more than a
         cap of keys split into nearly equal key ranges, ordered longest first
-        (CTAs start in grid order).  Without an explicit cap, the cap among
-        ``CAP_FRACTIONS`` of one SM's share of all keys with the shortest
-        modelled finish time is taken."""
-        total = int(key_start[-1])
-        if max_keys_per_item is not None:
-            return cls._split_items(key_start, max(1, int(max_keys_per_item)))
+        (CTAs start in grid order).  Without an explicit cap, the cap with the
+        shortest modelled finish time is taken (``vl1_mixed_work_items``).
+        Returns (items [n_items, 8] int32, n_splits, n_slots)."""
+        key_start = np.ascontiguousarray(key_start, dtype=np.int32)
+        n_tiles = len(key_start) - 1
+        cap = 0 if max_keys_per_item is None else max(1, int(max_keys_per_item))
         if n_sm is None:
-            import torch
+            n_sm = 1
+            if cap == 0:
+                import torch
 
-            n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()) \
-                .multi_processor_count
-        share = max(1, -(-total // max(1, n_sm)))
-        best = None
-        seen = set()
-        for f in cls.CAP_FRACTIONS:
-            cap = max(4, int(np.ceil(share * f)))
-            if cap in seen:
-                continue
-            seen.add(cap)
-            cand = cls._split_items(key_start, cap)
-            if best is not None and cls._makespan_bound(cand[0], n_sm) > best[0]:
-                continue   # cannot finish sooner (nor tie) than the best so far
-            t = cls._makespan(cand[0], n_sm)
-            if best is None or t < best[0]:
-                best = (t, cand)
-        return best[1]
-
-    @classmethod
-    def _makespan_bound(cls, items, n_sm):
-        """A lower bound of ``_makespan``: the longest item, and the mean load
-        per slot."""
-        if not items:
-            return 0.0
-        costs = [(it[2] - it[1]) + cls.ITEM_OVERHEAD_KEYS +
-                 ((cls.SPLIT_OVERHEAD_KEYS + (cls.LAST_PART_KEYS if it[4] == it[5] - 1
-                                              else 0.0)) if it[3] >= 0 else 0.0)
-                 for it in items]
-        return max(max(costs), sum(costs) / n_sm)
+                n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()) \
+                    .multi_processor_count
+        capacity = int(key_start[-1]) + n_tiles + 1
+        out = np.zeros((capacity, 8), dtype=np.int32)
+        n_items, n_splits, n_slots = C.c_int32(), C.c_int32(), C.c_int32()
+        _lib.check(_lib.lib().vl1_mixed_work_items(
+            key_start.ctypes.data, n_tiles, cap, int(n_sm), out.ctypes.data, capacity,
+            C.byref(n_items), C.byref(n_splits), C.byref(n_slots)), "vl1_mixed_work_items")
+        return out[:n_items.value].copy(), int(n_splits.value), int(n_slots.value)
 
     @staticmethod
     def _check_modes(keep, nq):
@@ -442,7 +388,8 @@ def get_schedule(plan, view, keep, nrhs, stream, max_keys_per_item=None, packing
     ``packing`` None takes whatever schedule is cached for the tree (a new one
     is built on the device); "device" or "greedy" asks for that packing and
     replaces the tree's schedules of the other packing."""
-    key = (id(plan), _tree_token(keep), int(nrhs), max_keys_per_item)
+    geo = plan.mixed_geometry()
+    key = (id(plan), _tree_token(keep), int(nrhs), (geo["kc"], geo["nch"]), max_keys_per_item)
     with _lock:
         hit = _cache.get(key)
         if hit is not None and (packing is None or hit[0].packing == packing):
@@ -451,11 +398,13 @@ def get_schedule(plan, view, keep, nrhs, stream, max_keys_per_item=None, packing
     base = None
     with _lock:
         for k, v in _cache.items():
+            # same plan, tree and nrhs (any tile shape and cap): its tile
+            # arrays are shared, only the work items and split scratch differ
             if k[:3] == key[:3] and (packing is None or v[0].packing == packing):
                 base = v[0]
                 break
     sched = MixedSchedule(plan, view, keep, nrhs, stream, max_keys_per_item, base=base,
-                          packing=packing or "device")
+                          packing=packing or "device", workspace=False)
     with _lock:
         if packing is not None:
             for k in [k for k, v in _cache.items()

@@ -204,11 +204,14 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
   if (!st) {
     // tensor-core digit operands of the blocks
     const MixedGeom g = mixed_geometry(d.nq, d.table_cplx);
+    p->mixed.geom = g;
     const int64_t elems = (int64_t)d.n_tables * d.n_cases * g.n_kc * kDigits * (int64_t)g.np * g.kc;
     void *ptr = nullptr;
     st = plan_alloc(p, &ptr, 2 * (size_t)elems);
     if (!st) {
       p->mixed.adig = static_cast<__half *>(ptr);
+      p->mixed.adig_alloc = p->n_allocs - 1;
+      p->mixed.adig_elems = elems;
       double amax = 0.0;
       const double *tv = static_cast<const double *>(desc->table_data);
       const int64_t ntv = (int64_t)d.n_tables * d.n_entries * (d.table_cplx ? 2 : 1);
@@ -350,6 +353,42 @@ int64_t vl1_mixed_workspace_bytes(const vl1_plan *plan, const vl1_tree_view *tre
                                   int32_t nrhs) {
   if (!plan || !tree || nrhs < 1) return -1;
   return mixed_workspace_bytes(plan, tree->nboxes, tree->n_target_boxes, nrhs);
+}
+
+int32_t vl1_plan_set_mixed_geometry(vl1_plan *plan, int32_t kc, int32_t nch) {
+  if (!plan || (kc != 16 && kc != 32) || (nch != 16 && nch != 32 && nch != 64)) {
+    set_error("vl1_plan_set_mixed_geometry: null plan, K chunk not 16 or 32 or column "
+              "chunk not 16, 32 or 64");
+    return VL1_E_ARG;
+  }
+  const DevDesc &d = plan->d;
+  const MixedGeom g = mixed_geometry(d.nq, d.table_cplx, kc, nch);
+  if (g.kc > g.kp) {
+    set_error("vl1_plan_set_mixed_geometry: K chunk %d above the %d padded source points",
+              kc, g.kp);
+    return VL1_E_ARG;
+  }
+  const MixedGeom &o = plan->mixed.geom;
+  if (g.kc == o.kc && g.nch == o.nch && g.np == o.np && g.kp == o.kp) return VL1_OK;
+  const int64_t elems =
+      (int64_t)d.n_tables * d.n_cases * g.n_kc * kDigits * (int64_t)g.np * g.kc;
+  // no evaluation may be in flight: the old operands are released
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "vl1_plan_set_mixed_geometry: synchronise");
+  void *ptr = nullptr;
+  e = cudaMalloc(&ptr, 2 * (size_t)elems);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(plan digit operands)");
+  const int k = plan->mixed.adig_alloc;
+  cudaFree(plan->allocs[k]);
+  plan->allocs[k] = ptr;
+  plan->device_bytes += 2 * (elems - plan->mixed.adig_elems);
+  plan->mixed.adig = static_cast<__half *>(ptr);
+  plan->mixed.adig_elems = elems;
+  plan->mixed.geom = g;
+  int32_t st = build_mixed_operands(plan, plan->mixed.table_absmax, 0);
+  if (st) return st;
+  e = cudaDeviceSynchronize();
+  return e == cudaSuccess ? VL1_OK : cuda_fail(e, "vl1_plan_set_mixed_geometry: rebuild");
 }
 
 int32_t vl1_mixed_geometry(const vl1_plan *plan, int32_t *out5) {

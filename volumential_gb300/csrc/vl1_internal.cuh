@@ -74,7 +74,9 @@ int32_t launch_expand_blocks(vl1_plan *plan, cudaStream_t s);
 int32_t launch_index_map(vl1_plan *plan, int32_t *rows, int8_t *signs, cudaStream_t s);
 int32_t launch_plain(vl1_plan *plan, const TreeDev &tree, const double *coefs,
                      int coef_cplx, int nrhs, double *result, cudaStream_t s);
-MixedGeom mixed_geometry(int nq, int table_cplx);
+// operand geometry; kc / nch 0: the default choice (else 16 or 32 / 16, 32
+// or 64, validated by the caller)
+MixedGeom mixed_geometry(int nq, int table_cplx, int kc = 0, int nch = 0);
 int32_t build_mixed_operands(vl1_plan *plan, double table_absmax, cudaStream_t s);
 int64_t mixed_workspace_bytes(const vl1_plan *plan, int64_t nboxes, int64_t n_tgt_boxes,
                               int nrhs);

@@ -495,11 +495,12 @@ struct MixedParams {
   int64_t n_particles;
   double *result;
   vl1_status *st;
-  // bounded waits: polls before a wait gives up (0: kSleepPolls); test hook
-  // (vl1_test_set_wait_fault): when nonzero, producer warp 0 of CTA (0, 0)
-  // withholds its arrival for that CTA's first pipeline unit, so that the
-  // tensor-core issuer's wait runs out and the launch reports VL1_E_TIMEOUT
-  uint32_t poll_limit;
+  // bounded waits: microseconds before a wait gives up (0: kWaitLimitUs);
+  // test hook (vl1_test_set_wait_fault): when nonzero, producer warp 0 of CTA
+  // (0, 0) withholds its arrival for that CTA's first pipeline unit, so that
+  // the tensor-core issuer's wait runs out and the launch reports
+  // VL1_E_TIMEOUT
+  uint32_t wait_limit_us;
   int32_t withhold_arrival;
 };
 
@@ -536,8 +537,8 @@ constexpr int kRowsPerProducer = 128 / kProducerWarps;
 constexpr int kLoaderWarp = 8;
 constexpr int kMmaWarp = 9;
 constexpr int kReadWarp0 = 10;
-constexpr uint32_t kSleepNs = 200000;      // longest sleep of one wait poll
-constexpr uint32_t kSleepPolls = 10000;    // polls before a wait gives up (~2 s)
+constexpr uint32_t kSleepNs = 200000;      // suspend hint of one barrier test
+constexpr uint32_t kWaitLimitUs = 2000000; // a wait gives up after 2 s
 // split-tile counters: parts in the low 16 bits, aborted parts also in the
 // high bits (a tile has fewer than 2^16 parts)
 constexpr int kSplitPoison = 1 << 16;
@@ -551,26 +552,50 @@ struct Barriers {
   uint64_t drain;            // after an abort: every issued MMA has completed
 };
 
-// Wait for `phase` of `bar`; gives up (returns false) when another role has
-// set the abort flag, or after `polls` polls (then it sets the flag itself).
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for `phase` of `bar`.  Gives up (returns false) when another role has
+// set the abort flag, or after `limit_us` microseconds (then it sets the
+// flag itself); both are looked at every 32 tests.  A warp whose test fails
+// sleeps between tests, so that waiting warps leave the issue slots of
+// their scheduler to the producer warps that share it: with `backoff` the
+// sleep doubles from 32 ns to 256 ns (warps with slack: producers, readout);
+// without it, it stays at 32 ns (the tensor-core issuer and the table
+// loader, whose reaction time is on the pipeline's critical path).
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t phase,
-                                              volatile int *abort_flag, uint32_t polls) {
-  for (uint32_t i = 0; i < polls; ++i) {
+                                              volatile int *abort_flag, uint32_t limit_us,
+                                              bool backoff) {
+  if (tc::mbar_try_wait_sleep(bar, phase, kSleepNs)) return true;
+  const uint64_t t0 = global_ns();
+  uint32_t ns = 32;
+  for (uint32_t i = 1;; ++i) {
+    __nanosleep(ns);
+    if (backoff) ns = ns < 256 ? 2 * ns : ns;
     if (tc::mbar_try_wait_sleep(bar, phase, kSleepNs)) return true;
-    if (*abort_flag) return false;
+    if ((i & 31u) == 0u) {
+      if (*abort_flag) return false;
+      if (global_ns() - t0 > (uint64_t)limit_us * 1000ull) break;
+    }
   }
   *abort_flag = 1;
   return false;
 }
 
-// Wait for `phase` of `bar` regardless of the abort flag, at most `polls`
-// polls: used after an abort for operations already issued (bulk copies
+// Wait for `phase` of `bar` regardless of the abort flag, at most
+// `limit_us`: used after an abort for operations already issued (bulk copies
 // into this CTA's shared memory, MMAs into its TMEM), which complete on
 // their own, before the CTA releases its TMEM and exits.
-__device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t phase, uint32_t polls) {
-  for (uint32_t i = 0; i < polls; ++i)
-    if (tc::mbar_try_wait_sleep(bar, phase, kSleepNs)) return true;
-  return false;
+__device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t phase, uint32_t limit_us) {
+  const uint64_t t0 = global_ns();
+  while (!tc::mbar_try_wait_sleep(bar, phase, kSleepNs)) {
+    if (global_ns() - t0 > (uint64_t)limit_us * 1000ull) return false;
+    __nanosleep(256);
+  }
+  return true;
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -588,7 +613,7 @@ struct BatchLaunch {
   const BatchItem *items;     // [n_items], launched in this order
   int n_items;
   int *queue;                 // next item to take; zero before the launch
-  uint32_t poll_limit;        // as MixedParams::poll_limit (persistent launches)
+  uint32_t wait_limit_us;     // as MixedParams::wait_limit_us (persistent launches)
   int32_t withhold_arrival;   // as MixedParams::withhold_arrival
 };
 
@@ -640,8 +665,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
-  const uint32_t lim = MULTI ? bl.poll_limit : p1.poll_limit;
-  const uint32_t polls = lim ? lim : kSleepPolls;
+  const uint32_t lim = MULTI ? bl.wait_limit_us : p1.wait_limit_us;
+  const uint32_t limit_us = lim ? lim : kWaitLimitUs;
   // test hook: this CTA's producer warp 0 withholds its first arrival
   const bool withhold = (MULTI ? bl.withhold_arrival : p1.withhold_arrival) != 0 &&
                         blockIdx.x == 0 && blockIdx.y == 0;
@@ -788,7 +813,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     auto expand = [&](int v) -> bool {
       const int s = (ubase + v) % kStages;
       const int use = (ubase + v) / kStages;
-      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, polls))
+      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, limit_us, true))
         return false;
       const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
       uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
@@ -1000,7 +1025,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
           const int s = (ubase + u) % kStages;
           const int use = (ubase + u) / kStages;
-          if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, polls)) {
+          if (use > 0 &&
+              !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, limit_us, false)) {
             aborted = true;
             break;
           }
@@ -1023,7 +1049,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         // copies of the last (up to kStages) issued units may still be in
         // flight into this CTA's stages: let them land before the CTA exits
         for (int v = u - kStages < 0 ? 0 : u - kStages; v < u; ++v)
-          wait_bounded(&bars.afull[(ubase + v) % kStages], ((ubase + v) / kStages) & 1, polls);
+          wait_bounded(&bars.afull[(ubase + v) % kStages], ((ubase + v) / kStages) & 1,
+                       limit_us);
       }
     }
     __syncwarp();
@@ -1036,7 +1063,8 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       for (int round = 0; round < n_rounds && !aborted; ++round) {
         const int R = rbase + round;
         const int b = R & 1;
-        if (R >= 2 && !wait_or_abort(&bars.acce[b], ((R >> 1) - 1) & 1, &s_abort, polls)) {
+        if (R >= 2 &&
+            !wait_or_abort(&bars.acce[b], ((R >> 1) - 1) & 1, &s_abort, limit_us, false)) {
           aborted = true;
           break;
         }
@@ -1045,11 +1073,11 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         for (int iu = 0; iu < upr; ++iu, ++u) {
           const int s = (ubase + u) % kStages;
           const uint32_t ph = ((ubase + u) / kStages) & 1;
-          if (!wait_or_abort(&bars.afull[s], ph, &s_abort, polls)) {
+          if (!wait_or_abort(&bars.afull[s], ph, &s_abort, limit_us, false)) {
             aborted = true;
             break;
           }
-          if (!wait_or_abort(&bars.xfull[s], ph, &s_abort, polls)) {
+          if (!wait_or_abort(&bars.xfull[s], ph, &s_abort, limit_us, false)) {
             aborted = true;
             break;
           }
@@ -1083,7 +1111,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         // MMAs issued before the abort still write TMEM and read the stages:
         // wait for all of them before the TMEM is released
         tc::mma_commit(&bars.drain);
-        wait_bounded(&bars.drain, 0, polls);
+        wait_bounded(&bars.drain, 0, limit_us);
       }
     }
     __syncwarp();
@@ -1105,7 +1133,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
     for (int round = 0; round < n_rounds; ++round) {
       const int R = rbase + round;
       const int b = R & 1;
-      if (!wait_or_abort(&bars.accf[b], (R >> 1) & 1, &s_abort, polls)) {
+      if (!wait_or_abort(&bars.accf[b], (R >> 1) & 1, &s_abort, limit_us, true)) {
         ok = false;
         break;
       }
@@ -1338,16 +1366,18 @@ int grid_for(int64_t n, int threads) {
 
 }  // namespace
 
-MixedGeom mixed_geometry(int nq, int table_cplx) {
+MixedGeom mixed_geometry(int nq, int table_cplx, int kc, int nch) {
   MixedGeom g;
   g.kp = ((nq + 15) / 16) * 16;
-  g.kc = g.kp <= 32 ? g.kp : 32;
-  // above one chunk, K is whole exact rounds of 64 (two chunks of 32)
+  g.kc = kc ? kc : (g.kp <= 32 ? g.kp : 32);
+  // above one chunk of 32, K is whole exact rounds of 64
   if (g.kp > 32) g.kp = ((g.kp + 63) / 64) * 64;
   g.n_kc = g.kp / g.kc;
   const int n = table_cplx ? 2 * nq : nq;
   g.np = ((n + 15) / 16) * 16;
-  if (g.np <= 16) {
+  if (nch) {
+    g.nch = nch;
+  } else if (g.np <= 16) {
     g.nch = 16;
   } else if (g.np <= 32) {
     g.nch = 32;
@@ -1360,10 +1390,10 @@ MixedGeom mixed_geometry(int nq, int table_cplx) {
 
 int32_t build_mixed_operands(vl1_plan *plan, double table_absmax, cudaStream_t s) {
   const DevDesc &d = plan->d;
-  MixedGeom g = mixed_geometry(d.nq, d.table_cplx);
+  const MixedGeom g = plan->mixed.geom;
+  plan->mixed.table_absmax = table_absmax;
   int e = 0;
   if (table_absmax > 0) frexp(table_absmax, &e);
-  plan->mixed.geom = g;
   plan->mixed.a_exp = table_absmax > 0 ? e : 0;
   const int64_t n_elems =
       (int64_t)d.n_tables * d.n_cases * g.n_kc * kDigits * (int64_t)g.np * g.kc;
@@ -1400,9 +1430,10 @@ int32_t launch_classify(vl1_plan *plan, const TreeDev &tree, int32_t *keys, cuda
 // stream right before and after the tensor-core kernel launches.
 cudaEvent_t g_kernel_begin = nullptr, g_kernel_end = nullptr;
 
-// Test hook (vl1_test_set_wait_fault): poll limit of the kernel's bounded
-// waits (0: the default) and the withheld arrival of CTA (0, 0).
-uint32_t g_test_poll_limit = 0;
+// Test hook (vl1_test_set_wait_fault): time limit of the kernel's bounded
+// waits in microseconds (0: the default) and the withheld arrival of CTA
+// (0, 0).
+uint32_t g_test_wait_limit_us = 0;
 int32_t g_test_withhold = 0;
 
 int32_t record_kernel_event(cudaEvent_t ev, cudaStream_t s) {
@@ -1421,6 +1452,11 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   if (!workspace || ws_bytes < need) {
     set_error("mixed workspace of %lld bytes required, %lld given", (long long)need,
               (long long)ws_bytes);
+    return VL1_E_ARG;
+  }
+  if (sched.n_splits > 0 && sched.n_chunks != g.np / g.nch) {
+    set_error("the schedule's split scratch is for %d column chunks, the plan has %d",
+              sched.n_chunks, g.np / g.nch);
     return VL1_E_ARG;
   }
   uint8_t *w = static_cast<uint8_t *>(workspace);
@@ -1478,7 +1514,7 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.n_particles = tree.n_particles;
   mp.result = result;
   mp.st = plan->status;
-  mp.poll_limit = g_test_poll_limit;
+  mp.wait_limit_us = g_test_wait_limit_us;
   mp.withhold_arrival = g_test_withhold;
   if (!mixed_kernel_ptr(g.nch, g.kc, false)) {
     set_error("mixed path: unsupported column chunk %d / K chunk %d", g.nch, g.kc);
@@ -1605,6 +1641,11 @@ int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t
     if (!mixed_kernel_ptr(g.nch, g.kc, true)) {
       set_error("%s: problem %d: unsupported kernel shape", who, i);
       return VL1_E_UNSUPPORTED;
+    }
+    if (sc.n_splits > 0 && sc.n_chunks != g.np / g.nch) {
+      set_error("%s: problem %d: the schedule's split scratch is for %d column chunks, the "
+                "plan has %d", who, i, sc.n_chunks, g.np / g.nch);
+      return VL1_E_ARG;
     }
     L.nrows[i] = tr.nboxes * q.nrhs;
     if (L.nrows[i] >= INT32_MAX) {
@@ -1974,7 +2015,7 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
   for (const SoloLaunch &sl : b->solos) {
     const BatchLaunch none{};
     MixedParams mp = sl.mp;
-    mp.poll_limit = g_test_poll_limit;
+    mp.wait_limit_us = g_test_wait_limit_us;
     mp.withhold_arrival = g_test_withhold;
     void *args[] = {&mp, const_cast<BatchLaunch *>(&none)};
     e = cudaLaunchKernel(mixed_kernel_ptr(sl.nch, sl.kc, false), dim3(sl.grid_x, sl.grid_y),
@@ -1988,7 +2029,7 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
     bl.items = static_cast<const BatchItem *>(b->d_items) + g.item0;
     bl.n_items = g.n_items;
     bl.queue = b->d_queue + gi;
-    bl.poll_limit = g_test_poll_limit;
+    bl.wait_limit_us = g_test_wait_limit_us;
     bl.withhold_arrival = g_test_withhold;
     void *args[] = {const_cast<MixedParams *>(&unused), &bl};
     e = cudaLaunchKernel(mixed_kernel_ptr(g.nch, g.kc, true), dim3(g.grid),
@@ -2012,12 +2053,20 @@ extern "C" int32_t vl1_batch_destroy(vl1_batch *b) {
 
 extern "C" int64_t vl1_batch_device_bytes(const vl1_batch *b) { return b ? b->bytes : -1; }
 
-extern "C" int32_t vl1_test_set_wait_fault(int32_t poll_limit, int32_t withhold_arrival) {
-  if (poll_limit < 0) {
-    set_error("vl1_test_set_wait_fault: negative poll limit");
+extern "C" int32_t vl1_batch_kernel_launches(const vl1_batch *b) {
+  if (!b) return -1;
+  int n = 0;
+  if (b->n_tasks > 0) n += 1 + (b->n_ttasks > 0 ? 1 : 0);
+  if (b->has_disp && b->n_tasks > 0) n += 1 + (b->n_ttasks > 0 ? 1 : 0);
+  return n + (int)b->solos.size() + (int)b->groups.size();
+}
+
+extern "C" int32_t vl1_test_set_wait_fault(int32_t wait_limit_us, int32_t withhold_arrival) {
+  if (wait_limit_us < 0) {
+    set_error("vl1_test_set_wait_fault: negative wait limit");
     return VL1_E_ARG;
   }
-  vl1::g_test_poll_limit = (uint32_t)poll_limit;
+  vl1::g_test_wait_limit_us = (uint32_t)wait_limit_us;
   vl1::g_test_withhold = withhold_arrival != 0;
   return VL1_OK;
 }

@@ -28,6 +28,8 @@ struct MixedGeom {
 
 struct MixedPlan {
   MixedGeom geom;
+  double table_absmax;      // largest |table value| (real and imaginary parts)
+  int adig_alloc;           // index of adig in the plan's allocations
   int a_exp;                // 2^a_exp > max |table value|
   __half *adig;             // [key][kchunk][digit][np][kc] FP16 digits, swizzled K-major tiles
   int64_t adig_elems;

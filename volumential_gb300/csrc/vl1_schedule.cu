@@ -27,6 +27,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <cmath>
 #include <numeric>
 #include <vector>
 
@@ -544,4 +545,134 @@ extern "C" int32_t vl1_schedule_builder_destroy(vl1_schedule_builder *b) {
   cudaError_t e = b->buf ? cudaFree(b->buf) : cudaSuccess;
   delete b;
   return e == cudaSuccess ? VL1_OK : cuda_fail(e, "cudaFree(schedule builder)");
+}
+
+// ---------------------------------------------------------------------------
+// Work items of a schedule (host code; the cost model of the Python layer's
+// MixedSchedule, run per new tree, so kept out of Python).
+
+namespace {
+
+// cost of one work item in units of one key's pipeline time: CTA start-up,
+// pipeline drain and result write-back; the partial-sum write of a split
+// part; the sum over the parts that the last part of a split tile reads back
+// (fitted to measured launches of a 3D q = 4 tree over caps 12 .. 100000:
+// within ~4 %)
+constexpr double kItemOverheadKeys = 4.0;
+constexpr double kSplitOverheadKeys = 1.5;
+constexpr double kLastPartKeys = 2.0;
+// candidate caps, as fractions of one SM's share of all keys
+constexpr double kCapFractions[] = {1.5, 1.25, 1.0, 0.85, 0.75, 0.67, 0.6,
+                                    0.5, 0.4, 0.33, 0.25, 0.2, 0.17};
+
+struct SplitResult {
+  std::vector<vl1_mixed_item> items;
+  int n_splits = 0, n_slots = 0;
+};
+
+// tiles with more than `cap` keys split into nearly equal key ranges; items
+// longest first (ties keep tile order)
+SplitResult split_items(const int32_t *ks, int n_tiles, int cap) {
+  SplitResult r;
+  for (int t = 0; t < n_tiles; ++t) {
+    const int k0 = ks[t], k1 = ks[t + 1], nk = k1 - k0;
+    const int nparts = std::max(1, (nk + cap - 1) / cap);
+    if (nparts == 1) {
+      r.items.push_back(vl1_mixed_item{t, k0, k1, -1, 0, 1, -1, 0});
+      continue;
+    }
+    for (int part = 0; part < nparts; ++part) {
+      const int b0 = k0 + (int)(((int64_t)nk * part) / nparts);
+      const int b1 = k0 + (int)(((int64_t)nk * (part + 1)) / nparts);
+      r.items.push_back(vl1_mixed_item{t, b0, b1, r.n_splits, part, nparts, r.n_slots + part, 0});
+    }
+    ++r.n_splits;
+    r.n_slots += nparts;
+  }
+  std::stable_sort(r.items.begin(), r.items.end(),
+                   [](const vl1_mixed_item &a, const vl1_mixed_item &b) {
+                     return (a.key_end - a.key_begin) > (b.key_end - b.key_begin);
+                   });
+  return r;
+}
+
+double item_cost(const vl1_mixed_item &it) {
+  double c = (it.key_end - it.key_begin) + kItemOverheadKeys;
+  if (it.split >= 0) c += kSplitOverheadKeys + (it.part == it.nparts - 1 ? kLastPartKeys : 0.0);
+  return c;
+}
+
+// lower bound of the finish time: the longest item, and the mean load per slot
+double makespan_bound(const std::vector<vl1_mixed_item> &items, int n_sm) {
+  if (items.empty()) return 0.0;
+  double mx = 0.0, sum = 0.0;
+  for (const vl1_mixed_item &it : items) {
+    const double c = item_cost(it);
+    mx = std::max(mx, c);
+    sum += c;
+  }
+  return std::max(mx, sum / n_sm);
+}
+
+// greedy list-scheduling finish time on n_sm one-CTA-per-SM slots, in order
+double makespan(const std::vector<vl1_mixed_item> &items, int n_sm) {
+  if ((int)items.size() <= n_sm) return items.empty() ? 0.0 : makespan_bound(items, n_sm);
+  std::vector<double> heap(n_sm, 0.0);   // min-heap
+  auto cmp = [](double a, double b) { return a > b; };
+  for (const vl1_mixed_item &it : items) {
+    std::pop_heap(heap.begin(), heap.end(), cmp);
+    heap.back() += item_cost(it);
+    std::push_heap(heap.begin(), heap.end(), cmp);
+  }
+  return *std::max_element(heap.begin(), heap.end());
+}
+
+}  // namespace
+
+extern "C" int32_t vl1_mixed_work_items(const int32_t *key_start, int32_t n_tiles, int32_t cap,
+                                        int32_t n_sm, vl1_mixed_item *items, int32_t capacity,
+                                        int32_t *n_items, int32_t *n_splits,
+                                        int32_t *n_slots) {
+  if (!key_start || n_tiles < 0 || n_sm < 1 || !n_items || !n_splits || !n_slots) {
+    set_error("vl1_mixed_work_items: null argument, n_tiles < 0 or n_sm < 1");
+    return VL1_E_ARG;
+  }
+  for (int t = 0; t < n_tiles; ++t)
+    if (key_start[t + 1] < key_start[t]) {
+      set_error("vl1_mixed_work_items: key_start decreases at tile %d", t);
+      return VL1_E_ARG;
+    }
+  SplitResult best;
+  if (cap > 0) {
+    best = split_items(key_start, n_tiles, cap);
+  } else {
+    const int64_t total = key_start[n_tiles];
+    const int64_t share = std::max<int64_t>(1, (total + n_sm - 1) / n_sm);
+    double best_t = 0.0;
+    bool have = false;
+    std::vector<int> seen;
+    for (double f : kCapFractions) {
+      const int c = std::max(4, (int)std::ceil((double)share * f));
+      if (std::find(seen.begin(), seen.end(), c) != seen.end()) continue;
+      seen.push_back(c);
+      SplitResult cand = split_items(key_start, n_tiles, c);
+      if (have && makespan_bound(cand.items, n_sm) > best_t) continue;
+      const double t = makespan(cand.items, n_sm);
+      if (!have || t < best_t) {
+        best_t = t;
+        best = std::move(cand);
+        have = true;
+      }
+    }
+  }
+  *n_items = (int32_t)best.items.size();
+  *n_splits = best.n_splits;
+  *n_slots = best.n_slots;
+  if (!items || capacity < (int32_t)best.items.size()) {
+    set_error("vl1_mixed_work_items: %d items need room, %d given", (int)best.items.size(),
+              capacity);
+    return VL1_E_ARG;
+  }
+  std::copy(best.items.begin(), best.items.end(), items);
+  return VL1_OK;
 }

@@ -21,6 +21,7 @@
 
 #include <cstdint>
 
+#include "vl1_hash.cuh"
 #include "vl1_internal.cuh"
 
 namespace vl1 {
@@ -30,16 +31,6 @@ constexpr int kMaxCand = 27 + 8 + 56;   // 3D: same + coarser + finer
 constexpr int kTreeThreads = 256;
 constexpr int kScanThreads = 1024;
 constexpr int kScanTile = 4 * kScanThreads;   // counts per scan block
-
-__device__ __forceinline__ uint64_t mix64(uint64_t x) {
-  // MurmurHash3's 64-bit finaliser (public domain): spreads keys over the table
-  x ^= x >> 33;
-  x *= 0xff51afd7ed558ccdull;
-  x ^= x >> 33;
-  x *= 0xc4ceb9fe1a85ec53ull;
-  x ^= x >> 33;
-  return x;
-}
 
 struct CsrArgs {
   int dim, nboxes, n_leaves, max_level;
@@ -55,18 +46,6 @@ struct CsrArgs {
   int32_t *lists;
   int32_t *status;            // [1]: 0 ok, 1 table full, 2 bad input
 };
-
-__device__ __forceinline__ long long level_offset(int dim, int lev) {
-  long long o = 0;
-  for (int j = 0; j < lev; ++j) o += 1ll << (dim * j);
-  return o;
-}
-
-__device__ __forceinline__ long long box_key(int dim, int lev, const long long *c) {
-  long long k = 0;
-  for (int a = 0; a < dim; ++a) k = (k << lev) | c[a];
-  return level_offset(dim, lev) + k;
-}
 
 __global__ void hash_insert_kernel(const CsrArgs A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -323,6 +323,27 @@ class Plan:
         _lib.check(self._lib.vl1_mixed_geometry(self.handle, out), "vl1_mixed_geometry")
         return dict(zip(("kp", "kc", "n_kc", "np", "nch"), list(out)))
 
+    def set_mixed_geometry(self, kc, nch):
+        """Tile shape of the tensor-core kernel: ``kc`` source points per
+        pipeline unit (16 or 32), ``nch`` output columns per CTA (16, 32 or
+        64).  Schedules are cached per shape."""
+        _lib.check(self._lib.vl1_plan_set_mixed_geometry(self.handle, int(kc), int(nch)),
+                   "vl1_plan_set_mixed_geometry")
+
+    def mixed_shapes(self):
+        """The tile shapes (kc, nch) this plan can take."""
+        geo = self.mixed_geometry()
+        n = self.nq * (2 if self.complex_table else 1)
+        out = []
+        for kc in (16, 32):
+            if kc > geo["kp"]:
+                continue
+            for nch in (16, 32, 64):
+                if nch > 16 and -(-n // 16) * 16 <= nch // 2:
+                    continue   # all padding beyond half a chunk
+                out.append((kc, nch))
+        return out
+
     def read_status(self, stream=None, reset=True):
         s = _lib.Status()
         _lib.check(self._lib.vl1_status_read(self.handle, C.byref(s), int(reset),

@@ -35,6 +35,9 @@ __all__ = [
     "build_adaptive_tree",
     "build_tree_from_leaves",
     "build_list1_traversal",
+    "build_list1_traversal_device",
+    "build_tree_from_leaves_device",
+    "build_adaptive_tree_device",
 ]
 
 
@@ -117,7 +120,8 @@ class Traversal:
 
     @property
     def nnz(self):
-        return int(self.neighbor_source_boxes_lists.size)
+        lists = self.neighbor_source_boxes_lists
+        return int(lists.numel() if hasattr(lists, "numel") else lists.size)
 
 
 # {{{ keys: one int64 per (level, integer coordinates)
@@ -367,12 +371,17 @@ def build_list1_traversal_device(tree: ParticleTree, stream=None, as_numpy=True)
     from . import _lib
 
     dim = tree.dim
-    leaves = np.ascontiguousarray(tree.leaf_boxes, dtype=np.int32)
-    n_leaves = len(leaves)
-    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to("cuda")  # noqa: E731
-    levels = dev(tree.box_levels.astype(np.uint8))
-    coords = dev(tree.box_coords.astype(np.int32))
-    lv = dev(leaves)
+
+    def dev(a, dt):   # host arrays or CUDA tensors of a tree built on the device
+        if torch.is_tensor(a):
+            return a.to(device="cuda", dtype=dt).contiguous()
+        return torch.from_numpy(np.ascontiguousarray(a)).to(device="cuda", dtype=dt)
+
+    levels = dev(tree.box_levels, torch.uint8)
+    coords = dev(tree.box_coords, torch.int32)
+    lv = dev(tree.leaf_boxes, torch.int32)
+    n_leaves = int(lv.numel())
+    leaves = lv.cpu().numpy() if as_numpy else lv
     lib = _lib.lib()
     ws = torch.empty(int(lib.vl1_list1_csr_workspace_bytes(n_leaves)), dtype=torch.uint8,
                      device="cuda")
@@ -381,7 +390,7 @@ def build_list1_traversal_device(tree: ParticleTree, stream=None, as_numpy=True)
     lists = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
     d = _lib.CsrDesc()
     d.dim, d.nboxes, d.n_leaves = dim, int(tree.nboxes), n_leaves
-    d.max_level = int(tree.box_levels.max())
+    d.max_level = int(levels.max()) if n_leaves else 0
     d.box_levels, d.box_coords, d.leaf_boxes = levels.data_ptr(), coords.data_ptr(), lv.data_ptr()
     d.starts, d.lists, d.lists_capacity = starts.data_ptr(), lists.data_ptr(), cap
     d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
@@ -396,3 +405,135 @@ def build_list1_traversal_device(tree: ParticleTree, stream=None, as_numpy=True)
     return Traversal(tree=tree, target_boxes=lv, neighbor_source_boxes_starts=starts,
                      neighbor_source_boxes_lists=lists)
 
+
+
+# {{{ trees built on the device
+
+def _ref_rule(dim, q):
+    """Reference nodes [dim, q^dim] on [-1, 1] (meshgrid "ij") and the
+    products of their weights [q^dim], as the host builder forms them."""
+    x, w = gauss_legendre_unit(q)
+    grids = np.meshgrid(*([x] * dim), indexing="ij")
+    ref = np.stack([g.ravel() for g in grids], axis=0)
+    wgrid = np.meshgrid(*([w] * dim), indexing="ij")
+    wref = np.prod(np.stack([g.ravel() for g in wgrid], axis=0), axis=0)
+    return np.ascontiguousarray(ref), np.ascontiguousarray(wref)
+
+
+def build_tree_from_leaves_device(leaf_levels, leaf_coords, *, dim, q_order, a=-0.5, b=0.5,
+                                  balance=True, stream=None, as_numpy=True):
+    """:func:`build_tree_from_leaves` on the GPU (``vl1_tree_balance``,
+    ``vl1_tree_build_*``): optional 2:1 level restriction of the leaves
+    (``leaf_levels`` [n] and integer ``leaf_coords`` [n, dim], device or host
+    arrays), then the boxes, centres and Gauss-Legendre particles.  The
+    arrays equal the host builder's (the weights to an ulp: the host raises
+    the half extent to the power dim with ``pow``).  ``as_numpy=False``
+    returns a tree whose arrays are CUDA tensors."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib
+
+    dim, q = int(dim), int(q_order)
+    lib = _lib.lib()
+    sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    lv = torch.as_tensor(np.asarray(leaf_levels) if not torch.is_tensor(leaf_levels)
+                         else leaf_levels).to(device="cuda", dtype=torch.uint8)
+    co = torch.as_tensor(np.asarray(leaf_coords) if not torch.is_tensor(leaf_coords)
+                         else leaf_coords).to(device="cuda", dtype=torch.int32).reshape(-1, dim)
+    n = int(lv.numel())
+    if balance:
+        cap = max(n, 1) * 4 + 64
+        while True:
+            lvb = torch.empty(cap, dtype=torch.uint8, device="cuda")
+            cob = torch.empty((cap, dim), dtype=torch.int32, device="cuda")
+            lvb[:n] = lv
+            cob[:n] = co
+            nn = C.c_int32(n)
+            st = lib.vl1_tree_balance(dim, C.byref(nn), cap, lvb.data_ptr(), cob.data_ptr(),
+                                      C.c_void_p(sh))
+            if st == _lib.VL1_E_ARG and "capacity" in _lib.last_error():
+                cap *= 4
+                continue
+            _lib.check(st, "vl1_tree_balance")
+            lv, co, n = lvb[:nn.value], cob[:nn.value].contiguous(), nn.value
+            break
+    root_extent = float(b - a)
+    rv = np.full(dim, float(a))
+    sizes = (C.c_int32 * 3)()
+    bld = C.c_void_p()
+    _lib.check(lib.vl1_tree_build_begin(dim, q, n, lv.data_ptr(), co.data_ptr(), root_extent,
+                                        rv.ctypes.data, C.byref(bld), sizes, C.c_void_p(sh)),
+               "vl1_tree_build_begin")
+    try:
+        nboxes, aligned, max_level = int(sizes[0]), int(sizes[1]), int(sizes[2])
+        level_start = np.empty(max_level + 2, dtype=np.int32)
+        _lib.check(lib.vl1_tree_build_level_starts(bld, level_start.ctypes.data),
+                   "vl1_tree_build_level_starts")
+        nq = q ** dim
+        ref, wref = _ref_rule(dim, q)
+        dev = lambda shape, dt: torch.empty(shape, dtype=dt, device="cuda")  # noqa: E731
+        out = {"levels": dev(nboxes, torch.uint8), "coords": dev((nboxes, dim), torch.int32),
+               "centers": dev((dim, aligned), torch.float64),
+               "is_leaf": dev(nboxes, torch.uint8), "starts": dev(nboxes, torch.int32),
+               "counts": dev(nboxes, torch.int32), "leaf_boxes": dev(n, torch.int32),
+               "targets": dev((dim, n * nq), torch.float64),
+               "weights": dev(n * nq, torch.float64)}
+        _lib.check(lib.vl1_tree_build_fill(
+            bld, ref.ctypes.data, wref.ctypes.data, out["levels"].data_ptr(),
+            out["coords"].data_ptr(), out["centers"].data_ptr(), out["is_leaf"].data_ptr(),
+            out["starts"].data_ptr(), out["counts"].data_ptr(), out["leaf_boxes"].data_ptr(),
+            out["targets"].data_ptr(), out["weights"].data_ptr(), C.c_void_p(sh)),
+            "vl1_tree_build_fill")
+    finally:
+        lib.vl1_tree_builder_destroy(bld)
+    cv = (lambda t: t.cpu().numpy()) if as_numpy else (lambda t: t)
+    return ParticleTree(
+        dim=dim, q_order=q, root_extent=root_extent, root_vertex=rv, nboxes=nboxes,
+        aligned_nboxes=aligned, box_centers=cv(out["centers"]), box_levels=cv(out["levels"]),
+        box_coords=cv(out["coords"].to(torch.int64)),
+        box_is_leaf=cv(out["is_leaf"].to(torch.bool)), box_target_starts=cv(out["starts"]),
+        box_target_counts_nonchild=cv(out["counts"]), leaf_boxes=cv(out["leaf_boxes"]),
+        targets=cv(out["targets"]), weights=cv(out["weights"]), level_start_box_nrs=level_start)
+
+
+def build_adaptive_tree_device(dim, q_order, refine_fn, *, max_level, min_level=0, a=-0.5,
+                               b=0.5, stream=None, as_numpy=True):
+    """:func:`build_adaptive_tree` with the tree on the GPU: per level, the
+    nodes of the active boxes are formed on the device and
+    ``refine_fn(nodes)`` (a CUDA tensor [dim, n_boxes, q^dim] -> bool tensor
+    [n_boxes], e.g. a density's variation over a leaf) decides the splits;
+    then the 2:1 restriction and the assembly run on the device."""
+    import itertools as it
+
+    import torch
+
+    dim, q = int(dim), int(q_order)
+    root_extent = float(b - a)
+    ref = torch.from_numpy(_ref_rule(dim, q)[0]).to("cuda")
+    kids = torch.tensor(list(it.product((0, 1), repeat=dim)), dtype=torch.int64, device="cuda")
+    lev_list, coord_list = [], []
+    active = torch.zeros((1, dim), dtype=torch.int64, device="cuda")
+    for lev in range(0, int(max_level) + 1):
+        if active.shape[0] == 0:
+            break
+        if lev < min_level:
+            split = torch.ones(active.shape[0], dtype=torch.bool, device="cuda")
+        elif lev == max_level:
+            split = torch.zeros(active.shape[0], dtype=torch.bool, device="cuda")
+        else:
+            ext = root_extent / 2 ** lev
+            ctr = a + (active.to(torch.float64) + 0.5) * ext
+            nodes = ctr.T[:, :, None] + 0.5 * ext * ref[:, None, :]
+            split = torch.as_tensor(refine_fn(nodes), device="cuda").to(torch.bool)
+        keep = active[~split]
+        lev_list.append(torch.full((keep.shape[0],), lev, dtype=torch.uint8, device="cuda"))
+        coord_list.append(keep)
+        active = (active[split][:, None, :] * 2 + kids[None]).reshape(-1, dim)
+    levels = torch.cat(lev_list)
+    coords = torch.cat(coord_list).to(torch.int32)
+    return build_tree_from_leaves_device(levels, coords, dim=dim, q_order=q, a=a, b=b,
+                                         balance=True, stream=stream, as_numpy=as_numpy)
+
+# }}}

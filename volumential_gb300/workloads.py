@@ -280,39 +280,44 @@ def config_c3(seed=3000, nrhs=256, k=20.0, tables="duffy", level=6):
     return w
 
 
-def config_c4(seed=4000, n_problems=64, levels=(3, 5), qs=(3, 4, 5), nrhs_range=(1, 32),
-              terms=(4, 16), width_range=(0.01, 0.1)):
+def config_c4(seed=4000, n_problems=64, levels=(3, 6), qs=(3, 4, 5), nrhs_range=(1, 32),
+              terms=(4, 16), width_range=(0.01, 0.1), tables="duffy", device_lists=True):
     """Uneven batch: ``n_problems`` independent 3D Laplace problems on uniform
-    octrees, level uniform in ``levels``, q uniform in ``qs``, rhs count
-    uniform in ``nrhs_range``, each density a sum of ``terms`` Gaussians.
+    octrees, level uniform in ``levels`` (inclusive), q uniform in ``qs``, rhs
+    count uniform in ``nrhs_range``, each density a sum of ``terms`` Gaussians.
 
     The densities are not evaluated here (``coefs`` has shape [nrhs, 0]):
     the mixtures are in ``meta["mixtures"]`` and are evaluated on the device
-    (``GaussianMixture.on_device``).  Problems of one q share one table set.
-    The configuration text asks for levels 3..6; level 6 is left out of the
-    default because one level-6, q=5 problem with 32 right-hand sides alone
-    holds 32.8M points x 32 densities (8.4 GB of coefficients and as much
-    output), and the 64-problem mix would not fit one run's device and host
-    budget.
+    (``GaussianMixture.on_device``).  Problems of one q share one table set
+    (3D Laplace, FP64 Duffy build unless ``tables="synthetic"``) and problems
+    of one (level, q) share one tree; ``device_lists`` builds the list-1 CSR
+    on the GPU (a level-6 octree takes ~4 s on the host).
     """
+    from .tree_build import build_list1_traversal_device
+
     rng = np.random.default_rng(seed)
     kernel = LaplaceKernel(3)
-    tables = {}
+    table_sets = {}
+    trees = {}
     out = []
     for i in range(n_problems):
         lev = int(rng.integers(levels[0], levels[1] + 1))
         q = int(rng.choice(qs))
         nrhs = int(rng.integers(nrhs_range[0], nrhs_range[1] + 1))
-        tree = build_uniform_tree(3, lev, q)
-        trav = build_list1_traversal(tree)
+        if (lev, q) not in trees:
+            tree = build_uniform_tree(3, lev, q)
+            trees[(lev, q)] = (build_list1_traversal_device(tree) if device_lists
+                               else build_list1_traversal(tree))
+        trav = trees[(lev, q)]
         mixes = [random_gaussian_mixture(rng, 3, int(rng.integers(terms[0], terms[1] + 1)),
                                          width_range) for _ in range(nrhs)]
-        if q not in tables:
-            tables[q] = synthetic_tables(3, q, kernel, seed=seed + 17 + q,
-                                         source_box_extent=tree.root_extent)
-        out.append(Workload(f"c4_p{i:02d}_l{lev}_q{q}", 3, q, kernel, trav, tables[q],
+        if q not in table_sets:
+            table_sets[q] = make_tables(tables, 3, q, kernel, seed=seed + 17 + q,
+                                        source_box_extent=trav.tree.root_extent)
+        out.append(Workload(f"c4_p{i:02d}_l{lev}_q{q}", 3, q, kernel, trav, table_sets[q],
                             np.zeros((nrhs, 0)), seed,
-                            meta={"level": lev, "mixtures": mixes, "table_key": q}))
+                            meta={"level": lev, "mixtures": mixes, "table_key": q,
+                                  "tree_key": (lev, q), "tables": tables}))
     return out
 
 
