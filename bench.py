@@ -807,7 +807,8 @@ def c4_main(args):
                    "problems_per_level": {str(l): levels.count(l)
                                           for l in range(3, args.c4_max_level + 1)},
                    "q": [3, 4, 5], "nrhs": [1, 32], "points_x_rhs": pts,
-                   "point_pairs_x_rhs": pairs, "tables": _table_source(ws[0]),
+                   "point_pairs_x_rhs": pairs,
+                   "tables": "; ".join(sorted({_table_source(w) for w in ws})),
                    "l2": "inputs (%.1f GB) far larger than L2" %
                          (sum(p.coefs.numel() * 8 for p in probs) / 1e9),
                    "path": "batch, CUDA graph replay", "waves": 1},

@@ -256,12 +256,12 @@ int32_t vl1_plan_set_mixed_geometry(vl1_plan *plan, int32_t kc, int32_t nch);
 
 /* Mixed-precision list-1 evaluation on the tensor cores: the same sum as
  * vl1_eval_fp64 (list1.py:1050-1159) computed from exact FP16 digit products:
- * table values as 5 balanced base-256 digits of a 39-bit fixed-point form,
- * scaled densities as 39-bit fixed point against each density row's own
- * power-of-two scale (requantised to each target row's reference scale),
- * exact FP32 partial sums of digit products, exact int64 sums and one
- * rounding to FP64; the relative error is ~2^-35 of an output's largest
- * contribution.
+ * table values and scaled densities as 5 balanced base-256 digits of a
+ * 39-bit fixed-point form (the table against one power-of-two scale per
+ * plan, the densities against one per right-hand side), exact FP32 partial
+ * sums of digit products, exact int64 sums and one rounding to FP64; each
+ * output's error is a few 2^-39 of (largest |table value|) x (largest
+ * |scaled density| of its rhs) x (its number of source points).
  * coefs: real [nrhs][n_particles] float64; result as in vl1_eval_fp64.
  * workspace: caller-provided device memory of vl1_mixed_workspace_bytes. */
 int32_t vl1_eval_mixed(vl1_plan *plan, const vl1_tree_view *tree,

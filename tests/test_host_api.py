@@ -647,9 +647,13 @@ def test_c5_mix_follows_its_sampling_rules():
     for key, p in probs.items():
         assert p.n_points == (2 ** p.dim) ** p.level * p.q ** p.dim
         assert p.q in (3, 4, 5)
-        assert (p.k == 0) == (p.kernel == "laplace") and 0 <= p.k <= 30
+        assert (p.k == 0) == (p.kernel == "laplace")
+        assert p.kernel == "laplace" or 1 <= p.k <= 30
         assert p.table_key == (p.dim, p.kernel, p.k, p.q)
         assert len(mixes[key]) == 4
+    # k is drawn from the real interval, not its integers
+    ks = [p.k for p in probs.values() if p.kernel == "helmholtz"]
+    assert len(set(ks)) == len(ks) and any(k != int(k) for k in ks)
     # nearest level in log: 2D q4 N=5000 -> level 4 (4096), 3D q3 N=3e5 -> 4 (110,592)
     assert _nearest_level(2, 4, 5000) == 4 and _nearest_level(3, 3, 3e5) == 4
     t = poisson_arrivals(20000, 1000.0, seed=1)

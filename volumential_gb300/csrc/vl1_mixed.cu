@@ -11,22 +11,23 @@
 // chunks of <= 64).
 //
 // Exactness (an Ozaki-type split).  The table blocks (per plan) and x' (per
-// call) are written in fixed point against per-plan / per-row power-of-two
-// scales, both as 39-bit magnitudes: the table in balanced base-256 digits
-// (|digit| <= 128, times the value's sign), the densities as a 7-bit top
-// digit and four base-256 digits carrying the value's sign (|digit| <= 127
-// for the top one, <= 255 for the others), all held exactly in FP16.
-// Densities are stored as bytes (sign in bit 7 of the top digit) and expanded
-// to FP16 in shared memory.  A diagonal i + j of digit products summed over
-// K <= 64 source points is an integer below 2^22 for i + j <= 3 and below
-// 2^24 for i + j = 4, exact in the FP32 accumulator.  Those diagonals (the
-// leading 32 bits) get their own TMEM accumulator, re-initialised per K round
-// and read after every round into int64 registers: one FADD with 1.5 * 2^23
-// turns an exact d <= 3 float into its integer bits, d = 4 takes a
-// conversion; diagonals i + j = 5, 6 accumulate across rounds in FP32 TMEM
-// (their rounding is below 2^-40 of the result); the products i + j >= 7 are
-// dropped, and with balanced table digits they are zero-mean.  Each output's
-// sum is then one exact integer, rounded once to FP64.
+// call) are written in fixed point against power-of-two scales, both as
+// 39-bit magnitudes in balanced base-256 digits (|digit| <= 128, times the
+// value's sign), held exactly in FP16: the table against one scale per plan,
+// the densities against one scale per right-hand side (the exponent of the
+// largest |x'| of that rhs over all boxes).  Because every density of an rhs
+// shares one scale, the FP16 digit planes are formed once per call by a
+// preparation kernel and the tensor-core kernel only gathers them.  A diagonal
+// i + j of digit products summed over K <= 64 source points is an integer of
+// magnitude at most 2^21 for i + j <= 3 and below 2^23 for i + j = 4, exact
+// in the FP32 accumulator.  Those diagonals (the leading 32 bits) get their
+// own TMEM accumulator, re-initialised per K round and read after every round
+// into int64 registers: one FADD with 1.5 * 2^23 turns an exact d <= 3 float
+// into its integer bits, d = 4 takes a conversion; diagonals i + j = 5, 6
+// accumulate across rounds in FP32 TMEM (their rounding is below 2^-40 of the
+// result); the products i + j >= 7 are dropped, and with balanced digits they
+// are zero-mean.  Each output's sum is then one exact integer, rounded once to
+// FP64.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -95,18 +96,6 @@ __device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits
     r = (r - lo) >> kDigitBits;
   }
   dig[0] = sgn * (int)r;   // m < 2^39: r <= 128
-}
-
-// density digit bytes: v = sign * 2^(e - 39) * m, m < 2^39; byte 0 holds
-// the sign (bit 7) and the top 7 bits of m, bytes 1..4 the following
-// base-256 digits of m (magnitudes)
-__device__ __forceinline__ void density_digit_bytes(double v, int e, uint8_t (&byt)[kDigits]) {
-  const unsigned long long m = fixed_magnitude<kXFixedBits>(v, e);
-  const unsigned sgn = __double_as_longlong(v) < 0 ? 0x80u : 0u;
-  byt[0] = (uint8_t)(sgn | (unsigned)((m >> (kXFixedBits - 7)) & 0x7F));
-#pragma unroll
-  for (int i = 1; i < kDigits; ++i)
-    byt[i] = (uint8_t)((m >> (kXFixedBits - 7 - kDigitBits * i)) & 0xFF);
 }
 
 // exponent e with |v| < 2^e, as frexp returns it (-1074 for v == 0), from the
@@ -179,15 +168,20 @@ __global__ void classify_pairs_kernel(DevDesc d, TreeDev tr, int32_t *keys, vl1_
 
 // Per-call preparation kernels: one warp per density row (source box b, rhs r).
 
+// Scale exponents: x_exp[r] holds kExpBias + E_r, E_r the exponent with
+// |scaling * coefficient| < 2^E_r over every box of rhs r (zeroed before the
+// exponent pass, which takes the maximum with atomics; an rhs that is zero
+// everywhere keeps 0, i.e. E_r = -kExpBias, and all its digits are zero).
+constexpr int kExpBias = 4096;
+
 // one problem of a batch, as the preparation kernels see it
 struct PrepProblem {
   DevDesc d;
   TreeDev tr;
   const double *coefs;
   int nrhs;
-  int *x_exp;     // per density row
-  int *ref_exp;   // per target row (target box index * nrhs + rhs)
-  uint8_t *xdig;
+  int *x_exp;      // per rhs: kExpBias + E_r
+  __half *xpl;     // density digit planes [row][K chunk][plane][kc]
   double *wbox, *disp;   // 2D log displacement scratch (nullptr: none)
   int kp, kc;
   vl1_status *st;
@@ -215,140 +209,110 @@ __device__ __forceinline__ int row_exponent(const DevDesc &d, const TreeDev &tr,
   return __reduce_max_sync(0xffffffffu, e);
 }
 
-// x digits: row R = b * nrhs + r holds [K chunk][digit][kc] bytes (kp * 5),
-// so that the digits of one pipeline unit are one contiguous 5 * kc-byte
-// piece at byte kchunk * 5 * kc; source points sit at their mode id.  One
-// warp per row: the row's exponent (written to x_exp), then its digit bytes
-// assembled in the warp's shared-memory slice `stage` (row_bytes, 16-byte
-// aligned) and written out with 16-byte stores.
-__device__ __forceinline__ void row_digits(const DevDesc &d, const TreeDev &tr,
-                                           const double *coefs, int nrhs, int *x_exp,
-                                           uint8_t *xdig, int kp, int kc, vl1_status *st,
+// the exponent pass: row idx's largest exponent into its rhs's maximum
+__device__ __forceinline__ void row_exponent_max(const DevDesc &d, const TreeDev &tr,
+                                                 const double *coefs, int nrhs, int *x_exp,
+                                                 int64_t idx, int lane) {
+  const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
+  if (lane == 0 && e > -1074) atomicMax(x_exp + idx % nrhs, e + kExpBias);
+}
+
+// Density digit planes of row R = b * nrhs + r: [K chunk][plane][kc] FP16
+// values (source points at their mode id, zero elsewhere), planes X1, X2, X3
+// (the three leading balanced digits) and R = X4 + X5 / 256 rounded once to
+// FP16 (the tails only), so that the four planes of one pipeline unit are one
+// contiguous 8 * kc-byte piece at byte kchunk * 8 * kc.  One warp per row:
+// assembled in the warp's shared-memory slice `stage` (8 * kp bytes) and
+// written out with 16-byte stores.
+constexpr int kXPlanes = 4;          // density planes: X1, X2, X3, R
+__device__ __forceinline__ void row_planes(const DevDesc &d, const TreeDev &tr,
+                                           const double *coefs, int nrhs, const int *x_exp,
+                                           __half *xpl, int kp, int kc, vl1_status *st,
                                            int64_t idx, int lane, uint8_t *stage) {
-  const int row_bytes = kp * kDigits;
+  const int row_bytes = kp * kXPlanes * 2;
   const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
   int cnt = tr.src_counts[b];
   const int s0 = tr.src_starts[b];
-  const int lev = tr.levels[b];
   if (cnt > d.nq) {
     if (lane == 0) report(st, VL1_E_LAYOUT, b, cnt);
     cnt = d.nq;
   }
   for (int k = lane * 16; k < row_bytes; k += 32 * 16)
     *reinterpret_cast<uint4 *>(stage + k) = make_uint4(0u, 0u, 0u, 0u);
-  if (cnt > 0 && cnt <= 64) {
-    // one pass (up to two values per lane): the scaled values, their mode
-    // ids and the row exponent are loaded / formed once
-    const double sc = box_scaling(d, tr, lev);
+  __syncwarp();
+  if (cnt > 0) {
+    const int e = x_exp[r] - kExpBias;
+    const double sc = box_scaling(d, tr, tr.levels[b]);
     const double *c = coefs + (int64_t)r * tr.n_particles + s0;
-    const bool h0 = lane < cnt, h1 = lane + 32 < cnt;
-    const double v0 = h0 ? sc * c[lane] : 0.0, v1 = h1 ? sc * c[lane + 32] : 0.0;
-    const int m0 = h0 ? tr.smode[s0 + lane] : 0, m1 = h1 ? tr.smode[s0 + lane + 32] : 0;
-    int e = max(h0 ? scale_exponent(v0) : -1074, h1 ? scale_exponent(v1) : -1074);
-    e = __reduce_max_sync(0xffffffffu, e);
-    if (lane == 0) x_exp[idx] = e;
-    __syncwarp();
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const bool have = h ? h1 : h0;
-      const int m = h ? m1 : m0;
-      if (!have) continue;
+    __half *sp = reinterpret_cast<__half *>(stage);
+    for (int s = lane; s < cnt; s += 32) {
+      const int m = tr.smode[s0 + s];
       if (m < 0 || m >= d.nq) {
-        report(st, VL1_E_LAYOUT, b, -1 - (lane + 32 * h));
+        report(st, VL1_E_LAYOUT, b, -1 - s);
         continue;
       }
-      uint8_t byt[kDigits];
-      density_digit_bytes(h ? v1 : v0, e, byt);
-      const int base = (m / kc) * kDigits * kc + (m % kc);
-#pragma unroll
-      for (int i = 0; i < kDigits; ++i) stage[base + i * kc] = byt[i];
-    }
-  } else {
-    const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
-    if (lane == 0) x_exp[idx] = e;
-    __syncwarp();
-    if (cnt > 0) {
-      const double sc = box_scaling(d, tr, lev);
-      const double *c = coefs + (int64_t)r * tr.n_particles + s0;
-      for (int s = lane; s < cnt; s += 32) {
-        const int m = tr.smode[s0 + s];
-        if (m < 0 || m >= d.nq) {
-          report(st, VL1_E_LAYOUT, b, -1 - s);
-          continue;
-        }
-        uint8_t byt[kDigits];
-        density_digit_bytes(sc * c[s], e, byt);
-        const int base = (m / kc) * kDigits * kc + (m % kc);
-#pragma unroll
-        for (int i = 0; i < kDigits; ++i) stage[base + i * kc] = byt[i];
-      }
+      int dig[kDigits];
+      fixed_digits(sc * c[s], e, dig);
+      __half *v = sp + (m / kc) * kXPlanes * kc + (m % kc);
+      v[0] = __int2half_rn(dig[0]);
+      v[kc] = __int2half_rn(dig[1]);
+      v[2 * kc] = __int2half_rn(dig[2]);
+      // exact in FP32 (|.| <= 128.5 in steps of 1/256), one rounding to FP16
+      v[3 * kc] = __float2half_rn((float)dig[3] + (float)dig[4] * (1.0f / 256.0f));
     }
   }
   __syncwarp();
-  uint8_t *row = xdig + idx * row_bytes;
+  uint8_t *row = reinterpret_cast<uint8_t *>(xpl) + idx * row_bytes;
   for (int k = lane * 16; k < row_bytes; k += 32 * 16)
     *reinterpret_cast<uint4 *>(row + k) = *reinterpret_cast<const uint4 *>(stage + k);
   __syncwarp();
 }
 
-// Scale exponents.  Every density row (source box, rhs) gets its own: the
-// exponent e with |scaling * coefficient| < 2^e over the box (-1074 for an
-// empty or zero row); its digits are fixed point against 2^e.  Every target
-// row (target box, rhs) gets the largest exponent of its list-1 source rows:
-// its sum is accumulated in units of that exponent, so the precision of an
-// output is relative to its own largest contribution.
-__device__ __forceinline__ int target_row_exponent(const TreeDev &tr, int nrhs,
-                                                   const int *x_exp, int64_t idx) {
-  const int tb = (int)(idx / nrhs), r = (int)(idx % nrhs);
-  int e = -1074;
-  for (int p = tr.starts[tb]; p < tr.starts[tb + 1]; ++p)
-    e = max(e, x_exp[(int64_t)tr.lists[p] * nrhs + r]);
-  return e;
-}
-
-__global__ void ref_exponent_kernel(TreeDev tr, int nrhs, const int *x_exp, int *ref_exp) {
-  const int64_t n = (int64_t)tr.n_tgt_boxes * nrhs;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
-       idx += (int64_t)gridDim.x * blockDim.x)
-    ref_exp[idx] = target_row_exponent(tr, nrhs, x_exp, idx);
-}
-
-// dynamic shared memory: (blockDim.x / 32) x kp * 5 bytes (kp <= 1024 modes,
-// a multiple of 16, so every warp's slice and row stays 16-byte aligned)
-// (five blocks of 256 per SM: 46 registers, no spills)
-__global__ void __launch_bounds__(256, 5)
-    x_digits_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs, int nrhs,
-                    int *x_exp, uint8_t *xdig, int kp, int kc, vl1_status *st) {
-  extern __shared__ __align__(16) uint8_t s_stage[];
+__global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
+                                  int nrhs, int *x_exp) {
   const int64_t n = (int64_t)nboxes * nrhs;
   const int lane = threadIdx.x & 31;
-  uint8_t *stage = s_stage + (threadIdx.x >> 5) * kp * kDigits;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
        idx += warps)
-    row_digits(d, tr, coefs, nrhs, x_exp, xdig, kp, kc, st, idx, lane, stage);
+    row_exponent_max(d, tr, coefs, nrhs, x_exp, idx, lane);
+}
+
+// dynamic shared memory: (blockDim.x / 32) x kp * 8 bytes (kp a multiple of
+// 16, so every warp's slice and row stays 16-byte aligned)
+__global__ void __launch_bounds__(128)
+    x_planes_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs, int nrhs,
+                    const int *x_exp, __half *xpl, int kp, int kc, vl1_status *st) {
+  extern __shared__ __align__(16) uint8_t s_stage[];
+  const int64_t n = (int64_t)nboxes * nrhs;
+  const int lane = threadIdx.x & 31;
+  uint8_t *stage = s_stage + (threadIdx.x >> 5) * kp * kXPlanes * 2;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
+       idx += warps)
+    row_planes(d, tr, coefs, nrhs, x_exp, xpl, kp, kc, st, idx, lane, stage);
 }
 
 // Batch versions: block i handles rows [row0, row0 + nrows) of one problem
-// (tasks built on the host).  Target rows: one thread each.
-__global__ void ref_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+// (tasks built on the host), its warps striding over them.
+__global__ void x_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
   const PrepTask t = tasks[blockIdx.x];
   const PrepProblem &P = probs[t.problem];
-  for (int i = threadIdx.x; i < t.nrows; i += blockDim.x)
-    P.ref_exp[t.row0 + i] = target_row_exponent(P.tr, P.nrhs, P.x_exp, t.row0 + i);
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5)
+    row_exponent_max(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, t.row0 + i, lane);
 }
 
-// Density rows: 8 warps striding over them.  Dynamic shared memory:
-// (blockDim.x / 32) x (largest kp) * 5 bytes, at most 8 x 1024 x 5 = 40 KB.
-__global__ void x_digits_batch_kernel(const PrepProblem *probs, const PrepTask *tasks,
-                                      int max_row_bytes) {
+// Dynamic shared memory: (blockDim.x / 32) x (largest kp) * 8 bytes.
+__global__ void __launch_bounds__(128)
+    x_planes_batch_kernel(const PrepProblem *probs, const PrepTask *tasks, int max_row_bytes) {
   extern __shared__ __align__(16) uint8_t s_stage[];
   const PrepTask t = tasks[blockIdx.x];
   const PrepProblem &P = probs[t.problem];
   const int lane = threadIdx.x & 31;
   uint8_t *stage = s_stage + (threadIdx.x >> 5) * max_row_bytes;
   for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5)
-    row_digits(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, P.xdig, P.kp, P.kc, P.st, t.row0 + i,
+    row_planes(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, P.xpl, P.kp, P.kc, P.st, t.row0 + i,
                lane, stage);
 }
 
@@ -483,11 +447,10 @@ struct MixedParams {
   MixedGeom g;
   int nrhs;
   vl1_mixed_schedule sched;
-  const uint8_t *xdig;   // density digit bytes [n_xrows][kp * 5]
+  const __half *xpl;     // density digit planes [n_xrows][n_kc][4][kc]
   int32_t n_xrows;
   const __half *adig;
-  const int *x_exp;     // per density row
-  const int *ref_exp;   // per target row
+  const int *x_exp;     // per rhs: kExpBias + the densities' scale exponent
   int a_exp;
   const double *disp;  // [n_tgt_boxes * nrhs] (x2 complex) or nullptr
   const int32_t *target_boxes, *tgt_starts, *tgt_counts;
@@ -505,15 +468,17 @@ struct MixedParams {
 };
 
 // Warp roles of mixed_kernel (warp index w):
-//   w <  8      producers: per pipeline unit, warp w gathers the density digit
-//               bytes of tile rows 16w .. 16w+15 with cp.async (consecutive
-//               lanes on consecutive 16-byte pieces of a row's 5 * kc bytes,
-//               zero-filled for rows without a source box) into a staging
-//               ring, then expands them to FP16 digit planes in the stage and
-//               arrives on full[stage].  Eight warps keep enough requests in
-//               flight to cover the L2 latency of these scattered rows.
+//   w <  8      producers: per pipeline unit, warp w copies the density digit
+//               planes of tile rows 16w .. 16w+15 into the unit's stage with
+//               cp.async (16-byte pieces straight into the swizzled K-major
+//               layout, zero-filled for rows without a source box); each
+//               lane's arrival on xfull[stage] fires when its copies land
+//               (cp.async.mbarrier.arrive), so the producers never wait for
+//               data, only for a free stage.  Eight warps keep enough
+//               requests in flight to cover the L2 latency of these scattered
+//               rows.
 //   w == 8      table loader (one lane): the five table digit tiles of the
-//               unit's key by bulk copies (TMA), counted on full[stage]
+//               unit's key by bulk copies (TMA), counted on afull[stage]
 //   w == 9      tensor-core issuer (one lane)
 //   w >= 10     readout: TMEM lane quadrant w % 4, RC columns each
 // Pipeline unit = (key, K chunk of kc <= 32 source points); a "round" = the
@@ -526,11 +491,9 @@ struct MixedParams {
 // column blocks land on consecutive diagonals i + j.
 // Density planes of a stage: the exact digits X1, X2, X3 and, for the tails
 // only, R = X4 + X5 / 256 rounded to FP16 (11 significant bits: the density
-// keeps ~2^-35 of its row's reference scale in the tails, far below the
-// 2^-24 weight of the tails; the exact diagonals use X1..X3 only).
-constexpr int kStages = 3;
-constexpr int kXPlanes = 4;          // density planes per stage: X1, X2, X3, R
-constexpr int kStgDepth = 3;         // byte staging ring per producer warp
+// keeps ~2^-36 of its rhs's scale in the tails, far below the 2^-24 weight of
+// the tails; the exact diagonals use X1..X3 only).
+constexpr int kStages = 4;
 constexpr uint32_t kExactCols = 3;   // accumulators per buffer
 constexpr int kProducerWarps = 8;
 constexpr int kRowsPerProducer = 128 / kProducerWarps;
@@ -544,7 +507,7 @@ constexpr uint32_t kWaitLimitUs = 2000000; // a wait gives up after 2 s
 constexpr int kSplitPoison = 1 << 16;
 
 struct Barriers {
-  uint64_t xfull[kStages];   // the producer warps' density planes are in the stage
+  uint64_t xfull[kStages];   // every producer lane's density copies have landed
   uint64_t afull[kStages];   // the table digit tiles have landed
   uint64_t empty[kStages];
   uint64_t accf[2];
@@ -674,7 +637,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   if (tid == 0) {
     tc::mbar_init(&bars.drain, 1);
     for (int s = 0; s < kStages; ++s) {
-      tc::mbar_init(&bars.xfull[s], kProducerWarps);   // one arrival per producer warp
+      tc::mbar_init(&bars.xfull[s], kProducerWarps * 32);   // one per producer lane
       tc::mbar_init(&bars.afull[s], 1);                // the loader's expect_tx
       tc::mbar_init(&bars.empty[s], 1);
     }
@@ -769,193 +732,38 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
 
   if (warp < kProducerWarps) {
     // ------------------------------------------------------------ producers
-    // Per unit: gather the byte digits of this warp's 16 rows (5 * KC bytes
-    // per row, cp.async into a kStgDepth-deep staging ring), then, kStgDepth
-    // - 1 units behind, expand that unit's bytes to FP16 digit planes in the
-    // unit's pipeline stage.  (One bulk copy per row instead was measured
-    // slower: the copies queue behind each other in the copy engine.)
-    constexpr int RB = kDigits * KC;           // bytes per row and unit
-    constexpr int PPR = RB / 16;               // 16-byte pieces per row and unit
-    constexpr int NH = KC / 16;                // 16-value halves per digit row
-    constexpr int LOOK = kStgDepth - 1;        // units gathered ahead of the expansion
-    const int64_t row_bytes = (int64_t)p.g.kp * kDigits;
-    uint8_t *stg = smem + (size_t)kStages * STAGE_BYTES +
-                   (size_t)warp * kStgDepth * kRowsPerProducer * RB;
-    // lanes < kRowsPerProducer hold the source row of tile row my_row and
-    // the reference exponent of its target row
+    // Per unit: wait for the unit's stage to be free, then copy the four
+    // digit planes of this warp's 16 rows (8 * KC bytes of a row: PPR 16-byte
+    // pieces of 8 values of one plane) into the stage's swizzled K-major
+    // planes with cp.async; each lane's arrival on xfull fires when its own
+    // copies have landed.  A warp none of whose rows has a source box in the
+    // unit's key writes zero planes (once per stage) and arrives at once.
+    constexpr int PPP = KC / 8;                          // pieces per row and plane
+    constexpr int PPR = kXPlanes * PPP;                  // pieces per row and unit
+    constexpr int NIT = kRowsPerProducer * PPR / 32;     // pieces per lane and unit
+    static_assert(kRowsPerProducer * PPR % 32 == 0, "whole pieces per lane");
+    const int64_t row_halves = (int64_t)p.g.kp * kXPlanes;   // FP16 values per density row
+    // lanes < kRowsPerProducer hold the density row of tile row my_row,
+    // fetched one key ahead
     const int my_row = kRowsPerProducer * warp + (lane % kRowsPerProducer);
-    int my_ref = 0;
-    {
-      const int v = s_rows[my_row];
-      if (v >= 0) my_ref = p.ref_exp[v];
-    }
-    // key id, this lane's source row and its exponent, fetched one key
-    // ahead; the source row two keys ahead, so that the exponent load never
-    // waits for the row load
-    int nkey = 0, nxr = -1, nxe = 0, nnxr = -1;
+    int nkey = 0, nxr = -1;
     if (n_keys > 0) {
       nkey = p.sched.key_ids[k0];
       nxr = p.sched.key_xrow[(int64_t)k0 * 128 + my_row];
-      if (nxr >= 0 && nxr < p.n_xrows) nxe = p.x_exp[nxr];
     }
-    if (n_keys > 1) nnxr = p.sched.key_xrow[(int64_t)(k0 + 1) * 128 + my_row];
-    // right shift of the staged digits of units with even / odd index: a
-    // source row's digits are fixed point against its own exponent and are
-    // moved to the target row's reference exponent as they are expanded
-    static_assert(kStgDepth == 3, "one shift register per staging slot");
-    int sh_s0 = 0, sh_s1 = 0, sh_s2 = 0;
-    // bit (u % kStgDepth): none of this warp's rows has a source box in unit
-    // u (nothing gathered, zero planes); bit s of zero_stages: this warp's
-    // rows of stage s hold zero planes (the stages are overwritten by the
-    // parked sums at the end of an item, so the bits start clear per item)
-    uint32_t empty_bits = 0, zero_stages = 0;
-    // expand the staged bytes of unit v into stage v % kStages
-    auto expand = [&](int v) -> bool {
-      const int s = (ubase + v) % kStages;
-      const int use = (ubase + v) / kStages;
-      if (use > 0 && !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, limit_us, true))
-        return false;
-      const uint8_t *sb = stg + (v % kStgDepth) * kRowsPerProducer * RB;
-      uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
-      if ((empty_bits >> (v % kStgDepth)) & 1u) {
-        // no source rows: zero planes (rows 16w .. 16w + 15 of a swizzled
-        // K-major plane are one contiguous block), written once per stage
-        if (!((zero_stages >> s) & 1u)) {
-          constexpr int BLK = kRowsPerProducer * (int)ROW_BYTES;
-#pragma unroll
-          for (int dg = 0; dg < kXPlanes; ++dg)
-            for (int o = lane * 16; o < BLK; o += 32 * 16)
-              *reinterpret_cast<uint4 *>(xs + dg * XBYTES + warp * BLK + o) =
-                  make_uint4(0u, 0u, 0u, 0u);
-          zero_stages |= 1u << s;
-        }
-        tc::fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0 && !(withhold && warp == 0 && ubase + v == 0))
-          mbar_arrive(&bars.xfull[s]);
-        return true;
-      }
-      zero_stages &= ~(1u << s);
-      const __half2 k1024 = __floats2half2_rn(1024.0f, 1024.0f);
-      constexpr int ITER = (kRowsPerProducer * NH + 31) / 32;
-      const int vs = v % kStgDepth;
-      const int shv = vs == 0 ? sh_s0 : (vs == 1 ? sh_s1 : sh_s2);
-      int shr[ITER];
-#pragma unroll
-      for (int i = 0; i < ITER; ++i)
-        shr[i] = __shfl_sync(0xffffffffu, shv, min((lane + 32 * i) / NH, kRowsPerProducer - 1));
-#pragma unroll
-      for (int i = 0; i < ITER; ++i) {
-        const int t = lane + 32 * i;
-        if (t >= kRowsPerProducer * NH) break;
-        const int rl = t / NH, h = t - (t / NH) * NH;
-        const uint8_t *src = sb + rl * RB + h * 16;
-        // sign masks of the FP16 pairs (values 4q + 0/1 and 4q + 2/3): the
-        // sign of a value is bit 7 of its top digit byte
-        const uint4 top = *reinterpret_cast<const uint4 *>(src);
-        const uint32_t tw4[4] = {top.x, top.y, top.z, top.w};
-        uint32_t sg[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t tw = tw4[q];
-          sg[2 * q] = ((tw << 8) & 0x8000u) | ((tw << 16) & 0x80000000u);
-          sg[2 * q + 1] = ((tw >> 8) & 0x8000u) | (tw & 0x80000000u);
-        }
-        // digit planes of 16 values, most significant first, 4 values per
-        // word, with the magnitude shifted right by sh (truncating): whole
-        // digits by reading output plane dg from staged plane dg - sh/8 (the
-        // top plane without its sign bits; zero above it), then the bit shift
-        // within bytes (per-byte masks keep the values of a word apart)
-        const int sh = shr[i];
-        const int a = sh >> 3, bsh = sh & 7;
-        uint32_t m[kDigits][4];
-#pragma unroll
-        for (int dg = 0; dg < kDigits; ++dg) {
-          const int j = dg - a;
-          uint4 x4 = make_uint4(0u, 0u, 0u, 0u);
-          if (j >= 0) x4 = *reinterpret_cast<const uint4 *>(src + j * KC);
-          const uint32_t keep = j == 0 ? 0x7F7F7F7Fu : 0xFFFFFFFFu;
-          m[dg][0] = x4.x & keep;
-          m[dg][1] = x4.y & keep;
-          m[dg][2] = x4.z & keep;
-          m[dg][3] = x4.w & keep;
-        }
-        if (bsh != 0) {
-          const uint32_t lo = 0x01010101u * (0xFFu >> bsh);
-#pragma unroll
-          for (int dg = kDigits - 1; dg >= 1; --dg)
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              m[dg][q] = ((m[dg][q] >> bsh) & lo) | ((m[dg - 1][q] << (8 - bsh)) & ~lo);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) m[0][q] = (m[0][q] >> bsh) & lo;
-        }
-        const int row = kRowsPerProducer * warp + rl;
-        // plane 3: R = X4 + X5 / 256 rounded to FP16: X4 and X5 are exact in
-        // FP16 and X5 / 256 too, so one packed FMA rounds the exact sum once
-        {
-          const __half2 k2m8 = __floats2half2_rn(1.0f / 256.0f, 1.0f / 256.0f);
-          uint32_t o[8];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            uint32_t a_lo = __byte_perm(m[3][q], 0x64646464u, 0x4140u);
-            uint32_t a_hi = __byte_perm(m[3][q], 0x64646464u, 0x4342u);
-            uint32_t b_lo = __byte_perm(m[4][q], 0x64646464u, 0x4140u);
-            uint32_t b_hi = __byte_perm(m[4][q], 0x64646464u, 0x4342u);
-            const __half2 x4lo = __hsub2(*reinterpret_cast<__half2 *>(&a_lo), k1024);
-            const __half2 x4hi = __hsub2(*reinterpret_cast<__half2 *>(&a_hi), k1024);
-            const __half2 x5lo = __hsub2(*reinterpret_cast<__half2 *>(&b_lo), k1024);
-            const __half2 x5hi = __hsub2(*reinterpret_cast<__half2 *>(&b_hi), k1024);
-            __half2 h01 = __hfma2(x5lo, k2m8, x4lo);
-            __half2 h23 = __hfma2(x5hi, k2m8, x4hi);
-            o[2 * q] = *reinterpret_cast<uint32_t *>(&h01) | sg[2 * q];
-            o[2 * q + 1] = *reinterpret_cast<uint32_t *>(&h23) | sg[2 * q + 1];
-          }
-          uint8_t *pl = xs + 3 * XBYTES;
-          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16, KC)) =
-              make_uint4(o[0], o[1], o[2], o[3]);
-          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16 + 8, KC)) =
-              make_uint4(o[4], o[5], o[6], o[7]);
-        }
-        // planes 0..2: the exact digits X1, X2, X3
-#pragma unroll
-        for (int dg = 0; dg < 3; ++dg) {
-          const uint32_t *w = m[dg];
-          // bytes (b0, b1) -> FP16 pair (1024 + b0, 1024 + b1) -> minus 1024:
-          // exact, two values per packed subtraction
-          uint32_t o[8];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            uint32_t lo = __byte_perm(w[q], 0x64646464u, 0x4140u);
-            uint32_t hi = __byte_perm(w[q], 0x64646464u, 0x4342u);
-            __half2 hlo = __hsub2(*reinterpret_cast<__half2 *>(&lo), k1024);
-            __half2 hhi = __hsub2(*reinterpret_cast<__half2 *>(&hi), k1024);
-            o[2 * q] = *reinterpret_cast<uint32_t *>(&hlo) | sg[2 * q];
-            o[2 * q + 1] = *reinterpret_cast<uint32_t *>(&hhi) | sg[2 * q + 1];
-          }
-          uint8_t *pl = xs + dg * XBYTES;
-          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16, KC)) =
-              make_uint4(o[0], o[1], o[2], o[3]);
-          *reinterpret_cast<uint4 *>(pl + tc::kmajor_swizzled_offset(row, h * 16 + 8, KC)) =
-              make_uint4(o[4], o[5], o[6], o[7]);
-        }
-      }
-      tc::fence_proxy_async_smem();   // generic writes -> tensor-core reads
-      __syncwarp();
-      if (lane == 0 && !(withhold && warp == 0 && ubase + v == 0)) mbar_arrive(&bars.xfull[s]);
-      return true;
-    };
+    // bit s: this warp's rows of stage s hold zero planes (the stages are
+    // overwritten by the parked sums at the end of an item, so the bits
+    // start clear per item)
+    uint32_t zero_stages = 0;
     int u = 0;
     bool aborted = false;
     for (int kidx = k0; kidx < k1 && !aborted; ++kidx) {
-      int key = nkey, xr_lane = nxr;
-      const int xe_lane = nxe;
+      const int key = nkey;
+      int xr_lane = nxr;
       if (kidx + 1 < k1) {
         nkey = p.sched.key_ids[kidx + 1];
-        nxr = nnxr;
-        nxe = (nxr >= 0 && nxr < p.n_xrows) ? p.x_exp[nxr] : 0;
+        nxr = p.sched.key_xrow[(int64_t)(kidx + 1) * 128 + my_row];
       }
-      if (kidx + 2 < k1) nnxr = p.sched.key_xrow[(int64_t)(kidx + 2) * 128 + my_row];
       const bool key_ok = key >= 0 && key < p.d.n_tables * p.d.n_cases;
       if (!key_ok) {
         if (warp == 0 && lane == 0) report(p.st, VL1_E_ARG, tile, kidx);
@@ -965,53 +773,59 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         report(p.st, VL1_E_ARG, tile, my_row);
         xr_lane = -1;
       }
-      // a source row above its target row's reference exponent is not one
-      // of that row's list-1 sources
-      int sh_lane = my_ref - xe_lane;
-      if (lane < kRowsPerProducer && xr_lane >= 0 && sh_lane < 0) {
-        report(p.st, VL1_E_ARG, tile, my_row);
-        xr_lane = -1;
-      }
-      sh_lane = min(max(sh_lane, 0), kXFixedBits + 1);   // past the width: zero
       const bool key_empty =
           __ballot_sync(0xffffffffu, lane < kRowsPerProducer && xr_lane >= 0) == 0u;
       for (int kc = 0; kc < p.g.n_kc; ++kc, ++u) {
-        {
-          const int us = u % kStgDepth;
-          sh_s0 = us == 0 ? sh_lane : sh_s0;
-          sh_s1 = us == 1 ? sh_lane : sh_s1;
-          sh_s2 = us == 2 ? sh_lane : sh_s2;
-          empty_bits = (empty_bits & ~(1u << us)) | (key_empty ? 1u << us : 0u);
+        const int s = (ubase + u) % kStages;
+        const int use = (ubase + u) / kStages;
+        if (use > 0 &&
+            !wait_or_abort(&bars.empty[s], (use - 1) & 1, &s_abort, limit_us, true)) {
+          aborted = true;
+          break;
         }
-        // gather unit u: piece pc of the warp's rows -> row pc / PPR, piece pc % PPR
-        uint8_t *sb = stg + (u % kStgDepth) * kRowsPerProducer * RB;
+        uint8_t *xs = smem + (size_t)s * STAGE_BYTES;
+        const bool hold = withhold && warp == 0 && ubase + u == 0;
+        if (key_empty) {
+          // no source rows: zero planes (rows 16w .. 16w + 15 of a swizzled
+          // K-major plane are one contiguous block), written once per stage
+          if (!((zero_stages >> s) & 1u)) {
+            constexpr int BLK = kRowsPerProducer * (int)ROW_BYTES;
 #pragma unroll
-        for (int it = 0; it < (kRowsPerProducer * PPR + 31) / 32; ++it) {
-          if (key_empty) break;
-          const int pc = it * 32 + lane;
-          const int rl = min(pc / PPR, kRowsPerProducer - 1), q = pc - (pc / PPR) * PPR;
-          const int xr = __shfl_sync(0xffffffffu, xr_lane, rl);
-          if (pc < kRowsPerProducer * PPR) {
-            const bool have = xr >= 0;
-            const uint8_t *src =
-                p.xdig + (have ? (int64_t)xr * row_bytes + (int64_t)kc * RB + q * 16 : 0);
-            tc::cp_async16_zfill(sb + rl * RB + q * 16, src, have ? 16u : 0u);
+            for (int dg = 0; dg < kXPlanes; ++dg)
+              for (int o = lane * 16; o < BLK; o += 32 * 16)
+                *reinterpret_cast<uint4 *>(xs + dg * XBYTES + warp * BLK + o) =
+                    make_uint4(0u, 0u, 0u, 0u);
+            zero_stages |= 1u << s;
           }
-        }
-        tc::cp_async_commit();
-        if (u >= LOOK) {
-          tc::cp_async_wait_group<LOOK>();   // unit u - LOOK landed (this lane's pieces)
+          tc::fence_proxy_async_smem();
           __syncwarp();
-          if (!expand(u - LOOK)) {
-            aborted = true;
-            break;
-          }
+          if (!hold) mbar_arrive(&bars.xfull[s]);
+          continue;
         }
+        zero_stages &= ~(1u << s);
+#pragma unroll
+        for (int it = 0; it < NIT; ++it) {
+          // piece pc of the warp's rows: row pc / PPR, plane q / PPP, values
+          // 8 (q % PPP) .. +7 of the K chunk (consecutive lanes read one
+          // row's 8 * KC contiguous bytes)
+          const int pc = it * 32 + lane;
+          const int rl = pc / PPR, q = pc - (pc / PPR) * PPR;
+          const int pl = q / PPP, k8 = q - (q / PPP) * PPP;
+          const int xr = __shfl_sync(0xffffffffu, xr_lane, rl);
+          const int row = kRowsPerProducer * warp + rl;
+          const bool have = xr >= 0;
+          const __half *src =
+              p.xpl + (have ? (int64_t)xr * row_halves + ((int64_t)kc * kXPlanes + pl) * KC +
+                                  k8 * 8
+                            : 0);
+          tc::cp_async16_zfill(xs + pl * XBYTES + tc::kmajor_swizzled_offset(row, k8 * 8, KC),
+                               src, have ? 16u : 0u);
+        }
+        if (!hold) tc::cp_async_mbar_arrive_noinc(&bars.xfull[s]);
       }
     }
     tc::cp_async_wait_all();
     __syncwarp();
-    for (int v = u - LOOK < 0 ? 0 : u - LOOK; v < u && !aborted; ++v) aborted = !expand(v);
   } else if (warp == kLoaderWarp) {
     // ---------------------------------------------------------- table loader
     if (lane == 0) {
@@ -1214,9 +1028,9 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       cnt = min(p.tgt_counts[tbox], p.d.nq);
       ob = (long long)r * p.n_particles + p.tgt_starts[tbox];
       // table values are m_a 2^(a_exp - kFixedBits), densities
-      // m_x 2^(e - kXFixedBits) with e the row's reference exponent; the
+      // m_x 2^(e - kXFixedBits) with e the scale exponent of the rhs; the
       // parked sums count units of 2^32 of m_a m_x
-      ex = p.a_exp + p.ref_exp[v] - (kFixedBits + kXFixedBits) + 32;
+      ex = p.a_exp + (p.x_exp[r] - kExpBias) - (kFixedBits + kXFixedBits) + 32;
     }
     s_obase[tid] = ob;
     s_ocnt[tid] = cnt;
@@ -1338,8 +1152,7 @@ const void *mixed_kernel_ptr(int nch, int kc, bool multi) {
 }
 
 size_t mixed_smem_bytes(int nch, int kc) {
-  const size_t pipe = (size_t)kStages * (kXPlanes * 128 + kDigits * nch) * kc * 2 +
-                      (size_t)kProducerWarps * kStgDepth * kRowsPerProducer * kDigits * kc;
+  const size_t pipe = (size_t)kStages * (kXPlanes * 128 + kDigits * nch) * kc * 2;
   const size_t park = (size_t)128 * (nch + 1) * 8;   // int64 sums, padded rows
   return (pipe > park ? pipe : park) + 1024;
 }
@@ -1409,9 +1222,8 @@ int64_t mixed_workspace_bytes(const vl1_plan *plan, int64_t nboxes, int64_t n_tg
   const MixedGeom &g = plan->mixed.geom;
   const int cv = plan->d.table_cplx ? 2 : 1;
   int64_t b = 0;
-  b += (nboxes * nrhs * 4 + 255) / 256 * 256;                    // density row exponents
-  b += (n_tgt_boxes * nrhs * 4 + 255) / 256 * 256;               // target row exponents
-  b += (nboxes * nrhs * g.kp * kDigits + 255) / 256 * 256;  // x digit bytes
+  b += ((int64_t)nrhs * 4 + 255) / 256 * 256;                       // rhs scale exponents
+  b += (nboxes * nrhs * g.kp * kXPlanes * 2 + 255) / 256 * 256;    // density digit planes
   if (plan->d.disp_kind == VL1_DISP_LOG2D) {
     b += (nboxes * nrhs * cv * 8 + 255) / 256 * 256;            // per-box displacement
     b += (n_tgt_boxes * nrhs * cv * 8 + 255) / 256 * 256;       // per-target displacement
@@ -1466,13 +1278,10 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
               (long long)n_xrows);
     return VL1_E_UNSUPPORTED;
   }
-  const int64_t n_trows = (int64_t)tree.n_tgt_boxes * nrhs;
   int *x_exp = reinterpret_cast<int *>(w);
-  w += (n_xrows * 4 + 255) / 256 * 256;
-  int *ref_exp = reinterpret_cast<int *>(w);
-  w += (n_trows * 4 + 255) / 256 * 256;
-  uint8_t *xdig = w;
-  w += (n_xrows * g.kp * kDigits + 255) / 256 * 256;
+  w += ((int64_t)nrhs * 4 + 255) / 256 * 256;
+  __half *xpl = reinterpret_cast<__half *>(w);
+  w += (n_xrows * g.kp * kXPlanes * 2 + 255) / 256 * 256;
   double *wbox = nullptr, *disp = nullptr;
   if (d.disp_kind == VL1_DISP_LOG2D) {
     wbox = reinterpret_cast<double *>(w);
@@ -1481,10 +1290,20 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   }
   cudaError_t e;
   const int64_t nbr = n_xrows;
-  // row exponents and digits in one pass, then the target rows' references
-  x_digits_kernel<<<grid_for(nbr * 32, 256), 256, 8 * g.kp * kDigits, s>>>(
-      d, tree, (int)nboxes, coefs, nrhs, x_exp, xdig, g.kp, g.kc, plan->status);
-  ref_exponent_kernel<<<grid_for(n_trows, 256), 256, 0, s>>>(tree, nrhs, x_exp, ref_exp);
+  // the rhs scale exponents (maximum over all density rows), then the digit
+  // planes of every density row
+  e = cudaMemsetAsync(x_exp, 0, sizeof(int) * nrhs, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(rhs exponents)");
+  x_exponent_kernel<<<grid_for(nbr * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
+                                                            x_exp);
+  const size_t plane_smem = (size_t)4 * g.kp * kXPlanes * 2;
+  if (plane_smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(x_planes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)plane_smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(x_planes_kernel)");
+  }
+  x_planes_kernel<<<grid_for(nbr * 32, 128), 128, plane_smem, s>>>(
+      d, tree, (int)nboxes, coefs, nrhs, x_exp, xpl, g.kp, g.kc, plan->status);
   if (disp) {
     disp_box_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
                                                       wbox);
@@ -1500,11 +1319,10 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   mp.g = g;
   mp.nrhs = nrhs;
   mp.sched = sched;
-  mp.xdig = xdig;
+  mp.xpl = xpl;
   mp.n_xrows = (int32_t)n_xrows;
   mp.adig = plan->mixed.adig;
   mp.x_exp = x_exp;
-  mp.ref_exp = ref_exp;
   mp.a_exp = plan->mixed.a_exp;
   mp.disp = disp;
   mp.target_boxes = tree.target_boxes;
@@ -1568,12 +1386,14 @@ struct vl1_batch {
   void *d_probs = nullptr, *d_prep = nullptr, *d_tasks = nullptr, *d_items = nullptr;
   int n_tasks = 0;
   int *d_queue = nullptr;
-  void *d_ttasks = nullptr;   // target-row tasks of the reference exponents
+  void *d_ttasks = nullptr;   // target-row tasks of the 2D displacement sums
   int n_ttasks = 0;
+  int *d_exp = nullptr;       // every problem's rhs scale exponents, contiguous
+  int n_exp = 0;
   std::vector<BatchGroup> groups;
   std::vector<SoloLaunch> solos;
   bool has_disp = false;
-  int max_row_bytes = 16;   // largest kp * 5 of the problems (digit staging)
+  int max_row_bytes = 16;   // largest kp * 8 of the problems (digit plane staging)
   // pinned staging of vl1_batch_update (two, so that one can be refilled
   // while the copy from the other is in flight)
   void *pinned[2] = {nullptr, nullptr};
@@ -1598,6 +1418,9 @@ struct BatchLayout {
   std::vector<BatchGroup> groups;
   std::vector<SoloLaunch> solos;
   int64_t o_probs = 0, o_prep = 0, o_tasks = 0, o_items = 0, o_queue = 0, o_ttasks = 0;
+  int64_t o_exp = 0;          // the rhs scale exponents of all problems
+  std::vector<int64_t> exp_off;   // a problem's first exponent in that region
+  int64_t n_exp = 0;
   int64_t param_bytes = 0;   // the parameter region [0, param_bytes)
   std::vector<int64_t> o_ws;
   int64_t total_bytes = 0;
@@ -1791,6 +1614,14 @@ int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t
   L.o_ttasks = off;
   off += round256(sizeof(PrepTask) * (L.ttasks.size() + 1));
   L.param_bytes = off;
+  L.exp_off.resize(n_problems);
+  L.n_exp = 0;
+  for (int i = 0; i < n_problems; ++i) {
+    L.exp_off[i] = L.n_exp;
+    L.n_exp += problems[i].nrhs;
+  }
+  L.o_exp = off;
+  off += round256(sizeof(int) * L.n_exp);
   L.o_ws.resize(n_problems);
   for (int i = 0; i < n_problems; ++i) {
     L.o_ws[i] = off;
@@ -1813,14 +1644,11 @@ void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems
     const MixedGeom &g = q.plan->mixed.geom;
     const int cv = q.plan->d.table_cplx ? 2 : 1;
     uint8_t *w = base + L.o_ws[i];
-    // the workspace layout of launch_mixed: [row exponents][target row
-    // exponents][x digits][disp]
-    int *x_exp = reinterpret_cast<int *>(w);
-    w += round256(L.nrows[i] * 4);
-    int *ref_exp = reinterpret_cast<int *>(w);
-    w += round256((int64_t)L.preps[i].tr.n_tgt_boxes * q.nrhs * 4);
-    uint8_t *xdig = w;
-    w += round256(L.nrows[i] * g.kp * kDigits);
+    // a problem's workspace: [digit planes][disp] (its rhs exponents are
+    // in the batch's exponent region, cleared by one memset per evaluation)
+    int *x_exp = reinterpret_cast<int *>(base + L.o_exp) + L.exp_off[i];
+    __half *xpl = reinterpret_cast<__half *>(w);
+    w += round256(L.nrows[i] * g.kp * kXPlanes * 2);
     double *wbox = nullptr, *disp = nullptr;
     if (q.plan->d.disp_kind == VL1_DISP_LOG2D) {
       wbox = reinterpret_cast<double *>(w);
@@ -1828,14 +1656,12 @@ void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems
       disp = reinterpret_cast<double *>(w);
       b->has_disp = true;
     }
-    L.mps[i].xdig = xdig;
+    L.mps[i].xpl = xpl;
     L.mps[i].x_exp = x_exp;
-    L.mps[i].ref_exp = ref_exp;
     L.mps[i].disp = disp;
     L.preps[i].x_exp = x_exp;
-    L.preps[i].ref_exp = ref_exp;
-    L.preps[i].xdig = xdig;
-    b->max_row_bytes = std::max(b->max_row_bytes, g.kp * kDigits);
+    L.preps[i].xpl = xpl;
+    b->max_row_bytes = std::max(b->max_row_bytes, g.kp * kXPlanes * 2);
     L.preps[i].wbox = wbox;
     L.preps[i].disp = disp;
   }
@@ -1850,6 +1676,8 @@ void place_batch(vl1_batch *b, BatchLayout &L, const vl1_batch_problem *problems
   b->d_queue = reinterpret_cast<int *>(base + L.o_queue);
   b->d_ttasks = base + L.o_ttasks;
   b->n_ttasks = (int)L.ttasks.size();
+  b->d_exp = reinterpret_cast<int *>(base + L.o_exp);
+  b->n_exp = (int)L.n_exp;
   b->groups = L.groups;
   uint8_t *h = host_ptr;
   if (host) {
@@ -1990,14 +1818,22 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemsetAsync(b->d_queue, 0, sizeof(int) * b->groups.size(), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(batch)");
+  if (b->n_exp > 0) {
+    e = cudaMemsetAsync(b->d_exp, 0, sizeof(int) * b->n_exp, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(batch exponents)");
+  }
   if (b->n_tasks > 0) {
-    x_digits_batch_kernel<<<b->n_tasks, 256, 8 * b->max_row_bytes, s>>>(
+    x_exponent_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
+        static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
+    const size_t plane_smem = (size_t)4 * b->max_row_bytes;
+    if (plane_smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(x_planes_batch_kernel,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plane_smem);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(x_planes_batch_kernel)");
+    }
+    x_planes_batch_kernel<<<b->n_tasks, 128, plane_smem, s>>>(
         static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks),
         b->max_row_bytes);
-    if (b->n_ttasks > 0)
-      ref_exponent_batch_kernel<<<b->n_ttasks, 256, 0, s>>>(
-          static_cast<const PrepProblem *>(b->d_prep),
-          static_cast<const PrepTask *>(b->d_ttasks));
   }
   if (b->has_disp && b->n_tasks > 0) {
     disp_box_batch_kernel<<<b->n_tasks, 64, 0, s>>>(static_cast<const PrepProblem *>(b->d_prep),
@@ -2056,7 +1892,7 @@ extern "C" int64_t vl1_batch_device_bytes(const vl1_batch *b) { return b ? b->by
 extern "C" int32_t vl1_batch_kernel_launches(const vl1_batch *b) {
   if (!b) return -1;
   int n = 0;
-  if (b->n_tasks > 0) n += 1 + (b->n_ttasks > 0 ? 1 : 0);
+  if (b->n_tasks > 0) n += 2;   // exponents, digit planes
   if (b->has_disp && b->n_tasks > 0) n += 1 + (b->n_ttasks > 0 ? 1 : 0);
   return n + (int)b->solos.size() + (int)b->groups.size();
 }

@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import collections
 import contextlib
+import copy
 import ctypes as C
 import gc
 import time
@@ -127,7 +128,7 @@ class ResidentBudget:
 
 class Request:
     __slots__ = ("rid", "key", "coefs", "out", "arrival", "t_start", "t_done", "step",
-                 "slot")
+                 "slot", "waited_build")
 
     def __init__(self, rid, key, coefs, out, arrival):
         self.rid, self.key, self.coefs, self.out = rid, key, coefs, out
@@ -135,6 +136,7 @@ class Request:
         self.t_start = self.t_done = None
         self.step = None
         self.slot = None
+        self.waited_build = False   # its table set was being built when it arrived
 
     @property
     def latency(self):
@@ -160,6 +162,15 @@ class ServingEngine:
     workload, table_key)`` declares a problem (built lazily, on its first
     request or by ``admit``); plans are shared by problems with the same
     ``table_key``.
+
+    A problem registered with ``build_tables`` (a function returning its
+    table set, e.g. the FP64 Duffy builder for its wave number) has no table
+    values yet: the first request for it starts the build on a worker thread
+    and its own CUDA stream, and the engine keeps serving the other problems
+    meanwhile; the request waits (in order) until the tables are built, then
+    the plan is admitted like any other.  Built table sets stay in a host
+    cache (host memory, outside the HBM budget), so a plan evicted from HBM
+    is rebuilt from them without a new table build.
     """
 
     def __init__(self, *, hbm_budget_bytes, step_capacity_bytes=1 << 30,
@@ -187,6 +198,14 @@ class ServingEngine:
         self.step_sizes = []
         self.cold_admissions = 0
         self._next_rid = 0
+        # table sets built on demand: host cache, builds in flight, stats
+        self._tables = {}           # table_key -> built table set
+        self._table_builders = {}   # table_key -> build function
+        self._building = {}         # table_key -> Future of a build in flight
+        self._builder = None
+        self._build_stream = None
+        self.table_builds = 0
+        self.table_build_s = 0.0
         # host seconds spent assembling and launching steps, and device
         # milliseconds of the finished steps (CUDA events around each step)
         self.host_s = 0.0
@@ -194,14 +213,62 @@ class ServingEngine:
 
     # ---- residents -----------------------------------------------------
 
-    def register(self, key, workload, table_key, tree_key=None, sched_key=None):
+    def register(self, key, workload, table_key, tree_key=None, sched_key=None,
+                 build_tables=None):
         """Declare problem ``key``: ``workload`` (tree, tables, kernel, q);
         problems with the same ``table_key`` share a plan, with the same
         ``tree_key`` a tree, and with the same ``sched_key`` (tree plus table
-        level structure and shape) a schedule."""
+        level structure and shape) a schedule.  ``build_tables()``, if given,
+        returns the table set (``workload.tables`` is then unused) and runs
+        on the engine's build thread when the tables are first needed."""
         tree_key = key if tree_key is None else tree_key
         sched_key = (tree_key, table_key) if sched_key is None else sched_key
         self.specs[key] = (workload, table_key, tree_key, sched_key)
+        if build_tables is not None:
+            self._table_builders.setdefault(table_key, build_tables)
+
+    # ---- table sets built on demand ------------------------------------
+
+    def _run_build(self, fn):
+        torch = self.torch
+        t0 = time.perf_counter()
+        with torch.cuda.stream(self._build_stream):
+            tables = fn()
+            torch.cuda.current_stream().synchronize()
+        return tables, time.perf_counter() - t0
+
+    def _tables_ready(self, key):
+        """True when problem ``key`` has its table values; otherwise its
+        build is started (once) and False is returned."""
+        table_key = self.specs[key][1]
+        fn = self._table_builders.get(table_key)
+        if fn is None or table_key in self._tables:
+            return True
+        fut = self._building.get(table_key)
+        if fut is None:
+            if self._builder is None:
+                import concurrent.futures
+
+                self._builder = concurrent.futures.ThreadPoolExecutor(max_workers=1)
+                self._build_stream = self.torch.cuda.Stream()
+            self._building[table_key] = self._builder.submit(self._run_build, fn)
+            return False
+        if not fut.done():
+            return False
+        tables, secs = fut.result()   # a failed build raises here
+        del self._building[table_key]
+        self._tables[table_key] = tables
+        self.table_builds += 1
+        self.table_build_s += secs
+        return True
+
+    def _workload(self, key):
+        workload, table_key = self.specs[key][:2]
+        if table_key not in self._table_builders:
+            return workload
+        w = copy.copy(workload)
+        w.tables = self._tables[table_key]
+        return w
 
     def _release(self, value):
         if isinstance(value, _Sched):
@@ -232,7 +299,11 @@ class ServingEngine:
         """Make problem ``key`` resident: its plan, tree and schedule (each
         built if needed, evicting idle entries to stay in the budget).
         Returns (plan, (view, keep), _Sched)."""
-        workload, table_key, tree_key, sched_key = self.specs[key]
+        _, table_key, tree_key, sched_key = self.specs[key]
+        if not self._tables_ready(key):
+            self._building[table_key].result()   # admit() waits for the build
+            self._tables_ready(key)
+        workload = self._workload(key)
         pkey, tkey, skey = ("plan", table_key), ("tree", tree_key), ("sched", sched_key)
         # pin each entry as soon as it is resident so that admitting the
         # next one cannot evict it
@@ -292,6 +363,7 @@ class ServingEngine:
         req = Request(self._next_rid, key, coefs, out,
                       time.perf_counter() if arrival is None else arrival)
         self._next_rid += 1
+        req.waited_build = not self._tables_ready(key)
         self.pending.append(req)
         return req
 
@@ -299,8 +371,12 @@ class ServingEngine:
         torch = self.torch
         t_host = time.perf_counter()
         reqs, probs, need = [], [], 0
+        waiting = []   # requests whose table set is still being built
         while self.pending and len(reqs) < self.max_step_requests:
             req = self.pending[0]
+            if not self._tables_ready(req.key):
+                waiting.append(self.pending.popleft())
+                continue
             plan, tree, sched = self.admit(req.key)
             add = (sched.ws_bytes + 255) // 256 * 256 + 4096
             if reqs and need + add > self.step_capacity // 2:
@@ -327,6 +403,8 @@ class ServingEngine:
             p.result = req.out.data_ptr()
             p.host_items = req.slot[1].items_np.ctypes.data
             probs.append(p)
+        if waiting:
+            self.pending.extendleft(reversed(waiting))
         if not reqs:
             return False
         arr = (_lib.BatchProblem * len(probs))(*probs)
@@ -379,7 +457,8 @@ class ServingEngine:
         is room in flight and requests are pending."""
         done = self.poll()
         if self.pending and len(self.inflight) < self.max_inflight:
-            self._launch_step()
+            if not self._launch_step() and not self.inflight:
+                time.sleep(50e-6)   # only requests waiting for table builds
         return done
 
     def drain(self):
@@ -419,6 +498,9 @@ class ServingEngine:
         while self.inflight:
             self.inflight[0][0].synchronize()
             self.poll()
+        if self._builder is not None:
+            self._builder.shutdown(wait=True)
+            self._builder = None
         if self.batch is not None:
             self.lib.vl1_batch_destroy(self.batch)
             self.batch = None

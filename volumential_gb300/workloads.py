@@ -37,7 +37,8 @@ from .tree_build import (
 __all__ = ["GaussianMixture", "random_gaussian_mixture", "synthetic_tables", "duffy_tables",
            "make_tables",
            "Workload", "config_c1", "config_c2", "config_c3", "uniform_workload",
-           "adaptive_workload", "config_c4", "config_c5", "C5Problem", "poisson_arrivals"]
+           "adaptive_workload", "config_c4", "config_c5", "config_c5_arrivals",
+           "c5_arrival_workloads", "C5Problem", "poisson_arrivals"]
 
 
 @dataclass
@@ -329,7 +330,7 @@ class C5Problem:
     key: tuple
     dim: int
     kernel: str          # "laplace" | "helmholtz"
-    k: int               # Helmholtz wave number (0 for Laplace)
+    k: float             # Helmholtz wave number (0 for Laplace)
     q: int
     level: int
     table_key: tuple
@@ -346,10 +347,11 @@ def _nearest_level(dim, q, n):
 def config_c5(seed=5000, n_requests=10000, n_range=(1e3, 5e5), qs=(3, 4, 5), k_range=(1, 30),
               densities_per_problem=4):
     """Serving mix: ``n_requests`` single-rhs requests; dim 2 or 3 with equal
-    probability, Laplace or Helmholtz with equal probability (k uniform over
-    the integers of ``k_range``: tables are resident per (dim, kernel, q, k)),
-    N log-uniform in ``n_range`` realised as q uniform in ``qs`` and the
-    uniform level whose N = 2^(dim L) q^dim is nearest to N in log.
+    probability, Laplace or Helmholtz with equal probability (k uniform in
+    ``k_range``, a real number kept to 6 decimals: every Helmholtz problem has
+    its own table set), N log-uniform in ``n_range`` realised as q uniform in
+    ``qs`` and the uniform level whose N = 2^(dim L) q^dim is nearest to N in
+    log.
 
     Returns (problems {key: C5Problem}, requests [(key, density index)],
     density terms {key: [GaussianMixture]}): each problem has
@@ -361,7 +363,7 @@ def config_c5(seed=5000, n_requests=10000, n_range=(1e3, 5e5), qs=(3, 4, 5), k_r
     for _ in range(n_requests):
         dim = 2 if rng.random() < 0.5 else 3
         kern = "laplace" if rng.random() < 0.5 else "helmholtz"
-        k = int(rng.integers(k_range[0], k_range[1] + 1)) if kern == "helmholtz" else 0
+        k = round(float(rng.uniform(k_range[0], k_range[1])), 6) if kern == "helmholtz" else 0.0
         n = float(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
         q = int(rng.choice(qs))
         lev = _nearest_level(dim, q, n)
@@ -394,7 +396,7 @@ def c5_workloads(problems, seed=5000):
     for key in sorted(problems):
         p = problems[key]
         if p.table_key not in tables:
-            tseed = seed + 7919 * p.dim + 101 * p.q + p.k
+            tseed = seed + 7919 * p.dim + 101 * p.q + int(p.k * 1e6)
             if p.kernel == "laplace":
                 tables[p.table_key] = synthetic_tables(p.dim, p.q, LaplaceKernel(p.dim),
                                                        seed=tseed, source_box_extent=1.0)
@@ -414,6 +416,51 @@ def c5_workloads(problems, seed=5000):
                             meta={"level": p.level, "table_key": p.table_key,
                                   "tree_key": tkey, "sched_key": (tkey, p.kernel)})
     return out
+
+
+def config_c5_arrivals(seed=5500, n_new=12, n_range=(1e3, 2e5), qs=(3, 4, 5), k_range=(1, 30)):
+    """Helmholtz problems that arrive while the serving mix runs: dim 2 or 3
+    with equal probability, k uniform in ``k_range`` (a real number kept to 6
+    decimals), N log-uniform in ``n_range`` realised as in :func:`config_c5`.
+    Their tables do not exist yet: each is built on arrival by the FP64 GPU
+    Duffy builder for its own k (:func:`c5_arrival_workloads`)."""
+    rng = np.random.default_rng(seed)
+    problems = {}
+    while len(problems) < n_new:
+        dim = 2 if rng.random() < 0.5 else 3
+        k = round(float(rng.uniform(k_range[0], k_range[1])), 6)
+        n = float(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+        q = int(rng.choice(qs))
+        lev = _nearest_level(dim, q, n)
+        key = (dim, "helmholtz", k, q, lev)
+        problems[key] = C5Problem(key, dim, "helmholtz", k, q, lev, (dim, "helmholtz", k, q, lev),
+                                  (2 ** dim) ** lev * q ** dim)
+    return problems
+
+
+def c5_arrival_workloads(problems, seed=5500):
+    """Trees of the arriving problems and, per problem, a function that
+    builds its table set: one FP64 Duffy table (GPU, the reference's default
+    orders) of the tree's level (source box extent 2^-level) for its k.
+    Returns ({key: Workload without tables}, {key: build function})."""
+    import functools
+
+    trees, out, builders = {}, {}, {}
+    for key in sorted(problems):
+        p = problems[key]
+        tkey = (p.dim, p.q, p.level)
+        if tkey not in trees:
+            trees[tkey] = build_list1_traversal(build_uniform_tree(p.dim, p.level, p.q))
+        kernel = HelmholtzKernel(p.dim)
+        out[key] = Workload(f"c5_new_{p.dim}d_helmholtz{p.k:g}_q{p.q}_l{p.level}", p.dim, p.q,
+                            kernel, trees[tkey], [], np.zeros((1, 0)), seed,
+                            meta={"level": p.level, "table_key": p.table_key,
+                                  "tree_key": tkey, "sched_key": (tkey, "helmholtz", p.level),
+                                  "tables": "duffy"})
+        builders[key] = functools.partial(duffy_tables, p.dim, p.q, kernel, n_tables=1,
+                                          source_box_extent=0.5 ** p.level, k=p.k,
+                                          complex_values=True)
+    return out, builders
 
 
 def poisson_arrivals(n, rate, seed=0):
