@@ -66,6 +66,10 @@ def parse_args(argv=None):
     p.add_argument("--c5-budget-gb", type=float, default=64.0,
                    help="C5: HBM budget of the resident plans, trees and schedules")
     p.add_argument("--c5-step", type=int, default=256, help="C5: most requests per step")
+    p.add_argument("--c5-new", type=int, default=12,
+                   help="C5: Helmholtz problems (continuous k) arriving with tables to build")
+    p.add_argument("--c5-pressure", type=float, default=0.5,
+                   help="C5 arrivals leg: HBM budget as a fraction of the mix's resident set")
     p.add_argument("--c5-rates", default="0.25,0.5,0.75,0.9",
                    help="C5: open-loop arrival rates as fractions of the closed-loop rate")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
@@ -932,6 +936,10 @@ def c5_main(args):
         torch.cuda.synchronize()
         errs.append(float(torch.linalg.norm(q.out - ref) / torch.linalg.norm(ref)))
     eng.check_status()
+    resident_set = eng.budget.used
+    evictions = eng.budget.evictions
+    pressure = c5_arrivals_leg(args, eng, ws, probs, reqs, dens, rate, resident_set) \
+        if args.c5_new > 0 else None
     hbm, bf16, peak_kind = peaks()
     kinds = {}
     for key, _ in reqs:
@@ -958,8 +966,9 @@ def c5_main(args):
         "unbatched_solves_per_s": serial_rate,
         "speedup_over_unbatched": rate / serial_rate,
         "rel_l2_max_vs_fp64": max(errs), "same_alone_and_in_mix": bool(same),
-        "resident_bytes": eng.budget.used, "hbm_budget_bytes": eng.budget.budget,
-        "evictions": eng.budget.evictions,
+        "resident_bytes": resident_set, "hbm_budget_bytes": eng.budget.budget,
+        "evictions": evictions,
+        "arrivals_under_pressure": pressure,
         "setup_s": {"host": t_host, "resident": t_resident},
         "e2e": None, "e2e_note": "resident trees, tables and densities (the serving "
                                  "configuration); results stay on the device",
@@ -970,6 +979,119 @@ def c5_main(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set):
+    """C5 under memory pressure, with table builds on arrival: a new engine
+    whose HBM budget is ``--c5-pressure`` times the mix's resident set serves
+    an open-loop Poisson stream of the mix's requests at half the closed-loop
+    rate, into which ``--c5-new`` new Helmholtz problems (k uniform in
+    [1, 30], real) arrive one after another; the first request of a new
+    problem starts the FP64 Duffy build of its table on the engine's build
+    thread (the engine keeps serving the others), and every problem, old or
+    new, is admitted cold and evicted least-recently-used under the budget.
+    Reports latency percentiles (all requests, those that waited for a table
+    build, the others), evictions, admissions and builds, the error of the
+    new problems against the FP64 path, and that sampled results are the
+    same bits alone and in the mix."""
+    import torch
+
+    from volumential_gb300 import workloads as W
+    from volumential_gb300.serving import ServingEngine, latency_stats
+
+    for _ in range(2):   # release the first engine's residents (trees after schedules)
+        eng.budget.make_room(eng.budget.budget)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    new_probs = W.config_c5_arrivals(n_new=args.c5_new)
+    new_ws, builders = W.c5_arrival_workloads(new_probs)
+    budget = int(args.c5_pressure * resident_set)
+    eng2 = ServingEngine(hbm_budget_bytes=budget, step_capacity_bytes=4 << 30,
+                         max_step_requests=args.c5_step)
+    for key, w in ws.items():
+        eng2.register(key, w, w.meta["table_key"], w.meta["tree_key"], w.meta["sched_key"])
+    rng = np.random.default_rng(77)
+    new_dens = {}
+    for key, w in new_ws.items():
+        eng2.register(key, w, w.meta["table_key"], w.meta["tree_key"], w.meta["sched_key"],
+                      build_tables=builders[key])
+        pts = torch.from_numpy(np.ascontiguousarray(w.tree.targets)).to("cuda")
+        mixes = [W.random_gaussian_mixture(rng, w.dim, int(rng.integers(4, 17)), (0.01, 0.1))
+                 for _ in range(4)]
+        new_dens[key] = [m.on_device(pts).contiguous() for m in mixes]
+    all_dens = dict(dens)
+    all_dens.update(new_dens)
+    # the stream: the mix's requests at half the closed-loop rate; new
+    # problem i starts at (0.1 + 0.5 i / n_new) of the run, then 24 requests
+    # at the rate of the stream's busiest problem
+    n_base = len(reqs)
+    rate = 0.5 * closed_rate
+    t_base = W.poisson_arrivals(n_base, rate, seed=78)
+    span = float(t_base[-1])
+    events = [(float(t), k, di) for t, (k, di) in zip(t_base, reqs)]
+    per_new = 24
+    for i, key in enumerate(sorted(new_ws)):
+        t0 = span * (0.1 + 0.5 * i / max(len(new_ws), 1))
+        ts = t0 + W.poisson_arrivals(per_new, per_new / (0.2 * span), seed=90 + i)
+        ts[0] = t0
+        events += [(float(t), key, int(j % 4)) for j, t in enumerate(ts)]
+    events.sort(key=lambda e: e[0])
+    sample_ids = set(rng.choice(len(events), size=min(40, len(events)), replace=False).tolist())
+    sample_ids |= {j for j, e in enumerate(events) if e[1] in new_ws and e[2] == 0}
+    arrivals, outs = [], {}
+    for j, (t, key, di) in enumerate(events):
+        w = ws.get(key) or new_ws[key]
+        cplx = w.kernel.is_complex_valued
+        if j in sample_ids:
+            out = torch.empty(w.n_points, dtype=torch.complex128 if cplx else torch.float64,
+                              device="cuda")
+        else:
+            out = outs.get(key)
+            if out is None:
+                out = outs[key] = torch.empty(
+                    w.n_points, dtype=torch.complex128 if cplx else torch.float64,
+                    device="cuda")
+        arrivals.append((t, key, all_dens[key][di], out))
+    torch.cuda.synchronize()
+    done, wall = eng2.run(arrivals)
+    eng2.check_status()
+    waited = [q for q in done if q.waited_build]
+    rest = [q for q in done if not q.waited_build]
+    # sampled requests again, one at a time: identical bits; new problems
+    # against the FP64 path
+    same, errs = True, []
+    sh = torch.cuda.current_stream().cuda_stream
+    for j in sorted(sample_ids):
+        q = done[j]
+        alone = eng2.submit(q.key, q.coefs)
+        eng2.drain()
+        same = same and torch.equal(alone.out, q.out)
+        if q.key in new_ws:
+            plan, (view, keep), _ = eng2.admit(q.key)
+            ref = torch.empty_like(q.out)
+            plan.eval_fp64(view, q.coefs, ref, stream=sh, nrhs=1)
+            torch.cuda.synchronize()
+            errs.append(float(torch.linalg.norm(q.out - ref) / torch.linalg.norm(ref)))
+    eng2.check_status()
+    out = {
+        "hbm_budget_bytes": budget, "mix_resident_set_bytes": resident_set,
+        "requests": len(done), "new_problems": len(new_ws),
+        "new_problem_k": sorted(float(k[2]) for k in new_ws),
+        "new_problem_shapes": sorted(f"{k[0]}d_q{k[3]}_l{k[4]}" for k in new_ws),
+        "tables_built_on_arrival": eng2.table_builds,
+        "table_build_s_total": eng2.table_build_s,
+        "table_source": "FP64 Duffy quadrature on the GPU per new k (reference default "
+                        "orders), on the engine's build thread and stream",
+        "offered_per_s": rate, "achieved_per_s": len(done) / wall, "wall_s": wall,
+        "latency_ms": latency_stats(done),
+        "latency_ms_waited_for_table_build": latency_stats(waited),
+        "latency_ms_others": latency_stats(rest),
+        "evictions": eng2.budget.evictions, "cold_admissions": eng2.cold_admissions,
+        "rel_l2_max_vs_fp64_new_problems": max(errs) if errs else None,
+        "same_alone_and_in_mix": bool(same), "sampled": len(sample_ids),
+    }
+    eng2.close()
+    return out
 
 
 def table_main(args):

@@ -135,3 +135,55 @@ def test_serving_under_a_small_budget_evicts_and_rebuilds(cuda):
     with pytest.raises(AdmissionError):
         tiny.admit(keys[0])
     tiny.close()
+
+
+def test_tables_built_on_arrival_do_not_stall_the_other_problems(cuda):
+    """A Helmholtz problem with a real wave number arrives without tables:
+    its first request starts the FP64 Duffy build on the engine's build
+    thread; requests of resident problems submitted after it complete while
+    the build runs (the build function holds an event the test sets only
+    once they are done), the new problem's requests are served once the
+    table exists, and its results match the oracle on that table and are the
+    same bits alone and in the mix."""
+    import threading
+
+    torch = cuda
+    probs, reqs, mixes, ws = _mix()
+    dens = _densities(torch, ws, mixes)
+    new = W.config_c5_arrivals(seed=5600, n_new=1, n_range=(1e3, 3e3), qs=(3,))
+    new_ws, builders = W.c5_arrival_workloads(new)
+    (nkey, nw), = new_ws.items()
+    assert nkey[2] != int(nkey[2])          # a real wave number
+    release = threading.Event()
+
+    def build():
+        assert release.wait(60.0)
+        return builders[nkey]()
+
+    eng = _engine(ws, hbm_budget_bytes=8 << 30, step_capacity_bytes=256 << 20,
+                  max_step_requests=8)
+    eng.register(nkey, nw, nw.meta["table_key"], nw.meta["tree_key"], nw.meta["sched_key"],
+                 build_tables=build)
+    pts = torch.from_numpy(np.ascontiguousarray(nw.tree.targets)).to("cuda")
+    rng = np.random.default_rng(3)
+    x = W.random_gaussian_mixture(rng, nw.dim, 6, (0.05, 0.2)).on_device(pts).contiguous()
+    first = eng.submit(nkey, x)
+    assert first.waited_build
+    others = [eng.submit(k, dens[k][di]) for k, di in reqs[:24]]
+    while any(q.t_done is None for q in others):
+        eng.pump()
+    assert first.t_done is None and eng.table_builds == 0
+    release.set()
+    eng.drain()
+    assert first.t_done is not None and eng.table_builds == 1
+    eng.check_status()
+    got = first.out.cpu().numpy()
+    alone = eng.submit(nkey, x)
+    eng.drain()
+    assert np.array_equal(alone.out.cpu().numpy(), got)
+    tables = eng._tables[nw.meta["table_key"]]
+    built = W.Workload(nw.name, nw.dim, nw.q, nw.kernel, nw.traversal, tables,
+                       np.zeros((1, 0)), nw.seed, meta=nw.meta)
+    ref = oracle_eval(oracle_for_workload(built, PER_LEVEL), built, x.cpu().numpy())
+    assert rel_l2(got, ref) <= TOL_MIXED
+    eng.close()

@@ -18,9 +18,10 @@
 // largest |x'| of that rhs over all boxes).  Because every density of an rhs
 // shares one scale, the FP16 digit planes are formed once per call by a
 // preparation kernel and the tensor-core kernel only gathers them.  A diagonal
-// i + j of digit products summed over K <= 64 source points is an integer of
-// magnitude at most 2^21 for i + j <= 3 and below 2^23 for i + j = 4, exact
-// in the FP32 accumulator.  Those diagonals (the leading 32 bits) get their
+// i + j of digit products summed over K <= 128 source points (one exact
+// round, which may span several table keys) is an integer of magnitude at
+// most 2^22 for i + j <= 3 and below 2^23 for i + j = 4, exact in the FP32
+// accumulator.  Those diagonals (the leading 32 bits) get their
 // own TMEM accumulator, re-initialised per K round and read after every round
 // into int64 registers: one FADD with 1.5 * 2^23 turns an exact d <= 3 float
 // into its integer bits, d = 4 takes a conversion; diagonals i + j = 5, 6
@@ -482,7 +483,8 @@ struct MixedParams {
 //   w == 9      tensor-core issuer (one lane)
 //   w >= 10     readout: TMEM lane quadrant w % 4, RC columns each
 // Pipeline unit = (key, K chunk of kc <= 32 source points); a "round" = the
-// units of one key that share an exact accumulation (K <= 64).  Exact
+// consecutive units (of one or more keys) that share an exact accumulation
+// (K <= kRoundK = 128).  Exact
 // diagonal accumulators (i+j = 2, 3, 4) are double-buffered in TMEM (one
 // buffer per round parity) so the readout of round r overlaps the products of
 // round r+1; the tail diagonals (i+j = 5, 6) accumulate over the whole tile.
@@ -494,6 +496,10 @@ struct MixedParams {
 // keeps ~2^-36 of its rhs's scale in the tails, far below the 2^-24 weight of
 // the tails; the exact diagonals use X1..X3 only).
 constexpr int kStages = 4;
+// source points of one exact round: with balanced digits (|digit| <= 128) a
+// diagonal sum over 128 points is at most 2^21 (i + j = 2), 2^22 (i + j = 3)
+// and 3 * 2^21 (i + j = 4), all exact in FP32
+constexpr int kRoundK = 128;
 constexpr uint32_t kExactCols = 3;   // accumulators per buffer
 constexpr int kProducerWarps = 8;
 constexpr int kRowsPerProducer = 128 / kProducerWarps;
@@ -716,9 +722,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
 
   const int k0 = item.key_begin, k1 = item.key_end;
   const int n_keys = k1 - k0;
-  const int upr = (p.g.kp < 64 ? p.g.kp : 64) / KC;   // units per round
-  const int rpk = (p.g.kp + 63) / 64;                  // rounds per key
-  const int n_rounds = n_keys * rpk;
+  // units of the item, and exact rounds of up to kRoundK source points (a
+  // round may span several keys: the exact diagonals of every key of a tile
+  // row are in the same units)
+  const int n_units = n_keys * p.g.n_kc;
+  constexpr int upr = kRoundK / KC;   // units per round
+  const int n_rounds = (n_units + upr - 1) / upr;
 
   if (tid < 128) {
     int v = p.sched.tile_rows[(int64_t)tile * 128 + tid];
@@ -884,7 +893,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         }
         tc::tc_fence_after();
         const uint32_t exact_col = tbase + (uint32_t)b * 5 * NCH;
-        for (int iu = 0; iu < upr; ++iu, ++u) {
+        for (int iu = 0; iu < upr && u < n_units; ++iu, ++u) {
           const int s = (ubase + u) % kStages;
           const uint32_t ph = ((ubase + u) / kStages) & 1;
           if (!wait_or_abort(&bars.afull[s], ph, &s_abort, limit_us, false)) {
@@ -954,19 +963,19 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       tc::tc_fence_after();
       const uint32_t col = tbase + lane_off + (uint32_t)b * 5 * NCH + cb * RC;
       uint32_t r2[16], r3[16];
-      tc::tmem_ld16(col, r2);                // i + j = 2: |x| <= 127 * 128 * 64 < 2^20
-      tc::tmem_ld16(col + NCH, r3);          // i + j = 3: |x| < 3.2e6 < 2^22
+      tc::tmem_ld16(col, r2);                // i + j = 2: |x| <= 128 * 128 * 128 = 2^21
+      tc::tmem_ld16(col + NCH, r3);          // i + j = 3: |x| <= 2 * 2^21 = 2^22
       tc::tmem_ld_wait();
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
-        // 1.5 * 2^23 + x for |x| < 2^22 is exact, with the integer x in its
-        // low bits (raw bits kMagicBits + x); weights 2^16 and 2^8 of the
-        // d = 2 and d = 3 terms
+        // 1.5 * 2^23 + x for |x| <= 2^22 is exact and its raw bits are
+        // kMagicBits + x (also at x = 2^22, where the sum is 2^24); weights
+        // 2^16 and 2^8 of the d = 2 and d = 3 terms
         const uint32_t b2 = __float_as_uint(__uint_as_float(r2[c]) + kMagic);
         const uint32_t b3 = __float_as_uint(__uint_as_float(r3[c]) + kMagic);
         acc[c] += (unsigned long long)b2 * 65536ull + (unsigned long long)b3 * 256ull;
       }
-      tc::tmem_ld16(col + 2 * NCH, r2);      // i + j = 4: |x| < 5.3e6 < 2^24
+      tc::tmem_ld16(col + 2 * NCH, r2);      // i + j = 4: |x| <= 3 * 2^21 < 2^24
       tc::tmem_ld_wait();
       tc::tc_fence_before();
       __syncwarp();
@@ -1133,7 +1142,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       }
     }
   }
-  ubase += n_rounds * upr;
+  ubase += n_units;
   rbase += n_rounds;
   __syncthreads();
   }   // work items
@@ -1183,7 +1192,8 @@ MixedGeom mixed_geometry(int nq, int table_cplx, int kc, int nch) {
   MixedGeom g;
   g.kp = ((nq + 15) / 16) * 16;
   g.kc = kc ? kc : (g.kp <= 32 ? g.kp : 32);
-  // above one chunk of 32, K is whole exact rounds of 64
+  // above one chunk of 32, K is padded to a multiple of 64 (whole units of
+  // either K chunk)
   if (g.kp > 32) g.kp = ((g.kp + 63) / 64) * 64;
   g.n_kc = g.kp / g.kc;
   const int n = table_cplx ? 2 * nq : nq;

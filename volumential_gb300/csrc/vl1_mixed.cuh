@@ -10,10 +10,10 @@ namespace vl1 {
 
 constexpr int kDigits = 5;         // 8-bit digits per operand (held exactly in FP16)
 constexpr int kDigitBits = 8;
-// Both operands are 39-bit fixed-point magnitudes (a 7-bit top digit and four
-// 8-bit digits) carrying the value's sign: with both top digits below 128, a
-// diagonal sum of digit products over K <= 64 source points stays below 2^22
-// for i + j <= 3, where one FP32 addition recovers its integer bits.
+// Both operands are 39-bit fixed-point magnitudes in balanced base-256
+// digits (|digit| <= 128) carrying the value's sign: a diagonal sum of digit
+// products over K <= 128 source points is at most 2^22 in magnitude for
+// i + j <= 3, where one FP32 addition recovers its integer bits.
 constexpr int kFixedBits = kDigits * kDigitBits - 1;   // table: 39 bits + sign
 constexpr int kXFixedBits = kDigits * kDigitBits - 1;  // densities: 39 bits + sign
 
