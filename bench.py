@@ -982,19 +982,21 @@ def c5_main(args):
 
 
 def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set):
-    """C5 under memory pressure, with table builds on arrival: a new engine
-    whose HBM budget is ``--c5-pressure`` times the mix's resident set serves
-    an open-loop Poisson stream at half the closed-loop rate of requests over
-    the mix's problems with Zipf popularity (s = 1.1), into which
+    """C5 under memory pressure, with table builds on arrival.  Engines whose
+    HBM budget is ``--c5-pressure`` times the mix's resident set serve
+    requests over the mix's problems with Zipf popularity (s = 1.1, a seeded
+    ranking; the most popular problems that fit 80 % of the budget are
+    admitted before the clock, every other one is admitted cold and the
+    least recently used idle entries are evicted).  (1) Closed loop: all
+    requests at once, giving the sustainable rate under pressure.  (2) Open
+    loop on a fresh engine: Poisson arrivals at half that rate, into which
     ``--c5-new`` new Helmholtz problems (k uniform in [1, 30], real) arrive
-    one after another; the first request of a new
-    problem starts the FP64 Duffy build of its table on the engine's build
-    thread (the engine keeps serving the others), and every problem, old or
-    new, is admitted cold and evicted least-recently-used under the budget.
-    Reports latency percentiles (all requests, those that waited for a table
-    build, the others), evictions, admissions and builds, the error of the
-    new problems against the FP64 path, and that sampled results are the
-    same bits alone and in the mix."""
+    one after another; the first request of a new problem starts the FP64
+    Duffy build of its table on the engine's build thread while the engine
+    keeps serving the others.  Reports latency percentiles (all requests,
+    those that waited for a table build, the others), evictions, admissions
+    and builds, the new problems' error against the FP64 path, and that
+    sampled results are the same bits alone and in the mix."""
     import torch
 
     from volumential_gb300 import workloads as W
@@ -1004,14 +1006,49 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
         eng.budget.make_room(eng.budget.budget)
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
+    budget = int(args.c5_pressure * resident_set)
+    keys = sorted(ws)
+    rng = np.random.default_rng(77)
+    rank = rng.permutation(len(keys))
+    pop = 1.0 / (1.0 + rank) ** 1.1
+    pop /= pop.sum()
+    n_base = len(reqs)
+    stream = [(keys[i], int(rng.integers(4))) for i in rng.choice(len(keys), size=n_base, p=pop)]
+
+    serve_stream = torch.cuda.Stream(priority=-1)   # ahead of the table builds
+
+    def engine():
+        e = ServingEngine(hbm_budget_bytes=budget, step_capacity_bytes=4 << 30,
+                          max_step_requests=args.c5_step, stream=serve_stream)
+        for key, w in ws.items():
+            e.register(key, w, w.meta["table_key"], w.meta["tree_key"], w.meta["sched_key"])
+        for i in np.argsort(rank):
+            if e.budget.used > 0.8 * budget:
+                break
+            e.admit(keys[i])
+        torch.cuda.synchronize()
+        return e
+
+    # (1) closed loop under pressure
+    e1 = engine()
+    t0 = time.perf_counter()
+    for key, di in stream:
+        e1.submit(key, dens[key][di])
+    e1.drain()
+    torch.cuda.synchronize()
+    closed_s = time.perf_counter() - t0
+    closed = {"solves_per_s": n_base / closed_s, "evictions": e1.budget.evictions,
+              "cold_admissions": e1.cold_admissions}
+    e1.budget.make_room(budget)
+    e1.budget.make_room(budget)
+    e1.close()
+    del e1
+    torch.cuda.empty_cache()
+
+    # (2) open loop at half the pressure rate, new problems arriving
     new_probs = W.config_c5_arrivals(n_new=args.c5_new)
     new_ws, builders = W.c5_arrival_workloads(new_probs)
-    budget = int(args.c5_pressure * resident_set)
-    eng2 = ServingEngine(hbm_budget_bytes=budget, step_capacity_bytes=4 << 30,
-                         max_step_requests=args.c5_step)
-    for key, w in ws.items():
-        eng2.register(key, w, w.meta["table_key"], w.meta["tree_key"], w.meta["sched_key"])
-    rng = np.random.default_rng(77)
+    eng2 = engine()
     new_dens = {}
     for key, w in new_ws.items():
         eng2.register(key, w, w.meta["table_key"], w.meta["tree_key"], w.meta["sched_key"],
@@ -1022,27 +1059,12 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
         new_dens[key] = [m.on_device(pts).contiguous() for m in mixes]
     all_dens = dict(dens)
     all_dens.update(new_dens)
-    # the stream: requests over the mix's problems with Zipf popularity
-    # (s = 1.1, a seeded ranking), Poisson at half the closed-loop rate; the
-    # most popular problems that fit are admitted before the clock starts;
-    # new problem i starts at (0.1 + 0.5 i / n_new) of the run, then 24
-    # requests within a fifth of it
-    keys = sorted(ws)
-    rank = rng.permutation(len(keys))
-    pop = 1.0 / (1.0 + rank) ** 1.1
-    pop /= pop.sum()
-    n_base = len(reqs)
-    pick = rng.choice(len(keys), size=n_base, p=pop)
-    stream = [(keys[i], int(rng.integers(4))) for i in pick]
-    for i in np.argsort(rank):
-        if eng2.budget.used > 0.8 * budget:
-            break
-        eng2.admit(keys[i])
-    torch.cuda.synchronize()
-    rate = 0.5 * closed_rate
+    rate = 0.5 * closed["solves_per_s"]
     t_base = W.poisson_arrivals(n_base, rate, seed=78)
     span = float(t_base[-1])
     events = [(float(t), k, di) for t, (k, di) in zip(t_base, stream)]
+    # new problem i starts at (0.1 + 0.5 i / n_new) of the run, then 24
+    # requests within a fifth of it
     per_new = 24
     for i, key in enumerate(sorted(new_ws)):
         t0 = span * (0.1 + 0.5 * i / max(len(new_ws), 1))
@@ -1055,16 +1077,13 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
     arrivals, outs = [], {}
     for j, (t, key, di) in enumerate(events):
         w = ws.get(key) or new_ws[key]
-        cplx = w.kernel.is_complex_valued
+        dt = torch.complex128 if w.kernel.is_complex_valued else torch.float64
         if j in sample_ids:
-            out = torch.empty(w.n_points, dtype=torch.complex128 if cplx else torch.float64,
-                              device="cuda")
+            out = torch.empty(w.n_points, dtype=dt, device="cuda")
         else:
             out = outs.get(key)
             if out is None:
-                out = outs[key] = torch.empty(
-                    w.n_points, dtype=torch.complex128 if cplx else torch.float64,
-                    device="cuda")
+                out = outs[key] = torch.empty(w.n_points, dtype=dt, device="cuda")
         arrivals.append((t, key, all_dens[key][di], out))
     torch.cuda.synchronize()
     done, wall = eng2.run(arrivals)
@@ -1074,7 +1093,7 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
     # sampled requests again, one at a time: identical bits; new problems
     # against the FP64 path
     same, errs = True, []
-    sh = torch.cuda.current_stream().cuda_stream
+    sh = serve_stream.cuda_stream
     for j in sorted(sample_ids):
         q = done[j]
         alone = eng2.submit(q.key, q.coefs)
@@ -1091,6 +1110,7 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
         "hbm_budget_bytes": budget, "mix_resident_set_bytes": resident_set,
         "popularity": "Zipf s = 1.1 over the mix's problems (seeded ranking); the most "
                       "popular that fit 80 % of the budget admitted before the clock",
+        "closed_loop": closed,
         "requests": len(done), "new_problems": len(new_ws),
         "new_problem_k": sorted(float(k[2]) for k in new_ws),
         "new_problem_shapes": sorted(f"{k[0]}d_q{k[3]}_l{k[4]}" for k in new_ws),

@@ -110,10 +110,10 @@ typedef struct {
 /* One CTA's share of the mixed-precision work: keys [key_begin, key_end) of
  * one tile (indices into key_ids / key_xrow, inside the tile's own range).
  * A tile with many keys is split into `nparts` items (part 0 .. nparts-1);
- * each writes its exact partial sums to partial slot `slot`, and the item that
- * finishes last adds the slots slot - part .. slot - part + nparts - 1 in slot
- * order and writes the tile's results.  Unsplit items have split = -1,
- * part = 0, nparts = 1, slot = -1. */
+ * each adds its exact int64 partial sums into the slot of part 0 (slot -
+ * part), and the item that finishes last writes the tile's results and
+ * clears the slot.  Unsplit items have split = -1, part = 0, nparts = 1,
+ * slot = -1. */
 typedef struct {
   int32_t tile;
   int32_t key_begin;
@@ -134,9 +134,12 @@ typedef struct {
  * has no list-1 pair of that key.
  * items: n_items work items, launched in this order (longest first balances
  * the GPU); n_items == 0 means one item per tile covering all its keys.
- * split_counters: n_splits * n_chunks int32, zero before the first call;
- * every call leaves them zero.  split_partials: n_slots * (128 * padded
- * output columns) * 8 bytes of scratch for split tiles.  n_chunks: the
+ * split_counters: n_splits * n_chunks * 16 int32 (the counter of split tile
+ * s and column chunk c at index (s * n_chunks + c) * 16), zero before the
+ * first call; every call leaves them zero.  split_partials: n_slots * (128 * padded
+ * output columns) * 8 bytes for split tiles (the parts of a split tile add
+ * their exact int64 sums into the slot of its part 0), zero before the first
+ * call; every call leaves it zero.  n_chunks: the
  * plan's output column chunks (padded output columns / columns per CTA) when
  * the split scratch was sized; a call on a plan with another count is
  * refused (VL1_E_ARG).
@@ -174,7 +177,15 @@ const char *vl1_last_error_string(void);
  * plus the per-pair RECONSTRUCT_ENTRY work of list1.py:604-854, which the
  * plan performs once per (table level, case, source mode, target point). */
 int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out);
+/* Waits for the device to be idle, then frees the plan. */
 int32_t vl1_plan_destroy(vl1_plan *plan);
+/* Frees the plan without a device-wide synchronisation: its device memory
+ * is released in the order of `stream` (stream-ordered allocator), so the
+ * caller guarantees that every call using the plan was issued on `stream` or
+ * has completed.  No reference counterpart (the reference's payload cache
+ * lives as long as its wrangler); a serving engine evicting idle plans while
+ * table builds run on another stream uses it. */
+int32_t vl1_plan_release(vl1_plan *plan, void *stream);
 
 /* Plain FP64 list-1 evaluation (the reference's near_field kernel,
  * list1.py:1050-1159, potential_kind=1) for nrhs right-hand sides.

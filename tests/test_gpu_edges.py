@@ -80,8 +80,9 @@ def test_densities_over_hundreds_of_decades(cuda, dim, policy):
             continue
         worst_p = max(worst_p, np.max(np.abs(plain[sl] - ref[sl])) / scale)
     assert worst_p <= 1e-11
-    assert rel_l2(mixed, ref) <= 1e-9
-    assert np.max(np.abs(mixed - ref)) <= 1e-9 * np.max(np.abs(ref))
+    s = np.max(np.abs(ref))   # norms of values near 1e250 would overflow
+    assert rel_l2(mixed / s, ref / s) <= 1e-9
+    assert np.max(np.abs(mixed - ref)) <= 1e-9 * s
 
 
 def test_densities_near_the_bottom_of_fp64(cuda):

@@ -173,6 +173,7 @@ SIGNATURES = {
     "vl1_last_error_string": (C.c_char_p, []),
     "vl1_plan_create": (C.c_int32, [C.POINTER(PlanDesc), C.POINTER(C.c_void_p)]),
     "vl1_plan_destroy": (C.c_int32, [C.c_void_p]),
+    "vl1_plan_release": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "vl1_eval_fp64": (C.c_int32, [C.c_void_p, C.POINTER(TreeView), C.c_void_p,
                                   C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "vl1_orbit_index_map": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p,

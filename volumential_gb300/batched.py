@@ -185,9 +185,10 @@ class MixedSchedule:
         self.items_np = np.ascontiguousarray(items if len(items)
                                              else np.zeros((1, 8), np.int32))
         self.items = torch.from_numpy(self.items_np).to("cuda")
-        self.split_counters = torch.zeros(max(1, n_splits * n_chunks), dtype=torch.int32,
+        # one counter per split tile and column chunk, spaced 16 apart
+        self.split_counters = torch.zeros(max(1, n_splits * n_chunks * 16), dtype=torch.int32,
                                           device="cuda")
-        self.split_partials = torch.empty(max(16, n_slots * ROWS_PER_TILE * geo["np"] * 8),
+        self.split_partials = torch.zeros(max(16, n_slots * ROWS_PER_TILE * geo["np"] * 8),
                                           dtype=torch.uint8, device="cuda")
         s = _lib.MixedSchedule()
         s.n_tiles = n_tiles

@@ -35,10 +35,13 @@ int32_t plan_alloc(vl1_plan *p, void **out, size_t bytes) {
     set_error("internal: too many plan allocations");
     return VL1_E_NOMEM;
   }
+  // stream-ordered allocation on the legacy stream: unlike cudaMalloc /
+  // cudaFree it never waits for work on other streams (a serving engine
+  // admits plans while table builds run on a stream of their own)
   void *ptr = nullptr;
-  cudaError_t e = cudaMalloc(&ptr, bytes ? bytes : 16);
+  cudaError_t e = cudaMallocAsync(&ptr, bytes ? bytes : 16, 0);
   if (e != cudaSuccess) {
-    set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    set_error("cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
     return VL1_E_NOMEM;
   }
   p->allocs[p->n_allocs++] = ptr;
@@ -60,8 +63,9 @@ int32_t upload(vl1_plan *p, const T **dev, const void *host, size_t bytes) {
   return VL1_OK;
 }
 
-void free_plan(vl1_plan *p) {
-  for (int i = 0; i < p->n_allocs; ++i) cudaFree(p->allocs[i]);
+// the plan's device memory is freed in the order of `s`
+void free_plan(vl1_plan *p, cudaStream_t s) {
+  for (int i = 0; i < p->n_allocs; ++i) cudaFreeAsync(p->allocs[i], s);
   p->n_allocs = 0;
   delete p;
 }
@@ -191,7 +195,8 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
     if (p->block_elems * (d.table_cplx ? 2 : 1) >= ((int64_t)1 << 31)) {
       set_error("expanded blocks (%lld values) exceed the 2^31 index range",
                 (long long)p->block_elems);
-      free_plan(p);
+      cudaStreamSynchronize(0);
+      free_plan(p, 0);
       return VL1_E_UNSUPPORTED;
     }
     void *ptr = nullptr;
@@ -225,7 +230,9 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
     }
   }
   if (!st) {
-    cudaError_t e = cudaDeviceSynchronize();
+    // the plan's own work (uploads, block expansion, digit operands) was
+    // ordered on the legacy stream; work on other streams is not waited for
+    cudaError_t e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) st = cuda_fail(e, "plan block expansion");
   }
   if (!st) {
@@ -240,7 +247,8 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
     }
   }
   if (st) {
-    free_plan(p);
+    cudaStreamSynchronize(0);
+    free_plan(p, 0);
     return st;
   }
   *plan_out = p;
@@ -250,7 +258,13 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
 int32_t vl1_plan_destroy(vl1_plan *plan) {
   if (!plan) return VL1_OK;
   cudaDeviceSynchronize();
-  free_plan(plan);
+  free_plan(plan, 0);
+  return VL1_OK;
+}
+
+int32_t vl1_plan_release(vl1_plan *plan, void *stream) {
+  if (!plan) return VL1_OK;
+  free_plan(plan, static_cast<cudaStream_t>(stream));
   return VL1_OK;
 }
 
@@ -376,10 +390,10 @@ int32_t vl1_plan_set_mixed_geometry(vl1_plan *plan, int32_t kc, int32_t nch) {
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "vl1_plan_set_mixed_geometry: synchronise");
   void *ptr = nullptr;
-  e = cudaMalloc(&ptr, 2 * (size_t)elems);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(plan digit operands)");
+  e = cudaMallocAsync(&ptr, 2 * (size_t)elems, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(plan digit operands)");
   const int k = plan->mixed.adig_alloc;
-  cudaFree(plan->allocs[k]);
+  cudaFreeAsync(plan->allocs[k], 0);
   plan->allocs[k] = ptr;
   plan->device_bytes += 2 * (elems - plan->mixed.adig_elems);
   plan->mixed.adig = static_cast<__half *>(ptr);

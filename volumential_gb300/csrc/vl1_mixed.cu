@@ -417,28 +417,17 @@ __device__ __forceinline__ double scaled_i64_to_double(long long v, int k) {
   return ldexp((double)v, k);   // subnormal or overflowing results
 }
 
-// round(x * 2^s) to the nearest int64 (ties to even) with integer operations
-// (64-bit conversions run on the narrow FP64 side of this GPU); |x| * 2^s
-// must stay below 2^62, which the FP32 tail accumulators do by far
-__device__ __forceinline__ long long f32_scaled_to_i64(float x, int s) {
-  const uint32_t b = __float_as_uint(x);
-  const int e = (int)((b >> 23) & 0xFFu);
-  if (e == 0) return 0;   // zero or subnormal: rounds to 0
-  const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
-  const int sh = e - 150 + s;   // |x| * 2^s = m * 2^sh
-  long long q;
-  if (sh >= 0) {
-    q = m << sh;
-  } else if (sh < -25) {
-    q = 0;                      // below 1/4
-  } else {
-    const int k = -sh;
-    q = m >> k;
-    const long long rem = m & ((1ll << k) - 1);
-    const long long half = 1ll << (k - 1);
-    q += (rem > half || (rem == half && (q & 1))) ? 1 : 0;
-  }
-  return (b >> 31) ? -q : q;
+// round(x * 2^s) to the nearest int64 for a tail accumulator x (|x| * 2^s
+// below 2^62), with 32-bit conversions only (64-bit conversions run on the
+// narrow FP64 side of this GPU): h = trunc(x * 2^s / 2^31) is exact in
+// FP32, the remainder x * 2^s - h * 2^31 (one FMA, exact: it is the low bits
+// of x's 24-bit significand) is below 2^31 in magnitude and rounds to
+// nearest in one conversion.
+__device__ __forceinline__ long long f32_scaled_to_i64(float x, float two_s) {
+  const float xs = x * two_s;                        // exact: a power of two
+  const float h = truncf(xs * 4.656612873077393e-10f);   // x * 2^s / 2^31, toward 0
+  const float rem = __fmaf_rn(-h, 2147483648.0f, xs);     // exact
+  return ((long long)__float2int_rz(h) << 31) + (long long)__float2int_rn(rem);
 }
 
 // ---------------------------------------------------------- main kernel
@@ -495,27 +484,42 @@ struct MixedParams {
 // only, R = X4 + X5 / 256 rounded to FP16 (11 significant bits: the density
 // keeps ~2^-36 of its rhs's scale in the tails, far below the 2^-24 weight of
 // the tails; the exact diagonals use X1..X3 only).
-constexpr int kStages = 4;
+// Roles and pipeline depth per column chunk width.  64 output columns: 8
+// producer warps, 4 stages, one CTA per SM (214 KB of shared memory, all 512
+// TMEM columns).  16 or 32 columns: 4 producer warps, 2 stages and two CTAs
+// per SM (at most 91 KB and 256 TMEM columns each, <= 73 registers per
+// thread), so that one CTA's pipeline fill, readout and result write overlap
+// the other's tensor-core work.
+template <int NCH>
+struct MixedRoles {
+  static constexpr int kProducers = NCH >= 64 ? 8 : 4;
+  static constexpr int kRowsPerProducer = 128 / kProducers;
+  static constexpr int kLoader = kProducers;
+  static constexpr int kMma = kProducers + 1;
+  static constexpr int kRead0 = kProducers + 2;
+  static constexpr int kStages = NCH >= 64 ? 4 : 2;
+  static constexpr int kCtasPerSm = NCH >= 64 ? 1 : 2;
+  static constexpr int kThreads = 32 * (kRead0 + 4 * (NCH / 16));
+};
+constexpr int kMaxStages = 4;
 // source points of one exact round: with balanced digits (|digit| <= 128) a
 // diagonal sum over 128 points is at most 2^21 (i + j = 2), 2^22 (i + j = 3)
 // and 3 * 2^21 (i + j = 4), all exact in FP32
 constexpr int kRoundK = 128;
 constexpr uint32_t kExactCols = 3;   // accumulators per buffer
-constexpr int kProducerWarps = 8;
-constexpr int kRowsPerProducer = 128 / kProducerWarps;
-constexpr int kLoaderWarp = 8;
-constexpr int kMmaWarp = 9;
-constexpr int kReadWarp0 = 10;
 constexpr uint32_t kSleepNs = 200000;      // suspend hint of one barrier test
 constexpr uint32_t kWaitLimitUs = 2000000; // a wait gives up after 2 s
 // split-tile counters: parts in the low 16 bits, aborted parts also in the
 // high bits (a tile has fewer than 2^16 parts)
 constexpr int kSplitPoison = 1 << 16;
+// split counters are spaced 16 apart (one per split tile and column chunk,
+// in a layout that leaves room for per-piece counts)
+constexpr int kSplitCounterStride = 16;
 
 struct Barriers {
-  uint64_t xfull[kStages];   // every producer lane's density copies have landed
-  uint64_t afull[kStages];   // the table digit tiles have landed
-  uint64_t empty[kStages];
+  uint64_t xfull[kMaxStages];   // every producer lane's density copies have landed
+  uint64_t afull[kMaxStages];   // the table digit tiles have landed
+  uint64_t empty[kMaxStages];
   uint64_t accf[2];
   uint64_t acce[2];
   uint64_t drain;            // after an abort: every issued MMA has completed
@@ -606,8 +610,15 @@ __device__ constexpr MmaGroup kGroups[kGroupCount] = {{1, 1, 3, 1}, {2, 1, 2, 1}
 // item's problem parameters are copied to shared memory, and the pipeline
 // barriers keep their phases across items (CTA-wide unit / round counters).
 template <int NCH, int KC, bool MULTI>
-__global__ void __launch_bounds__(32 * (kReadWarp0 + 4 * (NCH / 16)), 1)
+__global__ void __launch_bounds__(MixedRoles<NCH>::kThreads, MixedRoles<NCH>::kCtasPerSm)
 mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ BatchLaunch bl) {
+  using Roles = MixedRoles<NCH>;
+  constexpr int kStages = Roles::kStages;
+  constexpr int kProducerWarps = Roles::kProducers;
+  constexpr int kRowsPerProducer = Roles::kRowsPerProducer;
+  constexpr int kLoaderWarp = Roles::kLoader;
+  constexpr int kMmaWarp = Roles::kMma;
+  constexpr int kReadWarp0 = Roles::kRead0;
   constexpr int RC = 16;                            // columns per readout warp
   constexpr int NREAD = 4 * (NCH / RC);             // readout warps
   // TMEM: [buffer 0: 3 x NCH][tail d5][tail d6][buffer 1: 3 x NCH]
@@ -729,6 +740,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   constexpr int upr = kRoundK / KC;   // units per round
   const int n_rounds = (n_units + upr - 1) / upr;
 
+  // the rows of the tile, and (for the result write at the end of the item,
+  // loaded now so that their latency hides behind the pipeline) each row's
+  // first result index, point count and output exponent
+  __shared__ long long s_obase[128];   // result index of the row's first target point
+  __shared__ int s_ocnt[128];          // target points of the row's box (0: empty row)
+  __shared__ int s_oexp[128];          // an output is (parked sum) * 2^s_oexp
   if (tid < 128) {
     int v = p.sched.tile_rows[(int64_t)tile * 128 + tid];
     if (v >= (int64_t)p.n_tgt_boxes * p.nrhs) {
@@ -736,6 +753,21 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       v = -1;
     }
     s_rows[tid] = v;
+    int cnt = 0, ex = 0;
+    long long ob = 0;
+    if (v >= 0) {
+      const int j = v / p.nrhs, r = v - (v / p.nrhs) * p.nrhs;
+      const int tbox = p.target_boxes[j];
+      cnt = min(p.tgt_counts[tbox], p.d.nq);
+      ob = (long long)r * p.n_particles + p.tgt_starts[tbox];
+      // table values are m_a 2^(a_exp - kFixedBits), densities
+      // m_x 2^(e - kXFixedBits) with e the scale exponent of the rhs; the
+      // parked sums count units of 2^32 of m_a m_x
+      ex = p.a_exp + (p.x_exp[r] - kExpBias) - (kFixedBits + kXFixedBits) + 32;
+    }
+    s_obase[tid] = ob;
+    s_ocnt[tid] = cnt;
+    s_oexp[tid] = ex;
   }
   __syncthreads();
 
@@ -1003,12 +1035,12 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         tc::tmem_ld_wait();
 #pragma unroll
         for (int c = 0; c < 16; ++c)
-          acc[c] += (unsigned long long)f32_scaled_to_i64(__uint_as_float(r16[c]), 8);
+          acc[c] += (unsigned long long)f32_scaled_to_i64(__uint_as_float(r16[c]), 256.0f);
         tc::tmem_ld16(col + NCH, r16);           // d6, weight 2^32
         tc::tmem_ld_wait();
 #pragma unroll
         for (int c = 0; c < 16; ++c)
-          acc[c] += (unsigned long long)f32_scaled_to_i64(__uint_as_float(r16[c]), 0);
+          acc[c] += (unsigned long long)f32_scaled_to_i64(__uint_as_float(r16[c]), 1.0f);
       }
 #pragma unroll
       for (int c = 0; c < 16; ++c)
@@ -1024,56 +1056,37 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
   tc::tc_fence_before();
   __syncthreads();
   __shared__ int s_last, s_poison;
-  __shared__ long long s_obase[128];   // result index of the row's first target point
-  __shared__ int s_ocnt[128];          // target points of the row's box (0: empty row)
-  __shared__ int s_oexp[128];          // an output is (parked sum) * 2^s_oexp
-  if (tid < 128) {
-    const int v = s_rows[tid];
-    int cnt = 0, ex = 0;
-    long long ob = 0;
-    if (v >= 0) {
-      const int j = v / p.nrhs, r = v - (v / p.nrhs) * p.nrhs;
-      const int tbox = p.target_boxes[j];
-      cnt = min(p.tgt_counts[tbox], p.d.nq);
-      ob = (long long)r * p.n_particles + p.tgt_starts[tbox];
-      // table values are m_a 2^(a_exp - kFixedBits), densities
-      // m_x 2^(e - kXFixedBits) with e the scale exponent of the rhs; the
-      // parked sums count units of 2^32 of m_a m_x
-      ex = p.a_exp + (p.x_exp[r] - kExpBias) - (kFixedBits + kXFixedBits) + 32;
-    }
-    s_obase[tid] = ob;
-    s_ocnt[tid] = cnt;
-    s_oexp[tid] = ex;
-  }
   const long long *tot_src = reinterpret_cast<const long long *>(smem);
   bool write = !s_abort;
-  const uint8_t *g_parts = nullptr;   // slot region of part 0 of a split tile
+  // a split tile's accumulator: the parts add their exact int64 sums into
+  // the slot of part 0 (integer addition: the total does not depend on the
+  // order); the part that arrives last writes the results and clears it
+  unsigned long long *g_acc = nullptr;
   const int64_t slot_bytes = (int64_t)128 * NCH * 8;
-  const int64_t part_stride = (int64_t)n_chunks * slot_bytes;
+  int *g_ctr = nullptr;
   if (item.split >= 0) {
-    uint8_t *base = static_cast<uint8_t *>(p.sched.split_partials) +
-                    ((int64_t)(item.slot - item.part) * n_chunks + chunk) * slot_bytes;
-    g_parts = base;
+    g_acc = reinterpret_cast<unsigned long long *>(
+        static_cast<uint8_t *>(p.sched.split_partials) +
+        ((int64_t)(item.slot - item.part) * n_chunks + chunk) * slot_bytes);
+    g_ctr = p.sched.split_counters + ((int64_t)item.split * n_chunks + chunk) * kSplitCounterStride;
     if (!s_abort) {
-      long long *mine = reinterpret_cast<long long *>(base + item.part * part_stride);
       for (int i = tid; i < 128 * NCH; i += blockDim.x)
-        mine[i] = tot_src[(i / NCH) * PARK_STRIDE + i % NCH];
+        atomicAdd(g_acc + i, (unsigned long long)tot_src[(i / NCH) * PARK_STRIDE + i % NCH]);
     }
     __threadfence();
     __syncthreads();
     if (tid == 0) {
-      // parts count in the low 16 bits; a part that aborted (and stored no
-      // partial sums) also adds to the high bits, so that the last part
-      // writes nothing for the tile
+      // parts count in the low 16 bits; a part that aborted (and added no
+      // sums) also adds to the high bits, so that the last part writes
+      // nothing for the tile
       const int inc = s_abort ? kSplitPoison + 1 : 1;
-      const int done =
-          atomicAdd(p.sched.split_counters + item.split * n_chunks + chunk, inc) + inc;
+      const int done = atomicAdd(g_ctr, inc) + inc;
       s_last = (done & (kSplitPoison - 1)) == item.nparts;
       s_poison = done >= kSplitPoison;
     }
     __syncthreads();
     write = write && s_last && !s_poison;
-    if (write) __threadfence();
+    if (s_last) __threadfence();
   } else {
     __syncthreads();
   }
@@ -1090,8 +1103,7 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         tot[bi] = 0;
         if (it >= 128 * NCH) continue;
         if (item.split >= 0) {
-          for (int q = 0; q < item.nparts; ++q)
-            tot[bi] += __ldcg(reinterpret_cast<const long long *>(g_parts + q * part_stride) + it);
+          tot[bi] = (long long)__ldcg(g_acc + it);
         } else {
           tot[bi] = tot_src[(it / NCH) * PARK_STRIDE + it % NCH];
         }
@@ -1120,10 +1132,13 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
       }
     }
   }
-  // the last part leaves the counter at zero for the next call (also after
-  // an abort, so that a timed-out call does not spoil the schedule)
-  if (item.split >= 0 && tid == 0 && s_last)
-    p.sched.split_counters[item.split * n_chunks + chunk] = 0;
+  // the last part leaves the accumulator and the counter at zero for the
+  // next call (also after an abort, so that a timed-out call does not spoil
+  // the schedule); each thread clears the entries it read
+  if (item.split >= 0 && s_last) {
+    for (int i = tid; i < 128 * NCH; i += blockDim.x) g_acc[i] = 0ull;
+    if (tid == 0) *g_ctr = 0;
+  }
   __syncthreads();
   if (s_abort && tid == 0) {
     report(p.st, VL1_E_TIMEOUT, tile, chunk);
@@ -1136,9 +1151,18 @@ mixed_kernel(const __grid_constant__ MixedParams p1, const __grid_constant__ Bat
         const BatchItem bj = bl.items[wj];
         if (bj.item.split < 0) continue;
         const MixedParams *pj = bl.probs + bj.problem;
-        int *ctr = pj->sched.split_counters + bj.item.split * (pj->g.np / NCH) + bj.chunk;
+        const int nchk = pj->g.np / NCH;
+        int *ctr = pj->sched.split_counters +
+                   ((int64_t)bj.item.split * nchk + bj.chunk) * kSplitCounterStride;
         const int done = atomicAdd(ctr, kSplitPoison + 1) + kSplitPoison + 1;
-        if ((done & (kSplitPoison - 1)) == bj.item.nparts) *ctr = 0;
+        if ((done & (kSplitPoison - 1)) == bj.item.nparts) {
+          // the tile's last arrival: clear what its other parts added
+          unsigned long long *acc = reinterpret_cast<unsigned long long *>(
+              static_cast<uint8_t *>(pj->sched.split_partials) +
+              ((int64_t)(bj.item.slot - bj.item.part) * nchk + bj.chunk) * slot_bytes);
+          for (int i = 0; i < 128 * NCH; ++i) acc[i] = 0ull;
+          *ctr = 0;
+        }
       }
     }
   }
@@ -1161,12 +1185,18 @@ const void *mixed_kernel_ptr(int nch, int kc, bool multi) {
 }
 
 size_t mixed_smem_bytes(int nch, int kc) {
-  const size_t pipe = (size_t)kStages * (kXPlanes * 128 + kDigits * nch) * kc * 2;
+  const int stages = nch >= 64 ? MixedRoles<64>::kStages : MixedRoles<32>::kStages;
+  const size_t pipe = (size_t)stages * (kXPlanes * 128 + kDigits * nch) * kc * 2;
   const size_t park = (size_t)128 * (nch + 1) * 8;   // int64 sums, padded rows
   return (pipe > park ? pipe : park) + 1024;
 }
 
-int mixed_threads(int nch) { return 32 * (kReadWarp0 + 4 * (nch / 16)); }
+int mixed_threads(int nch) {
+  return nch >= 64 ? MixedRoles<64>::kThreads
+                   : (nch >= 32 ? MixedRoles<32>::kThreads : MixedRoles<16>::kThreads);
+}
+
+int mixed_ctas_per_sm(int nch) { return nch >= 64 ? 1 : 2; }
 
 cudaError_t launch_mixed_kernel(int nch, int kc, bool multi, dim3 grid, cudaStream_t s,
                                 const MixedParams &mp, const BatchLaunch &bl) {
@@ -1560,7 +1590,8 @@ int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t
     const MixedGeom &g = problems[i].plan->mixed.geom;
     const int64_t n_x = sc.n_items > 0 ? sc.n_items : sc.n_tiles;
     const int64_t ctas = n_x * (g.np / g.nch);
-    if (ctas >= 2ll * n_sm && n_x < INT32_MAX && mixed_kernel_ptr(g.nch, g.kc, false)) {
+    if (ctas >= 2ll * n_sm * mixed_ctas_per_sm(g.nch) && n_x < INT32_MAX &&
+        mixed_kernel_ptr(g.nch, g.kc, false)) {
       solo[i] = 1;
       SoloLaunch sl;
       sl.problem = i;
@@ -1595,7 +1626,7 @@ int32_t assemble_batch(const char *who, int dev, int n_sm, int ctas_opt, int32_t
     bg.kc = sh.second;
     bg.item0 = (int)L.all.size();
     bg.n_items = (int)cands.size();
-    const int ctas = ctas_opt > 0 ? ctas_opt : n_sm;
+    const int ctas = ctas_opt > 0 ? ctas_opt : n_sm * mixed_ctas_per_sm(sh.first);
     bg.grid = bg.n_items < ctas ? bg.n_items : ctas;
     for (const Cand &c : cands) L.all.push_back(c.it);
     if (bg.n_items > 0) L.groups.push_back(bg);

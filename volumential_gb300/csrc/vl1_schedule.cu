@@ -262,6 +262,7 @@ struct vl1_schedule_builder {
   int n_tiles = 0;
   int64_t n_entries = 0;
   void *buf = nullptr;   // one device allocation for all scratch
+  cudaStream_t stream = nullptr;   // the builder's stream (its scratch is freed there)
   int32_t *keys = nullptr, *pair_box = nullptr, *freq = nullptr, *rank = nullptr;
   unsigned long long *box_mask = nullptr, *sort_key = nullptr, *word_a = nullptr,
                      *word_b = nullptr, *tile_mask = nullptr;
@@ -329,9 +330,8 @@ extern "C" int32_t vl1_schedule_build_begin(vl1_plan *plan, const vl1_tree_view 
   const int32_t st = schedule_begin(plan, tree, nnz, nrhs, b, sizes,
                                     static_cast<cudaStream_t>(stream));
   if (st != VL1_OK) {
-    // let launched work finish before its scratch is released
-    cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
-    if (b->buf) cudaFree(b->buf);
+    // the scratch is released in stream order, after the launched work
+    if (b->buf) cudaFreeAsync(b->buf, static_cast<cudaStream_t>(stream));
     delete b;
     return st;
   }
@@ -390,11 +390,13 @@ int32_t schedule_begin(vl1_plan *plan, const vl1_tree_view *tree, int64_t nnz, i
       align256(sizeof(SchedStatus))};
   int64_t total = 0;
   for (int64_t v : sz) total += v;
-  cudaError_t e = cudaMalloc(&b->buf, total);
+  // stream-ordered: never waits for work on other streams
+  cudaError_t e = cudaMallocAsync(&b->buf, total, s);
   if (e != cudaSuccess) {
     b->buf = nullptr;
-    return cuda_fail(e, "cudaMalloc(schedule builder)");
+    return cuda_fail(e, "cudaMallocAsync(schedule builder)");
   }
+  b->stream = s;
   uint8_t *p = static_cast<uint8_t *>(b->buf);
   int k = 0;
   auto take = [&](auto *&ptr) {
@@ -542,9 +544,9 @@ extern "C" int32_t vl1_schedule_build_fill(vl1_schedule_builder *b, int32_t *til
 
 extern "C" int32_t vl1_schedule_builder_destroy(vl1_schedule_builder *b) {
   if (!b) return VL1_OK;
-  cudaError_t e = b->buf ? cudaFree(b->buf) : cudaSuccess;
+  cudaError_t e = b->buf ? cudaFreeAsync(b->buf, b->stream) : cudaSuccess;
   delete b;
-  return e == cudaSuccess ? VL1_OK : cuda_fail(e, "cudaFree(schedule builder)");
+  return e == cudaSuccess ? VL1_OK : cuda_fail(e, "cudaFreeAsync(schedule builder)");
 }
 
 // ---------------------------------------------------------------------------

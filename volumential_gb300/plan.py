@@ -297,6 +297,14 @@ class Plan:
             self._lib.vl1_plan_destroy(self._handle)
             self._handle = None
 
+    def release(self, stream):
+        """Free the plan without a device-wide synchronisation, in the order
+        of ``stream`` (a cudaStream_t handle): every call using the plan
+        must have been issued on that stream or have completed."""
+        if getattr(self, "_handle", None) is not None:
+            self._lib.vl1_plan_release(self._handle, C.c_void_p(stream))
+            self._handle = None
+
     def __del__(self):
         try:
             self.destroy()

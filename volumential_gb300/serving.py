@@ -34,7 +34,7 @@ import time
 import numpy as np
 
 from . import _lib
-from .batch import plan_for, tree_arrays
+from .batch import _plan_from, _plan_kwargs, tree_arrays
 from .batched import MixedSchedule
 
 __all__ = ["AdmissionError", "ResidentBudget", "Request", "ServingEngine", "latency_stats"]
@@ -166,9 +166,11 @@ class ServingEngine:
     A problem registered with ``build_tables`` (a function returning its
     table set, e.g. the FP64 Duffy builder for its wave number) has no table
     values yet: the first request for it starts the build on a worker thread
-    and its own CUDA stream, and the engine keeps serving the other problems
-    meanwhile; the request waits (in order) until the tables are built, then
-    the plan is admitted like any other.  Built table sets stay in a host
+    and its own lowest-priority CUDA stream, and the engine keeps serving the
+    other problems meanwhile (give the engine a high-priority ``stream``,
+    e.g. ``torch.cuda.Stream(priority=-1)``, so that its steps take free SMs
+    ahead of the build's CTAs); the request waits (in order) until the
+    tables are built, then the plan is admitted like any other.  Built table sets stay in a host
     cache (host memory, outside the HBM budget), so a plan evicted from HBM
     is rebuilt from them without a new table build.
     """
@@ -202,6 +204,7 @@ class ServingEngine:
         self._tables = {}           # table_key -> built table set
         self._table_builders = {}   # table_key -> build function
         self._building = {}         # table_key -> Future of a build in flight
+        self._plan_args = {}        # table_key -> host arguments of its plan
         self._builder = None
         self._build_stream = None
         self.table_builds = 0
@@ -250,7 +253,9 @@ class ServingEngine:
                 import concurrent.futures
 
                 self._builder = concurrent.futures.ThreadPoolExecutor(max_workers=1)
-                self._build_stream = self.torch.cuda.Stream()
+                # the lowest priority: the engine's steps (on a higher-priority
+                # stream) take free SMs ahead of the build's CTAs
+                self._build_stream = self.torch.cuda.Stream(priority=0)
             self._building[table_key] = self._builder.submit(self._run_build, fn)
             return False
         if not fut.done():
@@ -261,6 +266,17 @@ class ServingEngine:
         self.table_builds += 1
         self.table_build_s += secs
         return True
+
+    def _build_plan(self, table_key, workload):
+        """A new device plan of ``table_key``.  The host arguments (the
+        wrangler's payload: compact table, case metadata, normalisers) are
+        assembled once per table set and kept in host memory, so a plan
+        evicted from HBM is rebuilt with uploads and device kernels only."""
+        args = self._plan_args.get(table_key)
+        if args is None:
+            args = self._plan_args[table_key] = _plan_kwargs(workload)
+        nf, kw = args
+        return _plan_from(nf, kw, False)
 
     def _workload(self, key):
         workload, table_key = self.specs[key][:2]
@@ -277,7 +293,9 @@ class ServingEngine:
         elif isinstance(value, tuple):   # (view, keep) of a tree
             pass
         else:
-            value.destroy()
+            # an idle plan: its steps ran on the engine's stream and have
+            # completed, so no device-wide synchronisation is needed
+            value.release(self.stream.cuda_stream)
 
     def _entry(self, ekey, estimate, build, measure):
         """Admit one entry: room for ``estimate`` bytes, ``build()``, then
@@ -307,7 +325,7 @@ class ServingEngine:
         pkey, tkey, skey = ("plan", table_key), ("tree", tree_key), ("sched", sched_key)
         # pin each entry as soon as it is resident so that admitting the
         # next one cannot evict it
-        plan = self._entry(pkey, 1 << 20, lambda: plan_for(workload, cache=False),
+        plan = self._entry(pkey, 1 << 20, lambda: self._build_plan(table_key, workload),
                            lambda pl: pl.device_bytes())
         self.budget.pin(pkey)
         try:
@@ -377,7 +395,14 @@ class ServingEngine:
             if not self._tables_ready(req.key):
                 waiting.append(self.pending.popleft())
                 continue
-            plan, tree, sched = self.admit(req.key)
+            try:
+                plan, tree, sched = self.admit(req.key)
+            except AdmissionError:
+                # the budget is held by this step's and the in-flight steps'
+                # problems: the request waits for them to finish
+                if reqs or self.inflight:
+                    break
+                raise
             add = (sched.ws_bytes + 255) // 256 * 256 + 4096
             if reqs and need + add > self.step_capacity // 2:
                 break
