@@ -70,6 +70,9 @@ def parse_args(argv=None):
                    help="C5: Helmholtz problems (continuous k) arriving with tables to build")
     p.add_argument("--c5-pressure", type=float, default=0.5,
                    help="C5 arrivals leg: HBM budget as a fraction of the mix's resident set")
+    p.add_argument("--c5-build-ctas", type=int, default=-1,
+                   help="C5 arrivals leg: CTAs of a table build (0: one per work item, "
+                        "-1: a quarter of the SMs)")
     p.add_argument("--c5-rates", default="0.25,0.5,0.75,0.9",
                    help="C5: open-loop arrival rates as fractions of the closed-loop rate")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
@@ -1047,7 +1050,11 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
 
     # (2) open loop at half the pressure rate, new problems arriving
     new_probs = W.config_c5_arrivals(n_new=args.c5_new)
-    new_ws, builders = W.c5_arrival_workloads(new_probs)
+    # by default builds run on a quarter of the SMs, the rest stay with the solves
+    build_ctas = args.c5_build_ctas
+    if build_ctas < 0:
+        build_ctas = max(1, torch.cuda.get_device_properties(0).multi_processor_count // 4)
+    new_ws, builders = W.c5_arrival_workloads(new_probs, build_ctas=build_ctas)
     eng2 = engine()
     new_dens = {}
     for key, w in new_ws.items():
@@ -1115,10 +1122,15 @@ def c5_arrivals_leg(args, eng, ws, probs, reqs, dens, closed_rate, resident_set)
         "new_problem_k": sorted(float(k[2]) for k in new_ws),
         "new_problem_shapes": sorted(f"{k[0]}d_q{k[3]}_l{k[4]}" for k in new_ws),
         "tables_built_on_arrival": eng2.table_builds,
+        "table_build_ctas": build_ctas,
         "table_build_s_total": eng2.table_build_s,
         "table_source": "FP64 Duffy quadrature on the GPU per new k (reference default "
                         "orders), on the engine's build thread and stream",
         "offered_per_s": rate, "achieved_per_s": len(done) / wall, "wall_s": wall,
+        # the resident problems' requests alone: served over the arrivals'
+        # span (the run's wall time ends with the last table build)
+        "others_achieved_per_s": len(rest) / max(
+            max(q.t_done for q in rest) - min(q.arrival for q in done), 1e-9) if rest else None,
         "latency_ms": latency_stats(done),
         "latency_ms_waited_for_table_build": latency_stats(waited),
         "latency_ms_others": latency_stats(rest),

@@ -365,7 +365,9 @@ typedef struct {
   int32_t n_reg, n_rad;       /* 1D rule sizes */
   int32_t kernel;             /* VL1_DUFFY_* */
   int32_t complex_output;
-  int32_t reserved;
+  int32_t max_ctas;           /* 0: one CTA per (entry, Duffy sub-simplex); else at
+                                 most this many CTAs, striding over them (a build
+                                 that leaves most SMs to other work) */
   double extent;              /* source box [0, extent]^dim */
   double k;                   /* Helmholtz / plane-wave wave number */
   const double *target_points;          /* [dim][n_entries] */

@@ -56,6 +56,19 @@ def test_gpu_table_matches_the_cpu_restatement(cuda, dim, q, kind):
     assert np.max(np.abs(got - ref) / np.abs(ref)) <= 1e-12
 
 
+@pytest.mark.parametrize("dim,kind,cap", [(2, "helmholtz", 3), (3, "laplace", 7)])
+def test_capped_grid_gives_the_same_table_bit_for_bit(cuda, dim, kind, cap):
+    # a build on a few CTAs (beside other GPU work) adds the same partial
+    # sums in the same order as the one-CTA-per-item build
+    t = _table(dim, 2, kind, extent=0.25)
+    kw = dict(regular_quad_order=6, radial_quad_order=21, kernel=kind, k=3.0, store=False)
+    ids_a, full = TB.build_table_values(t, **kw)
+    ids_b, capped = TB.build_table_values(t, max_ctas=cap, **kw)
+    assert np.array_equal(ids_a, ids_b)
+    assert np.array_equal(np.ascontiguousarray(full).view(np.uint64),
+                          np.ascontiguousarray(capped).view(np.uint64))
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_gpu_constant_kernel_gives_the_exact_volume(cuda, dim):
     # test_duffy_batched_manufactured.py:129-150

@@ -126,7 +126,7 @@ class BatchOptions(C.Structure):
 class DuffyDesc(C.Structure):
     _fields_ = [("dim", C.c_int32), ("q", C.c_int32), ("n_entries", C.c_int32),
                 ("n_reg", C.c_int32), ("n_rad", C.c_int32), ("kernel", C.c_int32),
-                ("complex_output", C.c_int32), ("reserved", C.c_int32),
+                ("complex_output", C.c_int32), ("max_ctas", C.c_int32),
                 ("extent", C.c_double), ("k", C.c_double),
                 ("target_points", C.c_void_p), ("decomposition_targets", C.c_void_p),
                 ("mode_axes", C.c_void_p), ("regular_nodes", C.c_void_p),

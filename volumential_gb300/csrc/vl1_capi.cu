@@ -4,6 +4,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <cmath>
+#include <mutex>
 #include <new>
 
 #include "vl1_internal.cuh"
@@ -24,6 +25,49 @@ int32_t cuda_fail(cudaError_t e, const char *what) {
   return VL1_E_CUDA;
 }
 
+// The library's stream-ordered allocations (plans, schedule builders, table
+// build scratch) come from a memory pool of its own in which memory freed on
+// one stream is reused by another only once the free has completed: the
+// device's default pool would instead make the allocating stream wait for
+// the freeing stream's pending work, so that a plan admitted while a table
+// build runs on another stream waited for that build to finish.
+cudaError_t lib_malloc_async(void **ptr, size_t bytes, cudaStream_t s) {
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static cudaMemPool_t pools[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props;
+      memset(&props, 0, sizeof(props));
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t created = nullptr;
+      e = cudaMemPoolCreate(&created, &props);
+      if (e != cudaSuccess) return e;
+      int off = 0;
+      uint64_t keep = 1ull << 30;   // bytes kept cached across synchronisations
+      e = cudaMemPoolSetAttribute(created, cudaMemPoolReuseAllowInternalDependencies, &off);
+      if (e == cudaSuccess)
+        e = cudaMemPoolSetAttribute(created, cudaMemPoolAttrReleaseThreshold, &keep);
+      if (e != cudaSuccess) {
+        cudaMemPoolDestroy(created);
+        return e;
+      }
+      pools[dev] = created;
+    }
+    pool = pools[dev];
+  }
+  return cudaMallocFromPoolAsync(ptr, bytes, pool, s);
+}
+
 }  // namespace vl1
 
 using namespace vl1;
@@ -39,9 +83,9 @@ int32_t plan_alloc(vl1_plan *p, void **out, size_t bytes) {
   // cudaFree it never waits for work on other streams (a serving engine
   // admits plans while table builds run on a stream of their own)
   void *ptr = nullptr;
-  cudaError_t e = cudaMallocAsync(&ptr, bytes ? bytes : 16, 0);
+  cudaError_t e = lib_malloc_async(&ptr, bytes ? bytes : 16, 0);
   if (e != cudaSuccess) {
-    set_error("cudaMallocAsync(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    set_error("stream-ordered allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
     return VL1_E_NOMEM;
   }
   p->allocs[p->n_allocs++] = ptr;
@@ -390,8 +434,8 @@ int32_t vl1_plan_set_mixed_geometry(vl1_plan *plan, int32_t kc, int32_t nch) {
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "vl1_plan_set_mixed_geometry: synchronise");
   void *ptr = nullptr;
-  e = cudaMallocAsync(&ptr, 2 * (size_t)elems, 0);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(plan digit operands)");
+  e = lib_malloc_async(&ptr, 2 * (size_t)elems, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "allocation of the plan digit operands");
   const int k = plan->mixed.adig_alloc;
   cudaFreeAsync(plan->allocs[k], 0);
   plan->allocs[k] = ptr;

@@ -23,6 +23,8 @@
 
 #include <cstdint>
 
+#include <algorithm>
+
 #include "vl1_internal.cuh"
 
 namespace vl1 {
@@ -33,8 +35,8 @@ constexpr int kDuffyMaxQ = 16;
 
 struct DuffyArgs {
   vl1_duffy_desc d;
-  int n_perm, n_reg_tail, n_sub;
-  double *out;
+  int n_perm, n_reg_tail, n_sub, n_chunks;
+  double *part;   // [entry][chunk][re, im] partial sums
 };
 
 // axis orders in itertools.permutations order
@@ -81,10 +83,14 @@ __device__ __forceinline__ void green(int kind, double k, const double *dv, doub
   }
 }
 
+// One CTA per (entry, chunk) work item, or a capped grid striding over them:
+// a chunk is one (sign vector, axis order) of the entry's Duffy
+// sub-simplices, so an item runs for a fraction of a millisecond; the partial
+// sums are added per entry in chunk order by duffy_reduce_kernel (a fixed
+// order: the table is the same on every run, whatever the grid).
 template <int DIM>
 __global__ void __launch_bounds__(kDuffyThreads) duffy_entry_kernel(const DuffyArgs A) {
   const vl1_duffy_desc &D = A.d;
-  const int e = blockIdx.x;
   constexpr int dim = DIM;
   const int q = D.q;
   __shared__ double s_xi[kDuffyMaxQ], s_bw[kDuffyMaxQ];
@@ -94,6 +100,12 @@ __global__ void __launch_bounds__(kDuffyThreads) duffy_entry_kernel(const DuffyA
     s_bw[threadIdx.x] = D.interp_weights[threadIdx.x];
   }
   __syncthreads();
+  // work item w = (entry, chunk); a capped grid strides over them
+  const int n_chunks = A.n_chunks;
+  const int64_t n_work = (int64_t)D.n_entries * n_chunks;
+  for (int64_t item = blockIdx.x; item < n_work; item += gridDim.x) {
+  const int e = (int)(item / n_chunks);
+  const int chunk = (int)(item - (int64_t)e * n_chunks);   // isub * n_perm + iperm
   double t[3], dc[3];
   int mode[3];
   bool mode_ok = true;
@@ -104,24 +116,22 @@ __global__ void __launch_bounds__(kDuffyThreads) duffy_entry_kernel(const DuffyA
     mode[a] = D.mode_axes[(int64_t)a * D.n_entries + e];
     mode_ok = mode_ok && mode[a] >= 0 && mode[a] < q;
   }
+  double *part = A.part + ((int64_t)e * n_chunks + chunk) * 2;
   if (!mode_ok) {   // an invalid entry yields NaN (the host checks its inputs)
     if (threadIdx.x == 0) {
-      A.out[(D.complex_output ? 2 : 1) * (int64_t)e] = __longlong_as_double(0x7FF8000000000000ll);
-      if (D.complex_output) A.out[2 * (int64_t)e + 1] = __longlong_as_double(0x7FF8000000000000ll);
+      part[0] = __longlong_as_double(0x7FF8000000000000ll);
+      part[1] = __longlong_as_double(0x7FF8000000000000ll);
     }
-    return;
+    continue;   // uniform across the CTA
   }
-  const int64_t per_sub = (int64_t)A.n_perm * A.n_reg_tail * D.n_rad;
-  const int64_t n_nodes = (int64_t)A.n_sub * per_sub;
+  const int iperm = chunk % A.n_perm;
+  const int isub = chunk / A.n_perm;
+  const int64_t n_nodes = (int64_t)A.n_reg_tail * D.n_rad;   // nodes of this chunk
   double acc_re = 0.0, acc_im = 0.0;
   for (int64_t i = threadIdx.x; i < n_nodes; i += kDuffyThreads) {
-    // node index -> (sign vector, axis order, regular tail node, radial node)
+    // node index -> (regular tail node, radial node)
     const int irad = (int)(i % D.n_rad);
-    int64_t rest = i / D.n_rad;
-    int ireg = (int)(rest % A.n_reg_tail);
-    rest /= A.n_reg_tail;
-    const int iperm = (int)(rest % A.n_perm);
-    const int isub = (int)(rest / A.n_perm);
+    int ireg = (int)(i / D.n_rad);
     // sub-box lengths along each axis (sign bit of axis a: first axis slowest)
     double len[3], sg[3];
     bool active = true;
@@ -210,11 +220,28 @@ __global__ void __launch_bounds__(kDuffyThreads) duffy_entry_kernel(const DuffyA
       re += s_red[0][w2];
       im += s_red[1][w2];
     }
-    if (D.complex_output) {
-      A.out[2 * (int64_t)e] = re;
-      A.out[2 * (int64_t)e + 1] = im;
+    part[0] = re;
+    part[1] = im;
+  }
+  __syncthreads();   // s_red is reused by the next work item
+  }
+}
+
+// the entries' values: their chunks' partial sums added in chunk order
+__global__ void duffy_reduce_kernel(const double *part, int n_entries, int n_chunks,
+                                    int complex_output, double *out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_entries;
+       e += gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int c = 0; c < n_chunks; ++c) {
+      re += part[((int64_t)e * n_chunks + c) * 2];
+      im += part[((int64_t)e * n_chunks + c) * 2 + 1];
+    }
+    if (complex_output) {
+      out[2 * (int64_t)e] = re;
+      out[2 * (int64_t)e + 1] = im;
     } else {
-      A.out[e] = re;
+      out[e] = re;
     }
   }
 }
@@ -249,12 +276,31 @@ extern "C" int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, v
   A.n_perm = D.dim == 3 ? 6 : 2;
   A.n_reg_tail = D.dim == 3 ? D.n_reg * D.n_reg : D.n_reg;
   A.n_sub = 1 << D.dim;
-  A.out = result;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // partial sums per (entry, chunk): stream-ordered scratch, so that a build
+  // never waits for work on other streams
+  const int n_chunks = A.n_sub * A.n_perm;
+  void *scratch = nullptr;
+  cudaError_t e = lib_malloc_async(&scratch, sizeof(double) * 2 * (size_t)D.n_entries * n_chunks, s);
+  if (e != cudaSuccess) return cuda_fail(e, "allocation of the Duffy partial sums");
+  A.part = static_cast<double *>(scratch);
+  A.n_chunks = n_chunks;
+  // one CTA per (entry, chunk), or at most max_ctas CTAs striding over them
+  // (a build that must leave most SMs to other work)
+  const int64_t n_work = (int64_t)D.n_entries * n_chunks;
+  const int64_t cap = D.max_ctas > 0 ? D.max_ctas : n_work;
+  const dim3 grid((unsigned)std::min<int64_t>(std::min(n_work, cap), 0x7FFFFFFF));
   if (D.dim == 3)
-    duffy_entry_kernel<3><<<D.n_entries, kDuffyThreads, 0, s>>>(A);
+    duffy_entry_kernel<3><<<grid, kDuffyThreads, 0, s>>>(A);
   else
-    duffy_entry_kernel<2><<<D.n_entries, kDuffyThreads, 0, s>>>(A);
-  cudaError_t e = cudaGetLastError();
+    duffy_entry_kernel<2><<<grid, kDuffyThreads, 0, s>>>(A);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    const int blocks = (int)std::min<int64_t>(((int64_t)D.n_entries + 255) / 256, 4096);
+    duffy_reduce_kernel<<<blocks, 256, 0, s>>>(A.part, D.n_entries, n_chunks, D.complex_output,
+                                               result);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(scratch, s);
   return e == cudaSuccess ? VL1_OK : cuda_fail(e, "duffy_entry_kernel launch");
 }

@@ -66,6 +66,9 @@ namespace vl1 {
 
 void set_error(const char *fmt, ...);
 int32_t cuda_fail(cudaError_t e, const char *what);
+// stream-ordered allocation from the library's own pool (vl1_capi.cu); free
+// with cudaFreeAsync
+cudaError_t lib_malloc_async(void **ptr, size_t bytes, cudaStream_t s);
 // vl1_tree_view -> TreeDev with host validation (vl1_capi.cu)
 int32_t make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &tr);
 

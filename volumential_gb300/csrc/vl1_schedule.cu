@@ -391,10 +391,10 @@ int32_t schedule_begin(vl1_plan *plan, const vl1_tree_view *tree, int64_t nnz, i
   int64_t total = 0;
   for (int64_t v : sz) total += v;
   // stream-ordered: never waits for work on other streams
-  cudaError_t e = cudaMallocAsync(&b->buf, total, s);
+  cudaError_t e = lib_malloc_async(&b->buf, total, s);
   if (e != cudaSuccess) {
     b->buf = nullptr;
-    return cuda_fail(e, "cudaMallocAsync(schedule builder)");
+    return cuda_fail(e, "allocation of the schedule builder scratch");
   }
   b->stream = s;
   uint8_t *p = static_cast<uint8_t *>(b->buf);

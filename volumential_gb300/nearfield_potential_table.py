@@ -281,19 +281,21 @@ class NearFieldInteractionTable:
         in FP64 on the GPU (``nearfield_potential_table.py:2948-3195``; the
         fixed tanh-sinh rules of its batched path).  ``queue``: an optional
         ``torch.cuda.Stream``.  A Helmholtz kernel's wave number is passed by
-        its argument name (``k`` by default)."""
+        its argument name (``k`` by default).  ``max_ctas`` > 0 caps the
+        builder's grid."""
         from .plan import stream_handle
         from .table_builder import build_table_values
 
         name = getattr(self.integral_knl, "helmholtz_k_name", "k")
         k = kwargs.pop(name, kwargs.pop("k", None))
         kernel = kwargs.pop("kernel", None)
+        max_ctas = int(kwargs.pop("max_ctas", 0))
         if kwargs:
             raise TypeError(f"unexpected keyword arguments {sorted(kwargs)}")
         build_table_values(self, radial_rule_name=radial_rule,
                            regular_quad_order=regular_quad_order,
                            radial_quad_order=radial_quad_order, mp_dps=mp_dps, kernel=kernel,
-                           k=k, stream=stream_handle(queue))
+                           k=k, stream=stream_handle(queue), max_ctas=max_ctas)
 
     def build_table(self, cl_ctx=None, queue=None, build_config=None, **kwargs):
         """``nearfield_potential_table.py:3200``: the constant kernel's closed

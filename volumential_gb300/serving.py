@@ -167,9 +167,12 @@ class ServingEngine:
     table set, e.g. the FP64 Duffy builder for its wave number) has no table
     values yet: the first request for it starts the build on a worker thread
     and its own lowest-priority CUDA stream, and the engine keeps serving the
-    other problems meanwhile (give the engine a high-priority ``stream``,
-    e.g. ``torch.cuda.Stream(priority=-1)``, so that its steps take free SMs
-    ahead of the build's CTAs); the request waits (in order) until the
+    other problems meanwhile.  Give the engine a high-priority ``stream``
+    (``torch.cuda.Stream(priority=-1)``) and cap the build's grid (the
+    ``max_ctas`` of the Duffy builder, e.g. a quarter of the SMs): a step's
+    tensor-core CTA needs a whole SM's shared memory, and an SM that keeps
+    taking the build's small CTAs never frees it, so an uncapped build holds
+    the steps back until it ends.  The request waits (in order) until the
     tables are built, then the plan is admitted like any other.  Built table sets stay in a host
     cache (host memory, outside the HBM budget), so a plan evicted from HBM
     is rebuilt from them without a new table build.

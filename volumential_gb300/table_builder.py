@@ -150,10 +150,11 @@ def kernel_code(table, kernel=None):
 
 def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad_order=20,
                        radial_quad_order=61, mp_dps=50, kernel=None, k=None,
-                       entry_ids=None, stream=None, store=True):
+                       entry_ids=None, stream=None, store=True, max_ctas=0):
     """Compute the table's orbit-invariant entries on the GPU (FP64) and, with
     ``store``, keep them as its compact data (plus the 2D normalizers).
-    Returns (entry_ids, values)."""
+    ``max_ctas`` > 0 runs the build on at most that many CTAs (a build in the
+    background of other GPU work).  Returns (entry_ids, values)."""
     import torch
 
     from .plan import require_cuda
@@ -194,6 +195,7 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
     d.dim, d.q, d.n_entries = table.dim, table.quad_order, n
     d.n_reg, d.n_rad, d.kernel = len(gx), len(rx), code
     d.complex_output = int(cplx)
+    d.max_ctas = int(max_ctas)
     d.extent = float(table.source_box_extent)
     d.k = float(k) if k is not None else 0.0
     d.target_points, d.decomposition_targets = arrs["tp"].data_ptr(), arrs["dc"].data_ptr()
@@ -204,6 +206,10 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
     sh = stream if stream is not None else torch.cuda.current_stream().cuda_stream
     _lib.check(_lib.lib().vl1_duffy_table(C.byref(d), C.c_void_p(out.data_ptr() if n else 0),
                                           C.c_void_p(sh)), "vl1_duffy_table")
+    # wait for the build on its stream first: a device-to-host copy queued
+    # behind the build kernel holds up other host threads' CUDA calls (a
+    # serving loop's launches) until the kernel finishes
+    torch.cuda.ExternalStream(sh).synchronize()
     vals = out.cpu().numpy()
     if cplx:
         vals = vals[:, 0] + 1j * vals[:, 1]

@@ -111,12 +111,15 @@ _DUFFY_CACHE: dict = {}
 
 
 def duffy_tables(dim, q, kernel, *, n_tables=1, source_box_extent=1.0, k=None,
-                 complex_values=False, regular_quad_order=20, radial_quad_order=61):
+                 complex_values=False, regular_quad_order=20, radial_quad_order=61,
+                 max_ctas=0):
     """Tables of ``kernel`` with values from the FP64 GPU Duffy builder.
 
     Level ``l`` has source box extent ``source_box_extent / 2**l``; Helmholtz
     needs the wave number ``k``.  Orders default to the reference's
-    (``nearfield_potential_table.py:2948-2953``).  Needs a CUDA device."""
+    (``nearfield_potential_table.py:2948-2953``).  ``max_ctas`` > 0 caps the
+    builder's grid (same values; a build beside other GPU work).  Needs a CUDA
+    device."""
     kname = type(kernel).__name__
     key = (dim, q, kname, None if k is None else float(k), n_tables,
            float(source_box_extent), complex_values, regular_quad_order, radial_quad_order)
@@ -130,6 +133,8 @@ def duffy_tables(dim, q, kernel, *, n_tables=1, source_box_extent=1.0, k=None,
             source_box_extent=source_box_extent * 0.5 ** lev,
             dtype=np.complex128 if complex_values else np.float64)
         kw = {} if k is None else {"k": float(k)}
+        if max_ctas:
+            kw["max_ctas"] = int(max_ctas)
         t.build_table_via_duffy_radial(regular_quad_order=regular_quad_order,
                                        radial_quad_order=radial_quad_order, **kw)
         out.append(t)
@@ -441,10 +446,11 @@ def config_c5_arrivals(seed=5500, n_new=12, n_range=(1e3, 2e5), qs=(3, 4, 5), k_
     return problems
 
 
-def c5_arrival_workloads(problems, seed=5500):
+def c5_arrival_workloads(problems, seed=5500, build_ctas=0):
     """Trees of the arriving problems and, per problem, a function that
     builds its table set: one FP64 Duffy table (GPU, the reference's default
-    orders) of the tree's level (source box extent 2^-level) for its k.
+    orders) of the tree's level (source box extent 2^-level) for its k, on at
+    most ``build_ctas`` CTAs when that is > 0.
     Returns ({key: Workload without tables}, {key: build function})."""
     import functools
 
@@ -462,7 +468,7 @@ def c5_arrival_workloads(problems, seed=5500):
                                   "tables": "duffy"})
         builders[key] = functools.partial(duffy_tables, p.dim, p.q, kernel, n_tables=1,
                                           source_box_extent=0.5 ** p.level, k=p.k,
-                                          complex_values=True)
+                                          complex_values=True, max_ctas=build_ctas)
     return out, builders
 
 
