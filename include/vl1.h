@@ -347,7 +347,9 @@ int32_t vl1_batch_kernel_launches(const vl1_batch *batch);
  * tanh-sinh radial rule and a Gauss-Legendre tail rule.  G includes the
  * kernel's scaling constant: Laplace 2D -log(r)/(2 pi), 3D 1/(4 pi r);
  * Helmholtz 2D (i/4) H0^(1)(k r), 3D exp(i k r)/(4 pi r); constant 1;
- * plane wave cos(k d_0) (a test kernel).  All arrays are device arrays;
+ * plane wave cos(k d_0) (a test kernel); r^power and r^power log r (the
+ * Helmholtz split mode's extra term tables, expansion_wrangler_fpnd.py:
+ * 144-209, scaling constant 1).  All arrays are device arrays;
  * result is [n_entries] doubles, or [n_entries][2] (re, im) when
  * complex_output.  Replaces _batched_duffy_values_for_local_indices
  * (nearfield_potential_table.py:2331-2463). */
@@ -357,7 +359,9 @@ enum {
   VL1_DUFFY_HELMHOLTZ2D = 2,
   VL1_DUFFY_HELMHOLTZ3D = 3,
   VL1_DUFFY_CONSTANT = 4,
-  VL1_DUFFY_PLANE_WAVE = 5
+  VL1_DUFFY_PLANE_WAVE = 5,
+  VL1_DUFFY_POWER = 6,        /* r^power, power >= 0 */
+  VL1_DUFFY_POWER_LOG = 7     /* r^power log r, power >= 1 */
 };
 
 typedef struct {
@@ -368,6 +372,8 @@ typedef struct {
   int32_t max_ctas;           /* 0: one CTA per (entry, Duffy sub-simplex); else at
                                  most this many CTAs, striding over them (a build
                                  that leaves most SMs to other work) */
+  int32_t power;              /* VL1_DUFFY_POWER / _POWER_LOG: the power of r (<= 64) */
+  int32_t reserved;           /* 0 */
   double extent;              /* source box [0, extent]^dim */
   double k;                   /* Helmholtz / plane-wave wave number */
   const double *target_points;          /* [dim][n_entries] */
@@ -383,7 +389,8 @@ int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, void *stream
 
 /* ---- Helmholtz split correction ---------------------------------------
  * The split mode's list-1 remainder (volumential/expansion_wrangler_fpnd.py:
- * 3491-3836, split order 1, series remainder kernel :212-332):
+ * 3491-3836, series remainder kernel :212-332; for split orders above 1 the
+ * host zeroes the coefficients of the terms the extra tables carry):
  *   result[t] = sum over list-1 source points s (s != t when exclude_self)
  *               of weights[s] * R(|x_t - x_s|),
  *   2D: R(r) = c0 + sum_{n=1..N} (a_n log r + b_n) r^{2n},

@@ -73,9 +73,15 @@ def node_set(dim, regular_order, radial_order):
     return np.array(us).T, np.array(sgs).T, np.array(jacs)
 
 
-def green(kind, dvec, k=0.0):
-    """Kernel value times scaling constant at displacements dvec [dim, n]."""
+def green(kind, dvec, k=0.0, power=0):
+    """Kernel value times scaling constant at displacements dvec [dim, n]
+    ("power" r^p and "power_log" r^p log r: the split-term kernels of
+    ``volumential/expansion_wrangler_fpnd.py:144-209``, constant 1)."""
     r = np.sqrt(np.sum(dvec * dvec, axis=0))
+    if kind == "power":
+        return r ** power
+    if kind == "power_log":
+        return r ** power * np.log(r)
     if kind == "laplace":
         return -np.log(r) / (2 * np.pi) if dvec.shape[0] == 2 else 1.0 / (4 * np.pi * r)
     if kind == "helmholtz":
@@ -116,7 +122,8 @@ def _basis(xi, bw, m, y, extent):
     return np.where(any_hit, hit[m].astype(np.float64), num / np.where(den == 0, 1, den))
 
 
-def entry_values(dim, q, extent, kind, targets, modes, regular_order, radial_order, k=0.0):
+def entry_values(dim, q, extent, kind, targets, modes, regular_order, radial_order, k=0.0,
+                 power=0):
     """Table values of entries with target points ``targets`` [dim, n] and
     source mode axes ``modes`` [dim, n]."""
     u, sg, jac = node_set(dim, regular_order, radial_order)
@@ -141,6 +148,6 @@ def entry_values(dim, q, extent, kind, targets, modes, regular_order, radial_ord
             for a in range(dim):
                 basis *= _basis(xi, bw, int(modes[a, e]), y[a], extent)
         with np.errstate(divide="ignore", invalid="ignore"):
-            g = green(kind, np.where(active[None, :], dv, 1.0), k)
+            g = green(kind, np.where(active[None, :], dv, 1.0), k, power)
         out.append(np.sum(np.where(active, g * w * basis, 0.0)))
     return np.array(out)

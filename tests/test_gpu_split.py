@@ -87,3 +87,120 @@ def test_split_mode_approximates_the_helmholtz_table(cuda):
                                  trav.neighbor_source_boxes_lists, dens)
     assert rel_l2(lap_only[0].cpu().numpy(), b) > 100 * err
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("dim,kind,power", [(2, "power_log", 2), (2, "power_log", 4),
+                                            (3, "power", 1), (3, "power", 3)])
+def test_split_term_tables_match_the_cpu_restatement(cuda, dim, kind, power):
+    # the extra term kernels r^p / r^p log r (expansion_wrangler_fpnd.py:144-209)
+    from oracle import duffy_oracle as DO
+    from volumential_gb300 import table_builder as TB
+    from volumential_gb300.helmholtz_split import term_kernel
+
+    t = NearFieldInteractionTable(2, dim=dim, sumpy_kernel=term_kernel(dim, (kind, power)),
+                                  source_box_extent=0.5)
+    ids = t._get_invariant_entry_info()["entry_ids"]
+    pick = ids[np.linspace(0, len(ids) - 1, 30 if dim == 2 else 12).astype(int)]
+    reg, rad = (6, 21) if dim == 2 else (4, 11)
+    _, got = TB.build_table_values(t, regular_quad_order=reg, radial_quad_order=rad,
+                                   entry_ids=pick, store=False)
+    tp, _, axes = TB.entry_geometry(t, pick)
+    ref = DO.entry_values(dim, 2, 0.5, kind, tp, axes, reg, rad, power=power)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def _split_wrangler(w, k, order, lap, term_tables=None):
+    ti = FPNDTreeIndependentDataForWrangler(target_kernels=[HelmholtzKernel(w.dim)])
+    return FPNDExpansionWrangler(ti, w.traversal, [lap], dtype=np.complex128, quad_order=w.q,
+                                 kernel_extra_kwargs={"k": k}, helmholtz_split_order=order,
+                                 helmholtz_split_term_tables=term_tables)
+
+
+# a single term table at the root extent: scaled per level, plus the
+# point-to-point log(h/h0) r^{2n} part in 2D (expansion_wrangler_fpnd.py:
+# 3678-3806, 4777-4799, 4909-5016)
+@pytest.mark.parametrize("dim,level,q,k,order", [(2, 3, 3, 20.0, 2), (2, 3, 3, 12.0 + 0.5j, 3),
+                                                 (3, 2, 2, 7.0, 2), (3, 2, 3, 5.0 + 0.3j, 3)])
+def test_split_orders_above_one_match_the_restatement(cuda, dim, level, q, k, order):
+    import torch
+
+    from helpers import LAP3, oracle_eval, oracle_for_workload
+    from volumential_gb300.helmholtz_split import split_extra_terms, term_kernel
+
+    w = W.uniform_workload("splitp", dim, level, q, seed=93, kernel=HelmholtzKernel(dim))
+    tree, tr = w.tree, w.traversal
+    h0 = tree.root_extent
+    lap = NearFieldInteractionTable(q, dim=dim, sumpy_kernel=LaplaceKernel(dim),
+                                    source_box_extent=h0)
+    lap.build_table(regular_quad_order=6, radial_quad_order=21)
+    terms = split_extra_terms(dim, k, order)
+    tabs = {}
+    for key, _ in terms:
+        t = NearFieldInteractionTable(q, dim=dim, sumpy_kernel=term_kernel(dim, key),
+                                      source_box_extent=h0)
+        t.build_table(regular_quad_order=6, radial_quad_order=21)
+        tabs[key] = [t]
+    wr = _split_wrangler(w, k, order, lap, tabs)
+    dens = w.coefs[0]
+    wts = dens * tree.weights
+    corr, _ = wr.eval_direct_helmholtz_split_correction(
+        tr.target_boxes, tr.neighbor_source_boxes_starts, tr.neighbor_source_boxes_lists,
+        torch.from_numpy(wts).to("cuda"), src_func=torch.from_numpy(dens).to("cuda"))
+    got = corr[0].cpu().numpy()
+    # the restatement: closed-form remainder of order p, the self limit, and
+    # each term's table near field (scaled (h/h0)^(dim+p)) plus its
+    # point-to-point log(h/h0) r^p part in 2D
+    args = (tree.targets, wts.astype(np.complex128), tr.target_boxes,
+            tr.neighbor_source_boxes_starts, tr.neighbor_source_boxes_lists,
+            tree.box_target_starts, tree.box_target_counts_nonchild)
+    ref = SO.split_sum(dim, k, *args, split_order=order)
+    ref = ref + wts * SO.remainder(dim, k, np.zeros(1), 1)[0]
+    beta = SO.log_alpha(tree.box_levels, tree.box_target_starts,
+                        tree.box_target_counts_nonchild, tree.root_extent, h0)
+    for (kind, p, c) in SO.extracted_terms(dim, k, order):
+        tw = W.Workload("term", dim, q, term_kernel(dim, (kind, p)), tr, tabs[(kind, p)],
+                        w.coefs, w.seed)
+        policy = dict(LAP3, scaling_exponent=dim + p)
+        term = oracle_eval(oracle_for_workload(tw, policy), tw, dens)
+        if kind == "power_log":
+            term = term + SO.split_sum(dim, k, tree.targets, (wts * beta).astype(np.complex128),
+                                       *args[2:], kernel=lambda r, p=p: r ** p)
+        ref = ref + c * term
+    assert rel_l2(got, ref) <= 1e-12
+
+
+def test_split_order_two_tracks_the_helmholtz_table_closer(cuda):
+    """Order 2 integrates the r^2 log r term with its own table instead of
+    point quadrature; its list-1 field is much closer to the one of a
+    Helmholtz table than order 1's (5.1e-5 -> 4.3e-7 on GB300; term table
+    built on demand, the reference's default term orders)."""
+    import torch
+
+    k = 20.0
+    w = W.uniform_workload("split2d", 2, 4, 4, seed=92, kernel=HelmholtzKernel(2))
+    tree, trav = w.tree, w.traversal
+    lap = NearFieldInteractionTable(4, dim=2, sumpy_kernel=LaplaceKernel(2),
+                                    source_box_extent=tree.root_extent)
+    lap.build_table(regular_quad_order=8, radial_quad_order=31)
+    helm = NearFieldInteractionTable(4, dim=2, sumpy_kernel=HelmholtzKernel(2),
+                                     source_box_extent=tree.root_extent / 16,
+                                     dtype=np.complex128)
+    helm.build_table(regular_quad_order=8, radial_quad_order=31, k=k)
+    ti = FPNDTreeIndependentDataForWrangler(target_kernels=[HelmholtzKernel(2)])
+    dens = w.coefs[0]
+    weights = dens * tree.weights
+    wh = FPNDExpansionWrangler(ti, trav, [helm], dtype=np.complex128, quad_order=4,
+                               kernel_extra_kwargs={"k": k})
+    ph = drive_volume_fmm(trav, wh, weights, dens, list1_only=True, reorder_sources=False,
+                          reorder_potentials=False)
+    b = ph[0].cpu().numpy()
+    errs = {}
+    for order in (1, 2):
+        ws = _split_wrangler(w, k, order, lap)
+        ps = drive_volume_fmm(trav, ws, weights, dens, list1_only=True, reorder_sources=False,
+                              reorder_potentials=False)
+        errs[order] = rel_l2(ps[0].cpu().numpy(), b)
+    assert list(ws.helmholtz_split_term_tables) == [("power_log", 2)]
+    print("split order 1 / 2 vs Helmholtz table:", errs)
+    assert errs[2] <= 0.1 * errs[1] and errs[2] <= 1e-5, errs
+    torch.cuda.synchronize()

@@ -42,3 +42,65 @@ def test_max_neighbor_distance_follows_the_coarsest_active_box():
     t = build_uniform_tree(2, 3, 2)
     assert t.dimensions == 2
     assert abs(max_neighbor_distance(t) - 2 * np.sqrt(2) * t.root_extent / 8) < 1e-15
+
+
+@pytest.mark.parametrize("dim,k", [(2, 20.0), (3, 7.0), (2, 12.0 + 0.5j), (3, 5.0 + 0.3j)])
+@pytest.mark.parametrize("order", [2, 3])
+def test_split_orders_move_terms_out_of_the_series(dim, k, order):
+    # expansion_wrangler_fpnd.py:212-332 (terms left in the remainder) and
+    # :5052-5115 (the extracted terms' coefficients)
+    from volumential_gb300.helmholtz_split import split_extra_terms
+
+    r_max = 0.09
+    n = series_terms(dim, k, r_max)
+    r = np.concatenate([[0.0], np.geomspace(1e-7, r_max, 300)])
+    got = remainder_series(dim, k, r, n, order)
+    ref = SO.remainder(dim, k, r, order)
+    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+    terms = split_extra_terms(dim, k, order)
+    want = SO.extracted_terms(dim, k, order)
+    assert [key for key, _ in terms] == [(kind, p) for kind, p, _ in want]
+    for (_, c), (_, _, cw) in zip(terms, want):
+        assert abs(c - cw) <= 1e-14 * abs(cw)
+    # the series with the extracted terms added back is the order-1 series
+    back = got + sum(c * SO.radial_term(kind, p, r) for kind, p, c in want)
+    assert np.max(np.abs(back - remainder_series(dim, k, r, n, 1))) <= 1e-13 * np.max(
+        np.abs(ref))
+
+
+def test_split_term_keys_scaling_codes_and_key_forms():
+    from volumential_gb300.expansion_wrangler_fpnd import _normalize_term_key
+    from volumential_gb300.helmholtz_split import split_term_keys, term_scaling_code
+    from volumential_gb300.list1 import parse_scaling_code
+
+    assert split_term_keys(2, 1) == [] and split_term_keys(3, 1) == []
+    assert split_term_keys(2, 3) == [("power_log", 2), ("power_log", 4)]
+    assert split_term_keys(3, 3) == [("power", 1), ("power", 3)]
+    # (h / h0)^(dim + power): expansion_wrangler_fpnd.py:4777-4799
+    for dim, p in [(2, 2), (2, 4), (3, 1), (3, 3)]:
+        code = term_scaling_code(dim, p).replace("BOX", "sbox")
+        assert parse_scaling_code(code) == dim + p
+    assert _normalize_term_key(("power_log", 2)) == ("power_log", 2)
+    assert _normalize_term_key(3) == ("power", 3)
+    assert _normalize_term_key("constant") == ("power", 0)
+    assert _normalize_term_key("power:5") == ("power", 5)
+    assert _normalize_term_key("power_log:4") == ("power_log", 4)
+    for bad in [("power_log", 0), ("power", -1), ("cube", 2), "power-log:2", 2.5]:
+        with pytest.raises((ValueError, TypeError)):
+            _normalize_term_key(bad)
+
+
+def test_log_alpha_per_source_follows_the_boxes():
+    # expansion_wrangler_fpnd.py:4909-4974 on an adaptive tree
+    from volumential_gb300.helmholtz_split import log_alpha_per_source
+    from volumential_gb300.tree_build import build_adaptive_tree
+
+    def refine(nodes):   # boxes with a node near (0.3, 0.3)
+        return (np.linalg.norm(nodes - 0.3, axis=0) < 0.2).any(axis=1)
+
+    tree = build_adaptive_tree(2, 3, refine, max_level=4, min_level=1)
+    got = log_alpha_per_source(tree, 0.25)
+    ref = SO.log_alpha(tree.box_levels, tree.box_source_starts,
+                       tree.box_source_counts_nonchild, tree.root_extent, 0.25)
+    assert np.array_equal(got, ref)
+    assert len(np.unique(got)) > 1

@@ -127,6 +127,7 @@ class DuffyDesc(C.Structure):
     _fields_ = [("dim", C.c_int32), ("q", C.c_int32), ("n_entries", C.c_int32),
                 ("n_reg", C.c_int32), ("n_rad", C.c_int32), ("kernel", C.c_int32),
                 ("complex_output", C.c_int32), ("max_ctas", C.c_int32),
+                ("power", C.c_int32), ("reserved", C.c_int32),
                 ("extent", C.c_double), ("k", C.c_double),
                 ("target_points", C.c_void_p), ("decomposition_targets", C.c_void_p),
                 ("mode_axes", C.c_void_p), ("regular_nodes", C.c_void_p),
@@ -137,6 +138,7 @@ class DuffyDesc(C.Structure):
 
 VL1_DUFFY_LAPLACE2D, VL1_DUFFY_LAPLACE3D, VL1_DUFFY_HELMHOLTZ2D = 0, 1, 2
 VL1_DUFFY_HELMHOLTZ3D, VL1_DUFFY_CONSTANT, VL1_DUFFY_PLANE_WAVE = 3, 4, 5
+VL1_DUFFY_POWER, VL1_DUFFY_POWER_LOG = 6, 7
 VL1_SPLIT_REAL_K = 1
 
 

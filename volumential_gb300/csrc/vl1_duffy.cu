@@ -46,8 +46,8 @@ __device__ constexpr int8_t kPerm3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2},
 
 // G(dvec) times the kernel's scaling constant; (re, im)
 template <int DIM>
-__device__ __forceinline__ void green(int kind, double k, const double *dv, double &re,
-                                      double &im) {
+__device__ __forceinline__ void green(int kind, double k, int power, const double *dv,
+                                      double &re, double &im) {
   double r2 = 0.0;
 #pragma unroll
   for (int a = 0; a < DIM; ++a) r2 = fma(dv[a], dv[a], r2);
@@ -77,6 +77,14 @@ __device__ __forceinline__ void green(int kind, double k, const double *dv, doub
     case VL1_DUFFY_CONSTANT:
       re = 1.0;
       break;
+    case VL1_DUFFY_POWER:
+    case VL1_DUFFY_POWER_LOG: {   // r^p (times log r): r2^(p/2), times r for odd p
+      double v = 1.0;
+      for (int i = 0; i < power / 2; ++i) v *= r2;
+      if (power & 1) v *= sqrt(r2);
+      re = kind == VL1_DUFFY_POWER ? v : v * (0.5 * log(r2));
+      break;
+    }
     default:   // VL1_DUFFY_PLANE_WAVE: cos(k d_0)
       re = cos(k * dv[0]);
       break;
@@ -198,7 +206,7 @@ __global__ void __launch_bounds__(kDuffyThreads) duffy_entry_kernel(const DuffyA
     for (int a = 0; a < dim; ++a) r2 = fma(dv[a], dv[a], r2);
     if (!(r2 > 0.0)) continue;   // a node on the singular point: zero weight
     double gre, gim;
-    green<DIM>(D.kernel, D.k, dv, gre, gim);
+    green<DIM>(D.kernel, D.k, D.power, dv, gre, gim);
     const double f = w * jac * len_prod * basis;
     acc_re = fma(gre, f, acc_re);
     acc_im = fma(gim, f, acc_im);
@@ -259,9 +267,14 @@ extern "C" int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, v
   const vl1_duffy_desc &D = *desc;
   if (D.dim < 2 || D.dim > 3 || D.q < 1 || D.q > kDuffyMaxQ || D.n_entries < 0 ||
       D.n_reg < 1 || D.n_rad < 1 || !(D.extent > 0.0) || D.kernel < 0 ||
-      D.kernel > VL1_DUFFY_PLANE_WAVE) {
+      D.kernel > VL1_DUFFY_POWER_LOG) {
     set_error("vl1_duffy_table: dim %d, q %d, entries %d, rules %d/%d, extent %g or kernel %d "
               "out of range", D.dim, D.q, D.n_entries, D.n_reg, D.n_rad, D.extent, D.kernel);
+    return VL1_E_ARG;
+  }
+  if ((D.kernel == VL1_DUFFY_POWER && (D.power < 0 || D.power > 64)) ||
+      (D.kernel == VL1_DUFFY_POWER_LOG && (D.power < 1 || D.power > 64))) {
+    set_error("vl1_duffy_table: power %d out of range for kernel %d", D.power, D.kernel);
     return VL1_E_ARG;
   }
   if (D.n_entries == 0) return VL1_OK;

@@ -52,6 +52,38 @@ def _np(x):
     return np.asarray(x)
 
 
+def _normalize_term_key(key):
+    """A split term key as ("power" | "power_log", power): from a (kind,
+    power) tuple, an int (a power of r) or a string "constant", "power:<n>",
+    "power_log:<n>" (the accepted forms of expansion_wrangler_fpnd.py:
+    335-376)."""
+    if isinstance(key, tuple):
+        if len(key) != 2:
+            raise ValueError("helmholtz split term key tuples must have length 2: (kind, power)")
+        kind, power = key
+    elif isinstance(key, (int, np.integer)):
+        kind, power = "power", key
+    elif isinstance(key, str):
+        if key == "constant":
+            kind, power = "power", 0
+        elif ":" in key and key.split(":", 1)[0] in ("power", "power_log"):
+            kind, power = key.split(":", 1)
+        else:
+            raise ValueError("invalid helmholtz split term key string; expected one of: "
+                             "constant, power:<n>, power_log:<n>")
+    else:
+        raise TypeError("helmholtz split term key must be int, str, or (kind, power) tuple")
+    kind = str(kind)
+    if kind not in ("power", "power_log"):
+        raise ValueError("helmholtz split term key kind must be 'power' or 'power_log'")
+    power = int(power)
+    if power < 0:
+        raise ValueError("helmholtz split term key power must be >= 0")
+    if kind == "power_log" and power == 0:
+        raise ValueError("helmholtz split power_log term requires power >= 1")
+    return kind, power
+
+
 def _compute_box_local_ids(tree, n_q_points):
     """Box-local particle index of every particle, in tree order."""
     if not getattr(tree, "sources_are_targets", False):
@@ -198,7 +230,8 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                  self_extra_kwargs=None, list1_extra_kwargs=None, queue=None,
                  helmholtz_split=None, helmholtz_split_order=1,
                  helmholtz_split_smooth_quad_order=None,
-                 helmholtz_split_order1_legacy_subtraction=False, **kwargs):
+                 helmholtz_split_order1_legacy_subtraction=False,
+                 helmholtz_split_term_tables=None, **kwargs):
         self.tree_indep = tree_indep
         self.traversal = traversal
         self.tree = traversal.tree
@@ -228,7 +261,8 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
             self._check_table_levels(kn, lst)
         self._init_helmholtz_split(helmholtz_split, helmholtz_split_order,
                                    helmholtz_split_smooth_quad_order,
-                                   helmholtz_split_order1_legacy_subtraction)
+                                   helmholtz_split_order1_legacy_subtraction,
+                                   helmholtz_split_term_tables)
         self._payload_cache = collections.OrderedDict()
         self._payload_cache_max = 16
         self._view_cache = collections.OrderedDict()
@@ -248,7 +282,7 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                     return False, f"the near-field table of {kn} is not Laplace-backed"
         return True, ""
 
-    def _init_helmholtz_split(self, split, order, smooth_quad_order, legacy):
+    def _init_helmholtz_split(self, split, order, smooth_quad_order, legacy, term_tables):
         ok, reason = self._split_support()
         if split is None:
             split = ok
@@ -258,10 +292,22 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                 f"near-field tables; {reason}")
         self.helmholtz_split = bool(split)
         self.helmholtz_split_order = int(order) if split else order
+        # extra term tables of split orders > 1, keyed ("power_log", 2n) in
+        # 2D and ("power", 2j - 1) in 3D (expansion_wrangler_fpnd.py:2603-2647)
+        self.helmholtz_split_term_tables = {}
+        if term_tables is not None:
+            if not isinstance(term_tables, dict):
+                raise TypeError(
+                    "helmholtz_split_term_tables must be a dict mapping term keys to tables")
+            for key, tabs in term_tables.items():
+                self.helmholtz_split_term_tables[_normalize_term_key(key)] = (
+                    list(tabs) if isinstance(tabs, (list, tuple)) else [tabs])
         if self.helmholtz_split:
-            if int(order) != 1:
-                raise NotImplementedError("helmholtz_split_order > 1 (extra split-term "
-                                          "tables) is not built; use order 1")
+            if int(order) < 1:
+                raise ValueError("split_order must be >= 1")
+            if int(order) > 1 and len(self.tree_indep.target_kernels) > 1:
+                raise NotImplementedError(
+                    "multi-output split correction currently supports split_order=1")
             if smooth_quad_order is not None:
                 raise NotImplementedError("helmholtz_split_smooth_quad_order (resampled "
                                           "remainder sources) is not built")
@@ -284,19 +330,106 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
             return 0j
         return 0.25j - (np.log(0.5 * k) + np.euler_gamma) / (2.0 * np.pi)
 
+    def _split_term_tables(self, out_kernel, key):
+        """The term tables of ``key``: the given ones, else built on the GPU
+        by the Duffy builder at the base tables' source box extents with the
+        default term orders (expansion_wrangler_fpnd.py:4596-4619,
+        4700-4775)."""
+        from .helmholtz_split import term_build_orders, term_kernel
+        from .nearfield_potential_table import NearFieldInteractionTable
+
+        tabs = self.helmholtz_split_term_tables.get(key)
+        if tabs is not None:
+            return tabs
+        base = self.near_field_table[repr(out_kernel)]
+        dim = int(self.tree.dimensions)
+        q = int(base[0].quad_order)
+        reg, rad = term_build_orders(dim, q)
+        knl = term_kernel(dim, key)
+        tabs = []
+        for t in base:
+            tt = NearFieldInteractionTable(q, dim=dim, sumpy_kernel=knl,
+                                           source_box_extent=float(t.source_box_extent))
+            tt.build_table_via_duffy_radial(regular_quad_order=reg, radial_quad_order=rad,
+                                            queue=self.queue)
+            tabs.append(tt)
+        self.helmholtz_split_term_tables[key] = tabs
+        return tabs
+
+    def _split_term_contribution(self, out_kernel, key, tabs, target_boxes, starts, lists,
+                                 src_func, w, view, pts):
+        """One term's list-1 contribution (expansion_wrangler_fpnd.py:
+        3678-3806, 4835-4907): the term table's near field (a single table
+        scaled by (h/h0)^(dim + power), or one table per level), plus for a
+        single r^{2n} log r table the point-to-point sum of r^{2n} with
+        strengths x log(h/h0)."""
+        import torch
+
+        from .helmholtz_split import (
+            log_alpha_per_source,
+            radial_power_sum,
+            term_kernel,
+            term_scaling_code,
+        )
+        from .plan import as_device_tensor, stream_handle
+
+        kind, power = key
+        dim = int(self.tree.dimensions)
+        if len(tabs) > 1:
+            l1kw = {"infer_kernel_scaling": False}
+        else:
+            l1kw = {"infer_kernel_scaling": False,
+                    "kernel_scaling_code": term_scaling_code(dim, power),
+                    "kernel_displacement_code": "0.0"}
+        knl = term_kernel(dim, key)
+        payload = self.get_payload(knl, tabs)
+        near_field = NearFieldFromCSR(knl, payload["table_data_shapes"],
+                                      potential_kind=self.potential_kind, **l1kw)
+        coefs = as_device_tensor(src_func)
+        parts = [coefs.real, coefs.imag] if coefs.is_complex() else [coefs]
+        vals = []
+        for part in parts:
+            kw = self._near_field_kwargs(payload, target_boxes, starts, lists,
+                                         part.to(torch.float64).contiguous())
+            res = torch.zeros(int(self.tree.ntargets), dtype=torch.float64, device="cuda")
+            res, _ = near_field(self.queue, result=res, **kw)
+            vals.append(res)
+        term = vals[0].to(torch.complex128)
+        if len(vals) > 1:
+            term = term + 1j * vals[1]
+        if dim == 2 and kind == "power_log" and len(tabs) == 1:
+            beta = torch.from_numpy(log_alpha_per_source(
+                self.tree, float(tabs[0].source_box_extent))).to("cuda")
+            term = term + radial_power_sum(view, pts, w * beta, power,
+                                           exclude_self=bool(self.tree_indep.exclude_self),
+                                           stream=stream_handle(self.queue))
+        return term
+
     def eval_direct_helmholtz_split_correction(self, target_boxes, neighbor_source_boxes_starts,
                                                neighbor_source_boxes_lists, src_weights,
                                                src_func=None):
-        """The split mode's list-1 remainder sum, one complex [N] array per
-        target kernel (``expansion_wrangler_fpnd.py:3491-3836``, order 1).
-        ``src_weights``: density x quadrature weight in tree order."""
+        """The split mode's list-1 correction, one complex [N] array per
+        target kernel (``expansion_wrangler_fpnd.py:3491-3836``): the
+        remainder sum and, for split order p > 1, the extra terms' table
+        contributions times their coefficients (``src_func``: the density at
+        the points, needed for p > 1).  ``src_weights``: density x quadrature
+        weight in tree order."""
         import torch
 
-        from .helmholtz_split import max_neighbor_distance, series_terms, split_correction
+        from .helmholtz_split import (
+            max_neighbor_distance,
+            series_terms,
+            split_correction,
+            split_extra_terms,
+        )
         from .plan import as_device_tensor, stream_handle, tree_view_from_arrays
 
         if not self.helmholtz_split:
             return self.output_zeros(), _TimingFuture([])
+        order = int(self.helmholtz_split_order)
+        if order > 1 and src_func is None:
+            raise ValueError("split orders above 1 need the density (src_func) for the "
+                             "extra term tables")
         w = as_device_tensor(src_weights)
         pts = torch.from_numpy(np.ascontiguousarray(_np(self.tree.sources),
                                                     dtype=np.float64)).to("cuda")
@@ -316,7 +449,13 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
             exclude = bool(self.tree_indep.exclude_self)
             corr = split_correction(view, pts, w, wave, series_terms(self.tree.dimensions,
                                                                      wave, r_max),
-                                    exclude_self=exclude, stream=stream_handle(self.queue))
+                                    exclude_self=exclude, stream=stream_handle(self.queue),
+                                    split_order=order)
+            for key, coeff in split_extra_terms(self.tree.dimensions, wave, order):
+                tabs = self._split_term_tables(k, key)
+                corr = corr + coeff * self._split_term_contribution(
+                    k, key, tabs, target_boxes, neighbor_source_boxes_starts,
+                    neighbor_source_boxes_lists, src_func, w, view, pts)
             if exclude:
                 # self pairs excluded from the sum: add back the finite r -> 0
                 # limit of the remainder per point (expansion_wrangler_fpnd.py:

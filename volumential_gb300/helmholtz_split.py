@@ -14,8 +14,17 @@ split order 1 (the default) R is the series of ``:212-332``:
 
 truncated at the term count of ``:4337-4378`` (tolerance 1e-16 at the largest
 list-1 distance, at most 96 terms, plus 2).  ``split_correction`` evaluates
-the sum on the GPU (``vl1_split_correction``).  Split orders above 1 (which
-move r^{2n} log r / odd-power terms into extra tables) are not built.
+the sum on the GPU (``vl1_split_correction``).
+
+Split order p > 1 (``:212-332, 4552-4570, 5052-5115``) moves the non-smooth
+terms of the first p - 1 orders out of R into near-field tables of their
+own kernels, integrated by the Duffy builder instead of point quadrature:
+2D r^{2n} log r (n = 1..p-1, coefficient a_n), 3D r^{2j-1} (j = 1..p-1,
+coefficient c_{2j}).  A single term table of source box extent h0 serves
+every level through the scaling (h/h0)^(dim + power)
+(``:4777-4799``); for r^{2n} log r the remaining log(h/h0) r^{2n} part is a
+point-to-point sum of r^{2n} with strengths scaled by log(h/h0) per source
+box (``:4909-5016``, the default "p2p" mode).
 """
 
 from __future__ import annotations
@@ -28,7 +37,9 @@ import numpy as np
 from . import _lib
 
 __all__ = ["series_terms", "remainder_coefficients", "remainder_series",
-           "max_neighbor_distance", "split_scaling_codes", "split_correction"]
+           "max_neighbor_distance", "split_scaling_codes", "split_correction",
+           "split_term_keys", "split_extra_terms", "term_kernel", "term_scaling_code",
+           "term_build_orders", "log_alpha_per_source", "radial_power_sum"]
 
 _GAMMA = 0.5772156649015329   # Euler-Mascheroni
 
@@ -58,9 +69,14 @@ def series_terms(dim, k, r_max, tol=1.0e-16, max_n=96):
     return min(max_n, n + 2)
 
 
-def remainder_coefficients(dim, k, n_terms):
-    """Coefficient array [2, n_terms + 1, 2] of ``vl1_split_correction``."""
+def remainder_coefficients(dim, k, n_terms, split_order=1):
+    """Coefficient array [2, n_terms + 1, 2] of ``vl1_split_correction``;
+    split order p > 1 leaves out the terms the extra tables carry (2D the
+    log terms of n < p, 3D the even n <= 2 (p - 1))."""
     k = complex(k)
+    split_order = int(split_order)
+    if split_order < 1:
+        raise ValueError("split_order must be >= 1")
     out = np.zeros((2, n_terms + 1), dtype=np.complex128)
     if dim == 2:
         if k == 0:
@@ -71,17 +87,97 @@ def remainder_coefficients(dim, k, n_terms):
         for n in range(1, n_terms + 1):
             harmonic += 1.0 / n
             s_n = ((-1) ** n) * (k * k / 4.0) ** n / (math.factorial(n) ** 2)
-            out[0, n] = -s_n / (2 * np.pi)
+            if n >= split_order:
+                out[0, n] = -s_n / (2 * np.pi)
             out[1, n] = s_n * ((harmonic - lk) / (2 * np.pi) + 0.25j)
     else:
+        extracted = 2 * (split_order - 1)
         for n in range(1, n_terms + 1):
+            if n % 2 == 0 and n <= extracted:
+                continue
             out[0, n] = (1j * k) ** n / (4 * np.pi * math.factorial(n))
     return np.ascontiguousarray(np.stack([out.real, out.imag], axis=-1))
 
 
-def remainder_series(dim, k, r, n_terms):
+def split_term_keys(dim, split_order):
+    """The extra term tables split order p needs (``expansion_wrangler_fpnd.py:
+    4552-4570``): 2D ("power_log", 2n) for n = 1..p-1, 3D ("power", 2j - 1)
+    for j = 1..p-1."""
+    split_order = int(split_order)
+    if dim == 2:
+        return [("power_log", 2 * n) for n in range(1, split_order)]
+    if dim == 3:
+        return [("power", 2 * j - 1) for j in range(1, split_order)]
+    raise NotImplementedError("helmholtz split extra terms are implemented only for 2D/3D")
+
+
+def split_extra_terms(dim, k, split_order):
+    """[(term key, coefficient)] of split order p
+    (``expansion_wrangler_fpnd.py:5052-5115``): 2D a_n = -s_n / (2 pi) of
+    r^{2n} log r, 3D c_{2j} = (i k)^{2j} / (4 pi (2j)!) of r^{2j-1}."""
+    k = complex(k)
+    out = []
+    for key in split_term_keys(dim, split_order):
+        if dim == 2:
+            n = key[1] // 2
+            s_n = ((-1) ** n) * (k * k / 4.0) ** n / (math.factorial(n) ** 2)
+            out.append((key, complex(-s_n / (2 * np.pi))))
+        else:
+            n = key[1] + 1
+            out.append((key, complex((1j * k) ** n / (4 * np.pi * math.factorial(n)))))
+    return out
+
+
+def term_kernel(dim, key):
+    """The kernel of a term key: r^p or r^p log r."""
+    from .kernels import RadialPowerKernel, RadialPowerLogKernel
+
+    kind, power = key
+    if kind == "power":
+        return RadialPowerKernel(dim, power)
+    if kind == "power_log":
+        return RadialPowerLogKernel(dim, power)
+    raise ValueError(f"unsupported split term kind {kind!r}")
+
+
+def term_scaling_code(dim, power):
+    """Single-table scaling of a term table, (h / h0)^(dim + power)
+    (``expansion_wrangler_fpnd.py:4777-4799``, no derivatives)."""
+    e = int(dim) + int(power)
+    if e == 0:
+        return "1.0"
+    return ("(" + " * ".join(["BOX_extent"] * e) + ") / ("
+            + " * ".join(["table_root_extent"] * e) + ")")
+
+
+def term_build_orders(dim, q):
+    """Default Duffy orders of the term tables (regular, radial)
+    (``expansion_wrangler_fpnd.py:4596-4619``)."""
+    if dim == 2:
+        return max(8, 4 * q), max(21, 10 * q)
+    return (6, 21) if q <= 2 else (8, 31)
+
+
+def log_alpha_per_source(tree, table_root_extent):
+    """log(box extent / table_root_extent) for each source point, by its
+    box (``expansion_wrangler_fpnd.py:4909-4974``)."""
+    h0 = float(table_root_extent)
+    if h0 <= 0.0:
+        raise ValueError("table_root_extent must be positive")
+    starts = np.asarray(tree.box_source_starts, dtype=np.int64)
+    counts = np.asarray(tree.box_source_counts_nonchild, dtype=np.int64)
+    levels = np.asarray(tree.box_levels, dtype=np.int64)[: len(counts)]
+    n = int(np.max(starts + counts)) if starts.size else 0
+    beta = np.zeros(n, dtype=np.float64)
+    root = float(tree.root_extent)
+    for b in np.nonzero(counts > 0)[0]:
+        beta[starts[b]:starts[b] + counts[b]] = np.log(root * 0.5 ** int(levels[b]) / h0)
+    return beta
+
+
+def remainder_series(dim, k, r, n_terms, split_order=1):
     """R(r) from the truncated series (numpy, for checks)."""
-    c = remainder_coefficients(dim, k, n_terms)
+    c = remainder_coefficients(dim, k, n_terms, split_order)
     c = c[..., 0] + 1j * c[..., 1]
     r = np.asarray(r, dtype=np.float64)
     if dim == 2:
@@ -124,13 +220,43 @@ def split_scaling_codes(dim):
 
 
 def split_correction(tree_view, points, weights, k, n_terms, *, exclude_self=True,
-                     stream=None):
+                     stream=None, split_order=1):
     """The list-1 remainder sum on the GPU.
 
     ``tree_view``: a ``vl1_tree_view`` (device arrays); ``points``: CUDA
     float64 [dim, N] (tree order); ``weights``: CUDA float64 or complex128 [N]
     (density x quadrature weight).  Returns CUDA complex128 [N] (zero for
     points outside the target boxes)."""
+    dim = int(points.shape[0])
+    coef = remainder_coefficients(dim, k, n_terms, split_order)
+    # a real wave number: the kernel's two-sum form of the series (in 2D it
+    # needs every log term, i.e. split order 1)
+    real_k = complex(k).imag == 0.0 and (dim == 3 or int(split_order) == 1)
+    return _series_sum(tree_view, points, weights, coef, n_terms, exclude_self,
+                       _lib.VL1_SPLIT_REAL_K if real_k else 0, stream)
+
+
+def radial_power_sum(tree_view, points, weights, power, *, exclude_self=True, stream=None):
+    """sum over list-1 source points of weights x r^power on the GPU (the
+    series kernel with one coefficient; 2D: even powers)."""
+    dim = int(points.shape[0])
+    power = int(power)
+    if dim == 2:
+        if power < 2 or power % 2:
+            raise ValueError("2D radial power sums take even powers >= 2")
+        n_terms = power // 2
+        coef = np.zeros((2, n_terms + 1, 2))
+        coef[1, n_terms, 0] = 1.0
+    else:
+        if power < 0:
+            raise ValueError("power must be non-negative")
+        n_terms = power + 1
+        coef = np.zeros((2, n_terms + 1, 2))
+        coef[0, n_terms, 0] = 1.0
+    return _series_sum(tree_view, points, weights, coef, n_terms, exclude_self, 0, stream)
+
+
+def _series_sum(tree_view, points, weights, coef_np, n_terms, exclude_self, flags, stream):
     import torch
 
     dim = int(points.shape[0])
@@ -143,13 +269,12 @@ def split_correction(tree_view, points, weights, k, n_terms, *, exclude_self=Tru
         w = torch.view_as_real(w.to(torch.complex128)).contiguous()
     else:
         w = w.to(torch.float64)
-    coef = torch.from_numpy(remainder_coefficients(dim, k, n_terms)).to("cuda")
+    coef = torch.from_numpy(np.ascontiguousarray(coef_np)).to("cuda")
     out = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
     d = _lib.SplitDesc()
     d.dim, d.n_points, d.n_terms = dim, n, int(n_terms)
     d.exclude_self, d.weights_complex = int(bool(exclude_self)), int(wcplx)
-    # a real wave number: the kernel's two-sum form of the series
-    d.flags = _lib.VL1_SPLIT_REAL_K if complex(k).imag == 0.0 else 0
+    d.flags = int(flags)
     d.tree = C.cast(C.pointer(tree_view), C.c_void_p)
     pts = points.to(torch.float64).contiguous()
     d.points, d.weights = pts.data_ptr(), w.data_ptr()

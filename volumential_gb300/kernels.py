@@ -16,7 +16,8 @@ import math
 
 __all__ = [
     "LaplaceKernel", "HelmholtzKernel", "YukawaKernel", "ConstantKernel",
-    "AxisTargetDerivative", "AxisSourceDerivative", "base_kernel",
+    "AxisTargetDerivative", "AxisSourceDerivative", "RadialPowerKernel",
+    "RadialPowerLogKernel", "base_kernel",
     "kernel_class_name", "green_function_constants",
 ]
 
@@ -75,6 +76,34 @@ class ConstantKernel(_Kernel):
 
     def __repr__(self):
         return "CstKnl%dD" % self.dim
+
+
+class RadialPowerKernel(_Kernel):
+    """K = r^power (scaling constant 1): the 3D Helmholtz split mode's extra
+    term kernels (``volumential/expansion_wrangler_fpnd.py:144-175``)."""
+
+    def __init__(self, dim, power):
+        if int(power) < 0:
+            raise ValueError("power must be non-negative")
+        self.dim = int(dim)
+        self.power = int(power)
+
+    def __repr__(self):
+        return f"RadialPowerKernel(dim={self.dim}, power={self.power})"
+
+
+class RadialPowerLogKernel(_Kernel):
+    """K = r^power log r (scaling constant 1): the 2D Helmholtz split mode's
+    extra term kernels (``volumential/expansion_wrangler_fpnd.py:178-209``)."""
+
+    def __init__(self, dim, power):
+        if int(power) <= 0:
+            raise ValueError("power must be positive for r**power * log(r)")
+        self.dim = int(dim)
+        self.power = int(power)
+
+    def __repr__(self):
+        return f"RadialPowerLogKernel(dim={self.dim}, power={self.power})"
 
 
 class _Derivative(_Kernel):

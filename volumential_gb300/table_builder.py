@@ -124,18 +124,25 @@ def entry_geometry(table, entry_ids):
 
 def kernel_code(table, kernel=None):
     """(vl1 kernel code, complex) of a table's kernel or of an explicit
-    ``kernel`` name ("laplace", "helmholtz", "constant", "plane_wave")."""
+    ``kernel`` name ("laplace", "helmholtz", "constant", "plane_wave",
+    "power", "power_log")."""
     if kernel is None:
         if table.kernel_type == "const":
             kernel = "constant"
         else:
             name = type(table.integral_knl).__name__ if table.integral_knl is not None else ""
             kernel = {"LaplaceKernel": "laplace", "HelmholtzKernel": "helmholtz",
-                      "ConstantKernel": "constant"}.get(name)
+                      "ConstantKernel": "constant", "RadialPowerKernel": "power",
+                      "_RadialPowerKernel": "power", "RadialPowerLogKernel": "power_log",
+                      "_RadialPowerLogKernel": "power_log"}.get(name)
             if kernel is None:
                 raise NotImplementedError(
                     f"no GPU Duffy kernel for {name or table.kernel_type!r} (Laplace, "
-                    "Helmholtz and constant kernels are built)")
+                    "Helmholtz, constant and radial power kernels are built)")
+    if kernel == "power":
+        return _lib.VL1_DUFFY_POWER, False
+    if kernel == "power_log":
+        return _lib.VL1_DUFFY_POWER_LOG, False
     dim = table.dim
     if kernel == "laplace":
         return (_lib.VL1_DUFFY_LAPLACE2D if dim == 2 else _lib.VL1_DUFFY_LAPLACE3D), False
@@ -150,11 +157,12 @@ def kernel_code(table, kernel=None):
 
 def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad_order=20,
                        radial_quad_order=61, mp_dps=50, kernel=None, k=None,
-                       entry_ids=None, stream=None, store=True, max_ctas=0):
+                       entry_ids=None, stream=None, store=True, max_ctas=0, power=None):
     """Compute the table's orbit-invariant entries on the GPU (FP64) and, with
     ``store``, keep them as its compact data (plus the 2D normalizers).
     ``max_ctas`` > 0 runs the build on at most that many CTAs (a build in the
-    background of other GPU work).  Returns (entry_ids, values)."""
+    background of other GPU work); ``power``: the radial power kernels'
+    power (default: the table kernel's).  Returns (entry_ids, values)."""
     import torch
 
     from .plan import require_cuda
@@ -168,6 +176,11 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
             k = table.build_extra_kwargs.get(name)
         if k is None or not np.isfinite(k):
             raise ValueError("a finite wave number k is required for this kernel")
+    if code in (_lib.VL1_DUFFY_POWER, _lib.VL1_DUFFY_POWER_LOG):
+        if power is None:
+            power = getattr(table.integral_knl, "power", None)
+        if power is None:
+            raise ValueError("the radial power kernels need a power")
     if cplx and not np.issubdtype(np.dtype(table.dtype), np.complexfloating):
         raise TypeError("complex kernel values need a complex table dtype")
     if entry_ids is None:
@@ -196,6 +209,7 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
     d.n_reg, d.n_rad, d.kernel = len(gx), len(rx), code
     d.complex_output = int(cplx)
     d.max_ctas = int(max_ctas)
+    d.power = int(power or 0)
     d.extent = float(table.source_box_extent)
     d.k = float(k) if k is not None else 0.0
     d.target_points, d.decomposition_targets = arrs["tp"].data_ptr(), arrs["dc"].data_ptr()
