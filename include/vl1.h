@@ -44,7 +44,12 @@ enum {
 };
 
 enum { VL1_REAL64 = 0, VL1_COMPLEX128 = 1 };
-enum { VL1_RECON_SCALAR_ARITH = 0, VL1_RECON_SIGNED_ARITH = 1 };
+/* VL1_RECON_DENSE: table_data holds every entry of every level,
+ * [n_tables][n_cases][n_q_points (source mode)][n_q_points (target point)]
+ * (n_table_entries = n_cases * n_q_points^2), used as is; the case_* / axis_*
+ * orbit arrays are not read (list1.py:1018-1048, the dense fallback for
+ * kernels without an arithmetic orbit reconstruction). */
+enum { VL1_RECON_SCALAR_ARITH = 0, VL1_RECON_SIGNED_ARITH = 1, VL1_RECON_DENSE = 2 };
 enum { VL1_DISP_NONE = 0, VL1_DISP_LOG2D = 1 };
 enum { VL1_LEVEL_ZERO = 0, VL1_LEVEL_PER_LEVEL = 1 };
 
@@ -373,7 +378,9 @@ typedef struct {
                                  most this many CTAs, striding over them (a build
                                  that leaves most SMs to other work) */
   int32_t power;              /* VL1_DUFFY_POWER / _POWER_LOG: the power of r (<= 64) */
-  int32_t reserved;           /* 0 */
+  int32_t derivative;         /* Laplace / Helmholtz only: 0 none, a + 1 the target
+                                 derivative d/dt_a, -(a + 1) the source derivative
+                                 d/dy_a (AxisTarget/SourceDerivative) */
   double extent;              /* source box [0, extent]^dim */
   double k;                   /* Helmholtz / plane-wave wave number */
   const double *target_points;          /* [dim][n_entries] */

@@ -73,11 +73,27 @@ def node_set(dim, regular_order, radial_order):
     return np.array(us).T, np.array(sgs).T, np.array(jacs)
 
 
-def green(kind, dvec, k=0.0, power=0):
+def green(kind, dvec, k=0.0, power=0, derivative=0):
     """Kernel value times scaling constant at displacements dvec [dim, n]
     ("power" r^p and "power_log" r^p log r: the split-term kernels of
-    ``volumential/expansion_wrangler_fpnd.py:144-209``, constant 1)."""
+    ``volumential/expansion_wrangler_fpnd.py:144-209``, constant 1).
+    ``derivative`` a + 1: d/dt_a, -(a + 1): d/dy_a (Laplace, Helmholtz)."""
     r = np.sqrt(np.sum(dvec * dvec, axis=0))
+    if derivative:
+        a = abs(derivative) - 1
+        sgn = 1.0 if derivative > 0 else -1.0
+        da = dvec[a]
+        dim = dvec.shape[0]
+        if kind == "laplace":
+            g = -da / (2 * np.pi * r * r) if dim == 2 else -da / (4 * np.pi * r ** 3)
+        elif kind == "helmholtz":
+            if dim == 2:
+                g = -0.25j * k * special.hankel1(1, k * r) * da / r
+            else:
+                g = np.exp(1j * k * r) * (1j * k * r - 1.0) * da / (4 * np.pi * r ** 3)
+        else:
+            raise ValueError(f"no derivative of the {kind} kernel")
+        return sgn * g
     if kind == "power":
         return r ** power
     if kind == "power_log":
@@ -123,7 +139,7 @@ def _basis(xi, bw, m, y, extent):
 
 
 def entry_values(dim, q, extent, kind, targets, modes, regular_order, radial_order, k=0.0,
-                 power=0):
+                 power=0, derivative=0):
     """Table values of entries with target points ``targets`` [dim, n] and
     source mode axes ``modes`` [dim, n]."""
     u, sg, jac = node_set(dim, regular_order, radial_order)
@@ -148,6 +164,6 @@ def entry_values(dim, q, extent, kind, targets, modes, regular_order, radial_ord
             for a in range(dim):
                 basis *= _basis(xi, bw, int(modes[a, e]), y[a], extent)
         with np.errstate(divide="ignore", invalid="ignore"):
-            g = green(kind, np.where(active[None, :], dv, 1.0), k, power)
+            g = green(kind, np.where(active[None, :], dv, 1.0), k, power, derivative)
         out.append(np.sum(np.where(active, g * w * basis, 0.0)))
     return np.array(out)

@@ -685,3 +685,52 @@ def test_header_constants_match_the_python_binding():
     assert len(consts) >= 28
     for name, val in consts.items():
         assert getattr(_lib, name) == val, name
+
+
+def test_dense_fallback_takes_full_tables_only():
+    # list1.py:1018-1048: a kernel without the arithmetic orbit symmetry
+    # keeps a full table; a symmetry-reduced one would need the
+    # generated-orbit fallback, which is not built
+    import numpy as np
+    import pytest
+
+    from volumential_gb300.expansion_wrangler_fpnd import _prepare_table_data_and_entry_map
+    from volumential_gb300.kernels import PlaneWaveKernel
+    from volumential_gb300.nearfield_potential_table import NearFieldInteractionTable
+
+    t = NearFieldInteractionTable(2, dim=2, sumpy_kernel=PlaneWaveKernel(2),
+                                  source_box_extent=0.5)
+    assert t._get_invariant_entry_info() is None
+    rng = np.random.default_rng(0)
+    t.data = rng.standard_normal(t.n_cases * t.n_pairs)
+    tdc, nm, ext, ids, scales, info = _prepare_table_data_and_entry_map([t, t])
+    assert info["kind"] == "dense" and tdc.shape == (2, t.n_cases * t.n_pairs)
+    assert np.array_equal(tdc[1], t.data) and np.array_equal(ids, np.arange(tdc.shape[1]))
+    t.set_reduced_table_data(np.arange(10), np.ones(10))
+    with pytest.raises(NotImplementedError):
+        _prepare_table_data_and_entry_map([t])
+
+
+def test_derivative_kernels_take_the_signed_arithmetic_symmetry():
+    # orbit_arithmetic.py:176-300: differentiated axes fixed (own groups) and
+    # odd under reflection, the other axes one group
+    import numpy as np
+
+    from volumential_gb300.kernels import (
+        AxisSourceDerivative,
+        AxisTargetDerivative,
+        LaplaceKernel,
+        PlaneWaveKernel,
+        arithmetic_symmetry,
+    )
+
+    assert arithmetic_symmetry(LaplaceKernel(3), 3) is None
+    assert arithmetic_symmetry(PlaneWaveKernel(2), 2) is False
+    s = arithmetic_symmetry(AxisTargetDerivative(1, LaplaceKernel(3)), 3)
+    assert s["axis_groups"] == ((1,), (0, 2))
+    assert np.array_equal(s["axis_sign_power"], [0, 1, 0])
+    s2 = arithmetic_symmetry(AxisSourceDerivative(0, AxisTargetDerivative(0, LaplaceKernel(2))), 2)
+    assert s2["axis_groups"] == ((0,), (1,)) and np.array_equal(s2["axis_sign_power"], [0, 0])
+    s3 = arithmetic_symmetry(AxisSourceDerivative(2, AxisTargetDerivative(0, LaplaceKernel(3))), 3)
+    assert s3["axis_groups"] == ((0,), (2,), (1,))
+    assert np.array_equal(s3["axis_sign_power"], [1, 0, 1])

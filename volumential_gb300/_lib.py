@@ -45,6 +45,7 @@ VL1_REAL64 = 0
 VL1_COMPLEX128 = 1
 VL1_RECON_SCALAR_ARITH = 0
 VL1_RECON_SIGNED_ARITH = 1
+VL1_RECON_DENSE = 2
 VL1_DISP_NONE = 0
 VL1_DISP_LOG2D = 1
 VL1_LEVEL_ZERO = 0
@@ -127,7 +128,7 @@ class DuffyDesc(C.Structure):
     _fields_ = [("dim", C.c_int32), ("q", C.c_int32), ("n_entries", C.c_int32),
                 ("n_reg", C.c_int32), ("n_rad", C.c_int32), ("kernel", C.c_int32),
                 ("complex_output", C.c_int32), ("max_ctas", C.c_int32),
-                ("power", C.c_int32), ("reserved", C.c_int32),
+                ("power", C.c_int32), ("derivative", C.c_int32),
                 ("extent", C.c_double), ("k", C.c_double),
                 ("target_points", C.c_void_p), ("decomposition_targets", C.c_void_p),
                 ("mode_axes", C.c_void_p), ("regular_nodes", C.c_void_p),

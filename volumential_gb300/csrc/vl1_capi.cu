@@ -133,18 +133,21 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
     return VL1_E_UNSUPPORTED;
   }
   if (desc->reconstruction_kind != VL1_RECON_SCALAR_ARITH &&
-      desc->reconstruction_kind != VL1_RECON_SIGNED_ARITH) {
-    set_error("unsupported reconstruction kind %d: only the scalar/signed arithmetic "
-              "orbit reconstruction has a device path",
+      desc->reconstruction_kind != VL1_RECON_SIGNED_ARITH &&
+      desc->reconstruction_kind != VL1_RECON_DENSE) {
+    set_error("unsupported reconstruction kind %d: the scalar/signed arithmetic orbit "
+              "reconstruction and the dense table have device paths",
               desc->reconstruction_kind);
     return VL1_E_UNSUPPORTED_RECON;
   }
+  const bool dense = desc->reconstruction_kind == VL1_RECON_DENSE;
   if (desc->quad_order < 1 || desc->n_tables < 1 || desc->n_table_entries < 1 ||
-      desc->n_cases < 1 || desc->n_case_orbits < 1 || desc->n_case_codes < 1 ||
-      !desc->table_data || !desc->mode_nmlz || !desc->case_indices ||
-      !desc->case_orbit_ranks || !desc->case_axis_perm || !desc->case_axis_sign ||
-      !desc->case_axis_group || !desc->case_value_offsets || !desc->axis_sign_power ||
-      !desc->axis_direction_signs) {
+      desc->n_cases < 1 || desc->n_case_codes < 1 || !desc->table_data ||
+      !desc->mode_nmlz || !desc->case_indices ||
+      (!dense && (desc->n_case_orbits < 1 || !desc->case_orbit_ranks ||
+                  !desc->case_axis_perm || !desc->case_axis_sign ||
+                  !desc->case_axis_group || !desc->case_value_offsets ||
+                  !desc->axis_sign_power || !desc->axis_direction_signs))) {
     set_error("vl1_plan_create: invalid plan description");
     return VL1_E_ARG;
   }
@@ -153,6 +156,11 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
   if (nq > 1024) {
     set_error("q^dim = %lld exceeds the supported 1024 points per box", (long long)nq);
     return VL1_E_UNSUPPORTED;
+  }
+  if (dense && (int64_t)desc->n_table_entries != (int64_t)desc->n_cases * nq * nq) {
+    set_error("a dense table has n_cases * n_q_points^2 = %lld entries per level, not %d",
+              (long long)desc->n_cases * nq * nq, desc->n_table_entries);
+    return VL1_E_ARG;
   }
   if (desc->value_type != VL1_REAL64 && desc->value_type != VL1_COMPLEX128) {
     set_error("value_type must be VL1_REAL64 or VL1_COMPLEX128");
@@ -178,7 +186,7 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
   d.n_tables = desc->n_tables;
   d.n_entries = desc->n_table_entries;
   d.n_cases = desc->n_cases;
-  d.n_orbits = desc->n_case_orbits;
+  d.n_orbits = dense ? 0 : desc->n_case_orbits;
   d.n_case_codes = desc->n_case_codes;
   d.encoding_base = desc->encoding_base;
   d.direction_sign_axis = desc->direction_sign_axis;
@@ -198,13 +206,15 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
   if (!st) st = upload(p, &d.table, desc->table_data, vsz * d.n_tables * (size_t)d.n_entries);
   if (!st) st = upload(p, &d.nmlz, desc->mode_nmlz, vsz * d.n_tables * (size_t)nq);
   if (!st) st = upload(p, &d.case_indices, desc->case_indices, 8 * (size_t)d.n_case_codes);
-  if (!st) st = upload(p, &d.orbit_ranks, desc->case_orbit_ranks, 2 * (size_t)d.n_cases);
-  if (!st) st = upload(p, &d.perm, desc->case_axis_perm, dim * d.n_cases);
-  if (!st) st = upload(p, &d.sign, desc->case_axis_sign, dim * d.n_cases);
-  if (!st) st = upload(p, &d.group, desc->case_axis_group, dim * d.n_cases);
-  if (!st) st = upload(p, &d.offsets, desc->case_value_offsets, 4 * (size_t)(d.n_orbits + 1));
-  if (!st) st = upload(p, &d.sign_power, desc->axis_sign_power, dim);
-  if (!st) st = upload(p, &d.dir_signs, desc->axis_direction_signs, dim);
+  if (!dense) {
+    if (!st) st = upload(p, &d.orbit_ranks, desc->case_orbit_ranks, 2 * (size_t)d.n_cases);
+    if (!st) st = upload(p, &d.perm, desc->case_axis_perm, dim * d.n_cases);
+    if (!st) st = upload(p, &d.sign, desc->case_axis_sign, dim * d.n_cases);
+    if (!st) st = upload(p, &d.group, desc->case_axis_group, dim * d.n_cases);
+    if (!st) st = upload(p, &d.offsets, desc->case_value_offsets, 4 * (size_t)(d.n_orbits + 1));
+    if (!st) st = upload(p, &d.sign_power, desc->axis_sign_power, dim);
+    if (!st) st = upload(p, &d.dir_signs, desc->axis_direction_signs, dim);
+  }
   if (!st) {
     void *ptr = nullptr;
     st = plan_alloc(p, &ptr, sizeof(vl1_status));
@@ -214,7 +224,7 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
       if (e != cudaSuccess) st = cuda_fail(e, "cudaMemset(status)");
     }
   }
-  if (!st) {
+  if (!st && !dense) {
     // Validate the descriptor offsets on the host: every row the arithmetic
     // can produce must lie inside the table.
     const int32_t *off = desc->case_value_offsets;
@@ -243,11 +253,16 @@ int32_t vl1_plan_create(const vl1_plan_desc *desc, vl1_plan **plan_out) {
       free_plan(p, 0);
       return VL1_E_UNSUPPORTED;
     }
-    void *ptr = nullptr;
-    st = plan_alloc(p, &ptr, vsz * (size_t)p->block_elems);
-    if (!st) {
-      d.blocks = static_cast<const double *>(ptr);
-      st = launch_expand_blocks(p, 0);
+    if (dense) {
+      // the table is already laid out as the blocks [level][case][source][target]
+      d.blocks = d.table;
+    } else {
+      void *ptr = nullptr;
+      st = plan_alloc(p, &ptr, vsz * (size_t)p->block_elems);
+      if (!st) {
+        d.blocks = static_cast<const double *>(ptr);
+        st = launch_expand_blocks(p, 0);
+      }
     }
   }
   if (!st) {
@@ -502,6 +517,10 @@ int32_t vl1_orbit_index_map(vl1_plan *plan, int32_t *rows, int8_t *signs, void *
   if (!plan || !rows || !signs) {
     set_error("vl1_orbit_index_map: null argument");
     return VL1_E_ARG;
+  }
+  if (plan->d.n_orbits == 0) {
+    set_error("vl1_orbit_index_map: a dense-table plan has no orbit map");
+    return VL1_E_UNSUPPORTED_RECON;
   }
   return launch_index_map(plan, rows, signs, static_cast<cudaStream_t>(stream));
 }

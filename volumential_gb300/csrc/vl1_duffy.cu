@@ -44,6 +44,43 @@ __device__ constexpr int8_t kPerm2[2][2] = {{0, 1}, {1, 0}};
 __device__ constexpr int8_t kPerm3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2},
                                             {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 
+// d/dt_a of G(dvec) (dvec = target - source) times the scaling constant,
+// Laplace and Helmholtz: G'(r) d_a / r; (re, im)
+template <int DIM>
+__device__ __forceinline__ void green_gradient(int kind, double k, int axis, const double *dv,
+                                               double &re, double &im) {
+  double r2 = 0.0;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) r2 = fma(dv[a], dv[a], r2);
+  const double da = dv[axis];
+  im = 0.0;
+  switch (kind) {
+    case VL1_DUFFY_LAPLACE2D:   // -d_a / (2 pi r^2)
+      re = -da / r2 * (0.5 / 3.141592653589793);
+      break;
+    case VL1_DUFFY_LAPLACE3D:   // -d_a / (4 pi r^3)
+      re = -da / (r2 * sqrt(r2)) * (0.25 / 3.141592653589793);
+      break;
+    case VL1_DUFFY_HELMHOLTZ2D: {   // -(i/4) k H1(k r) d_a / r = (k/4)(Y1 - i J1) d_a / r
+      const double r = sqrt(r2);
+      const double f = 0.25 * k * da / r;
+      re = f * y1(k * r);
+      im = -f * j1(k * r);
+      break;
+    }
+    default: {   // VL1_DUFFY_HELMHOLTZ3D: exp(i k r) (i k r - 1) d_a / (4 pi r^3)
+      const double r = sqrt(r2);
+      double sn, cs;
+      sincos(k * r, &sn, &cs);
+      const double f = (0.25 / 3.141592653589793) * da / (r2 * r);
+      // (cs + i sn)(-1 + i k r) = (-cs - k r sn) + i (k r cs - sn)
+      re = f * (-cs - k * r * sn);
+      im = f * (k * r * cs - sn);
+      break;
+    }
+  }
+}
+
 // G(dvec) times the kernel's scaling constant; (re, im)
 template <int DIM>
 __device__ __forceinline__ void green(int kind, double k, int power, const double *dv,
@@ -206,7 +243,16 @@ __global__ void __launch_bounds__(kDuffyThreads) duffy_entry_kernel(const DuffyA
     for (int a = 0; a < dim; ++a) r2 = fma(dv[a], dv[a], r2);
     if (!(r2 > 0.0)) continue;   // a node on the singular point: zero weight
     double gre, gim;
-    green<DIM>(D.kernel, D.k, D.power, dv, gre, gim);
+    if (D.derivative == 0) {
+      green<DIM>(D.kernel, D.k, D.power, dv, gre, gim);
+    } else {
+      const int axis = (D.derivative > 0 ? D.derivative : -D.derivative) - 1;
+      green_gradient<DIM>(D.kernel, D.k, axis, dv, gre, gim);
+      if (D.derivative < 0) {   // d/dy_a G(t - y) = -d/dt_a G
+        gre = -gre;
+        gim = -gim;
+      }
+    }
     const double f = w * jac * len_prod * basis;
     acc_re = fma(gre, f, acc_re);
     acc_im = fma(gim, f, acc_im);
@@ -270,6 +316,12 @@ extern "C" int32_t vl1_duffy_table(const vl1_duffy_desc *desc, double *result, v
       D.kernel > VL1_DUFFY_POWER_LOG) {
     set_error("vl1_duffy_table: dim %d, q %d, entries %d, rules %d/%d, extent %g or kernel %d "
               "out of range", D.dim, D.q, D.n_entries, D.n_reg, D.n_rad, D.extent, D.kernel);
+    return VL1_E_ARG;
+  }
+  if (D.derivative != 0 &&
+      (D.derivative > D.dim || D.derivative < -D.dim || D.kernel > VL1_DUFFY_HELMHOLTZ3D)) {
+    set_error("vl1_duffy_table: derivative %d of kernel %d not supported (Laplace and "
+              "Helmholtz first derivatives along an axis)", D.derivative, D.kernel);
     return VL1_E_ARG;
   }
   if ((D.kernel == VL1_DUFFY_POWER && (D.power < 0 || D.power > 64)) ||

@@ -87,16 +87,21 @@ __device__ __forceinline__ unsigned long long fixed_magnitude(double v, int e) {
 // drops (i + j >= 7) zero-mean, so the dropped terms cancel instead of
 // adding up with the sign of the products, as sign-magnitude digits would.
 __device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits]) {
-  long long r = (long long)fixed_magnitude<kFixedBits>(v, e);
+  const unsigned long long m = fixed_magnitude<kFixedBits>(v, e);
   const int sgn = __double_as_longlong(v) < 0 ? -1 : 1;
+  // bytes of m (low to high) in 32-bit arithmetic; a byte >= 128 becomes
+  // byte - 256 and carries one into the next (a byte 255 plus a carry gives
+  // 0 and carries on)
+  const unsigned lo32 = (unsigned)m;
+  int carry = 0;
 #pragma unroll
   for (int i = kDigits - 1; i >= 1; --i) {
-    int lo = (int)(r & 0xFF);
-    lo -= lo >= 128 ? 256 : 0;
-    dig[i] = sgn * lo;
-    r = (r - lo) >> kDigitBits;
+    int t = (int)((lo32 >> (kDigitBits * (kDigits - 1 - i))) & 0xFFu) + carry;
+    carry = t >= 128 ? 1 : 0;
+    t -= carry << kDigitBits;
+    dig[i] = sgn * t;
   }
-  dig[0] = sgn * (int)r;   // m < 2^39: r <= 128
+  dig[0] = sgn * ((int)(m >> 32) + carry);   // m < 2^39: <= 128
 }
 
 // exponent e with |v| < 2^e, as frexp returns it (-1074 for v == 0), from the
@@ -194,127 +199,263 @@ struct PrepTask {
   int64_t row0;
 };
 
-// warp-wide maximum exponent of scaling * coefficient over row idx = b * nrhs
-// + r (-1074 for an empty row); the same value in every lane
-__device__ __forceinline__ int row_exponent(const DevDesc &d, const TreeDev &tr,
-                                            const double *coefs, int nrhs, int64_t idx,
-                                            int lane) {
-  const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-  const int cnt = min(tr.src_counts[b], d.nq);
-  int e = -1074;
-  if (cnt > 0) {
-    const double sc = box_scaling(d, tr, tr.levels[b]);
-    const double *c = coefs + (int64_t)r * tr.n_particles + tr.src_starts[b];
-    for (int s = lane; s < cnt; s += 32) e = max(e, scale_exponent(sc * c[s]));
+// The preparation passes take the density rows (R = b * nrhs + r) in groups
+// of kRowGroup consecutive rows per warp: lane j < kRowGroup loads row j's
+// box data, and every lane issues its loads of all rows of the group before
+// using them, so that the rows' memory latencies overlap (one row per warp
+// left both passes latency-bound at ~20 us each on a 26k-box tree).
+constexpr int kRowGroup = 8;
+
+struct RowGroup {
+  int n;                 // rows in the group (<= kRowGroup)
+  int cnt, start, rhs;   // lane j < n: row j's source count (clamped), first source, rhs
+  int level, box;
+};
+
+__device__ __forceinline__ RowGroup load_row_group(const DevDesc &d, const TreeDev &tr,
+                                                   int nrhs, int64_t r0, int n, int lane,
+                                                   vl1_status *st) {
+  RowGroup g;
+  g.n = n;
+  g.cnt = g.start = g.rhs = g.level = g.box = 0;
+  if (lane < n) {
+    const int64_t idx = r0 + lane;
+    const int b = (int)(idx / nrhs);
+    g.box = b;
+    g.rhs = (int)(idx - (int64_t)b * nrhs);
+    int cnt = tr.src_counts[b];
+    if (cnt > d.nq) {
+      if (st) report(st, VL1_E_LAYOUT, b, cnt);
+      cnt = d.nq;
+    }
+    g.cnt = cnt;
+    g.start = tr.src_starts[b];
+    g.level = tr.levels[b];
   }
-  return __reduce_max_sync(0xffffffffu, e);
+  return g;
 }
 
-// the exponent pass: row idx's largest exponent into its rhs's maximum
-__device__ __forceinline__ void row_exponent_max(const DevDesc &d, const TreeDev &tr,
-                                                 const double *coefs, int nrhs, int *x_exp,
-                                                 int64_t idx, int lane) {
-  const int e = row_exponent(d, tr, coefs, nrhs, idx, lane);
-  if (lane == 0 && e > -1074) atomicMax(x_exp + idx % nrhs, e + kExpBias);
+// warp-wide maximum of a 64-bit unsigned value
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+  const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32));
+  const unsigned lo = __reduce_max_sync(0xffffffffu,
+                                        (unsigned)(v >> 32) == hi ? (unsigned)v : 0u);
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+// The exponent pass: each row's largest exponent of scaling * coefficient
+// into its rhs's maximum.  Rounding is monotone, so the largest exponent of
+// sc * c over a row is the exponent of sc * max |c|: the row's maximum is
+// taken on the IEEE bit patterns of |c| (ordered like the values) and
+// multiplied once.  A block collects the maxima of its rows in shared memory
+// (rhs counts up to kExpSmemRhs) and adds one global atomic per rhs.
+constexpr int kExpSmemRhs = 1024;
+
+__device__ __forceinline__ void exp_block_begin(int nrhs, int *s_max) {
+  if (nrhs <= kExpSmemRhs)
+    for (int i = threadIdx.x; i < nrhs; i += blockDim.x) s_max[i] = 0;
+  __syncthreads();
+}
+
+__device__ __forceinline__ void group_exponent_max(const DevDesc &d, const TreeDev &tr,
+                                                   const double *coefs, int nrhs, int *x_exp,
+                                                   int64_t r0, int n, int lane, int *s_max) {
+  const RowGroup g = load_row_group(d, tr, nrhs, r0, n, lane, nullptr);
+  int cnt[kRowGroup];
+  const double *c[kRowGroup];
+#pragma unroll
+  for (int u = 0; u < kRowGroup; ++u) {
+    cnt[u] = __shfl_sync(0xffffffffu, g.cnt, u);
+    const int st = __shfl_sync(0xffffffffu, g.start, u);
+    const int rh = __shfl_sync(0xffffffffu, g.rhs, u);
+    c[u] = coefs + (int64_t)rh * tr.n_particles + st;
+    if (u >= n) cnt[u] = 0;
+  }
+  unsigned long long m[kRowGroup];
+#pragma unroll
+  for (int u = 0; u < kRowGroup; ++u) m[u] = 0ull;
+  for (int k = lane; k < d.nq; k += 32) {
+    double v[kRowGroup];
+#pragma unroll
+    for (int u = 0; u < kRowGroup; ++u) v[u] = k < cnt[u] ? c[u][k] : 0.0;
+#pragma unroll
+    for (int u = 0; u < kRowGroup; ++u) {
+      const unsigned long long a =
+          static_cast<unsigned long long>(__double_as_longlong(v[u])) & 0x7FFFFFFFFFFFFFFFull;
+      m[u] = a > m[u] ? a : m[u];
+    }
+  }
+  unsigned long long mine = 0ull;
+#pragma unroll
+  for (int u = 0; u < kRowGroup; ++u) {
+    const unsigned long long w = warp_max_u64(m[u]);
+    if (lane == u) mine = w;
+  }
+  if (lane < n && mine != 0ull) {
+    const double sc = box_scaling(d, tr, g.level);
+    const int e = scale_exponent(sc * __longlong_as_double((long long)mine));
+    if (e > -1074) {
+      if (nrhs <= kExpSmemRhs)
+        atomicMax(s_max + g.rhs, e + kExpBias);
+      else
+        atomicMax(x_exp + g.rhs, e + kExpBias);
+    }
+  }
+}
+
+// the block's maxima into the global ones (0: no nonzero value seen; the
+// biased exponents are positive)
+__device__ __forceinline__ void exp_block_end(int nrhs, const int *s_max, int *x_exp) {
+  __syncthreads();
+  if (nrhs <= kExpSmemRhs)
+    for (int i = threadIdx.x; i < nrhs; i += blockDim.x)
+      if (s_max[i] > 0) atomicMax(x_exp + i, s_max[i]);
 }
 
 // Density digit planes of row R = b * nrhs + r: [K chunk][plane][kc] FP16
 // values (source points at their mode id, zero elsewhere), planes X1, X2, X3
 // (the three leading balanced digits) and R = X4 + X5 / 256 rounded once to
 // FP16 (the tails only), so that the four planes of one pipeline unit are one
-// contiguous 8 * kc-byte piece at byte kchunk * 8 * kc.  One warp per row:
-// assembled in the warp's shared-memory slice `stage` (8 * kp bytes) and
-// written out with 16-byte stores.
+// contiguous 8 * kc-byte piece at byte kchunk * 8 * kc.  A warp takes a group
+// of rows, assembles each in its own slice of the warp's shared-memory
+// staging (G slices of 8 * kp bytes) and writes them out with 16-byte
+// stores.
 constexpr int kXPlanes = 4;          // density planes: X1, X2, X3, R
-__device__ __forceinline__ void row_planes(const DevDesc &d, const TreeDev &tr,
-                                           const double *coefs, int nrhs, const int *x_exp,
-                                           __half *xpl, int kp, int kc, vl1_status *st,
-                                           int64_t idx, int lane, uint8_t *stage) {
+#ifndef VL1_PLANE_GROUP
+#define VL1_PLANE_GROUP 4
+#endif
+// rows per warp group of the plane pass (its digit work holds every row's
+// state in registers, so it takes fewer rows than the exponent pass)
+constexpr int kPlaneGroup = VL1_PLANE_GROUP;
+template <int G>
+__device__ __forceinline__ void group_planes(const DevDesc &d, const TreeDev &tr,
+                                             const double *coefs, int nrhs, const int *x_exp,
+                                             __half *xpl, int kp, int kc, vl1_status *st,
+                                             int64_t r0, int n, int lane, uint8_t *stage) {
   const int row_bytes = kp * kXPlanes * 2;
-  const int b = (int)(idx / nrhs), r = (int)(idx % nrhs);
-  int cnt = tr.src_counts[b];
-  const int s0 = tr.src_starts[b];
-  if (cnt > d.nq) {
-    if (lane == 0) report(st, VL1_E_LAYOUT, b, cnt);
-    cnt = d.nq;
+  const RowGroup g = load_row_group(d, tr, nrhs, r0, n, lane, st);
+  int ex = 0;
+  double sc = 0.0;
+  if (lane < n) {
+    ex = x_exp[g.rhs] - kExpBias;
+    sc = box_scaling(d, tr, g.level);
   }
-  for (int k = lane * 16; k < row_bytes; k += 32 * 16)
+  for (int k = lane * 16; k < G * row_bytes; k += 32 * 16)
     *reinterpret_cast<uint4 *>(stage + k) = make_uint4(0u, 0u, 0u, 0u);
+  // every row's data in every lane (shuffles before the point loop, which
+  // not all lanes enter when nq is not a multiple of 32)
+  int cnt[G], st0[G], eu[G], bx[G];
+  double scu[G];
+  const double *c[G];
+#pragma unroll
+  for (int u = 0; u < G; ++u) {
+    cnt[u] = __shfl_sync(0xffffffffu, g.cnt, u);
+    st0[u] = __shfl_sync(0xffffffffu, g.start, u);
+    const int rh = __shfl_sync(0xffffffffu, g.rhs, u);
+    eu[u] = __shfl_sync(0xffffffffu, ex, u);
+    scu[u] = __shfl_sync(0xffffffffu, sc, u);
+    bx[u] = __shfl_sync(0xffffffffu, g.box, u);
+    c[u] = coefs + (int64_t)rh * tr.n_particles + st0[u];
+    if (u >= n) cnt[u] = 0;
+  }
   __syncwarp();
-  if (cnt > 0) {
-    const int e = x_exp[r] - kExpBias;
-    const double sc = box_scaling(d, tr, tr.levels[b]);
-    const double *c = coefs + (int64_t)r * tr.n_particles + s0;
-    __half *sp = reinterpret_cast<__half *>(stage);
-    for (int s = lane; s < cnt; s += 32) {
-      const int m = tr.smode[s0 + s];
-      if (m < 0 || m >= d.nq) {
-        report(st, VL1_E_LAYOUT, b, -1 - s);
+  for (int k = lane; k < d.nq; k += 32) {
+    double v[G];
+    int m[G];
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      const bool have = k < cnt[u];
+      v[u] = have ? c[u][k] : 0.0;
+      m[u] = have ? tr.smode[st0[u] + k] : -2;
+    }
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      if (m[u] == -2) continue;
+      if (m[u] < 0 || m[u] >= d.nq) {
+        report(st, VL1_E_LAYOUT, bx[u], -1 - k);
         continue;
       }
       int dig[kDigits];
-      fixed_digits(sc * c[s], e, dig);
-      __half *v = sp + (m / kc) * kXPlanes * kc + (m % kc);
-      v[0] = __int2half_rn(dig[0]);
-      v[kc] = __int2half_rn(dig[1]);
-      v[2 * kc] = __int2half_rn(dig[2]);
+      fixed_digits(scu[u] * v[u], eu[u], dig);
+      __half *hv = reinterpret_cast<__half *>(stage + u * row_bytes) +
+                   (m[u] / kc) * kXPlanes * kc + (m[u] % kc);
+      hv[0] = __int2half_rn(dig[0]);
+      hv[kc] = __int2half_rn(dig[1]);
+      hv[2 * kc] = __int2half_rn(dig[2]);
       // exact in FP32 (|.| <= 128.5 in steps of 1/256), one rounding to FP16
-      v[3 * kc] = __float2half_rn((float)dig[3] + (float)dig[4] * (1.0f / 256.0f));
+      hv[3 * kc] = __float2half_rn((float)dig[3] + (float)dig[4] * (1.0f / 256.0f));
     }
   }
   __syncwarp();
-  uint8_t *row = reinterpret_cast<uint8_t *>(xpl) + idx * row_bytes;
-  for (int k = lane * 16; k < row_bytes; k += 32 * 16)
-    *reinterpret_cast<uint4 *>(row + k) = *reinterpret_cast<const uint4 *>(stage + k);
+  for (int u = 0; u < n; ++u) {
+    uint8_t *row = reinterpret_cast<uint8_t *>(xpl) + (r0 + u) * row_bytes;
+    for (int k = lane * 16; k < row_bytes; k += 32 * 16)
+      *reinterpret_cast<uint4 *>(row + k) =
+          *reinterpret_cast<const uint4 *>(stage + u * row_bytes + k);
+  }
   __syncwarp();
 }
 
 __global__ void x_exponent_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs,
                                   int nrhs, int *x_exp) {
+  __shared__ int s_max[kExpSmemRhs];
+  exp_block_begin(nrhs, s_max);
   const int64_t n = (int64_t)nboxes * nrhs;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
-       idx += warps)
-    row_exponent_max(d, tr, coefs, nrhs, x_exp, idx, lane);
+  for (int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+       g * kRowGroup < n; g += warps) {
+    const int64_t r0 = g * kRowGroup;
+    group_exponent_max(d, tr, coefs, nrhs, x_exp, r0,
+                       (int)min((int64_t)kRowGroup, n - r0), lane, s_max);
+  }
+  exp_block_end(nrhs, s_max, x_exp);
 }
 
-// dynamic shared memory: (blockDim.x / 32) x kp * 8 bytes (kp a multiple of
-// 16, so every warp's slice and row stays 16-byte aligned)
+// dynamic shared memory: (blockDim.x / 32) x kPlaneGroup x kp * 8 bytes (kp a
+// multiple of 16, so every slice and row stays 16-byte aligned)
 __global__ void __launch_bounds__(128)
     x_planes_kernel(DevDesc d, TreeDev tr, int nboxes, const double *coefs, int nrhs,
                     const int *x_exp, __half *xpl, int kp, int kc, vl1_status *st) {
   extern __shared__ __align__(16) uint8_t s_stage[];
   const int64_t n = (int64_t)nboxes * nrhs;
   const int lane = threadIdx.x & 31;
-  uint8_t *stage = s_stage + (threadIdx.x >> 5) * kp * kXPlanes * 2;
+  uint8_t *stage = s_stage + (threadIdx.x >> 5) * kPlaneGroup * kp * kXPlanes * 2;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t idx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; idx < n;
-       idx += warps)
-    row_planes(d, tr, coefs, nrhs, x_exp, xpl, kp, kc, st, idx, lane, stage);
+  for (int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+       g * kPlaneGroup < n; g += warps) {
+    const int64_t r0 = g * kPlaneGroup;
+    group_planes<kPlaneGroup>(d, tr, coefs, nrhs, x_exp, xpl, kp, kc, st, r0,
+                              (int)min((int64_t)kPlaneGroup, n - r0), lane, stage);
+  }
 }
 
 // Batch versions: block i handles rows [row0, row0 + nrows) of one problem
-// (tasks built on the host), its warps striding over them.
+// (tasks built on the host), its warps taking groups of rows.
 __global__ void x_exponent_batch_kernel(const PrepProblem *probs, const PrepTask *tasks) {
+  __shared__ int s_max[kExpSmemRhs];
   const PrepTask t = tasks[blockIdx.x];
   const PrepProblem &P = probs[t.problem];
+  exp_block_begin(P.nrhs, s_max);
   const int lane = threadIdx.x & 31;
-  for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5)
-    row_exponent_max(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, t.row0 + i, lane);
+  for (int i = (threadIdx.x >> 5) * kRowGroup; i < t.nrows; i += (blockDim.x >> 5) * kRowGroup)
+    group_exponent_max(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, t.row0 + i,
+                       min(kRowGroup, t.nrows - i), lane, s_max);
+  exp_block_end(P.nrhs, s_max, P.x_exp);
 }
 
-// Dynamic shared memory: (blockDim.x / 32) x (largest kp) * 8 bytes.
+// Dynamic shared memory: (blockDim.x / 32) x kPlaneGroup x (largest kp) * 8 bytes.
 __global__ void __launch_bounds__(128)
     x_planes_batch_kernel(const PrepProblem *probs, const PrepTask *tasks, int max_row_bytes) {
   extern __shared__ __align__(16) uint8_t s_stage[];
   const PrepTask t = tasks[blockIdx.x];
   const PrepProblem &P = probs[t.problem];
   const int lane = threadIdx.x & 31;
-  uint8_t *stage = s_stage + (threadIdx.x >> 5) * max_row_bytes;
-  for (int64_t i = threadIdx.x >> 5; i < t.nrows; i += blockDim.x >> 5)
-    row_planes(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, P.xpl, P.kp, P.kc, P.st, t.row0 + i,
-               lane, stage);
+  uint8_t *stage = s_stage + (threadIdx.x >> 5) * kPlaneGroup * max_row_bytes;
+  for (int i = (threadIdx.x >> 5) * kPlaneGroup; i < t.nrows;
+       i += (blockDim.x >> 5) * kPlaneGroup)
+    group_planes<kPlaneGroup>(P.d, P.tr, P.coefs, P.nrhs, P.x_exp, P.xpl, P.kp, P.kc, P.st,
+                              t.row0 + i, min(kPlaneGroup, t.nrows - i), lane, stage);
 }
 
 // 2D log displacement: w[b, r] = dispfac(b) * sum_s nmlz[lev(b), s] * coef
@@ -1334,15 +1475,20 @@ int32_t launch_mixed(vl1_plan *plan, const TreeDev &tree, int64_t nboxes,
   // planes of every density row
   e = cudaMemsetAsync(x_exp, 0, sizeof(int) * nrhs, s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(rhs exponents)");
-  x_exponent_kernel<<<grid_for(nbr * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
-                                                            x_exp);
-  const size_t plane_smem = (size_t)4 * g.kp * kXPlanes * 2;
+  // a few blocks per SM, each warp striding over several rows: one global
+  // atomic per block and rhs
+  // one warp per group of kRowGroup rows
+  const int64_t n_groups = (nbr + kRowGroup - 1) / kRowGroup;
+  x_exponent_kernel<<<grid_for(n_groups * 32, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs,
+                                                                nrhs, x_exp);
+  const size_t plane_smem = (size_t)4 * kPlaneGroup * g.kp * kXPlanes * 2;
   if (plane_smem > 48 * 1024) {
     e = cudaFuncSetAttribute(x_planes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)plane_smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(x_planes_kernel)");
   }
-  x_planes_kernel<<<grid_for(nbr * 32, 128), 128, plane_smem, s>>>(
+  const int64_t n_plane_groups = (nbr + kPlaneGroup - 1) / kPlaneGroup;
+  x_planes_kernel<<<grid_for(n_plane_groups * 32, 128), 128, plane_smem, s>>>(
       d, tree, (int)nboxes, coefs, nrhs, x_exp, xpl, g.kp, g.kc, plan->status);
   if (disp) {
     disp_box_kernel<<<grid_for(nbr, 256), 256, 0, s>>>(d, tree, (int)nboxes, coefs, nrhs,
@@ -1866,7 +2012,7 @@ extern "C" int32_t vl1_batch_eval(vl1_batch *b, void *stream) {
   if (b->n_tasks > 0) {
     x_exponent_batch_kernel<<<b->n_tasks, 256, 0, s>>>(
         static_cast<const PrepProblem *>(b->d_prep), static_cast<const PrepTask *>(b->d_tasks));
-    const size_t plane_smem = (size_t)4 * b->max_row_bytes;
+    const size_t plane_smem = (size_t)4 * kPlaneGroup * b->max_row_bytes;
     if (plane_smem > 48 * 1024) {
       e = cudaFuncSetAttribute(x_planes_batch_kernel,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plane_smem);

@@ -123,7 +123,7 @@ def _build_fast_scalar_arithmetic_orbit_reconstruction(table):
     layout = np.asarray(info["entry_ids"], dtype=np.int64)
     n_orbits = int(np.asarray(md["case_value_offsets"]).size - 1)
     return {
-        "kind": "scalar-arithmetic-orbit",
+        "kind": info.get("kind", "scalar-arithmetic-orbit"),
         "case_orbit_ranks": np.asarray(md["case_orbit_ranks"], dtype=np.uint16),
         "case_axis_perm": np.asarray(md["case_axis_perm"], dtype=np.uint8),
         "case_axis_sign": np.asarray(md["case_axis_sign"], dtype=np.int8),
@@ -166,9 +166,7 @@ def _prepare_table_data_and_entry_map(table_levels):
     dtype = np.dtype(getattr(table0, "dtype", np.float64))
     info = _build_fast_scalar_arithmetic_orbit_reconstruction(table0)
     if info is None:
-        raise NotImplementedError(
-            "only the arithmetic orbit reconstruction has a GB300 kernel; this table "
-            "needs the generated-orbit or dense fallback (list1.py:903-1048)")
+        return _prepare_dense_table_data(table_levels, reduced[0], dtype)
     layout = info["layout_entry_ids"]
     if len(layout) == 0:
         raise RuntimeError("near-field reconstruction layout contains no entries")
@@ -187,6 +185,49 @@ def _prepare_table_data_and_entry_map(table_levels):
         nm[lev] = t.mode_normalizers
         ext[lev] = t.kernel_exterior_normalizers
     return (tdc, nm, ext, np.empty(0, dtype=np.int32), np.empty(0, dtype=dtype), info)
+
+
+def _prepare_dense_table_data(table_levels, reduced, dtype):
+    """The dense fallback (expansion_wrangler_fpnd.py:1887-1990, list1.py:
+    1018-1048) for a kernel without an arithmetic orbit reconstruction: every
+    level's full table, [level][case][source mode][target point], read as is
+    by the device (``VL1_RECON_DENSE``).  A symmetry-reduced table of such a
+    kernel would need the generated-orbit fallback, which is not built."""
+    table0 = table_levels[0]
+    if reduced:
+        raise NotImplementedError(
+            "this kernel has no arithmetic orbit reconstruction and its table is "
+            "symmetry-reduced: the generated-orbit fallback (list1.py:903-1017) is not "
+            "built; store the full table (the dense fallback)")
+    n_full = int(table0.n_cases * table0.n_pairs)
+    for t in table_levels:
+        if t._data is None or np.asarray(t.data).size != n_full:
+            raise RuntimeError("full near-field table has the wrong number of entries")
+        if not np.all(np.isfinite(np.asarray(t.data))):
+            raise RuntimeError("full near-field table contains non-finite entries")
+    tdc = np.stack([np.asarray(t.data, dtype=dtype) for t in table_levels])
+    nm = np.stack([np.asarray(t.mode_normalizers) for t in table_levels])
+    ext = np.stack([np.asarray(t.kernel_exterior_normalizers) for t in table_levels])
+    n_cases, dim = int(table0.n_cases), int(table0.dim)
+    info = {
+        "kind": "dense",
+        # orbit arrays of the plan descriptor, not read for a dense table
+        "case_orbit_ranks": np.zeros(n_cases, dtype=np.uint16),
+        "case_axis_perm": np.zeros((n_cases, dim), dtype=np.uint8),
+        "case_axis_sign": np.zeros((n_cases, dim), dtype=np.int8),
+        "case_axis_group": np.zeros((n_cases, dim), dtype=np.uint8),
+        "case_value_offsets": np.array([0, n_full], dtype=np.int32),
+        "axis_sign_power": np.zeros(dim, dtype=np.uint8),
+        "axis_direction_signs": np.zeros(dim, dtype=np.int8),
+        "direction_sign_axis": -1,
+        "layout_entry_ids": np.arange(n_full, dtype=np.int64),
+        "layout_entry_scales": np.ones(n_full, dtype=np.int8),
+        "n_case_orbits": 1,
+        "metadata_bytes": 0,
+        "compact_value_entry_count": n_full,
+    }
+    ids = np.arange(n_full, dtype=np.int32)
+    return tdc, nm, ext, ids, np.ones(n_full, dtype=dtype), info
 
 
 class FPNDTreeIndependentDataForWrangler:

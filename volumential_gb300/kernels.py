@@ -14,16 +14,22 @@ from __future__ import annotations
 
 import math
 
+import numpy as np
+
 __all__ = [
     "LaplaceKernel", "HelmholtzKernel", "YukawaKernel", "ConstantKernel",
     "AxisTargetDerivative", "AxisSourceDerivative", "RadialPowerKernel",
-    "RadialPowerLogKernel", "base_kernel",
+    "RadialPowerLogKernel", "PlaneWaveKernel", "arithmetic_symmetry", "base_kernel",
     "kernel_class_name", "green_function_constants",
 ]
 
 
 class _Kernel:
     is_complex_valued = False
+    # invariant under the box's axis permutations and reflections (the
+    # arithmetic orbit reconstruction); kernels that are not keep full tables
+    # and the dense reconstruction
+    has_orbit_symmetry = True
 
     def get_base_kernel(self):
         return self
@@ -106,6 +112,22 @@ class RadialPowerLogKernel(_Kernel):
         return f"RadialPowerLogKernel(dim={self.dim}, power={self.power})"
 
 
+class PlaneWaveKernel(_Kernel):
+    """K = cos(k d_0) (scaling constant 1), the plane wave of the reference's
+    manufactured Duffy tests (``test/test_duffy_batched_manufactured.py:
+    219-284``).  It is not invariant under axis permutations, so its tables
+    are full and take the dense reconstruction."""
+
+    has_orbit_symmetry = False
+
+    def __init__(self, dim, plane_wave_k_name="k"):
+        self.dim = int(dim)
+        self.plane_wave_k_name = plane_wave_k_name
+
+    def __repr__(self):
+        return f"PlaneWaveKnl{self.dim}D({self.plane_wave_k_name})"
+
+
 class _Derivative(_Kernel):
     def __init__(self, axis, inner_kernel):
         self.axis = int(axis)
@@ -128,6 +150,41 @@ class AxisTargetDerivative(_Derivative):
 class AxisSourceDerivative(_Derivative):
     def __repr__(self):
         return f"AxisSourceDerivative({self.axis}, {self.inner_kernel!r})"
+
+
+def arithmetic_symmetry(knl, dim):
+    """The arithmetic orbit symmetry of a derivative chain over an
+    orbit-symmetric kernel (``volumential/orbit_arithmetic.py:176-300``):
+    each differentiated axis is fixed (its own axis group) and odd under
+    reflection (sign power XOR 1 per derivative), the other axes form one
+    permutable group.  ``None`` for an undifferentiated kernel (the scalar
+    symmetry); ``False`` when the chain has no arithmetic symmetry."""
+    dim = int(dim)
+    fixed = set()
+    sign_power = np.zeros(dim, dtype=np.uint8)
+    k = knl
+    while k is not None:
+        name = type(k).__name__
+        if name in ("AxisTargetDerivative", "AxisSourceDerivative"):
+            axis = int(k.axis)
+            if not 0 <= axis < dim:
+                return False
+            fixed.add(axis)
+            sign_power[axis] ^= 1
+            k = k.inner_kernel
+            continue
+        if hasattr(k, "inner_kernel"):
+            return False   # other wrappers (directional derivatives) are not built
+        break
+    if not getattr(k, "has_orbit_symmetry", True):
+        return False
+    if not fixed:
+        return None
+    free = tuple(a for a in range(dim) if a not in fixed)
+    groups = tuple((a,) for a in sorted(fixed)) + ((free,) if free else ())
+    return {"axis_groups": groups, "axis_sign_power": sign_power,
+            "axis_direction_signs": np.zeros(dim, dtype=np.int8),
+            "direction_sign_axis": -1}
 
 
 def base_kernel(knl):

@@ -484,9 +484,12 @@ class NearFieldFromCSR(NearFieldEvalBase):
             return _lib.VL1_RECON_SCALAR_ARITH
         if self.reconstruction_kind == "signed-arithmetic-orbit":
             return _lib.VL1_RECON_SIGNED_ARITH
+        if self.reconstruction_kind == "dense":
+            return _lib.VL1_RECON_DENSE
         raise NotImplementedError(
             f"reconstruction kind {self.reconstruction_kind!r} has no GB300 kernel; "
-            "only the arithmetic orbit reconstruction (scalar/signed) is supported")
+            "the arithmetic orbit reconstruction (scalar/signed) and the dense table "
+            "are supported")
 
     def _policy_and_key(self):
         """(parsed policy, cache key), recomputed only when ``extra_kwargs``

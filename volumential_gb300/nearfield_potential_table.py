@@ -192,18 +192,30 @@ class NearFieldInteractionTable:
         return (self.dim, self.quad_order, repr(self.integral_knl))
 
     def _get_scalar_arithmetic_invariant_entry_info(self):
+        """Orbit representatives and arithmetic metadata: the scalar symmetry,
+        or for derivative kernels the signed one (differentiated axes fixed
+        and odd); ``None`` (full table, dense reconstruction) for kernels
+        without an arithmetic symmetry."""
+        from .kernels import arithmetic_symmetry
+
         if self.dim not in (2, 3):
             return None
-        key = ("scalar-arithmetic", self.dim, self.quad_order)
+        sym = (None if self.integral_knl is None
+               else arithmetic_symmetry(self.integral_knl, self.dim))
+        if sym is False:
+            return None   # full table, dense reconstruction
+        sym_key = None if sym is None else (
+            tuple(sym["axis_groups"]), tuple(int(v) for v in sym["axis_sign_power"]))
+        key = ("arithmetic", self.dim, self.quad_order, sym_key)
         hit = _INVARIANT_CACHE.get(key)
         if hit is not None:
             return hit
-        md = build_arithmetic_case_metadata(self)
+        md = build_arithmetic_case_metadata(self, sym)
         if md is None:
             return None
         entry_ids = enumerate_scalar_arithmetic_representatives(self, md)
         info = {
-            "kind": "scalar-arithmetic-orbit",
+            "kind": "scalar-arithmetic-orbit" if sym is None else "signed-arithmetic-orbit",
             "entry_ids": entry_ids,
             "case_indices": (entry_ids // self.n_pairs).astype(np.int32),
             "source_mode_indices": ((entry_ids % self.n_pairs)
@@ -286,7 +298,10 @@ class NearFieldInteractionTable:
         from .plan import stream_handle
         from .table_builder import build_table_values
 
-        name = getattr(self.integral_knl, "helmholtz_k_name", "k")
+        base = self.integral_knl
+        while hasattr(base, "inner_kernel"):
+            base = base.inner_kernel
+        name = getattr(base, "helmholtz_k_name", "k")
         k = kwargs.pop(name, kwargs.pop("k", None))
         kernel = kwargs.pop("kernel", None)
         max_ctas = int(kwargs.pop("max_ctas", 0))

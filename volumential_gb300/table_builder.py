@@ -122,6 +122,20 @@ def entry_geometry(table, entry_ids):
     return np.ascontiguousarray(tp), np.ascontiguousarray(dc), axes
 
 
+def kernel_derivative(knl):
+    """(base kernel, derivative code) of a kernel: 0 for an undifferentiated
+    one, a + 1 for ``AxisTargetDerivative(a, .)``, -(a + 1) for
+    ``AxisSourceDerivative(a, .)`` (first derivatives only)."""
+    name = type(knl).__name__
+    if name in ("AxisTargetDerivative", "AxisSourceDerivative"):
+        inner = knl.inner_kernel
+        if hasattr(inner, "inner_kernel"):
+            raise NotImplementedError("the GPU Duffy builder takes first derivatives only")
+        a = int(knl.axis)
+        return inner, (a + 1) if name == "AxisTargetDerivative" else -(a + 1)
+    return knl, 0
+
+
 def kernel_code(table, kernel=None):
     """(vl1 kernel code, complex) of a table's kernel or of an explicit
     ``kernel`` name ("laplace", "helmholtz", "constant", "plane_wave",
@@ -130,9 +144,12 @@ def kernel_code(table, kernel=None):
         if table.kernel_type == "const":
             kernel = "constant"
         else:
-            name = type(table.integral_knl).__name__ if table.integral_knl is not None else ""
+            base = (kernel_derivative(table.integral_knl)[0]
+                    if table.integral_knl is not None else None)
+            name = type(base).__name__ if base is not None else ""
             kernel = {"LaplaceKernel": "laplace", "HelmholtzKernel": "helmholtz",
-                      "ConstantKernel": "constant", "RadialPowerKernel": "power",
+                      "ConstantKernel": "constant", "PlaneWaveKernel": "plane_wave",
+                      "RadialPowerKernel": "power",
                       "_RadialPowerKernel": "power", "RadialPowerLogKernel": "power_log",
                       "_RadialPowerLogKernel": "power_log"}.get(name)
             if kernel is None:
@@ -172,7 +189,8 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
     if code in (_lib.VL1_DUFFY_HELMHOLTZ2D, _lib.VL1_DUFFY_HELMHOLTZ3D,
                 _lib.VL1_DUFFY_PLANE_WAVE):
         if k is None:
-            name = getattr(table.integral_knl, "helmholtz_k_name", "k")
+            base = kernel_derivative(table.integral_knl)[0]
+            name = getattr(base, "helmholtz_k_name", getattr(base, "plane_wave_k_name", "k"))
             k = table.build_extra_kwargs.get(name)
         if k is None or not np.isfinite(k):
             raise ValueError("a finite wave number k is required for this kernel")
@@ -183,11 +201,16 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
             raise ValueError("the radial power kernels need a power")
     if cplx and not np.issubdtype(np.dtype(table.dtype), np.complexfloating):
         raise TypeError("complex kernel values need a complex table dtype")
+    full = False
     if entry_ids is None:
-        info = table._get_invariant_entry_info()
-        if info is None:
+        if table.dim not in (2, 3):
             raise NotImplementedError("tables of dimension 2 and 3 only")
-        entry_ids = info["entry_ids"]
+        info = table._get_invariant_entry_info()
+        if info is None:   # no orbit symmetry: every entry (a dense table)
+            entry_ids = np.arange(table.n_cases * table.n_pairs, dtype=np.int64)
+            full = True
+        else:
+            entry_ids = info["entry_ids"]
     entry_ids = np.asarray(entry_ids, dtype=np.int64)
     if entry_ids.size and (entry_ids.min() < 0 or entry_ids.max() >= table.n_cases *
                            table.n_pairs):
@@ -210,6 +233,8 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
     d.complex_output = int(cplx)
     d.max_ctas = int(max_ctas)
     d.power = int(power or 0)
+    d.derivative = (kernel_derivative(table.integral_knl)[1]
+                    if table.integral_knl is not None else 0)
     d.extent = float(table.source_box_extent)
     d.k = float(k) if k is not None else 0.0
     d.target_points, d.decomposition_targets = arrs["tp"].data_ptr(), arrs["dc"].data_ptr()
@@ -229,7 +254,12 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
         vals = vals[:, 0] + 1j * vals[:, 1]
     if not np.all(np.isfinite(vals)):
         raise RuntimeError("the Duffy builder produced non-finite table values")
-    if store:
+    if store and full:
+        table.data = vals.astype(table.dtype)
+        table.is_built = True
+        if table.dim == 2:
+            table.build_normalizer_table()
+    elif store:
         table.set_reduced_table_data(entry_ids, vals.astype(table.dtype))
         if table.dim == 2:
             table.build_normalizer_table()
