@@ -95,3 +95,28 @@ def test_oracle_plane_wave_matches_the_closed_form(dim):
     x = tps[0]
     exact = (np.sin(k * (1.0 - x)) - np.sin(-k * x)) / k
     assert np.max(np.abs(vals - exact) / np.maximum(1.0, np.abs(exact))) < 1e-8
+
+
+def test_duffy_order_selection_rule():
+    # nearfield_potential_table.py:2576-2598: errors against the last
+    # candidate, floor = the smallest positive of the (up to three) before
+    # it (at least 128 eps), the first candidate within 8x the floor
+    from volumential_gb300.table_builder import DEFAULT_ORDER_CANDIDATES, select_duffy_orders
+
+    ref = np.array([1.0, -2.0, 0.5])
+    errs = [1e-3, 1e-6, 1e-10, 3e-13, 2e-13, 1e-13, 0.0]
+    vals = [ref + e for e in errs]
+    sel, info = select_duffy_orders(DEFAULT_ORDER_CANDIDATES, vals)
+    assert info["floor_estimate"] == pytest.approx(1e-13, rel=1e-3)
+    assert sel == 3   # 3e-13 <= 8e-13
+    # no tail to estimate from: the floor is 128 eps
+    sel2, info2 = select_duffy_orders([(4, 11), (12, 61)], [ref + 1e-15, ref])
+    assert info2["floor_estimate"] == 128 * np.finfo(float).eps and sel2 == 0
+    # no candidate within the floor: the last one
+    sel3, _ = select_duffy_orders([(4, 11), (12, 61)], [ref + 1e-3, ref])
+    assert sel3 == 1
+    # the floor is relative to the tail: errors 0.875, 0.375, 0.125 against
+    # the last candidate give a floor of 0.125 and accept the first
+    slow = [ref + e for e in (1.0, 0.5, 0.25, 0.125)]
+    sel4, info4 = select_duffy_orders([(4, 11), (6, 21), (8, 31), (12, 61)], slow)
+    assert info4["floor_estimate"] == 0.125 and sel4 == 0

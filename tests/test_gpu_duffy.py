@@ -141,3 +141,22 @@ def test_table_manager_builds_on_a_miss_and_reloads(cuda, tmp_path):
     tp, _, axes = TB.entry_geometry(t, ids[:6])
     ref = DO.entry_values(2, 2, 0.5, "laplace", tp, axes, 6, 21)
     assert np.max(np.abs(vals[:6] - ref) / np.abs(ref)) <= 1e-12
+
+
+def test_auto_tuned_orders_build_the_same_table_as_the_chosen_orders(cuda):
+    # nearfield_potential_table.py:2465-2619 (auto_tune_orders / "auto" orders)
+    from volumential_gb300.table_builder import DuffyBuildConfig
+
+    t = _table(2, 2, "laplace", extent=0.5)
+    t.build_table_via_duffy_radial(regular_quad_order="auto", radial_quad_order="auto")
+    info = t.last_duffy_order_selection
+    reg, rad = info["selected_regular_quad_order"], info["selected_radial_quad_order"]
+    assert (reg, rad) in info["candidates"] and len(info["sample_entry_ids"]) == 5
+    sel = info["candidates"].index((reg, rad))
+    assert info["relative_errors_vs_best"][sel] <= info["acceptance_threshold"]
+    ref = _table(2, 2, "laplace", extent=0.5)
+    ref.build_table_via_duffy_radial(build_config=DuffyBuildConfig(
+        regular_quad_order=reg, radial_quad_order=rad))
+    a = t.get_reduced_table_data()
+    b = ref.get_reduced_table_data()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])

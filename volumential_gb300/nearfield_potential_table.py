@@ -288,16 +288,32 @@ class NearFieldInteractionTable:
 
     def build_table_via_duffy_radial(self, radial_rule="tanh-sinh-fast",
                                      regular_quad_order=20, radial_quad_order=61,
-                                     mp_dps=50, queue=None, **kwargs):
+                                     mp_dps=50, queue=None, cl_ctx=None, build_config=None,
+                                     auto_tune_orders=False, auto_tune_samples=5,
+                                     auto_tune_floor_factor=8.0, auto_tune_candidates=None,
+                                     **kwargs):
         """Fill the table's orbit-invariant entries by Duffy radial quadrature
         in FP64 on the GPU (``nearfield_potential_table.py:2948-3195``; the
         fixed tanh-sinh rules of its batched path).  ``queue``: an optional
         ``torch.cuda.Stream``.  A Helmholtz kernel's wave number is passed by
         its argument name (``k`` by default).  ``max_ctas`` > 0 caps the
-        builder's grid."""
+        builder's grid.  Orders ``"auto"`` / ``None``, ``auto_tune_orders``
+        or a ``DuffyBuildConfig`` asking for it choose the orders by
+        convergence on sample entries (``:2465-2619``; the choice is kept in
+        ``last_duffy_order_selection``)."""
         from .plan import stream_handle
+        from .table_builder import DuffyBuildConfig, autotune_duffy_orders, is_auto_order
         from .table_builder import build_table_values
 
+        if build_config is None:
+            build_config = DuffyBuildConfig(
+                radial_rule=radial_rule, regular_quad_order=regular_quad_order,
+                radial_quad_order=radial_quad_order, mp_dps=mp_dps,
+                auto_tune_orders=auto_tune_orders, auto_tune_samples=auto_tune_samples,
+                auto_tune_floor_factor=auto_tune_floor_factor,
+                auto_tune_candidates=auto_tune_candidates)
+        elif not isinstance(build_config, DuffyBuildConfig):
+            raise TypeError("build_config must be a DuffyBuildConfig")
         base = self.integral_knl
         while hasattr(base, "inner_kernel"):
             base = base.inner_kernel
@@ -307,10 +323,23 @@ class NearFieldInteractionTable:
         max_ctas = int(kwargs.pop("max_ctas", 0))
         if kwargs:
             raise TypeError(f"unexpected keyword arguments {sorted(kwargs)}")
-        build_table_values(self, radial_rule_name=radial_rule,
-                           regular_quad_order=regular_quad_order,
-                           radial_quad_order=radial_quad_order, mp_dps=mp_dps, kernel=kernel,
-                           k=k, stream=stream_handle(queue), max_ctas=max_ctas)
+        sh = stream_handle(queue)
+        reg, rad = build_config.regular_quad_order, build_config.radial_quad_order
+        if (build_config.auto_tune_orders or is_auto_order(reg) or is_auto_order(rad)):
+            reg, rad, info = autotune_duffy_orders(
+                self, radial_rule=build_config.radial_rule, mp_dps=build_config.mp_dps,
+                sample_count=build_config.auto_tune_samples,
+                candidates=build_config.auto_tune_candidates,
+                floor_factor=build_config.auto_tune_floor_factor, kernel=kernel, k=k,
+                stream=sh)
+            self.last_duffy_order_selection = info
+        self.build_config = DuffyBuildConfig(
+            radial_rule=build_config.radial_rule, regular_quad_order=int(reg),
+            radial_quad_order=int(rad), mp_dps=build_config.mp_dps)
+        build_table_values(self, radial_rule_name=build_config.radial_rule,
+                           regular_quad_order=int(reg), radial_quad_order=int(rad),
+                           mp_dps=build_config.mp_dps, kernel=kernel, k=k, stream=sh,
+                           max_ctas=max_ctas)
 
     def build_table(self, cl_ctx=None, queue=None, build_config=None, **kwargs):
         """``nearfield_potential_table.py:3200``: the constant kernel's closed
@@ -319,6 +348,6 @@ class NearFieldInteractionTable:
         if self.kernel_type == "const" or name == "ConstantKernel":
             self.build_constant_table()
             return
-        self.build_table_via_duffy_radial(queue=queue, **kwargs)
+        self.build_table_via_duffy_radial(queue=queue, build_config=build_config, **kwargs)
 
     # }}}

@@ -26,6 +26,7 @@ Green's functions): Laplace 2D -log(r)/(2 pi), 3D 1/(4 pi r); Helmholtz 2D
 from __future__ import annotations
 
 import ctypes as C
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -33,7 +34,8 @@ from . import _lib
 
 __all__ = ["tanh_sinh_fast_rule", "radial_rule", "gauss_legendre_unit", "regular_rule",
            "lagrange_product_weights", "entry_geometry", "kernel_code",
-           "build_table_values", "DEFAULT_ORDERS"]
+           "build_table_values", "DEFAULT_ORDERS", "DuffyBuildConfig", "DEFAULT_ORDER_CANDIDATES",
+           "is_auto_order", "select_duffy_orders", "autotune_duffy_orders"]
 
 #: the reference's defaults (``nearfield_potential_table.py:2948-2953``)
 DEFAULT_ORDERS = {"regular_quad_order": 20, "radial_quad_order": 61}
@@ -264,3 +266,99 @@ def build_table_values(table, *, radial_rule_name="tanh-sinh-fast", regular_quad
         if table.dim == 2:
             table.build_normalizer_table()
     return entry_ids, vals
+
+
+# {{{ Duffy order selection (nearfield_potential_table.py:195-206, 2301-2326, 2465-2619)
+
+@dataclass(frozen=True)
+class DuffyBuildConfig:
+    """Build settings of a Duffy table (the reference's dataclass of the same
+    name): orders may be ``"auto"`` / ``None``, or ``auto_tune_orders`` set,
+    to choose them by convergence on sample entries."""
+    radial_rule: str = "tanh-sinh-fast"
+    regular_quad_order: object = 20
+    radial_quad_order: object = 61
+    mp_dps: int = 50
+    auto_tune_orders: bool = False
+    auto_tune_samples: int = 5
+    auto_tune_floor_factor: float = 8.0
+    auto_tune_candidates: object = None
+
+
+#: (regular, radial) candidates of dimensions 2 and 3, in increasing cost
+DEFAULT_ORDER_CANDIDATES = ((4, 11), (4, 21), (6, 21), (6, 31), (8, 31), (10, 41), (12, 61))
+
+
+def is_auto_order(value):
+    return value is None or (isinstance(value, str) and value.strip().lower() == "auto")
+
+
+def select_duffy_orders(candidates, candidate_values, floor_factor=8.0):
+    """Index of the cheapest candidate within the convergence floor, and the
+    diagnostics.  Errors are taken against the last (most accurate)
+    candidate, relative to max(1, |reference|) per entry; the floor is the
+    smallest positive error among the (up to three) candidates before the
+    last, at least 128 eps; a candidate is accepted within ``floor_factor``
+    times the floor (nearfield_potential_table.py:2576-2598)."""
+    ref = np.asarray(candidate_values[-1])
+    denom = np.maximum(1.0, np.abs(ref))
+    errs = [float(np.max(np.abs(np.asarray(v) - ref) / denom)) if ref.size else 0.0
+            for v in candidate_values]
+    floor = 0.0
+    if len(errs) > 2:
+        tail = np.asarray(errs[max(0, len(errs) - 4):-1], dtype=np.float64)
+        pos = tail[tail > 0]
+        if pos.size >= 2:
+            floor = float(np.min(pos))
+    floor = max(floor, 128.0 * np.finfo(np.float64).eps)
+    threshold = float(floor_factor) * floor
+    sel = len(candidates) - 1
+    for i, e in enumerate(errs):
+        if e <= threshold:
+            sel = i
+            break
+    return sel, {"relative_errors_vs_best": errs, "floor_estimate": floor,
+                 "acceptance_threshold": threshold}
+
+
+def autotune_duffy_orders(table, *, radial_rule="tanh-sinh-fast", mp_dps=50, sample_count=5,
+                          candidates=None, floor_factor=8.0, kernel=None, k=None,
+                          stream=None):
+    """Choose (regular, radial) orders for ``table``: its sample entries
+    (evenly spaced over the entries to build) evaluated on the GPU at every
+    candidate, the first within the convergence floor kept.  Returns
+    (regular, radial, info)."""
+    if radial_rule == "adaptive":
+        raise ValueError("Duffy order auto-tuning is only available for fixed radial rules")
+    cands = [tuple(int(x) for x in pair)
+             for pair in (DEFAULT_ORDER_CANDIDATES if candidates is None else candidates)]
+    if not cands:
+        raise ValueError("Duffy order auto-tuning candidate list cannot be empty")
+    info = table._get_invariant_entry_info()
+    ids = (np.asarray(info["entry_ids"], dtype=np.int64) if info is not None
+           else np.arange(table.n_cases * table.n_pairs, dtype=np.int64))
+    if ids.size == 0:
+        sample = ids
+    elif int(sample_count) >= ids.size:
+        sample = ids
+    else:
+        sample = ids[np.unique(np.linspace(0, ids.size - 1, num=max(1, int(sample_count)),
+                                           dtype=np.int64))]
+    values = []
+    for reg, rad in cands:
+        if sample.size:
+            _, v = build_table_values(table, radial_rule_name=radial_rule,
+                                      regular_quad_order=reg, radial_quad_order=rad,
+                                      mp_dps=mp_dps, kernel=kernel, k=k, entry_ids=sample,
+                                      stream=stream, store=False)
+        else:
+            v = np.zeros(0)
+        values.append(v)
+    sel, diag = select_duffy_orders(cands, values, floor_factor)
+    out = {"auto_tuned": True, "selected_regular_quad_order": cands[sel][0],
+           "selected_radial_quad_order": cands[sel][1],
+           "sample_entry_ids": [int(e) for e in sample], "candidates": cands}
+    out.update(diag)
+    return cands[sel][0], cands[sel][1], out
+
+# }}}
