@@ -62,19 +62,20 @@ __device__ __forceinline__ unsigned long long fixed_magnitude(double v, int e) {
   const int ev = ef ? ef - 1075 : -1074;
   const long long sh = (long long)ev + BITS - (long long)e;
   unsigned long long m;
-  if (M == 0) {
-    m = 0;
-  } else if (sh >= 0) {
-    // saturates when |v| is not below 2^e (m >= 2^BITS after the shift)
-    m = (sh > BITS || M >= (1ull << (BITS - sh))) ? (1ull << BITS) : (M << sh);
-  } else if (sh < -63) {
-    m = 0;
+  if (sh < 0) {
+    // the usual case (|v| < 2^e leaves at least 14 bits to drop): M / 2^k
+    // rounded to nearest, ties to even, as (M + 2^(k-1) - 1 + lsb) >> k
+    if (sh < -63) {
+      m = 0;
+    } else {
+      const int k = (int)-sh;
+      const unsigned long long half = 1ull << (k - 1);
+      m = (M + (half - 1ull) + ((M >> k) & 1ull)) >> k;
+    }
   } else {
-    const int k = (int)-sh;
-    const unsigned long long q = M >> k;
-    const unsigned long long rem = M & ((1ull << k) - 1ull);
-    const unsigned long long half = 1ull << (k - 1);
-    m = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+    // saturates when |v| is not below 2^e (m >= 2^BITS after the shift)
+    m = M == 0 ? 0
+               : ((sh > BITS || M >= (1ull << (BITS - sh))) ? (1ull << BITS) : (M << sh));
   }
   if (m >= (1ull << BITS)) m = (1ull << BITS) - 1;  // v at the scale bound
   return m;
@@ -333,6 +334,7 @@ __device__ __forceinline__ void group_planes(const DevDesc &d, const TreeDev &tr
                                              __half *xpl, int kp, int kc, vl1_status *st,
                                              int64_t r0, int n, int lane, uint8_t *stage) {
   const int row_bytes = kp * kXPlanes * 2;
+  const int kc_shift = 31 - __clz(kc);
   const RowGroup g = load_row_group(d, tr, nrhs, r0, n, lane, st);
   int ex = 0;
   double sc = 0.0;
@@ -377,8 +379,9 @@ __device__ __forceinline__ void group_planes(const DevDesc &d, const TreeDev &tr
       }
       int dig[kDigits];
       fixed_digits(scu[u] * v[u], eu[u], dig);
+      // kc is 16 or 32: chunk and column by shift and mask
       __half *hv = reinterpret_cast<__half *>(stage + u * row_bytes) +
-                   (m[u] / kc) * kXPlanes * kc + (m[u] % kc);
+                   ((m[u] >> kc_shift) * kXPlanes << kc_shift) + (m[u] & (kc - 1));
       hv[0] = __int2half_rn(dig[0]);
       hv[kc] = __int2half_rn(dig[1]);
       hv[2 * kc] = __int2half_rn(dig[2]);
