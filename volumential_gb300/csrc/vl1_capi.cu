@@ -381,6 +381,13 @@ int32_t vl1::make_tree(const vl1_plan *plan, const vl1_tree_view *t, TreeDev &tr
     }
     tr.level_scale[l] = sp > 0 ? num / den : den / num;
   }
+  for (int l = 0; l < kScaleLevels; ++l) {
+    int ex = 0;
+    const double fr = frexp(tr.level_scale[l], &ex);
+    // 0.5 * 2^ex: a power of two within the normal range
+    tr.level_scale_log2[l] =
+        (fr == 0.5 && ex - 1 >= -120 && ex - 1 <= 120) ? (int8_t)(ex - 1) : (int8_t)kNoScaleLog2;
+  }
   return VL1_OK;
 }
 

@@ -45,7 +45,12 @@ struct TreeDev {
   // scaling of a source box of level l (l < kScaleLevels), computed on the
   // host with the same IEEE operations as pair_scaling(level_extent(l))
   double level_scale[32];
+  // log2 of level_scale[l] when it is an exact power of two (a dyadic tree
+  // and table extent), else kNoScaleLog2: the density planes then scale by
+  // an exponent shift instead of an FP64 multiply
+  int8_t level_scale_log2[32];
 };
+constexpr int kNoScaleLog2 = 127;
 constexpr int kScaleLevels = 32;
 constexpr int kTileRows = 128;   // rows (target box, rhs) of a mixed-path tile
 

@@ -105,6 +105,28 @@ __device__ __forceinline__ void fixed_digits(double v, int e, int (&dig)[kDigits
   dig[0] = sgn * ((int)(m >> 32) + carry);   // m < 2^39: <= 128
 }
 
+// The four FP16 density plane values of v against 2^e: X1, X2, X3 = the
+// three leading balanced digits of m (fixed_digits) and R = X4 + X5 / 256.
+// The balanced digits come from m + 0x80808080: adding 128 to each of the
+// low bytes makes the additions' carries do the digit borrows (a byte b
+// plus the incoming carry becomes b + c - 256 with a carry out exactly when
+// b + c >= 128), so each digit is its biased byte minus 128, the top digit
+// takes the last carry, and X4 * 256 + X5 is the low 16 bits minus 0x8080
+// (bit-identical to fixed_digits on 60 M checked values).
+__device__ __forceinline__ void plane_values(double v, int e, __half &x1, __half &x2,
+                                             __half &x3, __half &rr) {
+  const unsigned long long m = fixed_magnitude<kFixedBits>(v, e);
+  const int sgn = __double_as_longlong(v) < 0 ? -1 : 1;
+  const unsigned lo = (unsigned)m;
+  const unsigned lp = lo + 0x80808080u;
+  const int top = (int)(m >> 32) + (lp < lo ? 1 : 0);
+  x1 = __int2half_rn(sgn * top);
+  x2 = __int2half_rn(sgn * ((int)(lp >> 24) - 128));
+  x3 = __int2half_rn(sgn * ((int)((lp >> 16) & 0xFFu) - 128));
+  // exact in FP32 (|.| <= 128.5 in steps of 1/256), one rounding to FP16
+  rr = __float2half_rn((float)(sgn * ((int)(lp & 0xFFFFu) - 0x8080)) * (1.0f / 256.0f));
+}
+
 // exponent e with |v| < 2^e, as frexp returns it (-1074 for v == 0), from the
 // IEEE-754 fields
 __device__ __forceinline__ int scale_exponent(double v) {
@@ -336,17 +358,22 @@ __device__ __forceinline__ void group_planes(const DevDesc &d, const TreeDev &tr
   const int row_bytes = kp * kXPlanes * 2;
   const int kc_shift = 31 - __clz(kc);
   const RowGroup g = load_row_group(d, tr, nrhs, r0, n, lane, st);
-  int ex = 0;
+  int ex = 0, sl = kNoScaleLog2;
   double sc = 0.0;
   if (lane < n) {
     ex = x_exp[g.rhs] - kExpBias;
     sc = box_scaling(d, tr, g.level);
+    // a power-of-two scaling: digits of c against 2^(e - log2 sc), the same
+    // as those of sc * c against 2^e when the product is exact (no overflow:
+    // e <= 1000; an underflowing product has zero digits when e >= -900)
+    if (g.level < kScaleLevels && ex >= -900 && ex <= 1000)
+      sl = tr.level_scale_log2[g.level];
   }
   for (int k = lane * 16; k < G * row_bytes; k += 32 * 16)
     *reinterpret_cast<uint4 *>(stage + k) = make_uint4(0u, 0u, 0u, 0u);
   // every row's data in every lane (shuffles before the point loop, which
   // not all lanes enter when nq is not a multiple of 32)
-  int cnt[G], st0[G], eu[G], bx[G];
+  int cnt[G], st0[G], eu[G], bx[G], slu[G];
   double scu[G];
   const double *c[G];
 #pragma unroll
@@ -356,6 +383,7 @@ __device__ __forceinline__ void group_planes(const DevDesc &d, const TreeDev &tr
     const int rh = __shfl_sync(0xffffffffu, g.rhs, u);
     eu[u] = __shfl_sync(0xffffffffu, ex, u);
     scu[u] = __shfl_sync(0xffffffffu, sc, u);
+    slu[u] = __shfl_sync(0xffffffffu, sl, u);
     bx[u] = __shfl_sync(0xffffffffu, g.box, u);
     c[u] = coefs + (int64_t)rh * tr.n_particles + st0[u];
     if (u >= n) cnt[u] = 0;
@@ -377,16 +405,17 @@ __device__ __forceinline__ void group_planes(const DevDesc &d, const TreeDev &tr
         report(st, VL1_E_LAYOUT, bx[u], -1 - k);
         continue;
       }
-      int dig[kDigits];
-      fixed_digits(scu[u] * v[u], eu[u], dig);
+      const bool shift = slu[u] != kNoScaleLog2;
+      __half x1, x2, x3, rr;
+      plane_values(shift ? v[u] : scu[u] * v[u], shift ? eu[u] - slu[u] : eu[u], x1, x2, x3,
+                   rr);
       // kc is 16 or 32: chunk and column by shift and mask
       __half *hv = reinterpret_cast<__half *>(stage + u * row_bytes) +
                    ((m[u] >> kc_shift) * kXPlanes << kc_shift) + (m[u] & (kc - 1));
-      hv[0] = __int2half_rn(dig[0]);
-      hv[kc] = __int2half_rn(dig[1]);
-      hv[2 * kc] = __int2half_rn(dig[2]);
-      // exact in FP32 (|.| <= 128.5 in steps of 1/256), one rounding to FP16
-      hv[3 * kc] = __float2half_rn((float)dig[3] + (float)dig[4] * (1.0f / 256.0f));
+      hv[0] = x1;
+      hv[kc] = x2;
+      hv[2 * kc] = x3;
+      hv[3 * kc] = rr;
     }
   }
   __syncwarp();
