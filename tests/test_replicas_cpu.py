@@ -41,7 +41,9 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_ranks_report_the_slowest_rank():
     world, port = 2, _free_port()
-    with mp.Manager() as m:
+    # the shared dict's server process is spawned too (no fork of a
+    # multi-threaded test process)
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
