@@ -267,3 +267,23 @@ def test_fast_reconstruction_info_shape():
     assert info["compact_value_entry_count"] == 1084
     assert rel_l2(t.get_entry_data_for_full_indices(info["layout_entry_ids"]),
                   t.mode_weights()[info["layout_entry_ids"] % 256 // 16]) == 0.0
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_derivative_kernel_tables_take_the_reference_signed_descriptors(dim):
+    # the symmetry derived from AxisTargetDerivative(0, Laplace) (orbit_arithmetic.py:
+    # 176-300) gives the signed descriptors and representatives that the
+    # reference's own module produced for that kernel
+    from volumential_gb300.kernels import AxisTargetDerivative, LaplaceKernel
+    from volumential_gb300.nearfield_potential_table import NearFieldInteractionTable
+
+    fx = np.load(os.path.join(GOLDEN, f"orbit_signed_d{dim}_q3.npz"))
+    knl = AxisTargetDerivative(0, LaplaceKernel(dim))
+    t = NearFieldInteractionTable(3, dim=dim, sumpy_kernel=knl)
+    info = t._get_invariant_entry_info()
+    assert info["kind"] == "signed-arithmetic-orbit"
+    md = info["arithmetic_metadata"]
+    for key in ("case_orbit_ranks", "case_axis_perm", "case_axis_sign", "case_axis_group",
+                "case_value_offsets", "axis_sign_power", "axis_direction_signs"):
+        assert np.array_equal(np.asarray(md[key]), fx[key]), key
+    assert np.array_equal(info["entry_ids"], fx["representatives"])
