@@ -120,3 +120,20 @@ def test_duffy_order_selection_rule():
     slow = [ref + e for e in (1.0, 0.5, 0.25, 0.125)]
     sel4, info4 = select_duffy_orders([(4, 11), (6, 21), (8, 31), (12, 61)], slow)
     assert info4["floor_estimate"] == 0.125 and sel4 == 0
+
+
+def test_duffy_build_config_defaults():
+    # nearfield_potential_table.py:195-206 and :2301-2308
+    from volumential_gb300.table_builder import (
+        DEFAULT_ORDER_CANDIDATES,
+        DuffyBuildConfig,
+        is_auto_order,
+    )
+
+    c = DuffyBuildConfig()
+    assert (c.radial_rule, c.regular_quad_order, c.radial_quad_order, c.mp_dps) == (
+        "tanh-sinh-fast", 20, 61, 50)
+    assert (c.auto_tune_orders, c.auto_tune_samples, c.auto_tune_floor_factor,
+            c.auto_tune_candidates) == (False, 5, 8.0, None)
+    assert DEFAULT_ORDER_CANDIDATES[0] == (4, 11) and DEFAULT_ORDER_CANDIDATES[-1] == (12, 61)
+    assert is_auto_order(None) and is_auto_order(" Auto ") and not is_auto_order(20)
