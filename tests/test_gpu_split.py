@@ -204,3 +204,36 @@ def test_split_order_two_tracks_the_helmholtz_table_closer(cuda):
     print("split order 1 / 2 vs Helmholtz table:", errs)
     assert errs[2] <= 0.1 * errs[1] and errs[2] <= 1e-5, errs
     torch.cuda.synchronize()
+
+
+def test_table_beta_mode_matches_the_point_sum(cuda):
+    # helmholtz_split_auto_config["power_log_single_table_beta_mode"]:
+    # "table" integrates the log(h/h0) r^2 part with an r^2 table instead of
+    # the point sum ("p2p"); both approximate the same integral
+    import torch
+
+    k = 20.0
+    w = W.uniform_workload("beta", 2, 4, 4, seed=94, kernel=HelmholtzKernel(2))
+    tree, trav = w.tree, w.traversal
+    lap = NearFieldInteractionTable(4, dim=2, sumpy_kernel=LaplaceKernel(2),
+                                    source_box_extent=tree.root_extent)
+    lap.build_table(regular_quad_order=8, radial_quad_order=31)
+    dens = w.coefs[0]
+    weights = dens * tree.weights
+    ti = FPNDTreeIndependentDataForWrangler(target_kernels=[HelmholtzKernel(2)])
+    out = {}
+    for mode in ("p2p", "table"):
+        wr = FPNDExpansionWrangler(ti, trav, [lap], dtype=np.complex128, quad_order=4,
+                                   kernel_extra_kwargs={"k": k}, helmholtz_split_order=2,
+                                   helmholtz_split_auto_config={
+                                       "power_log_single_table_beta_mode": mode})
+        corr, _ = wr.eval_direct_helmholtz_split_correction(
+            trav.target_boxes, trav.neighbor_source_boxes_starts,
+            trav.neighbor_source_boxes_lists, torch.from_numpy(weights).to("cuda"),
+            src_func=torch.from_numpy(dens).to("cuda"))
+        out[mode] = corr[0].cpu().numpy()
+        if mode == "table":
+            assert ("power", 2) in wr.helmholtz_split_term_tables
+    err = rel_l2(out["table"], out["p2p"])
+    print("beta table vs p2p:", err)
+    assert np.all(np.isfinite(out["table"])) and err <= 1e-6

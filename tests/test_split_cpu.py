@@ -104,3 +104,64 @@ def test_log_alpha_per_source_follows_the_boxes():
                        tree.box_source_counts_nonchild, tree.root_extent, 0.25)
     assert np.array_equal(got, ref)
     assert len(np.unique(got)) > 1
+
+
+def test_automatic_split_order_planner():
+    # expansion_wrangler_fpnd.py:385-405, 4252-4323
+    from volumential_gb300.helmholtz_split import (
+        choose_auto_split_order,
+        select_split_order_from_rho,
+    )
+
+    assert select_split_order_from_rho(0.1, (0.5, 1.5, 3.0), (2, 3, 4, 5)) == 2
+    assert select_split_order_from_rho(1.5, (0.5, 1.5, 3.0), (2, 3, 4, 5)) == 3
+    assert select_split_order_from_rho(9.0, (0.5, 1.5, 3.0), (2, 3, 4, 5)) == 5
+    with pytest.raises(ValueError):
+        select_split_order_from_rho(1.0, (0.5,), (2, 3, 4))
+    # geometric ladders: real 0.25 * 2^j, imaginary 0.5 * 2^j over orders 2..12
+    order, info = choose_auto_split_order({}, 0.3, 0.0)
+    assert order == 3 and info["orders"] == tuple(range(2, 13))
+    order, _ = choose_auto_split_order({}, 0.3, 1.9)
+    assert order == 4   # the imaginary part asks for more
+    order, info = choose_auto_split_order({}, 1e3, 0.0)
+    assert order == 12 and info["beyond_coverage"]
+    order, _ = choose_auto_split_order({"rho_thresholds": (0.5, 1.5, 3.0)}, 1.0, 0.0)
+    assert order == 3
+    order, _ = choose_auto_split_order({"orders": (1, 2), "rho_thresholds": (0.7,)}, 0.5, 0.0)
+    assert order == 1
+
+
+def test_wrangler_chooses_the_split_order_from_rho():
+    from volumential_gb300 import workloads as W
+    from volumential_gb300.expansion_wrangler_fpnd import (
+        FPNDExpansionWrangler,
+        FPNDTreeIndependentDataForWrangler,
+    )
+    from volumential_gb300.helmholtz_split import split_rho_components
+    from volumential_gb300.kernels import HelmholtzKernel, LaplaceKernel
+    from volumential_gb300.nearfield_potential_table import NearFieldInteractionTable
+
+    w = W.uniform_workload("auto", 2, 3, 3, kernel=HelmholtzKernel(2))
+    lap = NearFieldInteractionTable(3, dim=2, sumpy_kernel=LaplaceKernel(2),
+                                    source_box_extent=w.tree.root_extent)
+    ti = FPNDTreeIndependentDataForWrangler(target_kernels=[HelmholtzKernel(2)])
+    wr = FPNDExpansionWrangler(ti, w.traversal, [lap], dtype=np.complex128, quad_order=3,
+                               kernel_extra_kwargs={"k": 20.0}, helmholtz_split_order="auto")
+    rho_r, rho_i = split_rho_components(w.tree, [20.0])
+    assert rho_r == 20.0 * w.tree.root_extent / 8 and rho_i == 0.0
+    assert wr.helmholtz_split_order == wr.helmholtz_split_auto_selection["order"]
+    # rho 2.5: thresholds 0.25, 0.5, 1, 2, 4, ...: the fifth (4) is the first
+    # not exceeded, order 2 + 4
+    assert wr.helmholtz_split_order == 6
+    # several output kernels: clamped to order 1, as the reference does
+    ti2 = FPNDTreeIndependentDataForWrangler(
+        target_kernels=[HelmholtzKernel(2), HelmholtzKernel(2, helmholtz_k_name="k2")])
+    wr2 = FPNDExpansionWrangler(ti2, w.traversal, [lap], dtype=np.complex128, quad_order=3,
+                                kernel_extra_kwargs={"k": 20.0, "k2": 5.0},
+                                helmholtz_split_order=3)
+    assert wr2.helmholtz_split_order == 1
+    with pytest.raises(ValueError):
+        FPNDExpansionWrangler(ti, w.traversal, [lap], dtype=np.complex128, quad_order=3,
+                              kernel_extra_kwargs={"k": 20.0},
+                              helmholtz_split_auto_config={
+                                  "power_log_single_table_beta_mode": "other"})

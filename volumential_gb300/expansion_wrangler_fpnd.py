@@ -272,7 +272,8 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                  helmholtz_split=None, helmholtz_split_order=1,
                  helmholtz_split_smooth_quad_order=None,
                  helmholtz_split_order1_legacy_subtraction=False,
-                 helmholtz_split_term_tables=None, **kwargs):
+                 helmholtz_split_term_tables=None, helmholtz_split_auto_config=None,
+                 **kwargs):
         self.tree_indep = tree_indep
         self.traversal = traversal
         self.tree = traversal.tree
@@ -303,7 +304,7 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
         self._init_helmholtz_split(helmholtz_split, helmholtz_split_order,
                                    helmholtz_split_smooth_quad_order,
                                    helmholtz_split_order1_legacy_subtraction,
-                                   helmholtz_split_term_tables)
+                                   helmholtz_split_term_tables, helmholtz_split_auto_config)
         self._payload_cache = collections.OrderedDict()
         self._payload_cache_max = 16
         self._view_cache = collections.OrderedDict()
@@ -323,7 +324,10 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                     return False, f"the near-field table of {kn} is not Laplace-backed"
         return True, ""
 
-    def _init_helmholtz_split(self, split, order, smooth_quad_order, legacy, term_tables):
+    def _init_helmholtz_split(self, split, order, smooth_quad_order, legacy, term_tables,
+                              auto_config=None):
+        from .helmholtz_split import choose_auto_split_order, split_rho_components
+
         ok, reason = self._split_support()
         if split is None:
             split = ok
@@ -332,7 +336,34 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                 "helmholtz_split requires Helmholtz target kernels and Laplace-backed "
                 f"near-field tables; {reason}")
         self.helmholtz_split = bool(split)
-        self.helmholtz_split_order = int(order) if split else order
+        self._helmholtz_split_auto_config = dict(auto_config or {})
+        self.helmholtz_split_auto_selection = None
+        beta_mode = str(self._helmholtz_split_auto_config.get(
+            "power_log_single_table_beta_mode", "p2p")).strip().lower()
+        if beta_mode not in ("p2p", "table"):
+            raise ValueError("power_log_single_table_beta_mode must be 'table' or 'p2p'")
+        self._helmholtz_split_beta_mode = beta_mode
+        auto = bool(self._helmholtz_split_auto_config.get("enabled", False)) or (
+            isinstance(order, str) and order.strip().lower() == "auto")
+        if self.helmholtz_split and auto:
+            # expansion_wrangler_fpnd.py:2521-2575, 4252-4323: the order from
+            # rho = |k| h_max of the coarsest box holding sources
+            rho_r, rho_i = split_rho_components(
+                self.tree, [self._split_wave_number(k) for k in self.tree_indep.target_kernels])
+            order, info = choose_auto_split_order(self._helmholtz_split_auto_config, rho_r, rho_i)
+            self.helmholtz_split_auto_selection = dict(info, order=order)
+            if info["beyond_coverage"]:
+                logger.warning("rho_max=%.3g exceeds the planner's threshold coverage; "
+                               "split order clamped to %d", max(rho_r, rho_i), order)
+        elif isinstance(order, str) and not auto:
+            raise ValueError(f"helmholtz_split_order must be an integer or 'auto', got {order!r}")
+        if self.helmholtz_split and int(order) > 1 and len(self.tree_indep.target_kernels) > 1:
+            # the reference clamps to order 1 for several output kernels
+            logger.warning("split order %d requested with %d target kernels; clamping to "
+                           "order 1 for multi-output split mode", int(order),
+                           len(self.tree_indep.target_kernels))
+            order = 1
+        self.helmholtz_split_order = int(order) if split else 1
         # extra term tables of split orders > 1, keyed ("power_log", 2n) in
         # 2D and ("power", 2j - 1) in 3D (expansion_wrangler_fpnd.py:2603-2647)
         self.helmholtz_split_term_tables = {}
@@ -345,10 +376,7 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
                     list(tabs) if isinstance(tabs, (list, tuple)) else [tabs])
         if self.helmholtz_split:
             if int(order) < 1:
-                raise ValueError("split_order must be >= 1")
-            if int(order) > 1 and len(self.tree_indep.target_kernels) > 1:
-                raise NotImplementedError(
-                    "multi-output split correction currently supports split_order=1")
+                raise ValueError("helmholtz_split_order must be >= 1")
             if smooth_quad_order is not None:
                 raise NotImplementedError("helmholtz_split_smooth_quad_order (resampled "
                                           "remainder sources) is not built")
@@ -397,36 +425,28 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
         self.helmholtz_split_term_tables[key] = tabs
         return tabs
 
-    def _split_term_contribution(self, out_kernel, key, tabs, target_boxes, starts, lists,
-                                 src_func, w, view, pts):
-        """One term's list-1 contribution (expansion_wrangler_fpnd.py:
-        3678-3806, 4835-4907): the term table's near field (a single table
-        scaled by (h/h0)^(dim + power), or one table per level), plus for a
-        single r^{2n} log r table the point-to-point sum of r^{2n} with
-        strengths x log(h/h0)."""
+    def _split_term_table_field(self, key, tabs, target_boxes, starts, lists, coefs):
+        """The list-1 field of one term's table(s) for densities ``coefs``
+        (expansion_wrangler_fpnd.py:4835-4907): a single table scaled by
+        (h/h0)^(dim + power) without displacement, or one table per level;
+        complex densities as real and imaginary parts."""
         import torch
 
-        from .helmholtz_split import (
-            log_alpha_per_source,
-            radial_power_sum,
-            term_kernel,
-            term_scaling_code,
-        )
-        from .plan import as_device_tensor, stream_handle
+        from .helmholtz_split import term_kernel, term_scaling_code
+        from .plan import as_device_tensor
 
-        kind, power = key
         dim = int(self.tree.dimensions)
         if len(tabs) > 1:
             l1kw = {"infer_kernel_scaling": False}
         else:
             l1kw = {"infer_kernel_scaling": False,
-                    "kernel_scaling_code": term_scaling_code(dim, power),
+                    "kernel_scaling_code": term_scaling_code(dim, key[1]),
                     "kernel_displacement_code": "0.0"}
         knl = term_kernel(dim, key)
         payload = self.get_payload(knl, tabs)
         near_field = NearFieldFromCSR(knl, payload["table_data_shapes"],
                                       potential_kind=self.potential_kind, **l1kw)
-        coefs = as_device_tensor(src_func)
+        coefs = as_device_tensor(coefs)
         parts = [coefs.real, coefs.imag] if coefs.is_complex() else [coefs]
         vals = []
         for part in parts:
@@ -435,15 +455,41 @@ class FPNDExpansionWrangler(ExpansionWranglerInterface):
             res = torch.zeros(int(self.tree.ntargets), dtype=torch.float64, device="cuda")
             res, _ = near_field(self.queue, result=res, **kw)
             vals.append(res)
-        term = vals[0].to(torch.complex128)
+        field = vals[0].to(torch.complex128)
         if len(vals) > 1:
-            term = term + 1j * vals[1]
+            field = field + 1j * vals[1]
+        return field
+
+    def _split_term_contribution(self, out_kernel, key, tabs, target_boxes, starts, lists,
+                                 src_func, w, view, pts):
+        """One term's list-1 contribution (expansion_wrangler_fpnd.py:
+        3678-3806): the term table's near field, plus for a single
+        r^{2n} log r table its log(h/h0) r^{2n} part - the point-to-point sum
+        of r^{2n} with strengths x log(h/h0) (beta mode "p2p", the default),
+        or the near field of the r^{2n} table for densities x log(h/h0)
+        (beta mode "table", ``helmholtz_split_auto_config[
+        "power_log_single_table_beta_mode"]``)."""
+        import torch
+
+        from .helmholtz_split import log_alpha_per_source, radial_power_sum
+        from .plan import as_device_tensor, stream_handle
+
+        kind, power = key
+        dim = int(self.tree.dimensions)
+        term = self._split_term_table_field(key, tabs, target_boxes, starts, lists, src_func)
         if dim == 2 and kind == "power_log" and len(tabs) == 1:
             beta = torch.from_numpy(log_alpha_per_source(
                 self.tree, float(tabs[0].source_box_extent))).to("cuda")
-            term = term + radial_power_sum(view, pts, w * beta, power,
-                                           exclude_self=bool(self.tree_indep.exclude_self),
-                                           stream=stream_handle(self.queue))
+            if self._helmholtz_split_beta_mode == "p2p":
+                term = term + radial_power_sum(view, pts, w * beta, power,
+                                               exclude_self=bool(self.tree_indep.exclude_self),
+                                               stream=stream_handle(self.queue))
+            else:
+                pkey = ("power", power)
+                ptabs = self._split_term_tables(out_kernel, pkey)
+                dens = as_device_tensor(src_func)
+                term = term + self._split_term_table_field(
+                    pkey, ptabs, target_boxes, starts, lists, dens * beta.to(dens.dtype))
         return term
 
     def eval_direct_helmholtz_split_correction(self, target_boxes, neighbor_source_boxes_starts,

@@ -39,7 +39,8 @@ from . import _lib
 __all__ = ["series_terms", "remainder_coefficients", "remainder_series",
            "max_neighbor_distance", "split_scaling_codes", "split_correction",
            "split_term_keys", "split_extra_terms", "term_kernel", "term_scaling_code",
-           "term_build_orders", "log_alpha_per_source", "radial_power_sum"]
+           "term_build_orders", "log_alpha_per_source", "radial_power_sum",
+           "select_split_order_from_rho", "choose_auto_split_order", "split_rho_components"]
 
 _GAMMA = 0.5772156649015329   # Euler-Mascheroni
 
@@ -173,6 +174,77 @@ def log_alpha_per_source(tree, table_root_extent):
     for b in np.nonzero(counts > 0)[0]:
         beta[starts[b]:starts[b] + counts[b]] = np.log(root * 0.5 ** int(levels[b]) / h0)
     return beta
+
+
+def select_split_order_from_rho(rho, thresholds, orders):
+    """The order of the first threshold rho does not exceed, else the last
+    order (``expansion_wrangler_fpnd.py:385-393``)."""
+    if len(orders) != len(thresholds) + 1:
+        raise ValueError("orders must have one more element than thresholds")
+    for i, t in enumerate(thresholds):
+        if float(rho) <= float(t):
+            return int(orders[i])
+    return int(orders[-1])
+
+
+def split_rho_components(tree, wave_numbers):
+    """(|Re k| h_max, |Im k| h_max) over the wave numbers, h_max the extent
+    of the coarsest box holding sources (``expansion_wrangler_fpnd.py:
+    4213-4250``)."""
+    ks = [complex(k) for k in wave_numbers]
+    counts = np.asarray(tree.box_source_counts_nonchild)
+    levels = np.asarray(tree.box_levels)[: len(counts)]
+    active = levels[counts > 0]
+    if not ks or active.size == 0:
+        return 0.0, 0.0
+    h_max = float(tree.root_extent) * 0.5 ** int(active.min())
+    return (max(abs(k.real) for k in ks) * h_max, max(abs(k.imag) for k in ks) * h_max)
+
+
+def choose_auto_split_order(auto_cfg, rho_real, rho_imag):
+    """Split order for rho = |k| h_max (``expansion_wrangler_fpnd.py:
+    4252-4323``): thresholds and orders from ``auto_cfg`` ("rho_thresholds",
+    "orders", "rho_thresholds_real" / "_imag") or geometric ladders
+    rho_base * 2^j (real 0.25, imaginary 0.5 by default) over orders
+    order_min (2) .. order_max (12); the larger of the real and imaginary
+    parts' orders, clamped to [order_min, order_max] unless orders are
+    given.  Returns (order, info)."""
+    order_min = int(auto_cfg.get("order_min", 2))
+    order_max = int(auto_cfg.get("order_max", 12))
+    if order_max < order_min:
+        raise ValueError("order_max must be >= order_min")
+    if "rho_thresholds" in auto_cfg or "orders" in auto_cfg:
+        t_real = tuple(auto_cfg.get("rho_thresholds", (0.5, 1.5, 3.0)))
+        t_imag = t_real
+        orders = (tuple(auto_cfg["orders"]) if "orders" in auto_cfg
+                  else tuple(range(order_min, order_min + len(t_real) + 1)))
+    else:
+        r0, i0 = float(auto_cfg.get("rho_base_real", 0.25)), float(
+            auto_cfg.get("rho_base_imag", 0.5))
+        if r0 <= 0.0 or i0 <= 0.0:
+            raise ValueError("rho_base_real and rho_base_imag must be positive")
+        count = max(0, order_max - order_min)
+        t_real = tuple(r0 * 2.0 ** j for j in range(count))
+        t_imag = tuple(i0 * 2.0 ** j for j in range(count))
+        orders = tuple(range(order_min, order_max + 1))
+    if "rho_thresholds_real" in auto_cfg:
+        t_real = tuple(auto_cfg["rho_thresholds_real"])
+    if "rho_thresholds_imag" in auto_cfg:
+        t_imag = tuple(auto_cfg["rho_thresholds_imag"])
+    if "orders" not in auto_cfg:
+        if len(t_real) != len(t_imag):
+            raise ValueError("rho_thresholds_real and rho_thresholds_imag must have the "
+                             "same length when orders are not provided")
+        orders = tuple(range(order_min, order_min + len(t_real) + 1))
+    order = max(select_split_order_from_rho(rho_real, t_real, orders),
+                select_split_order_from_rho(rho_imag, t_imag, orders))
+    if "orders" not in auto_cfg:
+        order = max(order_min, min(order_max, order))
+    coverage = max(float(t_real[-1]) if t_real else 0.0, float(t_imag[-1]) if t_imag else 0.0)
+    return order, {"rho_real": float(rho_real), "rho_imag": float(rho_imag),
+                   "thresholds_real": t_real, "thresholds_imag": t_imag, "orders": orders,
+                   "beyond_coverage": bool(coverage > 0.0 and
+                                           max(rho_real, rho_imag) > coverage)}
 
 
 def remainder_series(dim, k, r, n_terms, split_order=1):
